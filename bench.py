@@ -1,0 +1,437 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 W-projection gridder.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload cfg1|cfg0|cfg2|cfg2b]
+
+Prints one JSON line (rank 0).  A step is one gridding call over the whole
+workload (placement, binning, sort, tile gridding, partial reduction) onto a
+complex64 grid that stays in HBM; inputs are resident on the device when the
+timed region starts (``value``).  ``e2e`` is the same metric through the
+reference-facing drop-in (oskar_grid_wproj_f, host buffers) with every host
+to device and device to host copy inside the timed region.
+
+``--impl reference`` times the reference's serial algorithm on the host
+cores instead: the CPU restatement in oracle/ (bit-identical to the
+reference's compiled oskar_grid_wproj_f, as the tests check), spread over all
+host threads by grid-row bands so each cell is still accumulated in the
+serial order.
+
+Multi-GPU: the gridding call has no exchange step; under torchrun each rank
+grids its own replica of the workload ("replicas only"), value = all ranks'
+visibilities / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = ("Mvis/s & GFLOP/s on 1 GB300, batched vs plain, grid err "
+          "≤1e-5 vs FP64 oracle")
+UNIT = "Mvis/s"
+PUBLISHED_P100_MVIS = {"cfg1": 2152800 / 0.074 / 1e6,
+                       "cfg2": 31395840 / 0.781 / 1e6,
+                       "cfg2b": 31395840 / 0.553 / 1e6}
+WORKLOAD_TEXT = {
+    "cfg0": "plain 200,000 vis on a 2048^2 grid, 128 w-planes, support "
+            "4..24, oversample 4",
+    "cfg1": "synthetic-challenge shape: 2,152,800 vis on an 8192^2 grid, "
+            "714 w-planes, support 4..36, oversample 4",
+    "cfg2": "SKA-LOW EL56-82 shape: 31,395,840 vis, 8192^2 grid, 601 "
+            "w-planes, support 4..72",
+    "cfg2b": "SKA-LOW EL82-70 shape: 31,395,840 vis, 8192^2 grid, 339 "
+             "w-planes, support 8..44",
+}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="cfg1",
+                    choices=sorted(WORKLOAD_TEXT))
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")),
+            int(os.environ.get("WORLD_SIZE", "1")))
+
+
+def load_workload(name):
+    synthetic = importlib.import_module("gpu-gridding_gb300.synthetic")
+    return synthetic.WORKLOADS[name]()
+
+
+L2_BYTES = 129 * 2 ** 20
+
+
+def grid_exceeds_l2(wl):
+    return 8 * wl.grid_size ** 2 > L2_BYTES
+
+
+def workload_config(name, wl, extra=None):
+    gmb = 8 * wl.grid_size ** 2 / 1e6
+    l2 = (f"inputs larger than L2: the {wl.grid_size}^2 complex64 grid "
+          f"({gmb:.0f} MB) is read and written every step"
+          if grid_exceeds_l2(wl) else
+          "L2 flushed between timed steps (256 MB write outside the "
+          "per-step events)")
+    cfg = {"workload": f"{name}: {WORKLOAD_TEXT[name]}",
+           "num_vis": wl.num_points, "grid_size": wl.grid_size,
+           "num_w_planes": wl.num_w_planes,
+           "support": [int(wl.support.min()), int(wl.support.max())],
+           "oversample": wl.oversample, "l2": l2,
+           "parallelism": "replicas (no exchange step)"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+# ---------------------------------------------------------------------------
+# Clock sampling (nvidia-smi) during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id=None):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}",
+               "--format=csv,noheader,nounits", "-lms", "200"]
+        if self.gpu_id:
+            cmd += ["-i", self.gpu_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=open(self.path, "w"),
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows
+                          for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows),
+                "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def gpu_uuid(torch, dev):
+    try:
+        u = torch.cuda.get_device_properties(dev).uuid
+        s = str(u)
+        return s if s.startswith("GPU-") else "GPU-" + s
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------------------
+# CPU runs (reference algorithm on the host cores)
+# ---------------------------------------------------------------------------
+def cpu_run(wl, threads):
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle
+    grid = np.zeros((wl.grid_size, wl.grid_size, 2), np.float32)
+    t0 = time.perf_counter()
+    oracle.grid_f_mt(wl, grid, 0.0, threads=threads)
+    return time.perf_counter() - t0
+
+
+def run_reference(args):
+    rank, _, world = rank_info()
+    if rank != 0:
+        return 0
+    wl = load_workload(args.workload)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_run(wl, threads)
+    times = [cpu_run(wl, threads) for _ in range(args.steps)]
+    t = statistics.mean(times)
+    value = wl.num_points / t / 1e6
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "impl": "reference",
+        "config": workload_config(args.workload, wl),
+        "cpu_baseline": {
+            "value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"whole workload ({wl.num_points} vis) per step; the "
+                      "oracle's restatement of oskar_grid_wproj_f "
+                      "(bit-identical to the reference build), grid rows "
+                      f"split over {threads} host threads"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU run
+# ---------------------------------------------------------------------------
+def read_traffic(kernel, workload):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/<kernel>_<workload>.txt, line 'dram_bytes_per_launch: X')."""
+    path = os.path.join(HERE, "profiles", f"{kernel}_{workload}.txt")
+    if not os.path.isfile(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def measured_peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.isfile(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def run_ours(args):
+    import torch
+    rank, local_rank, world = rank_info()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl", device_id=torch.device(
+            "cuda", local_rank))
+    else:
+        torch.cuda.set_device(0)
+    pkg = importlib.import_module("gpu-gridding_gb300")
+    if not os.path.isfile(pkg.LIB_PATH):
+        pkg.build()
+    wl = load_workload(args.workload)
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    def to_dev(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+    stack = pkg.KernelStack.from_workload(wl, "f")
+    plan = pkg.Plan()
+    uu, vv, ww = to_dev(wl.uu), to_dev(wl.vv), to_dev(wl.ww)
+    vis, weight = to_dev(wl.vis), to_dev(wl.weight)
+    G = wl.grid_size
+    grid = torch.zeros((G, G, 2), dtype=torch.float32, device=dev)
+    norm = torch.zeros(1, dtype=torch.float64, device=dev)
+    nskip = torch.zeros(1, dtype=torch.int64, device=dev)
+    cell, wsc = np.float32(wl.cell_size_rad), np.float32(wl.w_scale)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        pkg.grid_wproj_device(plan, stack, uu, vv, ww, vis, weight, cell,
+                              wsc, G, grid, norm, nskip, stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    barrier()
+    clocks = ClockSampler(gpu_uuid(torch, dev))
+    clocks.start()
+    barrier()
+    if grid_exceeds_l2(wl):
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(args.steps):
+            step()
+        t1.record(stream)
+        barrier()
+        ms = t0.elapsed_time(t1) / args.steps
+    else:
+        flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device=dev)
+        evs = [(torch.cuda.Event(enable_timing=True),
+                torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        for a, b in evs:
+            flush.fill_(1)
+            a.record(stream)
+            step()
+            b.record(stream)
+        barrier()
+        ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+    clk = clocks.stop()
+    ms_max = ms
+    if dist is not None:
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    stats = plan.stats()
+    num_vis = wl.num_points
+    value = world * num_vis / (ms_max * 1e-3) / 1e6
+    macs = stats["num_macs"]
+    gflops = world * 8.0 * macs / (ms_max * 1e-3) / 1e9
+
+    # Phase times of the same call, CUDA events on the launching stream.
+    plan.set_profiling(True)
+    phases = []
+    for _ in range(max(3, min(args.steps, 10))):
+        step()
+        torch.cuda.synchronize()
+        phases.append(plan.phase_ms())
+    plan.set_profiling(False)
+    phase_ms = {k: statistics.mean(p[k] for p in phases) for k in phases[0]}
+    grid_ms = phase_ms["grid_tiles"]
+    fma_peak = pkg.measure_fp32_fma_tflops()
+    achieved = 8.0 * macs / (grid_ms * 1e-3) / 1e12
+    peaks, peak_kind = measured_peaks()
+    traffic = read_traffic("k_grid_tiles", args.workload)
+    # Algorithmic bytes of one gridding-kernel launch: placed visibility
+    # (cell, meta, weighted vis: 16 B) once per visibility, one 4-byte record
+    # index per (visibility, tile), each re-laid kernel tap once (8 B), and
+    # the grid read and written once (16 B per cell).
+    stack_taps = int(sum(wl.oversample ** 2 *
+                         (((wl.oversample + 1) // 2 + int(s) * wl.oversample)
+                          // wl.oversample + 1) ** 2 for s in wl.support))
+    alg_bytes = (16 * num_vis + 4 * stats["num_records"] + 8 * stack_taps +
+                 16 * G * G)
+
+    # End to end through the drop-in with pinned host buffers.
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)),
+                        pin_memory=True)
+        t.numpy()[...] = a
+        return t.numpy()
+
+    h = {k: pinned(getattr(wl, k)) for k in
+         ("support", "conv_func", "uu", "vv", "ww", "vis", "weight")}
+    h_grid = pinned(np.zeros((G, G, 2), np.float32))
+
+    def e2e_step():
+        pkg.oskar_grid_wproj_f(wl.num_w_planes, h["support"], wl.oversample,
+                               wl.conv_size_half, h["conv_func"], num_vis,
+                               h["uu"], h["vv"], h["ww"], h["vis"],
+                               h["weight"], cell, wsc, G, h_grid, 0.0)
+
+    e2e_step()
+    barrier()
+    te = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    te = (time.perf_counter() - te) / args.e2e_steps
+    if dist is not None:
+        t = torch.tensor([te], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        te = float(t.item())
+    h2d = (24 * num_vis + wl.conv_func.nbytes + wl.support.nbytes +
+           8 * G * G + 8)
+    d2h = 8 * G * G + 16
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        tc = cpu_run(wl, threads)
+        cpu = {"value": num_vis / tc / 1e6, "unit": UNIT, "cores": threads,
+               "kind": "port",
+               "sample": f"whole workload ({num_vis} vis), one run; the "
+                         "oracle's restatement of oskar_grid_wproj_f "
+                         "(bit-identical to the reference build), grid rows "
+                         f"split over {threads} host threads"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": ms_max, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded PCG64, shape-matched to the "
+                    "reference's dataset)",
+            "config": workload_config(args.workload, wl, {
+                "macs_per_step": macs, "records_per_step":
+                    stats["num_records"], "tile": [stats["tile_u"],
+                                                    stats["tile_v"]]}),
+            "gflops": gflops,
+            "phase_ms": phase_ms,
+            "roofline": {
+                "bound": "fp32_fma", "kernel": "k_grid_tiles",
+                "achieved": achieved, "peak": fma_peak, "unit": "TFLOP/s",
+                "frac": achieved / fma_peak if fma_peak else None,
+                "peak_source": "measured in this run (FP32 FMA probe "
+                               "kernel, gg_measure_fp32_fma_tflops)",
+                "traffic": traffic,
+                "algorithmic_bytes": alg_bytes,
+                "hbm_achieved_gbs": alg_bytes / (grid_ms * 1e-3) / 1e9,
+                "hbm_peak_gbs": peaks.get("hbm_gbs"),
+                "hbm_peak_source": peak_kind},
+            "cpu_baseline": cpu,
+            "e2e": {"value": world * num_vis / te / 1e6, "unit": UNIT,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": args.steps * stats["num_launches"],
+            "clocks": clk,
+            "published_p100_mvis": PUBLISHED_P100_MVIS.get(args.workload),
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

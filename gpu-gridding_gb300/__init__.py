@@ -1,0 +1,372 @@
+"""GB300 W-projection gridder -- Python host interface.
+
+A thin ctypes layer over ``libgpugrid.so`` (C ABI in include/gpugrid.h):
+
+* ``oskar_grid_wproj_f`` / ``oskar_grid_wproj_d`` -- the reference's serial
+  gridding functions (oskar_grid_wproj.h:69-86, :114-131 of the reference),
+  same argument names and meaning, host (numpy) arrays.  ``grid`` is updated
+  in place; the function returns ``(num_skipped, norm)`` where the reference
+  writes them through pointers.
+* ``KernelStack``, ``Plan``, ``grid_wproj_device``, ``degrid_wproj_device``
+  -- device-resident inputs (torch CUDA tensors) on a CUDA stream.
+* ``GridWproj`` -- torch.autograd.Function whose backward pass is the
+  hand-written adjoint (degridding) kernel.
+
+There is no CPU fallback: if the library is missing or no GPU is present the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+GG_OK = 0
+_ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory",
+           4: "unsupported", 5: "capacity"}
+
+# Every entry point declared in include/gpugrid.h.
+EXPORTED_SYMBOLS = (
+    "oskar_grid_wproj_d", "oskar_grid_wproj_f", "gg_grid_wproj_d",
+    "gg_grid_wproj_f", "gg_last_error", "gg_version", "gg_kernels_create_f",
+    "gg_kernels_create_d", "gg_kernels_destroy", "gg_plan_create",
+    "gg_plan_destroy", "gg_plan_last_stats", "gg_plan_set_profiling",
+    "gg_plan_phase_ms", "gg_measure_fp32_fma_tflops", "gg_grid_wproj_f_device",
+    "gg_grid_wproj_d_device", "gg_place_wproj_f_device",
+    "gg_place_wproj_d_device", "gg_degrid_wproj_f_device",
+    "gg_degrid_wproj_d_device",
+)
+
+
+class GridError(RuntimeError):
+    """A gg_* call returned a non-zero status."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{_ERRORS.get(code, code)}: {message}")
+        self.code = code
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("num_points", ctypes.c_ulonglong),
+                ("num_skipped", ctypes.c_ulonglong),
+                ("num_records", ctypes.c_ulonglong),
+                ("num_macs", ctypes.c_ulonglong),
+                ("num_launches", ctypes.c_ulonglong),
+                ("tile_u", ctypes.c_int), ("tile_v", ctypes.c_int)]
+
+
+_lib = None
+_vp = ctypes.c_void_p
+_sz = ctypes.c_size_t
+
+
+def _declare(L):
+    f32, f64 = ctypes.c_float, ctypes.c_double
+    for suffix, real in (("f", f32), ("d", f64)):
+        grid_args = [_sz, _vp, ctypes.c_int, ctypes.c_int, _vp, _sz, _vp, _vp,
+                     _vp, _vp, _vp, real, real, ctypes.c_int, _vp, _vp, _vp]
+        fn = getattr(L, f"gg_grid_wproj_{suffix}")
+        fn.argtypes = grid_args
+        fn.restype = ctypes.c_int
+        fn = getattr(L, f"oskar_grid_wproj_{suffix}")
+        fn.argtypes = grid_args
+        fn.restype = None
+        fn = getattr(L, f"gg_kernels_create_{suffix}")
+        fn.argtypes = [ctypes.POINTER(_vp), _sz, _vp, ctypes.c_int,
+                       ctypes.c_int, _vp, ctypes.c_int, _vp]
+        fn.restype = ctypes.c_int
+        fn = getattr(L, f"gg_grid_wproj_{suffix}_device")
+        fn.argtypes = [_vp, _vp, _sz, _vp, _vp, _vp, _vp, _vp, real, real,
+                       ctypes.c_int, _vp, _vp, _vp, _vp]
+        fn.restype = ctypes.c_int
+        fn = getattr(L, f"gg_place_wproj_{suffix}_device")
+        fn.argtypes = [_vp, _sz, _vp, _vp, _vp, real, real, ctypes.c_int,
+                       _vp, _vp]
+        fn.restype = ctypes.c_int
+        fn = getattr(L, f"gg_degrid_wproj_{suffix}_device")
+        fn.argtypes = [_vp, _vp, _sz, _vp, _vp, _vp, real, real, ctypes.c_int,
+                       _vp, _vp, _vp]
+        fn.restype = ctypes.c_int
+    L.gg_last_error.restype = ctypes.c_char_p
+    L.gg_last_error.argtypes = []
+    L.gg_version.restype = ctypes.c_char_p
+    L.gg_version.argtypes = []
+    L.gg_kernels_destroy.argtypes = [_vp]
+    L.gg_kernels_destroy.restype = ctypes.c_int
+    L.gg_plan_create.argtypes = [ctypes.POINTER(_vp)]
+    L.gg_plan_create.restype = ctypes.c_int
+    L.gg_plan_destroy.argtypes = [_vp]
+    L.gg_plan_destroy.restype = ctypes.c_int
+    L.gg_plan_last_stats.argtypes = [_vp, ctypes.POINTER(Stats)]
+    L.gg_plan_last_stats.restype = ctypes.c_int
+    L.gg_plan_set_profiling.argtypes = [_vp, ctypes.c_int]
+    L.gg_plan_set_profiling.restype = ctypes.c_int
+    L.gg_plan_phase_ms.argtypes = [_vp, ctypes.POINTER(ctypes.c_float),
+                                   ctypes.c_int]
+    L.gg_plan_phase_ms.restype = ctypes.c_int
+    L.gg_measure_fp32_fma_tflops.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    L.gg_measure_fp32_fma_tflops.restype = ctypes.c_int
+
+
+def lib():
+    """The loaded libgpugrid.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.isfile(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with "
+                "__graft_entry__.build() (or python gpu-gridding_gb300/build.py)")
+        L = ctypes.CDLL(LIB_PATH)
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def build(force: bool = False) -> str:
+    """Compile libgpugrid.so for sm_103a (in-tree)."""
+    return _build.build(force=force)
+
+
+def last_error() -> str:
+    return lib().gg_last_error().decode()
+
+
+def _check(code: int) -> None:
+    if code != GG_OK:
+        raise GridError(code, last_error())
+
+
+def _ptr(a) -> int:
+    if a is None:
+        return 0
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()  # torch tensor
+
+
+def _host(a, dtype):
+    a = np.asarray(a)
+    if a.dtype != dtype or not a.flags.c_contiguous:
+        a = np.ascontiguousarray(a, dtype=dtype)
+    return a
+
+
+# ---------------------------------------------------------------------------
+# Drop-in (host arrays)
+# ---------------------------------------------------------------------------
+def _dropin(suffix, dtype, num_w_planes, support, oversample, conv_size_half,
+            conv_func, num_points, uu, vv, ww, vis, weight, cell_size_rad,
+            w_scale, grid_size, grid, norm):
+    if not (isinstance(grid, np.ndarray) and grid.dtype == dtype and
+            grid.flags.c_contiguous):
+        raise TypeError(f"grid must be a C-contiguous {np.dtype(dtype)} array")
+    if grid.size != 2 * grid_size * grid_size:
+        raise ValueError("grid must hold grid_size^2 complex values")
+    arrs = [_host(support, np.int32), _host(conv_func, dtype), _host(uu, dtype),
+            _host(vv, dtype), _host(ww, dtype), _host(vis, dtype),
+            _host(weight, dtype)]
+    ns = ctypes.c_size_t(0)
+    nm = ctypes.c_double(norm)
+    _check(getattr(lib(), f"gg_grid_wproj_{suffix}")(
+        num_w_planes, _ptr(arrs[0]), oversample, conv_size_half, _ptr(arrs[1]),
+        num_points, _ptr(arrs[2]), _ptr(arrs[3]), _ptr(arrs[4]), _ptr(arrs[5]),
+        _ptr(arrs[6]), cell_size_rad, w_scale, grid_size,
+        ctypes.addressof(ns), ctypes.addressof(nm), _ptr(grid)))
+    return int(ns.value), float(nm.value)
+
+
+def oskar_grid_wproj_f(num_w_planes, support, oversample, conv_size_half,
+                       conv_func, num_points, uu, vv, ww, vis, weight,
+                       cell_size_rad, w_scale, grid_size, grid, norm=0.0):
+    """GPU drop-in for oskar_grid_wproj_f (reference oskar_grid_wproj.c:
+    126-212).  grid (float32, grid_size^2 complex) is accumulated in place;
+    returns (num_skipped, norm + this call's normalisation)."""
+    return _dropin("f", np.float32, num_w_planes, support, oversample,
+                   conv_size_half, conv_func, num_points, uu, vv, ww, vis,
+                   weight, cell_size_rad, w_scale, grid_size, grid, norm)
+
+
+def oskar_grid_wproj_d(num_w_planes, support, oversample, conv_size_half,
+                       conv_func, num_points, uu, vv, ww, vis, weight,
+                       cell_size_rad, w_scale, grid_size, grid, norm=0.0):
+    """GPU drop-in for oskar_grid_wproj_d (reference oskar_grid_wproj.c:
+    37-123), FP64 throughout."""
+    return _dropin("d", np.float64, num_w_planes, support, oversample,
+                   conv_size_half, conv_func, num_points, uu, vv, ww, vis,
+                   weight, cell_size_rad, w_scale, grid_size, grid, norm)
+
+
+def grid_f(wl, grid=None, norm=0.0):
+    """oskar_grid_wproj_f on a synthetic.Workload; returns
+    (grid, num_skipped, norm) like the oracle's helper of the same name."""
+    if grid is None:
+        grid = np.zeros((wl.grid_size, wl.grid_size, 2), np.float32)
+    ns, nm = oskar_grid_wproj_f(
+        wl.num_w_planes, wl.support, wl.oversample, wl.conv_size_half,
+        wl.conv_func, wl.num_points, wl.uu, wl.vv, wl.ww, wl.vis, wl.weight,
+        np.float32(wl.cell_size_rad), np.float32(wl.w_scale), wl.grid_size,
+        grid, norm)
+    return grid, ns, nm
+
+
+def grid_d(wl, grid=None, norm=0.0):
+    """oskar_grid_wproj_d on a workload promoted to float64."""
+    if grid is None:
+        grid = np.zeros((wl.grid_size, wl.grid_size, 2), np.float64)
+    ns, nm = oskar_grid_wproj_d(
+        wl.num_w_planes, wl.support, wl.oversample, wl.conv_size_half,
+        wl.conv_func, wl.num_points, wl.uu, wl.vv, wl.ww, wl.vis, wl.weight,
+        float(wl.cell_size_rad), float(wl.w_scale), wl.grid_size, grid, norm)
+    return grid, ns, nm
+
+
+# ---------------------------------------------------------------------------
+# Device API (torch tensors)
+# ---------------------------------------------------------------------------
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream()
+    return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+
+
+class KernelStack:
+    """Device-resident, re-laid kernel stack (gg_kernels handle)."""
+
+    def __init__(self, num_w_planes, support, oversample, conv_size_half,
+                 conv_func, precision="f", stream=None):
+        self.precision = precision
+        self.num_w_planes = int(num_w_planes)
+        self.oversample = int(oversample)
+        self.conv_size_half = int(conv_size_half)
+        self.support = _host(support, np.int32)
+        h = ctypes.c_void_p(0)
+        on_device = 0 if isinstance(conv_func, np.ndarray) else 1
+        if on_device == 0:
+            conv_func = _host(conv_func, np.float32 if precision == "f"
+                              else np.float64)
+        self._keep = conv_func
+        _check(getattr(lib(), f"gg_kernels_create_{precision}")(
+            ctypes.byref(h), self.num_w_planes, _ptr(self.support),
+            self.oversample, self.conv_size_half, _ptr(conv_func), on_device,
+            _stream_ptr(stream) if on_device else None))
+        self._keep = None
+        self.handle = h
+
+    @classmethod
+    def from_workload(cls, wl, precision="f", stream=None):
+        return cls(wl.num_w_planes, wl.support, wl.oversample,
+                   wl.conv_size_half, wl.conv_func, precision, stream)
+
+    def close(self):
+        if self.handle and self.handle.value:
+            lib().gg_kernels_destroy(self.handle)
+            self.handle = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Plan:
+    """Device workspace (gg_plan handle); one call at a time."""
+
+    def __init__(self):
+        h = ctypes.c_void_p(0)
+        _check(lib().gg_plan_create(ctypes.byref(h)))
+        self.handle = h
+
+    PHASES = ("placement", "binning", "work_items", "grid_tiles",
+              "reduce_partials")
+
+    def stats(self) -> dict:
+        s = Stats()
+        _check(lib().gg_plan_last_stats(self.handle, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def set_profiling(self, enable: bool = True) -> None:
+        _check(lib().gg_plan_set_profiling(self.handle, int(enable)))
+
+    def phase_ms(self) -> dict:
+        """CUDA-event time of each phase of the last call (stream must be
+        synchronised; profiling must be enabled)."""
+        arr = (ctypes.c_float * len(self.PHASES))()
+        _check(lib().gg_plan_phase_ms(self.handle, arr, len(self.PHASES)))
+        return dict(zip(self.PHASES, list(arr)))
+
+    def close(self):
+        if self.handle and self.handle.value:
+            lib().gg_plan_destroy(self.handle)
+            self.handle = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def measure_fp32_fma_tflops() -> float:
+    """Measured FP32 FMA throughput of the current GPU (TFLOP/s)."""
+    out = ctypes.c_double(0)
+    _check(lib().gg_measure_fp32_fma_tflops(ctypes.byref(out)))
+    return float(out.value)
+
+
+def _require_cuda(*tensors):
+    for t in tensors:
+        if not t.is_cuda or not t.is_contiguous():
+            raise TypeError("device entry points take contiguous CUDA tensors")
+
+
+def grid_wproj_device(plan, stack, uu, vv, ww, vis, weight, cell_size_rad,
+                      w_scale, grid_size, grid, norm, num_skipped,
+                      stream=None):
+    """Grid device-resident visibilities onto a device grid.
+
+    uu, vv, ww, weight: [N]; vis: [N, 2]; grid: [G, G, 2] (accumulated);
+    norm: float64 [1] (accumulated); num_skipped: int64 [1] (set).  dtype
+    float32 with a precision "f" stack, float64 with "d"."""
+    import torch  # noqa: F401
+    _require_cuda(uu, vv, ww, vis, weight, grid, norm, num_skipped)
+    n = int(uu.shape[0])
+    fn = getattr(lib(), f"gg_grid_wproj_{stack.precision}_device")
+    _check(fn(plan.handle, stack.handle, n, _ptr(uu), _ptr(vv), _ptr(ww),
+              _ptr(vis), _ptr(weight), cell_size_rad, w_scale, grid_size,
+              _ptr(num_skipped), _ptr(norm), _ptr(grid), _stream_ptr(stream)))
+
+
+def place_wproj_device(stack, uu, vv, ww, cell_size_rad, w_scale, grid_size,
+                       stream=None):
+    """Per-visibility placement as the gridder computes it: int32 [N, 6] =
+    (cell u, cell v, off_u, off_v, plane, flags); flags bit 0 = skipped,
+    bit 1 = conjugated kernel (ww > 0)."""
+    import torch
+    _require_cuda(uu, vv, ww)
+    n = int(uu.shape[0])
+    out = torch.empty((n, 6), dtype=torch.int32, device=uu.device)
+    fn = getattr(lib(), f"gg_place_wproj_{stack.precision}_device")
+    _check(fn(stack.handle, n, _ptr(uu), _ptr(vv), _ptr(ww), cell_size_rad,
+              w_scale, grid_size, _ptr(out), _stream_ptr(stream)))
+    return out
+
+
+def degrid_wproj_device(plan, stack, uu, vv, ww, cell_size_rad, w_scale,
+                        grid_size, grid, out_vis, stream=None):
+    """Adjoint of grid_wproj_device: out_vis[N, 2] = G^H grid."""
+    _require_cuda(uu, vv, ww, grid, out_vis)
+    n = int(uu.shape[0])
+    fn = getattr(lib(), f"gg_degrid_wproj_{stack.precision}_device")
+    _check(fn(plan.handle, stack.handle, n, _ptr(uu), _ptr(vv), _ptr(ww),
+              cell_size_rad, w_scale, grid_size, _ptr(grid), _ptr(out_vis),
+              _stream_ptr(stream)))
+
+
+from .autograd import GridWproj  # noqa: E402,F401

@@ -1,0 +1,912 @@
+// Host orchestration and the C ABI of libgpugrid.so (declared in
+// include/gpugrid.h).
+//
+// One gridding call runs, on one CUDA stream:
+//   1. k_place         placement, skip flags, FP64 norm partials, records
+//                      per visibility (tiles its footprint touches)
+//   2. scan            record offsets per visibility
+//   3. k_emit          (key = tile|plane|offset class, value = visibility)
+//   4. radix sort      stable, so the record order is deterministic
+//   5. tile bounds     record range of every tile
+//   6. work items      tiles cut into chunks; split chunks get partial slots
+//   7. k_grid_tiles    persistent tile-owning accumulation
+//   8. reduce          split tiles: grid += partials, in chunk order
+// The host synchronises once, after step 2, to size the sort buffers.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "gg_internal.h"
+#include "../../include/gpugrid.h"
+
+using namespace gg;
+
+// ===========================================================================
+// Errors
+// ===========================================================================
+namespace {
+
+thread_local std::string t_last_error;
+
+int set_error(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  t_last_error = buf;
+  return code;
+}
+
+#define GG_CUDA(call)                                                      \
+  do {                                                                     \
+    cudaError_t e__ = (call);                                              \
+    if (e__ != cudaSuccess)                                                \
+      return set_error(e__ == cudaErrorMemoryAllocation ? GG_ERR_NO_MEMORY \
+                                                        : GG_ERR_CUDA,     \
+                       "%s failed: %s (%s:%d)", #call,                     \
+                       cudaGetErrorString(e__), __FILE__, __LINE__);       \
+  } while (0)
+
+#define GG_TRY(call)              \
+  do {                            \
+    int r__ = (call);             \
+    if (r__ != GG_OK) return r__; \
+  } while (0)
+
+// ===========================================================================
+// Device buffers
+// ===========================================================================
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  // Grows to at least n bytes (with 25% headroom); contents are not kept.
+  int ensure(size_t n) {
+    if (n <= bytes && p) return GG_OK;
+    release();
+    size_t want = std::max<size_t>(n + n / 4, 256);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      cudaGetLastError();
+      return set_error(GG_ERR_NO_MEMORY,
+                       "cudaMalloc of %zu bytes failed: %s", want,
+                       cudaGetErrorString(e));
+    }
+    bytes = want;
+    return GG_OK;
+  }
+  template <typename T>
+  T* as() const { return (T*)p; }
+};
+
+int ceil_log2(unsigned long long x) {
+  int b = 0;
+  while ((1ull << b) < x) ++b;
+  return b;
+}
+
+// ===========================================================================
+// Per-device state (mutex + stream for the drop-in entry points)
+// ===========================================================================
+struct DeviceState {
+  std::mutex mu;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  gg_plan* plan = nullptr;  // workspace of the host-pointer entry points
+};
+
+std::mutex g_devices_mu;
+std::vector<DeviceState*> g_devices;
+
+int current_device(int* dev) {
+  GG_CUDA(cudaGetDevice(dev));
+  return GG_OK;
+}
+
+int device_state(int dev, DeviceState** out) {
+  std::lock_guard<std::mutex> lk(g_devices_mu);
+  if ((int)g_devices.size() <= dev) g_devices.resize(dev + 1, nullptr);
+  if (!g_devices[dev]) {
+    DeviceState* st = new DeviceState();
+    int sms = 0;
+    cudaError_t e =
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) {
+      delete st;
+      return set_error(GG_ERR_CUDA, "cudaDeviceGetAttribute: %s",
+                       cudaGetErrorString(e));
+    }
+    st->num_sms = sms;
+    e = cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete st;
+      return set_error(GG_ERR_CUDA, "cudaStreamCreate: %s",
+                       cudaGetErrorString(e));
+    }
+    g_devices[dev] = st;
+  }
+  *out = g_devices[dev];
+  return GG_OK;
+}
+
+int num_sms_of_current(int* sms) {
+  int dev;
+  GG_TRY(current_device(&dev));
+  DeviceState* st;
+  GG_TRY(device_state(dev, &st));
+  *sms = st->num_sms;
+  return GG_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// Kernel stacks
+// ===========================================================================
+struct gg_kernels {
+  int device = 0;
+  bool is_double = false;
+  int num_planes = 0, oversample = 0, omax = 0, conv_size_half = 0;
+  int support_max = 0;
+  long long total_taps = 0;
+  std::vector<int> h_support;
+  DevBuf support, side, base, taps, tap_sum;
+
+  StackView view() const {
+    StackView v;
+    v.num_planes = num_planes;
+    v.oversample = oversample;
+    v.omax = omax;
+    v.conv_size_half = conv_size_half;
+    v.support = support.as<int>();
+    v.side = side.as<int>();
+    v.base = base.as<long long>();
+    v.taps = taps.p;
+    v.tap_sum = tap_sum.as<double>();
+    return v;
+  }
+};
+
+namespace {
+
+int validate_stack(size_t num_w_planes, const int* support, int oversample,
+                   int conv_size_half, const void* conv_func) {
+  if (num_w_planes < 1 || num_w_planes > (size_t)kMaxPlanes)
+    return set_error(GG_ERR_INVALID_ARG,
+                     "num_w_planes = %zu outside [1, %d]", num_w_planes,
+                     kMaxPlanes);
+  if (!support || !conv_func)
+    return set_error(GG_ERR_INVALID_ARG, "support or conv_func is NULL");
+  if (oversample < 1 || oversample > kMaxOversample)
+    return set_error(GG_ERR_INVALID_ARG, "oversample = %d outside [1, %d]",
+                     oversample, kMaxOversample);
+  if (conv_size_half < 1)
+    return set_error(GG_ERR_INVALID_ARG, "conv_size_half = %d < 1",
+                     conv_size_half);
+  for (size_t p = 0; p < num_w_planes; ++p) {
+    const long long s = support[p];
+    if (s < 0)
+      return set_error(GG_ERR_INVALID_ARG, "support[%zu] = %lld < 0", p, s);
+    // The reference reads taps up to |off| + s*os with |off| <= os/2; a cube
+    // smaller than that is read out of bounds by the reference.
+    if (s * oversample + oversample / 2 >= (long long)conv_size_half)
+      return set_error(GG_ERR_INVALID_ARG,
+                       "support[%zu] = %lld needs conv_size_half > %lld "
+                       "(got %d)",
+                       p, s, s * oversample + oversample / 2,
+                       conv_size_half);
+  }
+  return GG_OK;
+}
+
+template <typename Real>
+int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
+                   int oversample, int conv_size_half, const Real* conv_func,
+                   int on_device, cudaStream_t s) {
+  if (!out) return set_error(GG_ERR_INVALID_ARG, "out is NULL");
+  *out = nullptr;
+  GG_TRY(validate_stack(num_w_planes, support, oversample, conv_size_half,
+                        conv_func));
+  gg_kernels* k = new gg_kernels();
+  auto fail = [&](int code) {
+    delete k;
+    return code;
+  };
+  if (current_device(&k->device) != GG_OK) return fail(GG_ERR_CUDA);
+  k->is_double = sizeof(Real) == 8;
+  k->num_planes = (int)num_w_planes;
+  k->oversample = oversample;
+  k->omax = (oversample + 1) / 2;
+  k->conv_size_half = conv_size_half;
+  k->h_support.assign(support, support + num_w_planes);
+  std::vector<int> side(num_w_planes);
+  std::vector<long long> base(num_w_planes);
+  long long total = 0;
+  for (size_t p = 0; p < num_w_planes; ++p) {
+    const int M = (k->omax + support[p] * oversample) / oversample + 1;
+    side[p] = M;
+    base[p] = total;
+    total += (long long)oversample * oversample * M * M;
+    k->support_max = std::max(k->support_max, support[p]);
+  }
+  if (total > 0x7fffffffLL)
+    return fail(set_error(GG_ERR_UNSUPPORTED,
+                          "re-laid kernel stack has %lld taps; this build "
+                          "indexes at most 2^31-1",
+                          total));
+  k->total_taps = total;
+  int r;
+  if ((r = k->support.ensure(num_w_planes * sizeof(int))) ||
+      (r = k->side.ensure(num_w_planes * sizeof(int))) ||
+      (r = k->base.ensure(num_w_planes * sizeof(long long))) ||
+      (r = k->taps.ensure((size_t)total * 2 * sizeof(Real))) ||
+      (r = k->tap_sum.ensure(num_w_planes * (2 * k->omax + 1) *
+                             (2 * k->omax + 1) * sizeof(double))))
+    return fail(r);
+  auto cu = [&](cudaError_t e, const char* what) -> int {
+    if (e == cudaSuccess) return GG_OK;
+    return set_error(GG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  };
+  if ((r = cu(cudaMemcpyAsync(k->support.p, support,
+                              num_w_planes * sizeof(int),
+                              cudaMemcpyHostToDevice, s), "support H2D")) ||
+      (r = cu(cudaMemcpyAsync(k->side.p, side.data(),
+                              num_w_planes * sizeof(int),
+                              cudaMemcpyHostToDevice, s), "side H2D")) ||
+      (r = cu(cudaMemcpyAsync(k->base.p, base.data(),
+                              num_w_planes * sizeof(long long),
+                              cudaMemcpyHostToDevice, s), "base H2D")))
+    return fail(r);
+  const size_t cube = num_w_planes * (size_t)conv_size_half * conv_size_half *
+                      2 * sizeof(Real);
+  DevBuf staged;
+  const Real* d_conv = conv_func;
+  if (!on_device) {
+    if ((r = staged.ensure(cube))) return fail(r);
+    if ((r = cu(cudaMemcpyAsync(staged.p, conv_func, cube,
+                                cudaMemcpyHostToDevice, s), "conv_func H2D")))
+      return fail(r);
+    d_conv = staged.as<Real>();
+  }
+  StackView v = k->view();
+  if ((r = cu(launch_stack_relayout<Real>(d_conv, v, k->taps.p, total, s),
+              "relayout")))
+    return fail(r);
+  StackView raw = v;
+  raw.taps = d_conv;
+  if ((r = cu(launch_tap_sums<Real>(raw, k->tap_sum.as<double>(), s),
+              "tap sums")))
+    return fail(r);
+  // The staging copy (and the caller's host array) must outlive the
+  // kernels that read it.
+  if ((r = cu(cudaStreamSynchronize(s), "kernel stack sync"))) return fail(r);
+  *out = k;
+  return GG_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// Plans (workspace)
+// ===========================================================================
+struct gg_plan {
+  int device = 0;
+  DevBuf cell, meta, vw, rec_count, rec_offset;
+  DevBuf blk_norm, blk_skip, blk_macs;
+  DevBuf keys0, vals0, keys1, vals1, sort_tmp, scan_tmp;
+  DevBuf tile_start, item_a, item_b, items, split_tiles, partials;
+  DevBuf scalars;  // device scalars, see Scalar below
+  uint32_t* h_scalars = nullptr;  // pinned mirror
+  gg_stats stats{};
+  // Phase events (recorded only when profiling is enabled).
+  static constexpr int kEvents = 6;
+  bool profile = false;
+  bool events_valid = false;
+  cudaEvent_t ev[kEvents] = {};
+  // Staging of the host-pointer entry points.
+  DevBuf in_uu, in_vv, in_ww, in_vis, in_weight, in_grid, in_misc;
+  ~gg_plan() {
+    if (h_scalars) cudaFreeHost(h_scalars);
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+  void mark(int i, cudaStream_t s) {
+    if (profile) cudaEventRecord(ev[i], s);
+  }
+};
+
+namespace {
+
+enum Scalar {
+  kTotalRecords = 0,
+  kNumItems,
+  kNumSlots,
+  kNumSplit,
+  kCounter,
+  kScalarCount
+};
+// 64-bit device scalars live after the 32-bit ones.
+constexpr size_t kScalar64Offset = 64;
+enum Scalar64 { kMacs = 0, kSkipScratch, kScalar64Count };
+
+unsigned long long* scalar64(gg_plan* p, int i) {
+  return (unsigned long long*)((char*)p->scalars.p + kScalar64Offset) + i;
+}
+
+int plan_init(gg_plan* p) {
+  GG_TRY(current_device(&p->device));
+  GG_TRY(p->scalars.ensure(kScalar64Offset + kScalar64Count * 8));
+  GG_CUDA(cudaMallocHost(&p->h_scalars, 64));
+  return GG_OK;
+}
+
+// Tile shape of this build's gridding kernel (see gg_grid.cu).
+constexpr int kTileU = 32;
+constexpr int kTileV = 64;
+
+template <typename Real>
+int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
+                  const Real* uu, const Real* vv, const Real* ww,
+                  const Real* vis, const Real* weight, Real cell_size_rad,
+                  Real w_scale, int grid_size,
+                  unsigned long long* d_num_skipped, double* d_norm,
+                  Real* d_grid, cudaStream_t s) {
+  using R2 = typename Vec2<Real>::type;
+  if (!plan || !K) return set_error(GG_ERR_INVALID_ARG, "plan or kernels is NULL");
+  if (K->is_double != (sizeof(Real) == 8))
+    return set_error(GG_ERR_INVALID_ARG,
+                     "kernel stack precision does not match the call");
+  if (grid_size < 1 || grid_size > kMaxGridSize)
+    return set_error(GG_ERR_UNSUPPORTED, "grid_size = %d outside [1, %d]",
+                     grid_size, kMaxGridSize);
+  if (num_points > 0xFFFFFFF0ull)
+    return set_error(GG_ERR_UNSUPPORTED,
+                     "num_points = %zu exceeds 2^32-16 per call", num_points);
+  if (num_points > 0 && (!uu || !vv || !ww || !vis || !weight))
+    return set_error(GG_ERR_INVALID_ARG, "an input array is NULL");
+  if (!d_grid || !d_norm || !d_num_skipped)
+    return set_error(GG_ERR_INVALID_ARG, "an output pointer is NULL");
+  int dev;
+  GG_TRY(current_device(&dev));
+  if (dev != K->device || dev != plan->device)
+    return set_error(GG_ERR_INVALID_ARG,
+                     "plan, kernel stack and current device differ");
+
+  plan->stats = gg_stats{};
+  plan->stats.num_points = num_points;
+  plan->stats.tile_u = kTileU;
+  plan->stats.tile_v = kTileV;
+  plan->events_valid = false;
+
+  const StackView view = K->view();
+  TileGeom geom{};
+  geom.tile_u = kTileU;
+  geom.tile_v = kTileV;
+  geom.tiles_u = (grid_size + kTileU - 1) / kTileU;
+  geom.tiles_v = (grid_size + kTileV - 1) / kTileV;
+  geom.num_grids = 1;
+  const int num_tiles = geom.tiles_u * geom.tiles_v;
+  // Key = tile | plane | |offset| class, in 32 bits; low fields shrink
+  // (ordering within a tile gets coarser) if the grid has many tiles.
+  const int tile_bits = ceil_log2((unsigned long long)num_tiles);
+  int plane_bits = ceil_log2((unsigned long long)K->num_planes);
+  int phase_bits = ceil_log2((unsigned long long)(K->omax + 1) * (K->omax + 1));
+  if (tile_bits + plane_bits + phase_bits > 32) phase_bits = 0;
+  if (tile_bits + plane_bits + phase_bits > 32) plane_bits = 0;
+  geom.plane_bits = plane_bits;
+  geom.phase_bits = phase_bits;
+  geom.phase_side = K->omax + 1;
+  const int low_bits = plane_bits + phase_bits;
+  const int key_bits = tile_bits + low_bits;
+
+  const size_t n = num_points;
+  const int nblk = place_num_blocks(n);
+  GG_TRY(plan->cell.ensure(n * 4 + 4));
+  GG_TRY(plan->meta.ensure(n * 4 + 4));
+  GG_TRY(plan->vw.ensure(n * sizeof(R2) + sizeof(R2)));
+  GG_TRY(plan->rec_count.ensure(n * 4 + 4));
+  GG_TRY(plan->rec_offset.ensure(n * 4 + 4));
+  GG_TRY(plan->blk_norm.ensure(nblk * sizeof(double)));
+  GG_TRY(plan->blk_skip.ensure(nblk * 8));
+  GG_TRY(plan->blk_macs.ensure(nblk * 8));
+  GG_TRY(plan->scan_tmp.ensure(scan_temp_bytes(std::max<size_t>(n, num_tiles))));
+
+  uint32_t* sc = plan->scalars.as<uint32_t>();
+  PlaceParams<Real> pp;
+  pp.uu = uu; pp.vv = vv; pp.ww = ww; pp.vis = vis; pp.weight = weight;
+  // oskar_grid_wproj.c:148 (and :59): grid_scale = grid_size * cell_size
+  // in the call's precision.
+  pp.grid_scale = (Real)grid_size * cell_size_rad;
+  pp.w_scale = w_scale;
+  pp.grid_size = grid_size;
+  pp.grid_centre = grid_size / 2;
+  pp.num_points = n;
+
+  if (n == 0) {
+    GG_CUDA(cudaMemsetAsync(d_num_skipped, 0, sizeof(unsigned long long), s));
+    return GG_OK;
+  }
+
+  plan->mark(0, s);
+  PlaceOut po;
+  po.cell = plan->cell.as<uint32_t>();
+  po.meta = plan->meta.as<uint32_t>();
+  po.vw = plan->vw.p;
+  po.rec_count = plan->rec_count.as<uint32_t>();
+  po.blk_norm = plan->blk_norm.as<double>();
+  po.blk_skip = plan->blk_skip.as<unsigned long long>();
+  po.blk_macs = plan->blk_macs.as<unsigned long long>();
+  GG_CUDA(launch_place<Real>(pp, view, geom, 0, 0, po, s));
+  GG_CUDA(launch_place_finalize(po.blk_norm, po.blk_skip, po.blk_macs, nblk,
+                                d_norm, d_num_skipped, scalar64(plan, kMacs),
+                                s));
+  GG_CUDA(exclusive_scan_u32(po.rec_count, plan->rec_offset.as<uint32_t>(), n,
+                             sc + kTotalRecords, plan->scan_tmp.p, s));
+  plan->stats.num_launches = 5;  // place, finalize, 3-kernel scan
+  plan->mark(1, s);
+  // The one host synchronisation: the record total sizes the sort buffers.
+  GG_CUDA(cudaMemcpyAsync(plan->h_scalars, sc, 4 * kScalarCount,
+                          cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaMemcpyAsync((char*)plan->h_scalars + 32, scalar64(plan, kMacs),
+                          8, cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  const uint32_t total = plan->h_scalars[kTotalRecords];
+  plan->stats.num_records = total;
+  memcpy(&plan->stats.num_macs, (char*)plan->h_scalars + 32, 8);
+  // Record counts per visibility are at most a few dozen, so a 32-bit total
+  // can only wrap for inputs far beyond the per-call limit; guard anyway.
+  if ((unsigned long long)total > 0xFFFFFFF0ull)
+    return set_error(GG_ERR_UNSUPPORTED, "record count overflow");
+
+  if (total > 0) {
+    GG_TRY(plan->keys0.ensure((size_t)total * 4));
+    GG_TRY(plan->vals0.ensure((size_t)total * 4));
+    GG_TRY(plan->keys1.ensure((size_t)total * 4));
+    GG_TRY(plan->vals1.ensure((size_t)total * 4));
+    GG_TRY(plan->sort_tmp.ensure(radix_temp_bytes(total)));
+    GG_CUDA(launch_emit_records(po.cell, po.meta,
+                                plan->rec_offset.as<uint32_t>(), n, view, geom,
+                                0, 0, plan->keys0.as<uint32_t>(),
+                                plan->vals0.as<uint32_t>(), s));
+    bool in_alt = false;
+    GG_CUDA(radix_sort_pairs(plan->keys0.as<uint32_t>(),
+                             plan->vals0.as<uint32_t>(),
+                             plan->keys1.as<uint32_t>(),
+                             plan->vals1.as<uint32_t>(), total, key_bits,
+                             plan->sort_tmp.p, s, &in_alt));
+    const uint32_t* keys = in_alt ? plan->keys1.as<uint32_t>()
+                                  : plan->keys0.as<uint32_t>();
+    const uint32_t* vals = in_alt ? plan->vals1.as<uint32_t>()
+                                  : plan->vals0.as<uint32_t>();
+    plan->stats.num_launches += 1 + 5 * (unsigned)((key_bits + 7) / 8);
+    plan->mark(2, s);
+
+    GG_TRY(plan->tile_start.ensure((size_t)(num_tiles + 1) * 4));
+    GG_CUDA(launch_tile_bounds(keys, total, low_bits, num_tiles,
+                               plan->tile_start.as<uint32_t>(), s));
+
+    int sms = 0;
+    GG_TRY(num_sms_of_current(&sms));
+    const int num_ctas = sms * grid_tiles_ctas_per_sm<Real>();
+    const uint32_t chunk = (uint32_t)std::max<unsigned long long>(
+        64, ((unsigned long long)total + 4ull * num_ctas - 1) / (4ull * num_ctas));
+    const size_t item_cap = (size_t)num_tiles + 8 * (size_t)num_ctas + 16;
+    const size_t slot_cap = 8 * (size_t)num_ctas + 16;
+    GG_TRY(plan->item_a.ensure((size_t)num_tiles * 4 + 4));
+    GG_TRY(plan->item_b.ensure((size_t)num_tiles * 4 + 4));
+    GG_TRY(plan->items.ensure(item_cap * sizeof(WorkItem)));
+    GG_TRY(plan->split_tiles.ensure((size_t)num_tiles * sizeof(int4) + 16));
+    GG_TRY(plan->partials.ensure(slot_cap * kTileU * kTileV * sizeof(R2)));
+    ItemBuffers ib;
+    ib.chunks = plan->item_a.as<uint32_t>();
+    ib.split_chunks = plan->item_b.as<uint32_t>();
+    ib.num_items = sc + kNumItems;
+    ib.num_slots = sc + kNumSlots;
+    ib.items = plan->items.as<WorkItem>();
+    ib.split_tiles = plan->split_tiles.as<int4>();
+    ib.num_split = sc + kNumSplit;
+    ib.counter = sc + kCounter;
+    ib.scan_tmp = plan->scan_tmp.p;
+    GG_CUDA(launch_build_items(plan->tile_start.as<uint32_t>(), num_tiles,
+                               total, chunk, ib, s));
+    plan->mark(3, s);
+    GG_CUDA(launch_grid_tiles<Real>(
+        ib.items, ib.num_items, ib.counter, vals, po.cell, po.meta, po.vw,
+        view, geom, grid_size, d_grid, 0, plan->partials.as<Real>(), num_ctas,
+        s));
+    plan->mark(4, s);
+    GG_CUDA(launch_reduce_partials<Real>(ib.split_tiles, ib.num_split,
+                                         num_tiles, plan->partials.as<Real>(),
+                                         geom, grid_size, d_grid, 0, s));
+    plan->mark(5, s);
+    // tile bounds, item counts, 2 scans, item emit, gridding, reduction
+    plan->stats.num_launches += 1 + 1 + 6 + 1 + 1 + 1;
+    plan->events_valid = plan->profile;
+  }
+  return GG_OK;
+}
+
+template <typename Real>
+int degrid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
+                    const Real* uu, const Real* vv, const Real* ww,
+                    Real cell_size_rad, Real w_scale, int grid_size,
+                    const Real* d_grid, Real* d_out, cudaStream_t s) {
+  if (!plan || !K) return set_error(GG_ERR_INVALID_ARG, "plan or kernels is NULL");
+  if (K->is_double != (sizeof(Real) == 8))
+    return set_error(GG_ERR_INVALID_ARG,
+                     "kernel stack precision does not match the call");
+  if (grid_size < 1 || grid_size > kMaxGridSize)
+    return set_error(GG_ERR_UNSUPPORTED, "grid_size = %d outside [1, %d]",
+                     grid_size, kMaxGridSize);
+  if (num_points > 0 && (!uu || !vv || !ww || !d_grid || !d_out))
+    return set_error(GG_ERR_INVALID_ARG, "an array is NULL");
+  PlaceParams<Real> pp;
+  pp.uu = uu; pp.vv = vv; pp.ww = ww; pp.vis = nullptr; pp.weight = nullptr;
+  pp.grid_scale = (Real)grid_size * cell_size_rad;
+  pp.w_scale = w_scale;
+  pp.grid_size = grid_size;
+  pp.grid_centre = grid_size / 2;
+  pp.num_points = num_points;
+  GG_CUDA(launch_degrid<Real>(pp, K->view(), d_grid, d_out, s));
+  return GG_OK;
+}
+
+// Host-pointer drop-in: stage inputs, grid on the device, copy back.
+template <typename Real>
+int dropin(size_t num_w_planes, const int* support, int oversample,
+           int conv_size_half, const Real* conv_func, size_t num_points,
+           const Real* uu, const Real* vv, const Real* ww, const Real* vis,
+           const Real* weight, Real cell_size_rad, Real w_scale,
+           int grid_size, size_t* num_skipped, double* norm, Real* grid) {
+  if (!num_skipped || !norm || !grid)
+    return set_error(GG_ERR_INVALID_ARG, "num_skipped, norm or grid is NULL");
+  if (grid_size < 1 || grid_size > kMaxGridSize)
+    return set_error(GG_ERR_UNSUPPORTED, "grid_size = %d outside [1, %d]",
+                     grid_size, kMaxGridSize);
+  if (num_points > 0 && (!uu || !vv || !ww || !vis || !weight))
+    return set_error(GG_ERR_INVALID_ARG, "an input array is NULL");
+  GG_TRY(validate_stack(num_w_planes, support, oversample, conv_size_half,
+                        conv_func));
+  int dev;
+  GG_TRY(current_device(&dev));
+  DeviceState* st;
+  GG_TRY(device_state(dev, &st));
+  std::lock_guard<std::mutex> lk(st->mu);
+  cudaStream_t s = st->stream;
+  if (!st->plan) {
+    gg_plan* p = new gg_plan();
+    int r = plan_init(p);
+    if (r != GG_OK) {
+      delete p;
+      return r;
+    }
+    st->plan = p;
+  }
+  gg_plan* plan = st->plan;
+  gg_kernels* K = nullptr;
+  GG_TRY(kernels_create<Real>(&K, num_w_planes, support, oversample,
+                              conv_size_half, conv_func, 0, s));
+  struct KGuard {
+    gg_kernels* k;
+    ~KGuard() { delete k; }
+  } kguard{K};
+
+  const size_t n = num_points;
+  const size_t grid_bytes = (size_t)grid_size * grid_size * 2 * sizeof(Real);
+  GG_TRY(plan->in_uu.ensure(n * sizeof(Real) + 16));
+  GG_TRY(plan->in_vv.ensure(n * sizeof(Real) + 16));
+  GG_TRY(plan->in_ww.ensure(n * sizeof(Real) + 16));
+  GG_TRY(plan->in_vis.ensure(2 * n * sizeof(Real) + 16));
+  GG_TRY(plan->in_weight.ensure(n * sizeof(Real) + 16));
+  GG_TRY(plan->in_grid.ensure(grid_bytes));
+  GG_TRY(plan->in_misc.ensure(64));
+  double* d_norm = plan->in_misc.as<double>();
+  unsigned long long* d_skip = (unsigned long long*)(plan->in_misc.as<char>() + 8);
+  if (n) {
+    GG_CUDA(cudaMemcpyAsync(plan->in_uu.p, uu, n * sizeof(Real),
+                            cudaMemcpyHostToDevice, s));
+    GG_CUDA(cudaMemcpyAsync(plan->in_vv.p, vv, n * sizeof(Real),
+                            cudaMemcpyHostToDevice, s));
+    GG_CUDA(cudaMemcpyAsync(plan->in_ww.p, ww, n * sizeof(Real),
+                            cudaMemcpyHostToDevice, s));
+    GG_CUDA(cudaMemcpyAsync(plan->in_vis.p, vis, 2 * n * sizeof(Real),
+                            cudaMemcpyHostToDevice, s));
+    GG_CUDA(cudaMemcpyAsync(plan->in_weight.p, weight, n * sizeof(Real),
+                            cudaMemcpyHostToDevice, s));
+  }
+  GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, grid_bytes,
+                          cudaMemcpyHostToDevice, s));
+  const double norm_in = *norm;
+  GG_CUDA(cudaMemcpyAsync(d_norm, &norm_in, sizeof(double),
+                          cudaMemcpyHostToDevice, s));
+  GG_TRY(grid_pipeline<Real>(plan, K, n, plan->in_uu.as<Real>(),
+                             plan->in_vv.as<Real>(), plan->in_ww.as<Real>(),
+                             plan->in_vis.as<Real>(),
+                             plan->in_weight.as<Real>(), cell_size_rad,
+                             w_scale, grid_size, d_skip, d_norm,
+                             plan->in_grid.as<Real>(), s));
+  double norm_out = 0.0;
+  unsigned long long skip_out = 0;
+  GG_CUDA(cudaMemcpyAsync(grid, plan->in_grid.p, grid_bytes,
+                          cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaMemcpyAsync(&norm_out, d_norm, sizeof(double),
+                          cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaMemcpyAsync(&skip_out, d_skip, sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  *norm = norm_out;
+  *num_skipped = (size_t)skip_out;
+  return GG_OK;
+}
+
+template <typename Real>
+int place_only(const gg_kernels* K, size_t num_points, const Real* uu,
+               const Real* vv, const Real* ww, Real cell_size_rad,
+               Real w_scale, int grid_size, int* d_out, cudaStream_t s) {
+  if (!K) return set_error(GG_ERR_INVALID_ARG, "kernels is NULL");
+  if (K->is_double != (sizeof(Real) == 8))
+    return set_error(GG_ERR_INVALID_ARG,
+                     "kernel stack precision does not match the call");
+  if (num_points > 0 && (!uu || !vv || !ww || !d_out))
+    return set_error(GG_ERR_INVALID_ARG, "an array is NULL");
+  PlaceParams<Real> pp;
+  pp.uu = uu; pp.vv = vv; pp.ww = ww; pp.vis = nullptr; pp.weight = nullptr;
+  pp.grid_scale = (Real)grid_size * cell_size_rad;
+  pp.w_scale = w_scale;
+  pp.grid_size = grid_size;
+  pp.grid_centre = grid_size / 2;
+  pp.num_points = num_points;
+  GG_CUDA(launch_place_only<Real>(pp, K->view(), d_out, s));
+  return GG_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+GG_API const char* gg_last_error(void) { return t_last_error.c_str(); }
+
+GG_API const char* gg_version(void) { return "gpugrid-gb300 0.1.0"; }
+
+GG_API int gg_grid_wproj_f(size_t num_w_planes, const int* support,
+                           int oversample, int conv_size_half,
+                           const float* conv_func, size_t num_points,
+                           const float* uu, const float* vv, const float* ww,
+                           const float* vis, const float* weight,
+                           float cell_size_rad, float w_scale, int grid_size,
+                           size_t* num_skipped, double* norm, float* grid) {
+  t_last_error.clear();
+  return dropin<float>(num_w_planes, support, oversample, conv_size_half,
+                       conv_func, num_points, uu, vv, ww, vis, weight,
+                       cell_size_rad, w_scale, grid_size, num_skipped, norm,
+                       grid);
+}
+
+GG_API int gg_grid_wproj_d(size_t num_w_planes, const int* support,
+                           int oversample, int conv_size_half,
+                           const double* conv_func, size_t num_points,
+                           const double* uu, const double* vv,
+                           const double* ww, const double* vis,
+                           const double* weight, double cell_size_rad,
+                           double w_scale, int grid_size, size_t* num_skipped,
+                           double* norm, double* grid) {
+  t_last_error.clear();
+  return dropin<double>(num_w_planes, support, oversample, conv_size_half,
+                        conv_func, num_points, uu, vv, ww, vis, weight,
+                        cell_size_rad, w_scale, grid_size, num_skipped, norm,
+                        grid);
+}
+
+GG_API void oskar_grid_wproj_f(const size_t num_w_planes, const int* support,
+                               const int oversample, const int conv_size_half,
+                               const float* conv_func, const size_t num_points,
+                               const float* uu, const float* vv,
+                               const float* ww, const float* vis,
+                               const float* weight, const float cell_size_rad,
+                               const float w_scale, const int grid_size,
+                               size_t* num_skipped, double* norm,
+                               float* grid) {
+  if (gg_grid_wproj_f(num_w_planes, support, oversample, conv_size_half,
+                      conv_func, num_points, uu, vv, ww, vis, weight,
+                      cell_size_rad, w_scale, grid_size, num_skipped, norm,
+                      grid) != GG_OK)
+    fprintf(stderr, "oskar_grid_wproj_f (gpugrid): %s\n", gg_last_error());
+}
+
+GG_API void oskar_grid_wproj_d(const size_t num_w_planes, const int* support,
+                               const int oversample, const int conv_size_half,
+                               const double* conv_func,
+                               const size_t num_points, const double* uu,
+                               const double* vv, const double* ww,
+                               const double* vis, const double* weight,
+                               const double cell_size_rad,
+                               const double w_scale, const int grid_size,
+                               size_t* num_skipped, double* norm,
+                               double* grid) {
+  if (gg_grid_wproj_d(num_w_planes, support, oversample, conv_size_half,
+                      conv_func, num_points, uu, vv, ww, vis, weight,
+                      cell_size_rad, w_scale, grid_size, num_skipped, norm,
+                      grid) != GG_OK)
+    fprintf(stderr, "oskar_grid_wproj_d (gpugrid): %s\n", gg_last_error());
+}
+
+GG_API int gg_kernels_create_f(gg_kernels** out, size_t num_w_planes,
+                               const int* support, int oversample,
+                               int conv_size_half, const float* conv_func,
+                               int conv_func_on_device, void* stream) {
+  t_last_error.clear();
+  return kernels_create<float>(out, num_w_planes, support, oversample,
+                               conv_size_half, conv_func, conv_func_on_device,
+                               (cudaStream_t)stream);
+}
+
+GG_API int gg_kernels_create_d(gg_kernels** out, size_t num_w_planes,
+                               const int* support, int oversample,
+                               int conv_size_half, const double* conv_func,
+                               int conv_func_on_device, void* stream) {
+  t_last_error.clear();
+  return kernels_create<double>(out, num_w_planes, support, oversample,
+                                conv_size_half, conv_func,
+                                conv_func_on_device, (cudaStream_t)stream);
+}
+
+GG_API int gg_kernels_destroy(gg_kernels* k) {
+  delete k;
+  return GG_OK;
+}
+
+GG_API int gg_plan_create(gg_plan** out) {
+  t_last_error.clear();
+  if (!out) return set_error(GG_ERR_INVALID_ARG, "out is NULL");
+  gg_plan* p = new gg_plan();
+  int r = plan_init(p);
+  if (r != GG_OK) {
+    delete p;
+    *out = nullptr;
+    return r;
+  }
+  *out = p;
+  return GG_OK;
+}
+
+GG_API int gg_plan_destroy(gg_plan* plan) {
+  delete plan;
+  return GG_OK;
+}
+
+GG_API int gg_plan_last_stats(const gg_plan* plan, gg_stats* stats) {
+  if (!plan || !stats) return set_error(GG_ERR_INVALID_ARG, "NULL argument");
+  *stats = plan->stats;
+  return GG_OK;
+}
+
+GG_API int gg_plan_set_profiling(gg_plan* plan, int enable) {
+  t_last_error.clear();
+  if (!plan) return set_error(GG_ERR_INVALID_ARG, "plan is NULL");
+  if (enable && !plan->ev[0]) {
+    for (auto& e : plan->ev) GG_CUDA(cudaEventCreate(&e));
+  }
+  plan->profile = enable != 0;
+  plan->events_valid = false;
+  return GG_OK;
+}
+
+GG_API int gg_plan_phase_ms(const gg_plan* plan, float* ms, int n) {
+  t_last_error.clear();
+  if (!plan || !ms || n < 0)
+    return set_error(GG_ERR_INVALID_ARG, "NULL argument");
+  if (!plan->events_valid)
+    return set_error(GG_ERR_INVALID_ARG,
+                     "no profiled call: enable profiling and make a call "
+                     "that grids at least one visibility");
+  for (int i = 0; i < n && i < gg_plan::kEvents - 1; ++i)
+    GG_CUDA(cudaEventElapsedTime(&ms[i], plan->ev[i], plan->ev[i + 1]));
+  return GG_OK;
+}
+
+GG_API int gg_measure_fp32_fma_tflops(double* tflops) {
+  t_last_error.clear();
+  if (!tflops) return set_error(GG_ERR_INVALID_ARG, "tflops is NULL");
+  int sms = 0;
+  GG_TRY(num_sms_of_current(&sms));
+  GG_CUDA(gg::measure_fp32_fma(sms, tflops, nullptr));
+  return GG_OK;
+}
+
+GG_API int gg_grid_wproj_f_device(gg_plan* plan, const gg_kernels* kernels,
+                                  size_t num_points, const float* d_uu,
+                                  const float* d_vv, const float* d_ww,
+                                  const float* d_vis, const float* d_weight,
+                                  float cell_size_rad, float w_scale,
+                                  int grid_size,
+                                  unsigned long long* d_num_skipped,
+                                  double* d_norm, float* d_grid,
+                                  void* stream) {
+  t_last_error.clear();
+  return grid_pipeline<float>(plan, kernels, num_points, d_uu, d_vv, d_ww,
+                              d_vis, d_weight, cell_size_rad, w_scale,
+                              grid_size, d_num_skipped, d_norm, d_grid,
+                              (cudaStream_t)stream);
+}
+
+GG_API int gg_grid_wproj_d_device(gg_plan* plan, const gg_kernels* kernels,
+                                  size_t num_points, const double* d_uu,
+                                  const double* d_vv, const double* d_ww,
+                                  const double* d_vis, const double* d_weight,
+                                  double cell_size_rad, double w_scale,
+                                  int grid_size,
+                                  unsigned long long* d_num_skipped,
+                                  double* d_norm, double* d_grid,
+                                  void* stream) {
+  t_last_error.clear();
+  return grid_pipeline<double>(plan, kernels, num_points, d_uu, d_vv, d_ww,
+                               d_vis, d_weight, cell_size_rad, w_scale,
+                               grid_size, d_num_skipped, d_norm, d_grid,
+                               (cudaStream_t)stream);
+}
+
+GG_API int gg_place_wproj_f_device(const gg_kernels* kernels,
+                                   size_t num_points, const float* d_uu,
+                                   const float* d_vv, const float* d_ww,
+                                   float cell_size_rad, float w_scale,
+                                   int grid_size, int* d_out, void* stream) {
+  t_last_error.clear();
+  return place_only<float>(kernels, num_points, d_uu, d_vv, d_ww,
+                           cell_size_rad, w_scale, grid_size, d_out,
+                           (cudaStream_t)stream);
+}
+
+GG_API int gg_place_wproj_d_device(const gg_kernels* kernels,
+                                   size_t num_points, const double* d_uu,
+                                   const double* d_vv, const double* d_ww,
+                                   double cell_size_rad, double w_scale,
+                                   int grid_size, int* d_out, void* stream) {
+  t_last_error.clear();
+  return place_only<double>(kernels, num_points, d_uu, d_vv, d_ww,
+                            cell_size_rad, w_scale, grid_size, d_out,
+                            (cudaStream_t)stream);
+}
+
+GG_API int gg_degrid_wproj_f_device(gg_plan* plan, const gg_kernels* kernels,
+                                    size_t num_points, const float* d_uu,
+                                    const float* d_vv, const float* d_ww,
+                                    float cell_size_rad, float w_scale,
+                                    int grid_size, const float* d_grid,
+                                    float* d_out_vis, void* stream) {
+  t_last_error.clear();
+  return degrid_pipeline<float>(plan, kernels, num_points, d_uu, d_vv, d_ww,
+                                cell_size_rad, w_scale, grid_size, d_grid,
+                                d_out_vis, (cudaStream_t)stream);
+}
+
+GG_API int gg_degrid_wproj_d_device(gg_plan* plan, const gg_kernels* kernels,
+                                    size_t num_points, const double* d_uu,
+                                    const double* d_vv, const double* d_ww,
+                                    double cell_size_rad, double w_scale,
+                                    int grid_size, const double* d_grid,
+                                    double* d_out_vis, void* stream) {
+  t_last_error.clear();
+  return degrid_pipeline<double>(plan, kernels, num_points, d_uu, d_vv, d_ww,
+                                 cell_size_rad, w_scale, grid_size, d_grid,
+                                 d_out_vis, (cudaStream_t)stream);
+}
+
+}  // extern "C"

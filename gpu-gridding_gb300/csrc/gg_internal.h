@@ -1,0 +1,115 @@
+// Host-side declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "gg_common.cuh"
+
+namespace gg {
+
+// ---- device-wide exclusive scan of uint32 (gg_sort.cu) --------------------
+// out[i] = in[0] + ... + in[i-1]; *d_total (if non-null) = sum of all n.
+// in and out may alias.  tmp must hold scan_temp_bytes(n).
+size_t scan_temp_bytes(size_t n);
+cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n,
+                               uint32_t* d_total, void* tmp, cudaStream_t s);
+
+// ---- stable LSD radix sort of (key, value) pairs (gg_sort.cu) -------------
+// Sorts the first n pairs by key bits [0, end_bit).  Ping-pongs between
+// (keys, vals) and (keys_alt, vals_alt); on return *in_alt tells which pair
+// of buffers holds the result.  tmp must hold radix_temp_bytes(n).
+size_t radix_temp_bytes(size_t n);
+cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals,
+                             uint32_t* keys_alt, uint32_t* vals_alt, size_t n,
+                             int end_bit, void* tmp, cudaStream_t s,
+                             bool* in_alt);
+
+// ---- kernel stack preparation (gg_stack.cu) -------------------------------
+// Re-lays conv_func (device, [P][csh][csh] complex) into the residue-split
+// layout and forms the FP64 tap sums in the reference's summation order.
+template <typename Real>
+cudaError_t launch_stack_relayout(const Real* d_conv_func, StackView view,
+                                  void* d_taps_out, long long total_taps,
+                                  cudaStream_t s);
+template <typename Real>
+cudaError_t launch_tap_sums(StackView view, double* d_tap_sum,
+                            cudaStream_t s);
+
+// ---- placement and binning (gg_place.cu) ----------------------------------
+struct PlaceOut {
+  uint32_t* cell;             // [N]
+  uint32_t* meta;             // [N]
+  void* vw;                   // [N] weighted visibility, Real2
+  uint32_t* rec_count;        // [N] records (tiles touched) per visibility
+  double* blk_norm;           // [num_blocks]
+  unsigned long long* blk_skip;   // [num_blocks]
+  unsigned long long* blk_macs;   // [num_blocks]
+};
+int place_num_blocks(unsigned long long n);
+template <typename Real>
+cudaError_t launch_place(PlaceParams<Real> p, StackView view, TileGeom geom,
+                         int grid_index, unsigned long long vis_offset,
+                         PlaceOut out, cudaStream_t s);
+// Sums the per-block partials: *d_norm += norm, *d_num_skipped = skips,
+// *d_macs = macs (all device pointers).
+cudaError_t launch_place_finalize(const double* blk_norm,
+                                  const unsigned long long* blk_skip,
+                                  const unsigned long long* blk_macs,
+                                  int num_blocks, double* d_norm,
+                                  unsigned long long* d_num_skipped,
+                                  unsigned long long* d_macs, cudaStream_t s);
+template <typename Real>
+cudaError_t launch_place_only(PlaceParams<Real> p, StackView view, int* out,
+                              cudaStream_t s);
+cudaError_t launch_emit_records(const uint32_t* cell, const uint32_t* meta,
+                                const uint32_t* rec_offset,
+                                unsigned long long n, StackView view,
+                                TileGeom geom, int grid_index,
+                                unsigned long long vis_offset, uint32_t* keys,
+                                uint32_t* vals, cudaStream_t s);
+
+// ---- work decomposition and gridding (gg_grid.cu) -------------------------
+cudaError_t launch_tile_bounds(const uint32_t* keys, uint32_t n, int shift,
+                               int num_tiles, uint32_t* tile_start,
+                               cudaStream_t s);
+struct ItemBuffers {
+  uint32_t* chunks;       // [num_tiles] chunks per tile (then offsets)
+  uint32_t* split_chunks; // [num_tiles] chunks of split tiles (then slots)
+  uint32_t* num_items;    // [1]
+  uint32_t* num_slots;    // [1]
+  WorkItem* items;        // [capacity]
+  int4* split_tiles;      // [num_tiles] (tile, first slot, chunks, -)
+  uint32_t* num_split;    // [1]
+  uint32_t* counter;      // [1] work counter of the persistent kernel
+  void* scan_tmp;
+};
+cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
+                               uint32_t num_records, uint32_t chunk,
+                               ItemBuffers b, cudaStream_t s);
+template <typename Real>
+cudaError_t launch_grid_tiles(const WorkItem* items, const uint32_t* num_items,
+                              uint32_t* counter, const uint32_t* rec_vis,
+                              const uint32_t* cell, const uint32_t* meta,
+                              const void* vw, StackView view, TileGeom geom,
+                              int grid_size, Real* grid, long long grid_stride,
+                              Real* partials, int num_ctas, cudaStream_t s);
+template <typename Real>
+cudaError_t launch_reduce_partials(const int4* split_tiles,
+                                   const uint32_t* num_split, int max_split,
+                                   const Real* partials, TileGeom geom,
+                                   int grid_size, Real* grid,
+                                   long long grid_stride, cudaStream_t s);
+template <typename Real>
+int grid_tiles_ctas_per_sm();
+
+// ---- FP32 FMA throughput probe (gg_calib.cu) ------------------------------
+cudaError_t measure_fp32_fma(int num_sms, double* tflops_best, float* ms_out);
+
+// ---- adjoint (gg_degrid.cu) -----------------------------------------------
+template <typename Real>
+cudaError_t launch_degrid(PlaceParams<Real> p, StackView view,
+                          const Real* grid, Real* out_vis, cudaStream_t s);
+
+}  // namespace gg

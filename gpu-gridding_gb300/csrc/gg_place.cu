@@ -1,0 +1,223 @@
+// Placement of visibilities on the grid, per-visibility norm and skip
+// accounting, and emission of (tile, visibility) records for binning.
+//
+// Placement reproduces the reference's arithmetic exactly
+// (oskar_grid_wproj.c:146-187 for FP32, :57-98 for FP64): every product,
+// difference, square root and rounding is an explicitly rounded IEEE
+// operation (no contraction), so the cell, offset, plane and skip decisions
+// are bit-identical to the serial code for finite inputs.
+#include "gg_internal.h"
+#include "gg_placement.cuh"
+
+namespace gg {
+
+namespace {
+
+constexpr int kPlaceThreads = 256;
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  return x;
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kPlaceThreads)
+k_place(PlaceParams<Real> p, StackView v, TileGeom g, PlaceOut out) {
+  using R2 = typename Vec2<Real>::type;
+  const unsigned long long i =
+      (unsigned long long)blockIdx.x * kPlaceThreads + threadIdx.x;
+  double norm = 0.0;
+  unsigned long long skip = 0, macs = 0;
+  if (i < p.num_points) {
+    const Placement r = place_one(p, v, i);
+    const Real w = p.weight[i];
+    R2 vw;
+    vw.x = rmul(w, p.vis[2 * i]);
+    vw.y = rmul(w, p.vis[2 * i + 1]);
+    ((R2*)out.vw)[i] = vw;
+    out.cell[i] = pack_cell(r.gu, r.gv);
+    out.meta[i] = pack_meta(r.plane, r.ou, r.ov, r.conj_neg, r.skipped);
+    uint32_t count = 0;
+    if (r.skipped) {
+      skip = 1;
+    } else {
+      const int s = r.support;
+      const int tu0 = (r.gu - s) / g.tile_u, tu1 = (r.gu + s) / g.tile_u;
+      const int tv0 = (r.gv - s) / g.tile_v, tv1 = (r.gv + s) / g.tile_v;
+      count = (uint32_t)((tu1 - tu0 + 1) * (tv1 - tv0 + 1));
+      const unsigned long long f = 2ull * s + 1;
+      macs = f * f;
+      const int side = 2 * v.omax + 1;
+      const double ts = v.tap_sum[((size_t)r.plane * side + (r.ou + v.omax)) *
+                                      side + (r.ov + v.omax)];
+      // oskar_grid_wproj.c:210: *norm += sum * weight_i (FP64).
+      norm = __dmul_rn(ts, (double)w);
+    }
+    out.rec_count[i] = count;
+  }
+  // Block reductions by warp shuffles, then one partial per block; the
+  // partials are summed in block order by k_place_finalize, so the norm is
+  // the same on every run.
+  __shared__ double s_norm[kPlaceThreads / 32];
+  __shared__ unsigned long long s_skip[kPlaceThreads / 32];
+  __shared__ unsigned long long s_macs[kPlaceThreads / 32];
+  norm = warp_sum(norm);
+  skip = warp_sum(skip);
+  macs = warp_sum(macs);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { s_norm[warp] = norm; s_skip[warp] = skip; s_macs[warp] = macs; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double bn = 0.0;
+    unsigned long long bs = 0, bm = 0;
+    for (int w = 0; w < kPlaceThreads / 32; ++w) {
+      bn += s_norm[w]; bs += s_skip[w]; bm += s_macs[w];
+    }
+    out.blk_norm[blockIdx.x] = bn;
+    out.blk_skip[blockIdx.x] = bs;
+    out.blk_macs[blockIdx.x] = bm;
+  }
+}
+
+__global__ void k_place_finalize(const double* __restrict__ blk_norm,
+                                 const unsigned long long* __restrict__ blk_skip,
+                                 const unsigned long long* __restrict__ blk_macs,
+                                 int num_blocks, double* d_norm,
+                                 unsigned long long* d_num_skipped,
+                                 unsigned long long* d_macs) {
+  // One warp; lane l sums blocks l, l+32, ... then a fixed-order shuffle
+  // reduction: deterministic.
+  const int lane = threadIdx.x;
+  double n = 0.0;
+  unsigned long long s = 0, m = 0;
+  for (int b = lane; b < num_blocks; b += 32) {
+    n += blk_norm[b]; s += blk_skip[b]; m += blk_macs[b];
+  }
+  n = warp_sum(n); s = warp_sum(s); m = warp_sum(m);
+  if (lane == 0) {
+    if (d_norm) *d_norm += n;
+    if (d_num_skipped) *d_num_skipped = s;
+    if (d_macs) *d_macs = m;
+  }
+}
+
+// One thread per visibility writes one record per tile its footprint
+// touches.  Key = (tile, plane, |offset| class) so that after the sort each
+// tile's records are contiguous and grouped by kernel slice; value = the
+// visibility index.
+__global__ void k_emit(const uint32_t* __restrict__ cell,
+                       const uint32_t* __restrict__ meta,
+                       const uint32_t* __restrict__ rec_offset,
+                       unsigned long long n, StackView v, TileGeom g,
+                       int grid_index, unsigned long long vis_offset,
+                       uint32_t* __restrict__ keys,
+                       uint32_t* __restrict__ vals) {
+  const unsigned long long i =
+      (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t m = meta[i];
+  if (meta_skipped(m)) return;
+  const uint32_t c = cell[i];
+  const int gu = cell_u(c), gv = cell_v(c);
+  const int plane = meta_plane(m);
+  const int s = v.support[plane];
+  const int tu0 = (gu - s) / g.tile_u, tu1 = (gu + s) / g.tile_u;
+  const int tv0 = (gv - s) / g.tile_v, tv1 = (gv + s) / g.tile_v;
+  const int au = abs(meta_ou(m)), av = abs(meta_ov(m));
+  uint32_t low = 0;
+  if (g.phase_bits > 0) low = (uint32_t)(au * (v.omax + 1) + av);
+  if (g.plane_bits > 0) low |= (uint32_t)plane << g.phase_bits;
+  const int low_bits = g.plane_bits + g.phase_bits;
+  const uint32_t tiles_per_grid = (uint32_t)g.tiles_u * (uint32_t)g.tiles_v;
+  uint32_t pos = rec_offset[i];
+  const uint32_t vid = (uint32_t)(vis_offset + i);
+  for (int tv = tv0; tv <= tv1; ++tv) {
+    for (int tu = tu0; tu <= tu1; ++tu) {
+      const uint32_t tile = (uint32_t)grid_index * tiles_per_grid +
+                            (uint32_t)tv * g.tiles_u + (uint32_t)tu;
+      keys[pos] = low_bits >= 32 ? low : ((tile << low_bits) | low);
+      vals[pos] = vid;
+      ++pos;
+    }
+  }
+}
+
+// Diagnostic: per-visibility placement as the gridder computes it, as six
+// int32 per visibility (cell u, cell v, off_u, off_v, plane, flags) with
+// flags bit 0 = skipped, bit 1 = kernel conjugated (ww > 0).
+template <typename Real>
+__global__ void k_place_only(PlaceParams<Real> p, StackView v,
+                             int* __restrict__ out) {
+  const unsigned long long i =
+      (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.num_points) return;
+  const Placement r = place_one(p, v, i);
+  int* o = out + 6 * i;
+  o[0] = r.gu; o[1] = r.gv; o[2] = r.ou; o[3] = r.ov; o[4] = r.plane;
+  o[5] = r.skipped | (r.conj_neg << 1);
+}
+
+}  // namespace
+
+template <typename Real>
+cudaError_t launch_place_only(PlaceParams<Real> p, StackView view, int* out,
+                              cudaStream_t s) {
+  if (p.num_points == 0) return cudaSuccess;
+  const unsigned nb = (unsigned)((p.num_points + 255) / 256);
+  k_place_only<Real><<<nb, 256, 0, s>>>(p, view, out);
+  return cudaGetLastError();
+}
+template cudaError_t launch_place_only<float>(PlaceParams<float>, StackView,
+                                              int*, cudaStream_t);
+template cudaError_t launch_place_only<double>(PlaceParams<double>, StackView,
+                                               int*, cudaStream_t);
+
+int place_num_blocks(unsigned long long n) {
+  unsigned long long nb = (n + kPlaceThreads - 1) / kPlaceThreads;
+  return (int)(nb == 0 ? 1 : nb);
+}
+
+template <typename Real>
+cudaError_t launch_place(PlaceParams<Real> p, StackView view, TileGeom geom,
+                         int grid_index, unsigned long long vis_offset,
+                         PlaceOut out, cudaStream_t s) {
+  (void)grid_index; (void)vis_offset;
+  const int nb = place_num_blocks(p.num_points);
+  k_place<Real><<<nb, kPlaceThreads, 0, s>>>(p, view, geom, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_place_finalize(const double* blk_norm,
+                                  const unsigned long long* blk_skip,
+                                  const unsigned long long* blk_macs,
+                                  int num_blocks, double* d_norm,
+                                  unsigned long long* d_num_skipped,
+                                  unsigned long long* d_macs, cudaStream_t s) {
+  k_place_finalize<<<1, 32, 0, s>>>(blk_norm, blk_skip, blk_macs, num_blocks,
+                                    d_norm, d_num_skipped, d_macs);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_emit_records(const uint32_t* cell, const uint32_t* meta,
+                                const uint32_t* rec_offset,
+                                unsigned long long n, StackView view,
+                                TileGeom geom, int grid_index,
+                                unsigned long long vis_offset, uint32_t* keys,
+                                uint32_t* vals, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  k_emit<<<nb, 256, 0, s>>>(cell, meta, rec_offset, n, view, geom,
+                            grid_index, vis_offset, keys, vals);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_place<float>(PlaceParams<float>, StackView,
+                                         TileGeom, int, unsigned long long,
+                                         PlaceOut, cudaStream_t);
+template cudaError_t launch_place<double>(PlaceParams<double>, StackView,
+                                          TileGeom, int, unsigned long long,
+                                          PlaceOut, cudaStream_t);
+
+}  // namespace gg

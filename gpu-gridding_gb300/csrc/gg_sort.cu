@@ -1,0 +1,252 @@
+// Device-wide exclusive scan and stable LSD radix sort of (key, value)
+// pairs.  These order the (visibility, tile) records by (grid, tile, plane,
+// offset class) so the gridding kernel sees each tile's records contiguously
+// and grouped by kernel slice.  The reference bins with an atomic bucket
+// scatter whose in-bucket order changes from run to run
+// (oskar_grid_wproj_gpu.cu:520-649); this sort is stable, so the record
+// order -- and with it the accumulation order -- is the same on every call.
+#include "gg_internal.h"
+
+namespace gg {
+
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;  // 2048
+
+__device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t x) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  return x;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the exclusive
+// prefix and writes the block total to *total.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x,
+                                                         uint32_t* total) {
+  __shared__ uint32_t warp_sums[33];  // [32] holds the block total
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  uint32_t inc = warp_inclusive_scan(x);
+  if (lane == 31) warp_sums[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < nwarps ? warp_sums[lane] : 0;
+    uint32_t wi = warp_inclusive_scan(w);
+    if (lane < nwarps) warp_sums[lane] = wi - w;
+    if (lane == nwarps - 1) warp_sums[32] = wi;
+  }
+  __syncthreads();
+  uint32_t result = warp_sums[warp] + inc - x;
+  *total = warp_sums[32];
+  __syncthreads();
+  return result;
+}
+
+__global__ void k_scan_reduce(const uint32_t* __restrict__ in, size_t n,
+                              uint32_t* __restrict__ block_sums) {
+  const size_t base = (size_t)blockIdx.x * kScanTile;
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    size_t idx = base + (size_t)i * kScanThreads + threadIdx.x;
+    if (idx < n) s += in[idx];
+  }
+  uint32_t total;
+  block_exclusive_scan(s, &total);
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// Exclusive scan of the block sums in place by one block, chunk by chunk.
+__global__ void k_scan_top(uint32_t* __restrict__ sums, size_t nb,
+                           uint32_t* __restrict__ d_total) {
+  uint32_t carry = 0;
+  for (size_t base = 0; base < nb; base += blockDim.x) {
+    size_t idx = base + threadIdx.x;
+    uint32_t x = idx < nb ? sums[idx] : 0;
+    uint32_t total;
+    uint32_t ex = block_exclusive_scan(x, &total);
+    if (idx < nb) sums[idx] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0 && d_total) *d_total = carry;
+}
+
+__global__ void k_scan_down(const uint32_t* __restrict__ in,
+                            uint32_t* __restrict__ out, size_t n,
+                            const uint32_t* __restrict__ block_offsets) {
+  __shared__ uint32_t tile[kScanTile];
+  const size_t base = (size_t)blockIdx.x * kScanTile;
+  // Striped, coalesced load into shared memory.
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    int t = i * kScanThreads + threadIdx.x;
+    size_t idx = base + t;
+    tile[t] = idx < n ? in[idx] : 0;
+  }
+  __syncthreads();
+  // Each thread scans its kScanItems consecutive entries.
+  uint32_t v[kScanItems];
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    v[i] = tile[threadIdx.x * kScanItems + i];
+    s += v[i];
+  }
+  uint32_t total;
+  uint32_t pre = block_exclusive_scan(s, &total) + block_offsets[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    tile[threadIdx.x * kScanItems + i] = pre;
+    pre += v[i];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    int t = i * kScanThreads + threadIdx.x;
+    size_t idx = base + t;
+    if (idx < n) out[idx] = tile[t];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Radix sort: 8-bit digits, 4096 keys per block, reduce-then-scan per pass.
+// ---------------------------------------------------------------------------
+constexpr int kRadixThreads = 256;
+constexpr int kRadixWarps = kRadixThreads / 32;
+constexpr int kRadixRounds = 16;
+constexpr int kRadixTile = kRadixThreads * kRadixRounds;  // 4096
+constexpr int kRadixDigits = 256;
+
+__global__ void __launch_bounds__(kRadixThreads)
+k_radix_hist(const uint32_t* __restrict__ keys, size_t n, int shift,
+             int num_blocks, uint32_t* __restrict__ hist) {
+  __shared__ uint32_t h[kRadixDigits];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const size_t base = (size_t)blockIdx.x * kRadixTile;
+#pragma unroll 4
+  for (int r = 0; r < kRadixRounds; ++r) {
+    size_t idx = base + (size_t)r * kRadixThreads + threadIdx.x;
+    if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 0xFF], 1u);
+  }
+  __syncthreads();
+  // Digit-major layout: the scan then yields, for each (digit, block), the
+  // global position of that block's first key with that digit.
+  hist[(size_t)threadIdx.x * num_blocks + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kRadixThreads)
+k_radix_scatter(const uint32_t* __restrict__ keys,
+                const uint32_t* __restrict__ vals, size_t n, int shift,
+                int num_blocks, const uint32_t* __restrict__ offsets,
+                uint32_t* __restrict__ keys_out,
+                uint32_t* __restrict__ vals_out) {
+  __shared__ uint32_t digit_base[kRadixDigits];
+  __shared__ uint32_t warp_count[kRadixWarps][kRadixDigits];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  digit_base[threadIdx.x] =
+      offsets[(size_t)threadIdx.x * num_blocks + blockIdx.x];
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const size_t base = (size_t)blockIdx.x * kRadixTile;
+  for (int r = 0; r < kRadixRounds; ++r) {
+    if (base + (size_t)r * kRadixThreads >= n) break;  // block-uniform
+#pragma unroll
+    for (int w = 0; w < kRadixWarps; ++w) warp_count[w][threadIdx.x] = 0;
+    __syncthreads();
+    size_t idx = base + (size_t)r * kRadixThreads + threadIdx.x;
+    bool valid = idx < n;
+    uint32_t key = valid ? keys[idx] : 0u;
+    uint32_t val = valid ? vals[idx] : 0u;
+    // Invalid lanes take digit 256 so they never match a valid one.
+    uint32_t digit = valid ? ((key >> shift) & 0xFF) : 256u;
+    uint32_t peers = __match_any_sync(0xffffffffu, digit);
+    uint32_t rank = __popc(peers & lt_mask);
+    int leader = __ffs(peers) - 1;
+    if (valid && lane == leader) warp_count[warp][digit] = __popc(peers);
+    __syncthreads();
+    // Per-digit exclusive prefix across warps (thread t owns digit t).
+    {
+      uint32_t running = digit_base[threadIdx.x];
+#pragma unroll
+      for (int w = 0; w < kRadixWarps; ++w) {
+        uint32_t c = warp_count[w][threadIdx.x];
+        warp_count[w][threadIdx.x] = running;
+        running += c;
+      }
+      digit_base[threadIdx.x] = running;
+    }
+    __syncthreads();
+    if (valid) {
+      uint32_t pos = warp_count[warp][digit] + rank;
+      keys_out[pos] = key;
+      vals_out[pos] = val;
+    }
+    __syncthreads();
+  }
+}
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+size_t scan_temp_bytes(size_t n) {
+  size_t nb = (n + kScanTile - 1) / kScanTile;
+  return align_up((nb + 1) * sizeof(uint32_t), 256);
+}
+
+cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n,
+                               uint32_t* d_total, void* tmp, cudaStream_t s) {
+  if (n == 0) {
+    if (d_total) return cudaMemsetAsync(d_total, 0, sizeof(uint32_t), s);
+    return cudaSuccess;
+  }
+  size_t nb = (n + kScanTile - 1) / kScanTile;
+  uint32_t* sums = (uint32_t*)tmp;
+  k_scan_reduce<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, sums);
+  k_scan_top<<<1, 1024, 0, s>>>(sums, nb, d_total);
+  k_scan_down<<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, sums);
+  return cudaGetLastError();
+}
+
+size_t radix_temp_bytes(size_t n) {
+  size_t nb = (n + kRadixTile - 1) / kRadixTile;
+  if (nb == 0) nb = 1;
+  size_t hist = align_up(nb * kRadixDigits * sizeof(uint32_t), 256);
+  return 2 * hist + scan_temp_bytes(nb * kRadixDigits);
+}
+
+cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals,
+                             uint32_t* keys_alt, uint32_t* vals_alt, size_t n,
+                             int end_bit, void* tmp, cudaStream_t s,
+                             bool* in_alt) {
+  *in_alt = false;
+  if (n <= 1 || end_bit <= 0) return cudaSuccess;
+  size_t nb = (n + kRadixTile - 1) / kRadixTile;
+  size_t hist_bytes = align_up(nb * kRadixDigits * sizeof(uint32_t), 256);
+  uint32_t* hist = (uint32_t*)tmp;
+  uint32_t* offs = (uint32_t*)((char*)tmp + hist_bytes);
+  void* scan_tmp = (char*)tmp + 2 * hist_bytes;
+  uint32_t *k_in = keys, *v_in = vals, *k_out = keys_alt, *v_out = vals_alt;
+  for (int shift = 0; shift < end_bit; shift += 8) {
+    k_radix_hist<<<(unsigned)nb, kRadixThreads, 0, s>>>(k_in, n, shift,
+                                                        (int)nb, hist);
+    cudaError_t e = exclusive_scan_u32(hist, offs, nb * kRadixDigits, nullptr,
+                                       scan_tmp, s);
+    if (e != cudaSuccess) return e;
+    k_radix_scatter<<<(unsigned)nb, kRadixThreads, 0, s>>>(
+        k_in, v_in, n, shift, (int)nb, offs, k_out, v_out);
+    uint32_t* t;
+    t = k_in; k_in = k_out; k_out = t;
+    t = v_in; v_in = v_out; v_out = t;
+    *in_alt = !*in_alt;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace gg

@@ -1,0 +1,214 @@
+/*
+ * gpugrid.h -- C ABI of the GB300 W-projection gridder (libgpugrid.so).
+ *
+ * The library is a drop-in for the reference's serial gridding functions
+ * (oskar_grid_wproj.h:69-86 and :114-131 of the reference project) plus the
+ * entry points a GPU caller needs: status codes, device-pointer variants on
+ * a caller's CUDA stream, reusable kernel-stack handles, a batched
+ * multi-channel path, the adjoint (degridding) map and the uniform-weighting
+ * density step.  Every signature uses plain pointers, sizes and scalars;
+ * streams are passed as `void*` (a cudaStream_t, NULL for the legacy default
+ * stream) so this header needs no CUDA include.
+ *
+ * Threading: calls may come from several host threads; work for one device
+ * is serialised by a per-device lock.  Results are deterministic: the same
+ * inputs give bit-identical grids, norms and counts on every call.
+ */
+#ifndef GPUGRID_H_
+#define GPUGRID_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GG_API __attribute__((visibility("default")))
+#else
+#define GG_API
+#endif
+
+/* Status codes returned by every gg_* entry point that returns int. */
+enum
+{
+    GG_OK = 0,
+    GG_ERR_INVALID_ARG = 1,   /* a size, pointer or parameter is invalid */
+    GG_ERR_CUDA = 2,          /* a CUDA runtime call failed */
+    GG_ERR_NO_MEMORY = 3,     /* a device or host allocation failed */
+    GG_ERR_UNSUPPORTED = 4,   /* valid input outside this build's limits */
+    GG_ERR_CAPACITY = 5       /* a reserved workspace was too small */
+};
+
+/* ---------------------------------------------------------------------- */
+/* Drop-in replacements                                                   */
+/* ---------------------------------------------------------------------- */
+
+/* Same signature and semantics as oskar_grid_wproj_d (reference
+ * oskar_grid_wproj.h:69-86, oskar_grid_wproj.c:37-123).  Host pointers;
+ * synchronous; *num_skipped is set, *norm and grid are accumulated.  FP64
+ * placement and FP64 accumulation on the GPU.  On failure the outputs are
+ * left untouched and gg_last_error() describes the failure. */
+GG_API void oskar_grid_wproj_d(const size_t num_w_planes, const int* support,
+        const int oversample, const int conv_size_half,
+        const double* conv_func, const size_t num_points, const double* uu,
+        const double* vv, const double* ww, const double* vis,
+        const double* weight, const double cell_size_rad,
+        const double w_scale, const int grid_size, size_t* num_skipped,
+        double* norm, double* grid);
+
+/* Same signature and semantics as oskar_grid_wproj_f (reference
+ * oskar_grid_wproj.h:114-131, oskar_grid_wproj.c:126-212).  Placement,
+ * plane choice and num_skipped are bit-exact with the reference's FP32 rules;
+ * the grid is accumulated in compensated FP32; norm is FP64. */
+GG_API void oskar_grid_wproj_f(const size_t num_w_planes, const int* support,
+        const int oversample, const int conv_size_half,
+        const float* conv_func, const size_t num_points, const float* uu,
+        const float* vv, const float* ww, const float* vis,
+        const float* weight, const float cell_size_rad, const float w_scale,
+        const int grid_size, size_t* num_skipped, double* norm, float* grid);
+
+/* Status-returning forms of the two drop-ins (same arguments). */
+GG_API int gg_grid_wproj_d(size_t num_w_planes, const int* support,
+        int oversample, int conv_size_half, const double* conv_func,
+        size_t num_points, const double* uu, const double* vv,
+        const double* ww, const double* vis, const double* weight,
+        double cell_size_rad, double w_scale, int grid_size,
+        size_t* num_skipped, double* norm, double* grid);
+GG_API int gg_grid_wproj_f(size_t num_w_planes, const int* support,
+        int oversample, int conv_size_half, const float* conv_func,
+        size_t num_points, const float* uu, const float* vv,
+        const float* ww, const float* vis, const float* weight,
+        float cell_size_rad, float w_scale, int grid_size,
+        size_t* num_skipped, double* norm, float* grid);
+
+/* Message for the last failure on the calling host thread ("" if none). */
+GG_API const char* gg_last_error(void);
+
+/* Library version string. */
+GG_API const char* gg_version(void);
+
+/* ---------------------------------------------------------------------- */
+/* Kernel stacks (re-laid, device-resident W-kernel cubes)                */
+/* ---------------------------------------------------------------------- */
+
+/* A kernel stack is the reference's (support, oversample, conv_size_half,
+ * conv_func) tuple (oskar_grid_wproj.h:114-119) uploaded once and re-laid on
+ * the device for the gridding kernels, together with the per-plane,
+ * per-offset FP64 tap sums used for the norm.  The handle owns its device
+ * memory; the caller may change or free conv_func after creation.  It is
+ * tied to the device current at creation. */
+typedef struct gg_kernels gg_kernels;
+
+/* conv_func_on_device = 0: conv_func is host memory; 1: device memory.
+ * support is always host memory.  stream: cudaStream_t or NULL. */
+GG_API int gg_kernels_create_f(gg_kernels** out, size_t num_w_planes,
+        const int* support, int oversample, int conv_size_half,
+        const float* conv_func, int conv_func_on_device, void* stream);
+GG_API int gg_kernels_create_d(gg_kernels** out, size_t num_w_planes,
+        const int* support, int oversample, int conv_size_half,
+        const double* conv_func, int conv_func_on_device, void* stream);
+GG_API int gg_kernels_destroy(gg_kernels* k);
+
+/* ---------------------------------------------------------------------- */
+/* Device-pointer gridding                                                */
+/* ---------------------------------------------------------------------- */
+
+/* A plan owns the device workspace (placement arrays, sort buffers, work
+ * items, partial tiles) and grows it on demand.  One plan serves one call
+ * at a time; use one plan per concurrent stream. */
+typedef struct gg_plan gg_plan;
+
+GG_API int gg_plan_create(gg_plan** out);
+GG_API int gg_plan_destroy(gg_plan* plan);
+
+/* Statistics of the last call made with a plan (valid after the stream
+ * has been synchronised). */
+typedef struct
+{
+    unsigned long long num_points;
+    unsigned long long num_skipped;
+    unsigned long long num_records;     /* (visibility, tile) pairs */
+    unsigned long long num_macs;        /* complex multiply-adds performed */
+    unsigned long long num_launches;    /* kernels this library launched */
+    int tile_u, tile_v;                 /* tile shape used */
+} gg_stats;
+
+GG_API int gg_plan_last_stats(const gg_plan* plan, gg_stats* stats);
+
+/* Phase timing.  With profiling enabled, every gridding call made with the
+ * plan records CUDA events on its stream around five phases:
+ *   0 placement (placement, skip/norm reduction, record offsets)
+ *   1 binning (record emission and radix sort)
+ *   2 work decomposition (tile ranges and work items)
+ *   3 the tile-gridding kernel
+ *   4 the partial-tile reduction
+ * gg_plan_phase_ms fills ms[0..n-1] for the last call; the call's stream
+ * must have been synchronised.  Off by default (no events recorded). */
+GG_API int gg_plan_set_profiling(gg_plan* plan, int enable);
+GG_API int gg_plan_phase_ms(const gg_plan* plan, float* ms, int n);
+
+/* Measured FP32 fused-multiply-add throughput of the current device, in
+ * TFLOP/s (2 FLOP per FMA): the roofline denominator of the FP32 gridding
+ * kernel.  Runs for a few tens of milliseconds. */
+GG_API int gg_measure_fp32_fma_tflops(double* tflops);
+
+/* Grid num_points visibilities held in device memory onto a device grid.
+ * Semantics are those of oskar_grid_wproj_f with device pointers:
+ * *d_num_skipped (device, 64-bit) is set, *d_norm (device) and d_grid
+ * (device, complex64 grid_size^2, row-major with v as the row) are
+ * accumulated.  Runs on `stream`; the call returns once the work is queued
+ * (it synchronises the stream once, to size the sort buffers). */
+GG_API int gg_grid_wproj_f_device(gg_plan* plan, const gg_kernels* kernels,
+        size_t num_points, const float* d_uu, const float* d_vv,
+        const float* d_ww, const float* d_vis, const float* d_weight,
+        float cell_size_rad, float w_scale, int grid_size,
+        unsigned long long* d_num_skipped, double* d_norm, float* d_grid,
+        void* stream);
+GG_API int gg_grid_wproj_d_device(gg_plan* plan, const gg_kernels* kernels,
+        size_t num_points, const double* d_uu, const double* d_vv,
+        const double* d_ww, const double* d_vis, const double* d_weight,
+        double cell_size_rad, double w_scale, int grid_size,
+        unsigned long long* d_num_skipped, double* d_norm, double* d_grid,
+        void* stream);
+
+/* Placement only (diagnostic): writes, per visibility, six int32 --
+ * cell u, cell v, off_u, off_v, w-plane (after the clamp to the last plane)
+ * and flags (bit 0 skipped, bit 1 kernel conjugated because ww > 0) --
+ * exactly as the gridding entry points compute them.  This is the
+ * per-visibility state of reference oskar_grid_wproj.c:155-187 (FP32 rules)
+ * and :66-98 (FP64 rules).  d_out: device int32[6 * num_points]. */
+GG_API int gg_place_wproj_f_device(const gg_kernels* kernels,
+        size_t num_points, const float* d_uu, const float* d_vv,
+        const float* d_ww, float cell_size_rad, float w_scale, int grid_size,
+        int* d_out, void* stream);
+GG_API int gg_place_wproj_d_device(const gg_kernels* kernels,
+        size_t num_points, const double* d_uu, const double* d_vv,
+        const double* d_ww, double cell_size_rad, double w_scale,
+        int grid_size, int* d_out, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Adjoint (degridding)                                                   */
+/* ---------------------------------------------------------------------- */
+
+/* The exact adjoint of the map v -> grid that oskar_grid_wproj_f applies
+ * to the weighted visibilities v_i = weight_i * vis_i (reference
+ * oskar_grid_wproj.c:190-209 defines the forward map; the reference has no
+ * degridder):  d_out_vis[i] = sum over the footprint of
+ * conj(c~_i(cell)) * d_grid(cell), with c~ the tap whose imaginary part is
+ * negated for ww > 0, and the same placement rules as the forward call.
+ * Skipped visibilities get 0.  Device pointers, complex interleaved. */
+GG_API int gg_degrid_wproj_f_device(gg_plan* plan, const gg_kernels* kernels,
+        size_t num_points, const float* d_uu, const float* d_vv,
+        const float* d_ww, float cell_size_rad, float w_scale, int grid_size,
+        const float* d_grid, float* d_out_vis, void* stream);
+GG_API int gg_degrid_wproj_d_device(gg_plan* plan, const gg_kernels* kernels,
+        size_t num_points, const double* d_uu, const double* d_vv,
+        const double* d_ww, double cell_size_rad, double w_scale,
+        int grid_size, const double* d_grid, double* d_out_vis, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPUGRID_H_ */

@@ -1,0 +1,239 @@
+"""GPU parity tests of the gridder (run with -m gpu on a GB300).
+
+Bars (the tolerances are written in each assertion):
+* cell, offset and plane assignment and num_skipped: bit-exact with the
+  reference's FP32 (and FP64) rules;
+* norm: relative 1e-12 (it is the same FP64 per-visibility sums, added in a
+  different order);
+* FP32 grid: max |err| / max |grid| <= 1e-5 against the reference's _f
+  output and against the FP64 oracle with the same placement;
+* FP64 grid: relative 1e-12 against the reference's _d output.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden, max_rel, rms_rel
+
+pytestmark = pytest.mark.gpu
+
+GRID_CASES = [n for n in golden_names() if not n.startswith("weights")]
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+    assert t.cuda.is_available(), "GPU tests need a CUDA device"
+    return t
+
+
+def _dev(torch, a, dtype=None):
+    t = torch.from_numpy(np.ascontiguousarray(a))
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.cuda()
+
+
+@pytest.mark.parametrize("name", GRID_CASES)
+def test_dropin_matches_reference_golden(pkg, oracle_mod, torch, name):
+    wl, z = load_golden(name)
+    grid = z["grid_in"].copy()
+    if str(z["precision"]) == "f":
+        ns, nm = pkg.oskar_grid_wproj_f(
+            wl.num_w_planes, wl.support, wl.oversample, wl.conv_size_half,
+            wl.conv_func, wl.num_points, wl.uu, wl.vv, wl.ww, wl.vis,
+            wl.weight, np.float32(wl.cell_size_rad), np.float32(wl.w_scale),
+            wl.grid_size, grid, float(z["norm_in"]))
+        tol = 1e-5
+    else:
+        ns, nm = pkg.oskar_grid_wproj_d(
+            wl.num_w_planes, wl.support, wl.oversample, wl.conv_size_half,
+            wl.conv_func, wl.num_points, wl.uu, wl.vv, wl.ww, wl.vis,
+            wl.weight, float(wl.cell_size_rad), float(wl.w_scale),
+            wl.grid_size, grid, float(z["norm_in"]))
+        tol = 1e-12
+    assert ns == int(z["num_skipped"])
+    assert abs(nm - float(z["norm_out"])) <= 1e-12 * abs(float(z["norm_out"]))
+    assert max_rel(grid, z["grid_out"]) <= tol
+    if str(z["precision"]) == "f":
+        g64, _, _ = oracle_mod.grid_f_fp64acc(
+            wl, z["grid_in"].astype(np.float64), float(z["norm_in"]))
+        assert max_rel(grid, g64) <= 1e-5
+
+
+@pytest.mark.parametrize("name", ["small_f", "small_d", "edges_f",
+                                  "edges_d", "os1_f", "os3_f", "os8_f"])
+def test_placement_bit_exact_golden(pkg, oracle_mod, torch, name):
+    wl, z = load_golden(name)
+    prec = str(z["precision"])
+    dt = torch.float32 if prec == "f" else torch.float64
+    stack = pkg.KernelStack.from_workload(wl, prec)
+    cast = np.float32 if prec == "f" else float
+    out = pkg.place_wproj_device(
+        stack, _dev(torch, wl.uu, dt), _dev(torch, wl.vv, dt),
+        _dev(torch, wl.ww, dt), cast(wl.cell_size_rad), cast(wl.w_scale),
+        wl.grid_size).cpu().numpy()
+    p = oracle_mod.place(wl, prec)
+    skipped = out[:, 5] & 1
+    assert np.array_equal(skipped, p["skipped"])
+    assert np.array_equal(out[:, 5] >> 1, p["conj_neg"])
+    keep = p["skipped"] == 0
+    for col, key in enumerate(("gu", "gv", "ou", "ov", "plane")):
+        assert np.array_equal(out[keep, col], p[key][keep]), key
+    assert int(skipped.sum()) == int(z["num_skipped"])
+
+
+@pytest.mark.parametrize("which", ["cfg0", "cfg1_sub", "skalow_small"])
+def test_placement_bit_exact_synthetic(pkg, oracle_mod, synthetic, torch,
+                                       which):
+    if which == "cfg0":
+        wl = synthetic.config0()
+    elif which == "cfg1_sub":
+        wl = synthetic.config1().subset(400_000)
+    else:
+        wl = _skalow_small(synthetic)
+    for prec in ("f", "d"):
+        dt = torch.float32 if prec == "f" else torch.float64
+        stack = pkg.KernelStack.from_workload(wl, prec)
+        cast = np.float32 if prec == "f" else float
+        out = pkg.place_wproj_device(
+            stack, _dev(torch, wl.uu, dt), _dev(torch, wl.vv, dt),
+            _dev(torch, wl.ww, dt), cast(wl.cell_size_rad),
+            cast(wl.w_scale), wl.grid_size).cpu().numpy()
+        p = oracle_mod.place(wl, prec)
+        assert np.array_equal(out[:, 5] & 1, p["skipped"])
+        keep = p["skipped"] == 0
+        for col, key in enumerate(("gu", "gv", "ou", "ov", "plane")):
+            assert np.array_equal(out[keep, col], p[key][keep]), (prec, key)
+
+
+def _skalow_small(synthetic):
+    """SKA-LOW-shaped array at reduced size (64 stations, 60 times)."""
+    import dataclasses
+    rng = np.random.Generator(np.random.PCG64(3))
+    u, v, w = synthetic.ska_low_uvw_metres(rng, num_stations=64,
+                                           num_times=60)
+    sc = 100e6 / synthetic.SPEED_OF_LIGHT
+    u, v, w = u * sc, v * sc, w * sc
+    G, planes, s_min, s_max = 2048, 96, 4, 24
+    cell = synthetic._fit_cell_size(float(max(abs(u).max(), abs(v).max())),
+                                    G, s_max)
+    support = synthetic.linear_supports(planes, s_min, s_max)
+    wl = synthetic._finish("skalow_small", rng, support, 4, G, cell, u, v, w,
+                           float(abs(w).max()),
+                           weight=np.ones(u.shape[0], np.float32))
+    return dataclasses.replace(wl)
+
+
+def test_cfg0_error_vs_fp64_oracle(pkg, oracle_mod, synthetic, torch):
+    wl = synthetic.config0()
+    g, ns, nm = pkg.grid_f(wl)
+    g64, ns64, nm64 = oracle_mod.grid_f_fp64acc(wl)
+    gref, nsr, nmr = oracle_mod.grid_f(wl)
+    assert ns == ns64 == nsr
+    assert abs(nm - nm64) <= 1e-12 * abs(nm64)
+    err = max_rel(g, g64)
+    err_ref = max_rel(gref, g64)
+    print(f"cfg0 max-rel vs FP64: gpu {err:.3e} (reference _f {err_ref:.3e}); "
+          f"rms gpu {rms_rel(g, g64):.3e} ref {rms_rel(gref, g64):.3e}")
+    assert err <= 1e-5
+    # Compensated accumulation is at least as accurate as the serial FP32.
+    assert rms_rel(g, g64) <= rms_rel(gref, g64)
+    assert max_rel(g, gref) <= 1e-5
+
+
+def test_device_entry_equals_drop_in_and_is_deterministic(pkg, synthetic,
+                                                          torch):
+    wl = synthetic.config0().subset(50_000)
+    g_host, ns_h, nm_h = pkg.grid_f(wl)
+    stack = pkg.KernelStack.from_workload(wl, "f")
+    plan = pkg.Plan()
+    grids = []
+    for _ in range(2):
+        grid = torch.zeros((wl.grid_size, wl.grid_size, 2),
+                           dtype=torch.float32, device="cuda")
+        norm = torch.zeros(1, dtype=torch.float64, device="cuda")
+        ns = torch.full((1,), -1, dtype=torch.int64, device="cuda")
+        pkg.grid_wproj_device(plan, stack, _dev(torch, wl.uu),
+                              _dev(torch, wl.vv), _dev(torch, wl.ww),
+                              _dev(torch, wl.vis), _dev(torch, wl.weight),
+                              np.float32(wl.cell_size_rad),
+                              np.float32(wl.w_scale), wl.grid_size, grid,
+                              norm, ns)
+        torch.cuda.synchronize()
+        grids.append(grid.cpu().numpy())
+        assert int(ns.item()) == ns_h
+        assert norm.item() == nm_h
+    assert np.array_equal(grids[0].view(np.uint32), grids[1].view(np.uint32))
+    assert np.array_equal(grids[0].view(np.uint32), g_host.view(np.uint32))
+    st = plan.stats()
+    assert st["num_points"] == wl.num_points and st["num_macs"] > 0
+
+
+def test_accumulate_semantics(pkg, synthetic, torch):
+    """grid and norm accumulate across calls, num_skipped is set."""
+    wl = synthetic.config0().subset(20_000)
+    g1, ns1, nm1 = pkg.grid_f(wl)
+    g2, ns2, nm2 = pkg.grid_f(wl, g1.copy(), nm1)
+    assert ns2 == ns1
+    assert abs(nm2 - 2 * nm1) <= 1e-12 * abs(nm2)
+    assert max_rel(g2, 2 * g1) <= 1e-6
+
+
+def test_linearity_exact_full_cfg1(pkg, oracle_mod, synthetic, torch):
+    """Scaling visibilities by 2 scales the grid by exactly 2 (every
+    operation on the path is exact under a power-of-two scale)."""
+    wl = synthetic.config1()
+    stack = pkg.KernelStack.from_workload(wl, "f")
+    plan = pkg.Plan()
+    outs = []
+    for scale in (1.0, 2.0):
+        grid = torch.zeros((wl.grid_size, wl.grid_size, 2),
+                           dtype=torch.float32, device="cuda")
+        norm = torch.zeros(1, dtype=torch.float64, device="cuda")
+        ns = torch.zeros(1, dtype=torch.int64, device="cuda")
+        pkg.grid_wproj_device(plan, stack, _dev(torch, wl.uu),
+                              _dev(torch, wl.vv), _dev(torch, wl.ww),
+                              _dev(torch, wl.vis * np.float32(scale)),
+                              _dev(torch, wl.weight),
+                              np.float32(wl.cell_size_rad),
+                              np.float32(wl.w_scale), wl.grid_size, grid,
+                              norm, ns)
+        torch.cuda.synchronize()
+        outs.append((grid, int(ns.item()), norm.item()))
+    assert torch.equal(outs[1][0], 2 * outs[0][0])
+    assert outs[0][1] == outs[1][1] == oracle_mod.place(wl)["num_skipped"]
+    assert plan.stats()["num_macs"] == oracle_mod.mac_count(wl)
+
+
+def test_cfg1_vs_reference_rules(pkg, oracle_mod, synthetic, torch):
+    """Full synthetic-challenge shape against the host-parallel oracle,
+    which is bit-identical to the reference's serial _f."""
+    wl = synthetic.config1()
+    g, ns, nm = pkg.grid_f(wl)
+    gref, nsr, nmr = oracle_mod.grid_f_mt(wl)
+    assert ns == nsr
+    assert abs(nm - nmr) <= 1e-12 * abs(nmr)
+    err = max_rel(g, gref)
+    print(f"cfg1 max-rel vs reference _f: {err:.3e}")
+    assert err <= 1e-5
+
+
+def test_fp64_path_vs_reference_d(pkg, oracle_mod, synthetic, torch):
+    wl = synthetic.config0().subset(30_000)
+    g, ns, nm = pkg.grid_d(wl)
+    gr, nsr, nmr = oracle_mod.grid_d(wl)
+    assert ns == nsr
+    assert abs(nm - nmr) <= 1e-12 * abs(nmr)
+    assert max_rel(g, gr) <= 1e-12
+
+
+def test_empty_and_all_skipped_device(pkg, synthetic, torch):
+    wl = synthetic.config0().subset(0)
+    g, ns, nm = pkg.grid_f(wl, norm=3.5)
+    assert ns == 0 and nm == 3.5 and not g.any()
+    wl = synthetic.config0().subset(100)
+    wl.uu = np.full(100, 1e9, np.float32)
+    g, ns, nm = pkg.grid_f(wl, norm=1.0)
+    assert ns == 100 and nm == 1.0 and not g.any()

@@ -1,0 +1,117 @@
+"""CPU tests: the oracle is pinned to the reference.
+
+The oracle (oracle/oskar_grid_oracle.c) restates the reference's serial
+gridder.  It must reproduce the reference's golden outputs bit for bit
+(num_skipped, norm and every grid word), and -- where the reference source
+tree is present -- the compiled reference itself on fresh inputs.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden, max_rel
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names()
+                                  if not n.startswith("weights")])
+def test_oracle_matches_golden_bit_exact(oracle_mod, name):
+    wl, z = load_golden(name)
+    if str(z["precision"]) == "f":
+        g, ns, nm = oracle_mod.grid_f(wl, z["grid_in"].copy(),
+                                      float(z["norm_in"]))
+    else:
+        g, ns, nm = oracle_mod.grid_d(wl, z["grid_in"].copy(),
+                                      float(z["norm_in"]))
+    assert ns == int(z["num_skipped"])
+    assert nm == float(z["norm_out"])          # bit-exact FP64
+    assert np.array_equal(g.view(np.uint8), z["grid_out"].view(np.uint8))
+
+
+@pytest.mark.parametrize("name", ["small_f", "edges_f", "os3_f"])
+def test_multithreaded_oracle_bit_exact(oracle_mod, name):
+    wl, z = load_golden(name)
+    g, ns, nm = oracle_mod.grid_f_mt(wl, z["grid_in"].copy(),
+                                     float(z["norm_in"]), threads=4)
+    assert ns == int(z["num_skipped"])
+    assert nm == float(z["norm_out"])
+    assert np.array_equal(g.view(np.uint8), z["grid_out"].view(np.uint8))
+
+
+@pytest.mark.parametrize("name", ["weights_f", "weights_d"])
+def test_weights_oracle_matches_golden(oracle_mod, name):
+    _, z = load_golden(name)
+    real = z["uu"].dtype.type
+    suffix = "f" if real == np.float32 else "d"
+    L = oracle_mod.lib()
+    G = int(z["grid_size"])
+    dens = np.zeros((G, G), real)
+    ns = ctypes.c_size_t(0)
+    n = z["uu"].shape[0]
+    getattr(L, f"oracle_grid_weights_write_{suffix}")(
+        n, z["uu"], z["vv"], z["weight"], real(z["cell_size_rad"]), G,
+        ctypes.byref(ns), dens.reshape(-1))
+    assert ns.value == int(z["num_skipped_write"])
+    assert np.array_equal(dens.view(np.uint8), z["density"].view(np.uint8))
+    out = np.full(n, -7.0, real)
+    getattr(L, f"oracle_grid_weights_read_{suffix}")(
+        n, z["uu"], z["vv"], z["weight"], out, real(z["cell_size_rad"]), G,
+        ctypes.byref(ns), dens.reshape(-1))
+    assert ns.value == int(z["num_skipped_read"])
+    assert np.array_equal(out.view(np.uint8), z["weight_out"].view(np.uint8))
+
+
+def test_placement_matches_serial_skip_count(oracle_mod):
+    wl, z = load_golden("small_f")
+    p = oracle_mod.place(wl, "f")
+    assert p["num_skipped"] == int(z["num_skipped"])
+    assert p["ou"].min() >= -2 and p["ou"].max() <= 2
+    assert p["plane"].max() == wl.num_w_planes - 1   # clamp exercised
+
+
+def test_fp64_yardstick_close_to_reference_f(oracle_mod):
+    """The FP64-accumulation oracle agrees with the reference _f to FP32
+    rounding, with identical placement (same skip count, same norm)."""
+    wl, z = load_golden("small_f")
+    g64, ns, nm = oracle_mod.grid_f_fp64acc(
+        wl, z["grid_in"].astype(np.float64), float(z["norm_in"]))
+    assert ns == int(z["num_skipped"])
+    assert nm == float(z["norm_out"])
+    assert max_rel(z["grid_out"], g64) < 1e-5
+
+
+def test_adjoint_oracle_dot_product(oracle_mod):
+    """<G x, y> = <x, G^H y> for the FP64 oracle pair."""
+    wl, _ = load_golden("small_f")
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((wl.num_points, 2))
+    y = rng.standard_normal((wl.grid_size, wl.grid_size, 2))
+    wl1 = wl.subset(wl.num_points)
+    wl1.vis = x.astype(np.float32)
+    wl1.weight = np.ones(wl.num_points, np.float32)
+    gx, _, _ = oracle_mod.grid_f_fp64acc(wl1)
+    # Use the float32-rounded x on both sides.
+    xs = wl1.vis.astype(np.float64)
+    aty = oracle_mod.degrid_fp64(wl1, y)
+    lhs = (gx[..., 0] * y[..., 0] + gx[..., 1] * y[..., 1]).sum()
+    rhs = (xs[:, 0] * aty[:, 0] + xs[:, 1] * aty[:, 1]).sum()
+    assert abs(lhs - rhs) <= 1e-10 * abs(lhs)
+
+
+@pytest.mark.skipif("not __import__('oracle').ref_available()",
+                    reason="reference source tree not present")
+@pytest.mark.parametrize("seed", [1, 2])
+def test_oracle_matches_compiled_reference(oracle_mod, synthetic, seed):
+    wl = synthetic.random_uniform_workload(
+        "fresh", 4000, 192, 12, 1, 9, seed=seed, cell_size_rad=6e-4,
+        w_max=500.0, sigma_frac=0.18, clip_frac=0.55)
+    a, nsa, nma = oracle_mod.grid_f(wl, use_reference=True)
+    b, nsb, nmb = oracle_mod.grid_f(wl)
+    assert (nsa, nma) == (nsb, nmb)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    a, nsa, nma = oracle_mod.grid_d(wl, use_reference=True)
+    b, nsb, nmb = oracle_mod.grid_d(wl)
+    assert (nsa, nma) == (nsb, nmb)
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
