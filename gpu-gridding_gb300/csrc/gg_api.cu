@@ -165,7 +165,8 @@ struct gg_kernels {
   int support_max = 0;
   long long total_taps = 0;
   std::vector<int> h_support;
-  DevBuf support, side, base, taps, tap_sum;
+  std::vector<long long> h_base;
+  DevBuf support, base, taps, tap_sum;
 
   StackView view() const {
     StackView v;
@@ -174,7 +175,6 @@ struct gg_kernels {
     v.omax = omax;
     v.conv_size_half = conv_size_half;
     v.support = support.as<int>();
-    v.side = side.as<int>();
     v.base = base.as<long long>();
     v.taps = taps.p;
     v.tap_sum = tap_sum.as<double>();
@@ -234,14 +234,14 @@ int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
   k->omax = (oversample + 1) / 2;
   k->conv_size_half = conv_size_half;
   k->h_support.assign(support, support + num_w_planes);
-  std::vector<int> side(num_w_planes);
-  std::vector<long long> base(num_w_planes);
+  std::vector<long long>& base = k->h_base;
+  base.resize(num_w_planes);
   long long total = 0;
+  const long long classes = (long long)(k->omax + 1) * (k->omax + 1);
   for (size_t p = 0; p < num_w_planes; ++p) {
-    const int M = (k->omax + support[p] * oversample) / oversample + 1;
-    side[p] = M;
+    const long long F = 2LL * support[p] + 1;
     base[p] = total;
-    total += (long long)oversample * oversample * M * M;
+    total += classes * F * F;
     k->support_max = std::max(k->support_max, support[p]);
   }
   if (total > 0x7fffffffLL)
@@ -252,7 +252,6 @@ int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
   k->total_taps = total;
   int r;
   if ((r = k->support.ensure(num_w_planes * sizeof(int))) ||
-      (r = k->side.ensure(num_w_planes * sizeof(int))) ||
       (r = k->base.ensure(num_w_planes * sizeof(long long))) ||
       (r = k->taps.ensure((size_t)total * 2 * sizeof(Real))) ||
       (r = k->tap_sum.ensure(num_w_planes * (2 * k->omax + 1) *
@@ -265,9 +264,6 @@ int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
   if ((r = cu(cudaMemcpyAsync(k->support.p, support,
                               num_w_planes * sizeof(int),
                               cudaMemcpyHostToDevice, s), "support H2D")) ||
-      (r = cu(cudaMemcpyAsync(k->side.p, side.data(),
-                              num_w_planes * sizeof(int),
-                              cudaMemcpyHostToDevice, s), "side H2D")) ||
       (r = cu(cudaMemcpyAsync(k->base.p, base.data(),
                               num_w_planes * sizeof(long long),
                               cudaMemcpyHostToDevice, s), "base H2D")))

@@ -48,45 +48,38 @@ template <>
 struct Vec2<double> { using type = double2; };
 
 // ---------------------------------------------------------------------------
-// Re-laid kernel stack.
+// Re-laid kernel stack: one dense slice per (plane, |offset| class).
 // ---------------------------------------------------------------------------
 // The reference stores, per plane, the first quadrant K[t][c] of an
-// oversampled kernel, t = |off_v + j*os| (row), c = |off_u + k*os| (column)
-// (oskar_grid_wproj.c:196-203).  For a given offset the taps a footprint
-// needs are every os-th row and column, so the device copy splits each plane
-// by residue: index t = rho_v + os*m_v, c = rho_u + os*m_u is stored at
-//   base[p] + ((rho_v*os + rho_u)*M[p] + m_v)*M[p] + m_u,
-// M[p] = (omax + support[p]*os)/os + 1.  A warp whose lanes hold consecutive
-// k then reads consecutive words, and each (rho_v, rho_u) block is a dense
-// M x M square that can be staged into shared memory in one bulk copy.
+// oversampled kernel and reads the tap of footprint cell (j, k) at
+// t = |off_v + j*os|, c = |off_u + k*os| (oskar_grid_wproj.c:196-203).  For
+// a given offset those taps form a (2s+1)^2 matrix; the device copy stores
+// that matrix explicitly, for every plane and every absolute offset class
+// (cu, cv) in [0, omax]^2:
+//   S[jj][kk] = K[|cv + (jj - s)*os|][|cu + (kk - s)*os|],  jj, kk in [0, 2s]
+// at slice_base(p, cu, cv) = base[p] + (cu*(omax+1) + cv) * F^2, F = 2s+1.
+// A negative offset reads the mirrored slice: |-c + k*os| = |c + (-k)*os|,
+// so the tap of (j, k) for offsets (ou, ov) is
+//   S_{|ou|,|ov|}[s + sgn(ov)*j][s + sgn(ou)*k].
+// Each slice is contiguous (one bulk copy stages it in shared memory) and a
+// warp whose lanes hold consecutive k reads consecutive words.
 struct StackView {
   int num_planes;
   int oversample;
   int omax;                 // (oversample + 1) / 2: largest |offset|
   int conv_size_half;
   const int* support;       // [P]
-  const int* side;          // [P] M[p]
-  const long long* base;    // [P] first element of plane p (complex units)
+  const long long* base;    // [P] first tap of plane p (complex units)
   const void* taps;         // float2 or double2
   const double* tap_sum;    // [P][2*omax+1][2*omax+1] sum of Re(tap), FP64
 };
 
-// Residue decomposition of x = |o + k*os| for a fixed signed offset o:
-// for o + k*os >= 0, x = rp + os*(k + dp); otherwise x = rn + os*(-k + dn).
-struct ResidueSplit {
-  int rp, dp, rn, dn;
-};
-__host__ __device__ inline ResidueSplit residue_split(int o, int os) {
-  // floor division and non-negative remainder of o and -o by os.
-  ResidueSplit r;
-  int q = o >= 0 ? o / os : -((-o + os - 1) / os);
-  r.dp = q;
-  r.rp = o - q * os;
-  int on = -o;
-  int qn = on >= 0 ? on / os : -((-on + os - 1) / os);
-  r.dn = qn;
-  r.rn = on - qn * os;
-  return r;
+// Offset of the slice of plane p for absolute offsets (cu, cv).
+__host__ __device__ inline long long slice_offset(long long plane_base,
+                                                  int s, int omax, int cu,
+                                                  int cv) {
+  const long long F = 2 * s + 1;
+  return plane_base + (long long)(cu * (omax + 1) + cv) * F * F;
 }
 
 // ---------------------------------------------------------------------------

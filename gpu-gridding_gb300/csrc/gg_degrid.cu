@@ -28,7 +28,6 @@ k_degrid(PlaceParams<Real> p, StackView v, const Real* __restrict__ grid,
       (unsigned long long)gridDim.x * (kDegridThreads / 32);
   const R2* __restrict__ taps = (const R2*)v.taps;
   const R2* __restrict__ g2 = (const R2*)grid;
-  const int os = v.oversample;
   for (unsigned long long i =
            (unsigned long long)blockIdx.x * (kDegridThreads / 32) +
            (threadIdx.x >> 5);
@@ -37,22 +36,18 @@ k_degrid(PlaceParams<Real> p, StackView v, const Real* __restrict__ grid,
     Real acc_re = 0, acc_im = 0;
     if (!r.skipped) {
       const int s = r.support;
-      const int M = v.side[r.plane], M2 = M * M;
-      const long long base = v.base[r.plane];
-      const ResidueSplit su = residue_split(r.ou, os);
-      const ResidueSplit sv = residue_split(r.ov, os);
+      const long long F = 2 * s + 1;
+      const R2* __restrict__ slice =
+          taps + slice_offset(v.base[r.plane], s, v.omax, abs(r.ou),
+                              abs(r.ov));
+      const int su = r.ou < 0 ? -1 : 1, sv = r.ov < 0 ? -1 : 1;
       const Real sgn = r.conj_neg ? (Real)-1 : (Real)1;
       for (int j = -s; j <= s; ++j) {
-        const long long rowpart =
-            (j >= -sv.dp) ? (long long)sv.rp * os * M2 + (long long)(j + sv.dp) * M
-                          : (long long)sv.rn * os * M2 + (long long)(-j + sv.dn) * M;
+        const R2* __restrict__ trow = slice + (s + sv * j) * F + s;
         const R2* __restrict__ grow =
             g2 + (size_t)(r.gv + j) * p.grid_size + r.gu;
         for (int k = lane - s; k <= s; k += 32) {
-          const long long lanepart =
-              (k >= -su.dp) ? (long long)su.rp * M2 + (k + su.dp)
-                            : (long long)su.rn * M2 + (-k + su.dn);
-          const R2 c = __ldg(taps + base + rowpart + lanepart);
+          const R2 c = __ldg(trow + su * k);
           const R2 gv = grow[k];
           const Real cim = sgn * c.y;
           // conj(c~) * g

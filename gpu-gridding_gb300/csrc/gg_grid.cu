@@ -67,25 +67,71 @@ struct GridArgs {
   typename Vec2<Real>::type* partials;
 };
 
-__device__ __forceinline__ uint32_t pack_split(int o, int os) {
-  const ResidueSplit r = residue_split(o, os);
-  return (uint32_t)r.rp | ((uint32_t)(r.dp + 8) << 4) |
-         ((uint32_t)r.rn << 8) | ((uint32_t)(r.dn + 8) << 12);
+// Per-record data staged in shared memory once per CTA (the first kBatch
+// threads each prepare one record), then read by every warp with broadcast
+// loads.
+struct RecGeo {           // int4
+  int gu_t, gv_t;         // cell of the visibility relative to the tile
+  int s, F;               // support and slice side 2s+1
+};
+struct RecAddr {          // int4
+  int slice;              // first tap of the (plane, |offset|) slice
+  int su, sv;             // mirror signs of the slice (offset signs)
+  int pad;
+};
+
+// Loads the kWRows taps of one record for this warp's rows into t[]; taps
+// outside the footprint (rows or lanes) are zero, so the multiply-adds that
+// follow need no predicates.
+template <typename R2>
+__device__ __forceinline__ void load_record_taps(
+    const R2* __restrict__ taps, const RecGeo g, const RecAddr ad, int lane,
+    int row0, R2 (&t)[kWRows]) {
+  const int k = lane - g.gu_t;
+  const bool act = (unsigned)(k + g.s) <= (unsigned)(2 * g.s);
+  const int rlo = max(0, g.gv_t - g.s - row0);
+  const int rhi = min(kWRows - 1, g.gv_t + g.s - row0);
+  const int rstep = ad.sv * g.F;
+  // Slice row of register row 0; columns mirrored by su.
+  const R2* __restrict__ p = taps + ad.slice +
+                             (g.s + ad.sv * (row0 - g.gv_t)) * g.F +
+                             (g.s + ad.su * k);
+#pragma unroll
+  for (int r = 0; r < kWRows; ++r) {
+    t[r].x = 0;
+    t[r].y = 0;
+    if (r >= rlo && r <= rhi && act) t[r] = __ldg(p + r * rstep);
+  }
+}
+
+template <typename Real, typename R2>
+__device__ __forceinline__ void mac_record(R2 (&acc)[kWRows],
+                                           const R2 (&t)[kWRows],
+                                           const Coef<Real> cf) {
+#pragma unroll
+  for (int r = 0; r < kWRows; ++r) {
+    acc[r].x = fma(cf.b, t[r].y, fma(cf.a, t[r].x, acc[r].x));
+    acc[r].y = fma(cf.d, t[r].y, fma(cf.c, t[r].x, acc[r].y));
+  }
 }
 
 template <typename Real, bool kCompensate>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, sizeof(Real) == 4 ? 3 : 2)
 k_grid_tiles(GridArgs<Real> a) {
   using R2 = typename Vec2<Real>::type;
-  __shared__ int4 s_geo[kBatch];           // gu_t, gv_t, support, M
+  __shared__ int4 s_geo[kBatch];
   __shared__ Coef<Real> s_coef[kBatch];
-  __shared__ int2 s_addr[kBatch];          // plane base, split packs
+  __shared__ int4 s_addr[kBatch];
+  // Compensated running sums (hi, lo) of each thread's cells: the register
+  // accumulators hold one batch at a time and are folded in after it.
+  __shared__ R2 s_hi[kCompensate ? kWRows : 1][kThreads];
+  __shared__ R2 s_lo[kCompensate ? kWRows : 1][kThreads];
   __shared__ int s_item;
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int row0 = warp * kWRows;
-  const int os = a.view.oversample;
   const int G = a.grid_size;
+  const int omax = a.view.omax;
   const R2* __restrict__ taps = (const R2*)a.view.taps;
   const int tiles_per_grid = a.geom.tiles_u * a.geom.tiles_v;
 
@@ -100,83 +146,85 @@ k_grid_tiles(GridArgs<Real> a) {
     const int u0 = (tl % a.geom.tiles_u) * kTU;
     const int v0 = (tl / a.geom.tiles_u) * kTV;
 
-    R2 acc[kWRows], hi[kWRows], lo[kWRows];
+    R2 acc[kWRows];
 #pragma unroll
     for (int r = 0; r < kWRows; ++r) {
       acc[r].x = acc[r].y = 0;
-      hi[r].x = hi[r].y = 0;
-      lo[r].x = lo[r].y = 0;
+      if constexpr (kCompensate) {
+        s_hi[r][threadIdx.x] = acc[r];
+        s_lo[r][threadIdx.x] = acc[r];
+      }
     }
 
     for (int b0 = item.rec_begin; b0 < item.rec_end; b0 += kBatch) {
       const int nb = min(kBatch, item.rec_end - b0);
-      // ---- stage the batch's record data in shared memory --------------
+      // ---- stage the batch's records ------------------------------------
       if (threadIdx.x < nb) {
         const uint32_t vid = a.rec_vis[b0 + threadIdx.x];
         const uint32_t c = a.cell[vid], m = a.meta[vid];
         const R2 v = a.vw[vid];
         const int plane = meta_plane(m);
+        const int ou = meta_ou(m), ov = meta_ov(m);
+        const int s = a.view.support[plane];
         int4 geo;
         geo.x = cell_u(c) - u0;
         geo.y = cell_v(c) - v0;
-        geo.z = a.view.support[plane];
-        geo.w = a.view.side[plane];
+        geo.z = s;
+        geo.w = 2 * s + 1;
         Coef<Real> cf;
         cf.a = v.x;
         cf.c = v.y;
         if (meta_conj(m)) { cf.b = v.y; cf.d = -v.x; }
         else { cf.b = -v.y; cf.d = v.x; }
-        int2 ad;
-        ad.x = (int)a.view.base[plane];
-        ad.y = (int)(pack_split(meta_ou(m), os) |
-                     (pack_split(meta_ov(m), os) << 16));
+        int4 ad;
+        ad.x = (int)slice_offset(a.view.base[plane], s, omax, abs(ou),
+                                 abs(ov));
+        ad.y = ou < 0 ? -1 : 1;
+        ad.z = ov < 0 ? -1 : 1;
+        ad.w = 0;
         s_geo[threadIdx.x] = geo;
         s_coef[threadIdx.x] = cf;
         s_addr[threadIdx.x] = ad;
       }
       __syncthreads();
-      // ---- accumulate ---------------------------------------------------
-      for (int t = 0; t < nb; ++t) {
-        const int4 geo = s_geo[t];
-        const int s = geo.z;
-        const int jl = max(-s, row0 - geo.y);
-        const int jh = min(s, row0 + kWRows - 1 - geo.y);
-        if (jl > jh) continue;  // warp-uniform: no rows of this warp
-        const Coef<Real> cf = s_coef[t];
-        const int2 ad = s_addr[t];
-        const int k = lane - geo.x;
-        const bool act = (k >= -s) && (k <= s);
-        const int M = geo.w, M2 = M * M;
-        const uint32_t cp = (uint32_t)ad.y & 0xFFFFu, rp = (uint32_t)ad.y >> 16;
-        const int rpu = cp & 15, dpu = (int)((cp >> 4) & 15) - 8;
-        const int rnu = (cp >> 8) & 15, dnu = (int)((cp >> 12) & 15) - 8;
-        const int rpv = rp & 15, dpv = (int)((rp >> 4) & 15) - 8;
-        const int rnv = (rp >> 8) & 15, dnv = (int)((rp >> 12) & 15) - 8;
-        int lanepart;
-        if (k >= -dpu) lanepart = rpu * M2 + (k + dpu);
-        else lanepart = rnu * M2 + (-k + dnu);
-        const R2* __restrict__ tp = taps + ad.x + lanepart;
-#pragma unroll
-        for (int r = 0; r < kWRows; ++r) {
-          const int j = row0 + r - geo.y;
-          if (j >= jl && j <= jh) {
-            int rowpart;
-            if (j >= -dpv) rowpart = rpv * os * M2 + (j + dpv) * M;
-            else rowpart = rnv * os * M2 + (-j + dnv) * M;
-            if (act) {
-              const R2 tap = __ldg(tp + rowpart);
-              acc[r].x = fma(cf.b, tap.y, fma(cf.a, tap.x, acc[r].x));
-              acc[r].y = fma(cf.d, tap.y, fma(cf.c, tap.x, acc[r].y));
-            }
+      // ---- this warp's records: those whose footprint meets its rows ----
+      for (int c0 = 0; c0 < nb; c0 += 32) {
+        bool touch = false;
+        if (c0 + lane < nb) {
+          const int4 g = s_geo[c0 + lane];
+          touch = (g.y - g.z <= row0 + kWRows - 1) && (g.y + g.z >= row0);
+        }
+        uint32_t m = __ballot_sync(0xffffffffu, touch);
+        // Two records at a time: 2*kWRows tap loads in flight per warp.
+        while (m) {
+          const int tA = c0 + __ffs(m) - 1;
+          m &= m - 1;
+          const int tB = m ? c0 + __ffs(m) - 1 : -1;
+          if (m) m &= m - 1;
+          R2 ta[kWRows], tb[kWRows];
+          const int4 gA = s_geo[tA];
+          const int4 aA = s_addr[tA];
+          load_record_taps(taps, RecGeo{gA.x, gA.y, gA.z, gA.w},
+                           RecAddr{aA.x, aA.y, aA.z, aA.w}, lane, row0, ta);
+          if (tB >= 0) {
+            const int4 gB = s_geo[tB];
+            const int4 aB = s_addr[tB];
+            load_record_taps(taps, RecGeo{gB.x, gB.y, gB.z, gB.w},
+                             RecAddr{aB.x, aB.y, aB.z, aB.w}, lane, row0, tb);
           }
+          mac_record<Real>(acc, ta, s_coef[tA]);
+          if (tB >= 0) mac_record<Real>(acc, tb, s_coef[tB]);
         }
       }
       if constexpr (kCompensate) {
 #pragma unroll
         for (int r = 0; r < kWRows; ++r) {
+          R2 hi = s_hi[r][threadIdx.x], lo = s_lo[r][threadIdx.x];
           float s, e;
-          two_sum(hi[r].x, acc[r].x, s, e); hi[r].x = s; lo[r].x += e;
-          two_sum(hi[r].y, acc[r].y, s, e); hi[r].y = s; lo[r].y += e;
+          two_sum(hi.x, acc[r].x, s, e); hi.x = s; lo.x += e;
+          two_sum(hi.y, acc[r].y, s, e); hi.y = s; lo.y += e;
+          s_hi[r][threadIdx.x] = hi;
+          s_lo[r][threadIdx.x] = lo;
           acc[r].x = acc[r].y = 0;
         }
       }
@@ -187,8 +235,9 @@ k_grid_tiles(GridArgs<Real> a) {
 #pragma unroll
     for (int r = 0; r < kWRows; ++r) {
       if constexpr (kCompensate) {
-        out[r].x = hi[r].x + lo[r].x;
-        out[r].y = hi[r].y + lo[r].y;
+        const R2 hi = s_hi[r][threadIdx.x], lo = s_lo[r][threadIdx.x];
+        out[r].x = hi.x + lo.x;
+        out[r].y = hi.y + lo.y;
       } else {
         out[r] = acc[r];
       }

@@ -13,24 +13,28 @@ namespace gg {
 namespace {
 
 
-// One thread per output tap; blockIdx.y is the plane.
+// One thread per output tap; blockIdx.y is the plane.  Output: for each
+// absolute offset class (cu, cv) the (2s+1)^2 slice S[jj][kk] =
+// K[|cv + (jj-s)*os|][|cu + (kk-s)*os|] (see StackView).
 template <typename Real>
 __global__ void k_relayout(const Real* __restrict__ conv, StackView v,
                            typename Vec2<Real>::type* __restrict__ out) {
   using R2 = typename Vec2<Real>::type;
   const int p = blockIdx.y;
   const int os = v.oversample, csh = v.conv_size_half;
-  const long long M = v.side[p];
-  const long long n = (long long)os * os * M * M;
+  const int s = v.support[p];
+  const long long F = 2 * s + 1;
+  const int classes = (v.omax + 1) * (v.omax + 1);
+  const long long n = (long long)classes * F * F;
   const long long base = v.base[p];
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
        e += (long long)gridDim.x * blockDim.x) {
-    const long long mu = e % M;
-    const long long mv = (e / M) % M;
-    const long long ru = (e / (M * M)) % os;
-    const long long rv = e / (M * M * os);
-    const long long t = rv + os * mv;   // row    = |off_v + j*os|
-    const long long c = ru + os * mu;   // column = |off_u + k*os|
+    const int kk = (int)(e % F);
+    const int jj = (int)((e / F) % F);
+    const int cls = (int)(e / (F * F));
+    const int cu = cls / (v.omax + 1), cv = cls % (v.omax + 1);
+    const int t = abs(cv + (jj - s) * os);   // row    = |off_v + j*os|
+    const int c = abs(cu + (kk - s) * os);   // column = |off_u + k*os|
     R2 val;
     if (t < csh && c < csh) {
       const size_t src = (((size_t)p * csh + t) * csh + c) * 2;
