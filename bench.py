@@ -53,6 +53,8 @@ WORKLOAD_TEXT = {
             "w-planes, support 4..72",
     "cfg2b": "SKA-LOW EL82-70 shape: 31,395,840 vis, 8192^2 grid, 339 "
              "w-planes, support 8..44",
+    "cfg2s": "SKA-LOW EL56-82 array with 60 time samples (7,848,960 vis), "
+             "8192^2 grid, 601 w-planes, support 4..72 (profiling size)",
 }
 
 
@@ -66,6 +68,8 @@ def parse_args():
                     choices=sorted(WORKLOAD_TEXT))
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tile-shape", type=int, default=0,
+                    help="force the tile width (32, 16, 8); 0 = automatic")
     return ap.parse_args()
 
 
@@ -263,6 +267,7 @@ def run_ours(args):
 
     stack = pkg.KernelStack.from_workload(wl, "f")
     plan = pkg.Plan()
+    plan.set_tile_shape(args.tile_shape)
     uu, vv, ww = to_dev(wl.uu), to_dev(wl.vv), to_dev(wl.ww)
     vis, weight = to_dev(wl.vis), to_dev(wl.weight)
     G = wl.grid_size

@@ -35,7 +35,8 @@ EXPORTED_SYMBOLS = (
     "oskar_grid_wproj_d", "oskar_grid_wproj_f", "gg_grid_wproj_d",
     "gg_grid_wproj_f", "gg_last_error", "gg_version", "gg_kernels_create_f",
     "gg_kernels_create_d", "gg_kernels_destroy", "gg_plan_create",
-    "gg_plan_destroy", "gg_plan_last_stats", "gg_plan_set_profiling",
+    "gg_plan_destroy", "gg_plan_last_stats", "gg_plan_set_tile_shape",
+    "gg_plan_set_profiling",
     "gg_plan_phase_ms", "gg_measure_fp32_fma_tflops", "gg_grid_wproj_f_device",
     "gg_grid_wproj_d_device", "gg_place_wproj_f_device",
     "gg_place_wproj_d_device", "gg_degrid_wproj_f_device",
@@ -104,6 +105,8 @@ def _declare(L):
     L.gg_plan_destroy.restype = ctypes.c_int
     L.gg_plan_last_stats.argtypes = [_vp, ctypes.POINTER(Stats)]
     L.gg_plan_last_stats.restype = ctypes.c_int
+    L.gg_plan_set_tile_shape.argtypes = [_vp, ctypes.c_int]
+    L.gg_plan_set_tile_shape.restype = ctypes.c_int
     L.gg_plan_set_profiling.argtypes = [_vp, ctypes.c_int]
     L.gg_plan_set_profiling.restype = ctypes.c_int
     L.gg_plan_phase_ms.argtypes = [_vp, ctypes.POINTER(ctypes.c_float),
@@ -290,6 +293,10 @@ class Plan:
         s = Stats()
         _check(lib().gg_plan_last_stats(self.handle, ctypes.byref(s)))
         return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def set_tile_shape(self, tile_u: int = 0) -> None:
+        """Force the tile width (32, 16 or 8); 0 = chosen per call."""
+        _check(lib().gg_plan_set_tile_shape(self.handle, int(tile_u)))
 
     def set_profiling(self, enable: bool = True) -> None:
         _check(lib().gg_plan_set_profiling(self.handle, int(enable)))

@@ -311,6 +311,7 @@ struct gg_plan {
   gg_stats stats{};
   // Phase events (recorded only when profiling is enabled).
   static constexpr int kEvents = 6;
+  int forced_shape = -1;  // tile shape index, -1 = chosen per call
   bool profile = false;
   bool events_valid = false;
   cudaEvent_t ev[kEvents] = {};
@@ -334,6 +335,7 @@ enum Scalar {
   kNumSlots,
   kNumSplit,
   kCounter,
+  kShape,
   kScalarCount
 };
 // 64-bit device scalars live after the 32-bit ones.
@@ -351,9 +353,39 @@ int plan_init(gg_plan* p) {
   return GG_OK;
 }
 
-// Tile shape of this build's gridding kernel (see gg_grid.cu).
-constexpr int kTileU = 32;
-constexpr int kTileV = 64;
+// Tile geometry and sort-key layout for one tile shape (see gg_grid.cu).
+// Key = tile | plane | |offset| class in 32 bits; the low fields shrink
+// (ordering within a tile gets coarser) if the grids have many tiles.
+TileGeom make_geom(int shape, int grid_size, int num_grids,
+                   const gg_kernels* K, int* key_bits) {
+  TileGeom g{};
+  g.tile_u = tile_u_of_shape(shape);
+  g.tile_v = tile_v_of_shape(shape);
+  g.tiles_u = (grid_size + g.tile_u - 1) / g.tile_u;
+  g.tiles_v = (grid_size + g.tile_v - 1) / g.tile_v;
+  g.num_grids = num_grids;
+  const int tile_bits = ceil_log2((unsigned long long)num_grids *
+                                  g.tiles_u * g.tiles_v);
+  int plane_bits = ceil_log2((unsigned long long)K->num_planes);
+  int phase_bits =
+      ceil_log2((unsigned long long)(K->omax + 1) * (K->omax + 1));
+  if (tile_bits + plane_bits + phase_bits > 32) phase_bits = 0;
+  if (tile_bits + plane_bits + phase_bits > 32) plane_bits = 0;
+  g.plane_bits = plane_bits;
+  g.phase_bits = phase_bits;
+  g.phase_side = K->omax + 1;
+  *key_bits = tile_bits + plane_bits + phase_bits;
+  return g;
+}
+
+int max_tiles(int grid_size, int num_grids) {
+  int m = 0;
+  for (int sh = 0; sh < kNumTileShapes; ++sh) {
+    const int tu = tile_u_of_shape(sh), tv = tile_v_of_shape(sh);
+    m = std::max(m, ((grid_size + tu - 1) / tu) * ((grid_size + tv - 1) / tv));
+  }
+  return m * num_grids;
+}
 
 template <typename Real>
 int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
@@ -385,30 +417,10 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
 
   plan->stats = gg_stats{};
   plan->stats.num_points = num_points;
-  plan->stats.tile_u = kTileU;
-  plan->stats.tile_v = kTileV;
   plan->events_valid = false;
 
   const StackView view = K->view();
-  TileGeom geom{};
-  geom.tile_u = kTileU;
-  geom.tile_v = kTileV;
-  geom.tiles_u = (grid_size + kTileU - 1) / kTileU;
-  geom.tiles_v = (grid_size + kTileV - 1) / kTileV;
-  geom.num_grids = 1;
-  const int num_tiles = geom.tiles_u * geom.tiles_v;
-  // Key = tile | plane | |offset| class, in 32 bits; low fields shrink
-  // (ordering within a tile gets coarser) if the grid has many tiles.
-  const int tile_bits = ceil_log2((unsigned long long)num_tiles);
-  int plane_bits = ceil_log2((unsigned long long)K->num_planes);
-  int phase_bits = ceil_log2((unsigned long long)(K->omax + 1) * (K->omax + 1));
-  if (tile_bits + plane_bits + phase_bits > 32) phase_bits = 0;
-  if (tile_bits + plane_bits + phase_bits > 32) plane_bits = 0;
-  geom.plane_bits = plane_bits;
-  geom.phase_bits = phase_bits;
-  geom.phase_side = K->omax + 1;
-  const int low_bits = plane_bits + phase_bits;
-  const int key_bits = tile_bits + low_bits;
+  const int tiles_cap = max_tiles(grid_size, 1);
 
   const size_t n = num_points;
   const int nblk = place_num_blocks(n);
@@ -420,7 +432,7 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   GG_TRY(plan->blk_norm.ensure(nblk * sizeof(double)));
   GG_TRY(plan->blk_skip.ensure(nblk * 8));
   GG_TRY(plan->blk_macs.ensure(nblk * 8));
-  GG_TRY(plan->scan_tmp.ensure(scan_temp_bytes(std::max<size_t>(n, num_tiles))));
+  GG_TRY(plan->scan_tmp.ensure(scan_temp_bytes(std::max<size_t>(n, tiles_cap))));
 
   uint32_t* sc = plan->scalars.as<uint32_t>();
   PlaceParams<Real> pp;
@@ -447,23 +459,33 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   po.blk_norm = plan->blk_norm.as<double>();
   po.blk_skip = plan->blk_skip.as<unsigned long long>();
   po.blk_macs = plan->blk_macs.as<unsigned long long>();
-  GG_CUDA(launch_place<Real>(pp, view, geom, 0, 0, po, s));
+  GG_CUDA(launch_place<Real>(pp, view, TileGeom{}, 0, 0, po, s));
   GG_CUDA(launch_place_finalize(po.blk_norm, po.blk_skip, po.blk_macs, nblk,
-                                d_norm, d_num_skipped, scalar64(plan, kMacs),
-                                s));
+                                n, plan->forced_shape, d_norm, d_num_skipped,
+                                scalar64(plan, kMacs), sc + kShape, s));
+  GG_CUDA(launch_count_records(po.cell, po.meta, n, view, sc + kShape,
+                               po.rec_count, s));
   GG_CUDA(exclusive_scan_u32(po.rec_count, plan->rec_offset.as<uint32_t>(), n,
                              sc + kTotalRecords, plan->scan_tmp.p, s));
-  plan->stats.num_launches = 5;  // place, finalize, 3-kernel scan
+  plan->stats.num_launches = 6;  // place, finalize, count, 3-kernel scan
   plan->mark(1, s);
-  // The one host synchronisation: the record total sizes the sort buffers.
+  // The one host synchronisation: the record total sizes the sort buffers
+  // and the tile shape picks the kernel.
   GG_CUDA(cudaMemcpyAsync(plan->h_scalars, sc, 4 * kScalarCount,
                           cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaMemcpyAsync((char*)plan->h_scalars + 32, scalar64(plan, kMacs),
                           8, cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaStreamSynchronize(s));
   const uint32_t total = plan->h_scalars[kTotalRecords];
+  const int shape = (int)plan->h_scalars[kShape];
   plan->stats.num_records = total;
   memcpy(&plan->stats.num_macs, (char*)plan->h_scalars + 32, 8);
+  int key_bits = 0;
+  const TileGeom geom = make_geom(shape, grid_size, 1, K, &key_bits);
+  const int num_tiles = geom.tiles_u * geom.tiles_v;
+  const int low_bits = geom.plane_bits + geom.phase_bits;
+  plan->stats.tile_u = geom.tile_u;
+  plan->stats.tile_v = geom.tile_v;
   // Record counts per visibility are at most a few dozen, so a 32-bit total
   // can only wrap for inputs far beyond the per-call limit; guard anyway.
   if ((unsigned long long)total > 0xFFFFFFF0ull)
@@ -498,7 +520,7 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
 
     int sms = 0;
     GG_TRY(num_sms_of_current(&sms));
-    const int num_ctas = sms * grid_tiles_ctas_per_sm<Real>();
+    const int num_ctas = sms * grid_tiles_ctas_per_sm<Real>(geom.tile_u);
     const uint32_t chunk = (uint32_t)std::max<unsigned long long>(
         64, ((unsigned long long)total + 4ull * num_ctas - 1) / (4ull * num_ctas));
     const size_t item_cap = (size_t)num_tiles + 8 * (size_t)num_ctas + 16;
@@ -507,7 +529,8 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
     GG_TRY(plan->item_b.ensure((size_t)num_tiles * 4 + 4));
     GG_TRY(plan->items.ensure(item_cap * sizeof(WorkItem)));
     GG_TRY(plan->split_tiles.ensure((size_t)num_tiles * sizeof(int4) + 16));
-    GG_TRY(plan->partials.ensure(slot_cap * kTileU * kTileV * sizeof(R2)));
+    GG_TRY(plan->partials.ensure(slot_cap * geom.tile_u * geom.tile_v *
+                                 sizeof(R2)));
     ItemBuffers ib;
     ib.chunks = plan->item_a.as<uint32_t>();
     ib.split_chunks = plan->item_b.as<uint32_t>();
@@ -792,6 +815,23 @@ GG_API int gg_plan_last_stats(const gg_plan* plan, gg_stats* stats) {
   if (!plan || !stats) return set_error(GG_ERR_INVALID_ARG, "NULL argument");
   *stats = plan->stats;
   return GG_OK;
+}
+
+GG_API int gg_plan_set_tile_shape(gg_plan* plan, int tile_u) {
+  t_last_error.clear();
+  if (!plan) return set_error(GG_ERR_INVALID_ARG, "plan is NULL");
+  if (tile_u == 0) {
+    plan->forced_shape = -1;
+    return GG_OK;
+  }
+  for (int sh = 0; sh < kNumTileShapes; ++sh)
+    if (tile_u_of_shape(sh) == tile_u) {
+      plan->forced_shape = sh;
+      return GG_OK;
+    }
+  return set_error(GG_ERR_INVALID_ARG,
+                   "tile_u = %d: supported tile widths are 32, 16, 8 (0 = "
+                   "automatic)", tile_u);
 }
 
 GG_API int gg_plan_set_profiling(gg_plan* plan, int enable) {

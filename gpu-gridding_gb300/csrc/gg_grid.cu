@@ -1,16 +1,21 @@
 // Tile-owning gridding.
 //
-// The grid is cut into tiles of 32 (u) x TV (v) cells.  After the sort each
-// tile's (visibility, tile) records are contiguous; a tile's record range is
-// cut into work items of at most `chunk` records.  A persistent CTA takes
-// work items from a queue and keeps the item's whole tile in registers: lane
-// l of warp w owns column l and rows w*WROWS .. w*WROWS+WROWS-1.  For every
-// record each warp multiplies the visibility by the kernel taps of its own
-// rows and columns and accumulates -- no atomics, no shared-memory
-// read-modify-write.  A tile with one item is then added to the grid in
-// place with one coalesced read-modify-write; a tile split over several
-// items writes one partial tile per item and k_reduce_partials adds them to
-// the grid in item order, so the result does not depend on scheduling.
+// The grid is cut into tiles of TW (u) x TV (v) cells.  After the sort each
+// tile's (visibility, tile) records are contiguous and ordered by (plane,
+// |offset| class); a tile's record range is cut into work items of at most
+// `chunk` records.  A persistent CTA takes work items from a queue and keeps
+// the item's whole tile in registers: lane (lx, ly) of warp w owns column lx
+// and R consecutive rows of the warp's band.  For every record, each warp
+// whose band meets the footprint multiplies the visibility by the kernel taps
+// of its own cells and accumulates -- no atomics, no shared-memory
+// read-modify-write.  A tile with one item is then added to the grid in place
+// with one coalesced read-modify-write; a tile split over several items
+// writes one partial tile per item and k_reduce_partials adds them to the
+// grid in item order, so the result does not depend on scheduling.
+//
+// Three warp shapes share the 2048-cell tile: TW = 32 (32 x 64 tiles, for
+// large footprints), 16 (16 x 128) and 8 (8 x 256, for small footprints,
+// where a 32-wide warp would leave most lanes outside the footprint).
 //
 // The reference's equivalent is oskar_process_tiles_dynamic
 // (oskar_grid_wproj_gpu.cu:840-1309), a one-warp-per-32x16-tile kernel that
@@ -28,13 +33,19 @@ namespace gg {
 
 namespace {
 
-
-constexpr int kTU = 32;      // tile width = warp width
-constexpr int kWRows = 8;    // rows per warp
-constexpr int kWarps = 8;    // warps per CTA
-constexpr int kTV = kWRows * kWarps;
+constexpr int kRows = 8;       // rows per lane (registers)
+constexpr int kWarps = 8;      // warps per CTA
 constexpr int kThreads = kWarps * 32;
-constexpr int kBatch = kThreads;   // records staged per round
+constexpr int kCells = kThreads * kRows;   // 2048 cells per tile
+constexpr int kBatch = kThreads;           // records staged per round
+
+template <int TW>
+struct WarpShape {
+  static constexpr int kLanesY = 32 / TW;          // lane rows per warp
+  static constexpr int kBand = kLanesY * kRows;    // rows per warp band
+  static constexpr int kTileU = TW;
+  static constexpr int kTileV = kWarps * kBand;
+};
 
 // Visibility coefficients of one record with the conjugation folded in:
 // re += a*t.re + b*t.im, im += c*t.re + d*t.im.
@@ -67,69 +78,68 @@ struct GridArgs {
   typename Vec2<Real>::type* partials;
 };
 
-// Per-record data staged in shared memory once per CTA (the first kBatch
-// threads each prepare one record), then read by every warp with broadcast
-// loads.
-struct RecGeo {           // int4
-  int gu_t, gv_t;         // cell of the visibility relative to the tile
-  int s, F;               // support and slice side 2s+1
+// Per-record data, staged in shared memory once per CTA (the first kBatch
+// threads each prepare one record) and read by every warp with broadcast
+// loads.  With tile-relative cell (row, col), the record's tap for that cell
+// is taps[org + row * rstep + col * su], valid when row is in [vlo, vhi]
+// and col in [ulo, ulo + s2].
+struct RecGeo {   // int4
+  int vlo, vhi;   // footprint rows (tile-relative)
+  int ulo, s2;    // first footprint column (tile-relative), 2 * support
 };
-struct RecAddr {          // int4
-  int slice;              // first tap of the (plane, |offset|) slice
-  int su, sv;             // mirror signs of the slice (offset signs)
+struct RecAddr {  // int4
+  int org;        // tap index of tile cell (0, 0) on the record's slice
+  int rstep;      // +-(2s+1): slice rows per tile row (mirrored for ov < 0)
+  int su;         // +-1: slice columns per tile column (mirrored for ou < 0)
   int pad;
 };
 
-// Loads the kWRows taps of one record for this warp's rows into t[]; taps
-// outside the footprint (rows or lanes) are zero, so the multiply-adds that
-// follow need no predicates.
-template <typename R2>
-__device__ __forceinline__ void load_record_taps(
-    const R2* __restrict__ taps, const RecGeo g, const RecAddr ad, int lane,
-    int row0, R2 (&t)[kWRows]) {
-  const int k = lane - g.gu_t;
-  const bool act = (unsigned)(k + g.s) <= (unsigned)(2 * g.s);
-  const int rlo = max(0, g.gv_t - g.s - row0);
-  const int rhi = min(kWRows - 1, g.gv_t + g.s - row0);
-  const int rstep = ad.sv * g.F;
-  // Slice row of register row 0; columns mirrored by su.
-  const R2* __restrict__ p = taps + ad.slice +
-                             (g.s + ad.sv * (row0 - g.gv_t)) * g.F +
-                             (g.s + ad.su * k);
+template <typename Real, typename R2>
+__device__ __forceinline__ void load_taps(const R2* __restrict__ taps,
+                                          const int4 geo, const int4 adr,
+                                          int lx, int rowl, uint32_t& mask,
+                                          R2 (&t)[kRows]) {
+  const bool colok = (unsigned)(lx - geo.z) <= (unsigned)geo.w;
+  const int lo = max(geo.x - rowl, 0);
+  const int hi = min(geo.y - rowl, kRows - 1);
+  mask = (colok && lo <= hi) ? ((2u << hi) - (1u << lo)) : 0u;
+  const R2* __restrict__ p = taps + (adr.x + rowl * adr.y + lx * adr.z);
 #pragma unroll
-  for (int r = 0; r < kWRows; ++r) {
-    t[r].x = 0;
-    t[r].y = 0;
-    if (r >= rlo && r <= rhi && act) t[r] = __ldg(p + r * rstep);
-  }
+  for (int r = 0; r < kRows; ++r)
+    if (mask & (1u << r)) t[r] = __ldg(p + r * adr.y);
 }
 
 template <typename Real, typename R2>
-__device__ __forceinline__ void mac_record(R2 (&acc)[kWRows],
-                                           const R2 (&t)[kWRows],
-                                           const Coef<Real> cf) {
+__device__ __forceinline__ void mac_taps(R2 (&acc)[kRows],
+                                         const R2 (&t)[kRows], uint32_t mask,
+                                         const Coef<Real> cf) {
 #pragma unroll
-  for (int r = 0; r < kWRows; ++r) {
-    acc[r].x = fma(cf.b, t[r].y, fma(cf.a, t[r].x, acc[r].x));
-    acc[r].y = fma(cf.d, t[r].y, fma(cf.c, t[r].x, acc[r].y));
+  for (int r = 0; r < kRows; ++r) {
+    if (mask & (1u << r)) {
+      acc[r].x = fma(cf.b, t[r].y, fma(cf.a, t[r].x, acc[r].x));
+      acc[r].y = fma(cf.d, t[r].y, fma(cf.c, t[r].x, acc[r].y));
+    }
   }
 }
 
-template <typename Real, bool kCompensate>
+template <typename Real, bool kCompensate, int TW>
 __global__ void __launch_bounds__(kThreads, sizeof(Real) == 4 ? 3 : 2)
 k_grid_tiles(GridArgs<Real> a) {
   using R2 = typename Vec2<Real>::type;
+  using WS = WarpShape<TW>;
   __shared__ int4 s_geo[kBatch];
   __shared__ Coef<Real> s_coef[kBatch];
-  __shared__ int4 s_addr[kBatch];
+  __shared__ int4 s_adr[kBatch];
   // Compensated running sums (hi, lo) of each thread's cells: the register
   // accumulators hold one batch at a time and are folded in after it.
-  __shared__ R2 s_hi[kCompensate ? kWRows : 1][kThreads];
-  __shared__ R2 s_lo[kCompensate ? kWRows : 1][kThreads];
+  __shared__ R2 s_hi[kCompensate ? kRows : 1][kThreads];
+  __shared__ R2 s_lo[kCompensate ? kRows : 1][kThreads];
   __shared__ int s_item;
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int row0 = warp * kWRows;
+  const int lx = lane % TW, ly = lane / TW;
+  const int band0 = warp * WS::kBand;          // first row of the band
+  const int rowl = band0 + ly * kRows;         // this lane's row 0
   const int G = a.grid_size;
   const int omax = a.view.omax;
   const R2* __restrict__ taps = (const R2*)a.view.taps;
@@ -143,12 +153,12 @@ k_grid_tiles(GridArgs<Real> a) {
     const WorkItem item = a.items[it];
     const int gi = item.tile / tiles_per_grid;
     const int tl = item.tile - gi * tiles_per_grid;
-    const int u0 = (tl % a.geom.tiles_u) * kTU;
-    const int v0 = (tl / a.geom.tiles_u) * kTV;
+    const int u0 = (tl % a.geom.tiles_u) * WS::kTileU;
+    const int v0 = (tl / a.geom.tiles_u) * WS::kTileV;
 
-    R2 acc[kWRows];
+    R2 acc[kRows];
 #pragma unroll
-    for (int r = 0; r < kWRows; ++r) {
+    for (int r = 0; r < kRows; ++r) {
       acc[r].x = acc[r].y = 0;
       if constexpr (kCompensate) {
         s_hi[r][threadIdx.x] = acc[r];
@@ -166,59 +176,48 @@ k_grid_tiles(GridArgs<Real> a) {
         const int plane = meta_plane(m);
         const int ou = meta_ou(m), ov = meta_ov(m);
         const int s = a.view.support[plane];
-        int4 geo;
-        geo.x = cell_u(c) - u0;
-        geo.y = cell_v(c) - v0;
-        geo.z = s;
-        geo.w = 2 * s + 1;
+        const int F = 2 * s + 1;
+        const int gu = cell_u(c) - u0, gv = cell_v(c) - v0;
+        const int su = ou < 0 ? -1 : 1, sv = ov < 0 ? -1 : 1;
+        const int slice = (int)slice_offset(a.view.base[plane], s, omax,
+                                            abs(ou), abs(ov));
+        s_geo[threadIdx.x] = make_int4(gv - s, gv + s, gu - s, 2 * s);
+        s_adr[threadIdx.x] = make_int4(
+            slice + (s - sv * gv) * F + (s - su * gu), sv * F, su, 0);
         Coef<Real> cf;
         cf.a = v.x;
         cf.c = v.y;
         if (meta_conj(m)) { cf.b = v.y; cf.d = -v.x; }
         else { cf.b = -v.y; cf.d = v.x; }
-        int4 ad;
-        ad.x = (int)slice_offset(a.view.base[plane], s, omax, abs(ou),
-                                 abs(ov));
-        ad.y = ou < 0 ? -1 : 1;
-        ad.z = ov < 0 ? -1 : 1;
-        ad.w = 0;
-        s_geo[threadIdx.x] = geo;
         s_coef[threadIdx.x] = cf;
-        s_addr[threadIdx.x] = ad;
       }
       __syncthreads();
-      // ---- this warp's records: those whose footprint meets its rows ----
+      // ---- this warp's records: those whose footprint meets its band ----
       for (int c0 = 0; c0 < nb; c0 += 32) {
         bool touch = false;
         if (c0 + lane < nb) {
           const int4 g = s_geo[c0 + lane];
-          touch = (g.y - g.z <= row0 + kWRows - 1) && (g.y + g.z >= row0);
+          touch = (g.x <= band0 + WS::kBand - 1) && (g.y >= band0);
         }
         uint32_t m = __ballot_sync(0xffffffffu, touch);
-        // Two records at a time: 2*kWRows tap loads in flight per warp.
+        // Two records at a time: up to 2*kRows tap loads in flight.
         while (m) {
           const int tA = c0 + __ffs(m) - 1;
           m &= m - 1;
           const int tB = m ? c0 + __ffs(m) - 1 : -1;
           if (m) m &= m - 1;
-          R2 ta[kWRows], tb[kWRows];
-          const int4 gA = s_geo[tA];
-          const int4 aA = s_addr[tA];
-          load_record_taps(taps, RecGeo{gA.x, gA.y, gA.z, gA.w},
-                           RecAddr{aA.x, aA.y, aA.z, aA.w}, lane, row0, ta);
-          if (tB >= 0) {
-            const int4 gB = s_geo[tB];
-            const int4 aB = s_addr[tB];
-            load_record_taps(taps, RecGeo{gB.x, gB.y, gB.z, gB.w},
-                             RecAddr{aB.x, aB.y, aB.z, aB.w}, lane, row0, tb);
-          }
-          mac_record<Real>(acc, ta, s_coef[tA]);
-          if (tB >= 0) mac_record<Real>(acc, tb, s_coef[tB]);
+          R2 ta[kRows], tb[kRows];
+          uint32_t ma, mb = 0;
+          load_taps<Real>(taps, s_geo[tA], s_adr[tA], lx, rowl, ma, ta);
+          if (tB >= 0)
+            load_taps<Real>(taps, s_geo[tB], s_adr[tB], lx, rowl, mb, tb);
+          mac_taps<Real>(acc, ta, ma, s_coef[tA]);
+          if (tB >= 0) mac_taps<Real>(acc, tb, mb, s_coef[tB]);
         }
       }
       if constexpr (kCompensate) {
 #pragma unroll
-        for (int r = 0; r < kWRows; ++r) {
+        for (int r = 0; r < kRows; ++r) {
           R2 hi = s_hi[r][threadIdx.x], lo = s_lo[r][threadIdx.x];
           float s, e;
           two_sum(hi.x, acc[r].x, s, e); hi.x = s; lo.x += e;
@@ -231,9 +230,9 @@ k_grid_tiles(GridArgs<Real> a) {
       __syncthreads();
     }
     // ---- flush ------------------------------------------------------------
-    R2 out[kWRows];
+    R2 out[kRows];
 #pragma unroll
-    for (int r = 0; r < kWRows; ++r) {
+    for (int r = 0; r < kRows; ++r) {
       if constexpr (kCompensate) {
         const R2 hi = s_hi[r][threadIdx.x], lo = s_lo[r][threadIdx.x];
         out[r].x = hi.x + lo.x;
@@ -242,12 +241,12 @@ k_grid_tiles(GridArgs<Real> a) {
         out[r] = acc[r];
       }
     }
-    const int col = u0 + lane;
+    const int col = u0 + lx;
     if (item.slot < 0) {
       R2* g = (R2*)(a.grid + (long long)gi * a.grid_stride);
 #pragma unroll
-      for (int r = 0; r < kWRows; ++r) {
-        const int row = v0 + row0 + r;
+      for (int r = 0; r < kRows; ++r) {
+        const int row = v0 + rowl + r;
         if (row < G && col < G) {
           R2* p = g + (size_t)row * G + col;
           R2 old = *p;
@@ -257,37 +256,45 @@ k_grid_tiles(GridArgs<Real> a) {
         }
       }
     } else {
-      R2* p = a.partials + (size_t)item.slot * (kTU * kTV);
+      // Partial tile, thread-major: entry r * kThreads + thread.
+      R2* p = a.partials + (size_t)item.slot * kCells;
 #pragma unroll
-      for (int r = 0; r < kWRows; ++r) p[(row0 + r) * kTU + lane] = out[r];
+      for (int r = 0; r < kRows; ++r) p[r * kThreads + threadIdx.x] = out[r];
     }
   }
 }
 
-template <typename Real>
+// grid(tile) += sum of the tile's partials in chunk order, accumulated in
+// FP64 and rounded once.  The partial layout is the kernel's thread-major
+// one: entry e = r * kThreads + thread.
+template <typename Real, int TW>
 __global__ void k_reduce_partials(const int4* __restrict__ split_tiles,
                                   const uint32_t* __restrict__ num_split,
                                   const typename Vec2<Real>::type* __restrict__ partials,
                                   TileGeom g, int G, Real* grid,
                                   long long grid_stride) {
   using R2 = typename Vec2<Real>::type;
+  using WS = WarpShape<TW>;
   const int tiles_per_grid = g.tiles_u * g.tiles_v;
   const int n = (int)*num_split;
   for (int st = blockIdx.x; st < n; st += gridDim.x) {
     const int4 d = split_tiles[st];  // tile, first slot, chunks
     const int gi = d.x / tiles_per_grid;
     const int tl = d.x - gi * tiles_per_grid;
-    const int u0 = (tl % g.tiles_u) * kTU;
-    const int v0 = (tl / g.tiles_u) * kTV;
+    const int u0 = (tl % g.tiles_u) * WS::kTileU;
+    const int v0 = (tl / g.tiles_u) * WS::kTileV;
     R2* gp = (R2*)(grid + (long long)gi * grid_stride);
-    for (int cellix = threadIdx.x; cellix < kTU * kTV; cellix += blockDim.x) {
-      const int row = v0 + cellix / kTU, col = u0 + cellix % kTU;
+    for (int e = threadIdx.x; e < kCells; e += blockDim.x) {
+      const int r = e / kThreads, t = e % kThreads;
+      const int w = t >> 5, ln = t & 31;
+      const int row = v0 + w * WS::kBand + (ln / TW) * kRows + r;
+      const int col = u0 + ln % TW;
       if (row >= G || col >= G) continue;
       R2* p = gp + (size_t)row * G + col;
       const R2 old = *p;
       double sx = old.x, sy = old.y;
       for (int c = 0; c < d.z; ++c) {
-        const R2 q = partials[(size_t)(d.y + c) * (kTU * kTV) + cellix];
+        const R2 q = partials[(size_t)(d.y + c) * kCells + e];
         sx += q.x;
         sy += q.y;
       }
@@ -362,6 +369,11 @@ __global__ void k_item_emit(const uint32_t* __restrict__ tile_start,
   }
 }
 
+template <typename Real, int TW>
+void* grid_kernel_ptr() {
+  return (void*)k_grid_tiles<Real, std::is_same<Real, float>::value, TW>;
+}
+
 }  // namespace
 
 cudaError_t launch_tile_bounds(const uint32_t* keys, uint32_t n, int shift,
@@ -384,7 +396,7 @@ cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
   cudaError_t e;
   e = exclusive_scan_u32(A, A, num_tiles, b.num_slots, b.scan_tmp, s);
   if (e != cudaSuccess) return e;
-  // num_items is reused as scratch for B's total until k_item_emit.
+  // The work counter doubles as scratch for B's total until k_item_emit.
   e = exclusive_scan_u32(B, B, num_tiles, b.counter, b.scan_tmp, s);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(b.num_split, 0, sizeof(uint32_t), s);
@@ -399,11 +411,13 @@ cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
 }
 
 template <typename Real>
-int grid_tiles_ctas_per_sm() {
+int grid_tiles_ctas_per_sm(int tile_u) {
+  void* fn = tile_u == 32   ? grid_kernel_ptr<Real, 32>()
+             : tile_u == 16 ? grid_kernel_ptr<Real, 16>()
+                            : grid_kernel_ptr<Real, 8>();
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &n, k_grid_tiles<Real, std::is_same<Real, float>::value>, kThreads,
-          0) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kThreads, 0) !=
+      cudaSuccess)
     n = 1;
   return n < 1 ? 1 : n;
 }
@@ -429,8 +443,13 @@ cudaError_t launch_grid_tiles(const WorkItem* items, const uint32_t* num_items,
   a.grid = grid;
   a.grid_stride = grid_stride;
   a.partials = (typename Vec2<Real>::type*)partials;
-  k_grid_tiles<Real, std::is_same<Real, float>::value>
-      <<<num_ctas, kThreads, 0, s>>>(a);
+  constexpr bool comp = std::is_same<Real, float>::value;
+  switch (geom.tile_u) {
+    case 32: k_grid_tiles<Real, comp, 32><<<num_ctas, kThreads, 0, s>>>(a); break;
+    case 16: k_grid_tiles<Real, comp, 16><<<num_ctas, kThreads, 0, s>>>(a); break;
+    case 8: k_grid_tiles<Real, comp, 8><<<num_ctas, kThreads, 0, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
@@ -442,15 +461,24 @@ cudaError_t launch_reduce_partials(const int4* split_tiles,
                                    long long grid_stride, cudaStream_t s) {
   if (max_split <= 0) return cudaSuccess;
   const int blocks = std::min(max_split, 4096);
-  k_reduce_partials<Real><<<blocks, 256, 0, s>>>(
-      split_tiles, num_split,
-      (const typename Vec2<Real>::type*)partials, geom, grid_size, grid,
-      grid_stride);
+  using P2 = const typename Vec2<Real>::type*;
+  switch (geom.tile_u) {
+    case 32: k_reduce_partials<Real, 32><<<blocks, 256, 0, s>>>(
+        split_tiles, num_split, (P2)partials, geom, grid_size, grid,
+        grid_stride); break;
+    case 16: k_reduce_partials<Real, 16><<<blocks, 256, 0, s>>>(
+        split_tiles, num_split, (P2)partials, geom, grid_size, grid,
+        grid_stride); break;
+    case 8: k_reduce_partials<Real, 8><<<blocks, 256, 0, s>>>(
+        split_tiles, num_split, (P2)partials, geom, grid_size, grid,
+        grid_stride); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
-template int grid_tiles_ctas_per_sm<float>();
-template int grid_tiles_ctas_per_sm<double>();
+template int grid_tiles_ctas_per_sm<float>(int);
+template int grid_tiles_ctas_per_sm<double>(int);
 template cudaError_t launch_grid_tiles<float>(
     const WorkItem*, const uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,

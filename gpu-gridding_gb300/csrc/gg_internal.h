@@ -38,6 +38,16 @@ cudaError_t launch_tap_sums(StackView view, double* d_tap_sum,
                             cudaStream_t s);
 
 // ---- placement and binning (gg_place.cu) ----------------------------------
+// Tile shapes of the gridding kernel: every tile holds 2048 cells, tile_u
+// columns by 2048 / tile_u rows.  Shape index 0, 1, 2 = tile_u 32, 16, 8.
+constexpr int kNumTileShapes = 3;
+__host__ __device__ inline int tile_u_of_shape(int shape) {
+  return 32 >> shape;
+}
+__host__ __device__ inline int tile_v_of_shape(int shape) {
+  return 2048 / (32 >> shape);
+}
+
 struct PlaceOut {
   uint32_t* cell;             // [N]
   uint32_t* meta;             // [N]
@@ -53,13 +63,22 @@ cudaError_t launch_place(PlaceParams<Real> p, StackView view, TileGeom geom,
                          int grid_index, unsigned long long vis_offset,
                          PlaceOut out, cudaStream_t s);
 // Sums the per-block partials: *d_norm += norm, *d_num_skipped = skips,
-// *d_macs = macs (all device pointers).
+// *d_macs = macs (all device pointers), and picks the tile shape for the
+// call into *d_shape: forced_shape if >= 0, else from the mean footprint
+// area (macs / gridded points).
 cudaError_t launch_place_finalize(const double* blk_norm,
                                   const unsigned long long* blk_skip,
                                   const unsigned long long* blk_macs,
-                                  int num_blocks, double* d_norm,
+                                  int num_blocks, unsigned long long n,
+                                  int forced_shape, double* d_norm,
                                   unsigned long long* d_num_skipped,
-                                  unsigned long long* d_macs, cudaStream_t s);
+                                  unsigned long long* d_macs,
+                                  uint32_t* d_shape, cudaStream_t s);
+// count[i] = tiles of shape *d_shape touched by visibility i (0 if skipped).
+cudaError_t launch_count_records(const uint32_t* cell, const uint32_t* meta,
+                                 unsigned long long n, StackView view,
+                                 const uint32_t* d_shape, uint32_t* count,
+                                 cudaStream_t s);
 template <typename Real>
 cudaError_t launch_place_only(PlaceParams<Real> p, StackView view, int* out,
                               cudaStream_t s);
@@ -102,7 +121,7 @@ cudaError_t launch_reduce_partials(const int4* split_tiles,
                                    int grid_size, Real* grid,
                                    long long grid_stride, cudaStream_t s);
 template <typename Real>
-int grid_tiles_ctas_per_sm();
+int grid_tiles_ctas_per_sm(int tile_u);
 
 // ---- FP32 FMA throughput probe (gg_calib.cu) ------------------------------
 cudaError_t measure_fp32_fma(int num_sms, double* tflops_best, float* ms_out);

@@ -39,14 +39,10 @@ k_place(PlaceParams<Real> p, StackView v, TileGeom g, PlaceOut out) {
     ((R2*)out.vw)[i] = vw;
     out.cell[i] = pack_cell(r.gu, r.gv);
     out.meta[i] = pack_meta(r.plane, r.ou, r.ov, r.conj_neg, r.skipped);
-    uint32_t count = 0;
     if (r.skipped) {
       skip = 1;
     } else {
       const int s = r.support;
-      const int tu0 = (r.gu - s) / g.tile_u, tu1 = (r.gu + s) / g.tile_u;
-      const int tv0 = (r.gv - s) / g.tile_v, tv1 = (r.gv + s) / g.tile_v;
-      count = (uint32_t)((tu1 - tu0 + 1) * (tv1 - tv0 + 1));
       const unsigned long long f = 2ull * s + 1;
       macs = f * f;
       const int side = 2 * v.omax + 1;
@@ -55,7 +51,6 @@ k_place(PlaceParams<Real> p, StackView v, TileGeom g, PlaceOut out) {
       // oskar_grid_wproj.c:210: *norm += sum * weight_i (FP64).
       norm = __dmul_rn(ts, (double)w);
     }
-    out.rec_count[i] = count;
   }
   // Block reductions by warp shuffles, then one partial per block; the
   // partials are summed in block order by k_place_finalize, so the norm is
@@ -84,23 +79,69 @@ k_place(PlaceParams<Real> p, StackView v, TileGeom g, PlaceOut out) {
 __global__ void k_place_finalize(const double* __restrict__ blk_norm,
                                  const unsigned long long* __restrict__ blk_skip,
                                  const unsigned long long* __restrict__ blk_macs,
-                                 int num_blocks, double* d_norm,
+                                 int num_blocks, unsigned long long n_points,
+                                 int forced_shape, double* d_norm,
                                  unsigned long long* d_num_skipped,
-                                 unsigned long long* d_macs) {
-  // One warp; lane l sums blocks l, l+32, ... then a fixed-order shuffle
-  // reduction: deterministic.
-  const int lane = threadIdx.x;
+                                 unsigned long long* d_macs,
+                                 uint32_t* d_shape) {
+  // One block; thread t sums blocks t, t+blockDim, ... in order, then a
+  // fixed-shape shuffle and shared-memory tree: the same association on
+  // every run, so the norm is deterministic.
+  __shared__ double s_n[32];
+  __shared__ unsigned long long s_s[32], s_m[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   double n = 0.0;
   unsigned long long s = 0, m = 0;
-  for (int b = lane; b < num_blocks; b += 32) {
+  for (int b = threadIdx.x; b < num_blocks; b += blockDim.x) {
     n += blk_norm[b]; s += blk_skip[b]; m += blk_macs[b];
   }
   n = warp_sum(n); s = warp_sum(s); m = warp_sum(m);
-  if (lane == 0) {
-    if (d_norm) *d_norm += n;
-    if (d_num_skipped) *d_num_skipped = s;
-    if (d_macs) *d_macs = m;
+  if (lane == 0) { s_n[warp] = n; s_s[warp] = s; s_m[warp] = m; }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    n = lane < nw ? s_n[lane] : 0.0;
+    s = lane < nw ? s_s[lane] : 0ull;
+    m = lane < nw ? s_m[lane] : 0ull;
+    n = warp_sum(n); s = warp_sum(s); m = warp_sum(m);
+    if (lane == 0) {
+      if (d_norm) *d_norm += n;
+      if (d_num_skipped) *d_num_skipped = s;
+      if (d_macs) *d_macs = m;
+      // Tile shape: narrow tiles for small footprints, where a 32-wide
+      // warp would leave most lanes outside the footprint.
+      int shape = forced_shape;
+      if (shape < 0) {
+        const unsigned long long gridded = n_points - s;
+        const double side = gridded ? sqrt((double)m / (double)gridded) : 0.0;
+        shape = side >= 40.0 ? 0 : (side >= 18.0 ? 1 : 2);
+      }
+      *d_shape = (uint32_t)shape;
+    }
   }
+}
+
+// Records per visibility: tiles of the chosen shape its footprint touches.
+__global__ void k_count(const uint32_t* __restrict__ cell,
+                        const uint32_t* __restrict__ meta,
+                        unsigned long long n, StackView v,
+                        const uint32_t* __restrict__ d_shape,
+                        uint32_t* __restrict__ count) {
+  const unsigned long long i =
+      (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t m = meta[i];
+  uint32_t c = 0;
+  if (!meta_skipped(m)) {
+    const int shape = (int)*d_shape;
+    const int tw = tile_u_of_shape(shape), th = tile_v_of_shape(shape);
+    const uint32_t ce = cell[i];
+    const int gu = cell_u(ce), gv = cell_v(ce);
+    const int s = v.support[meta_plane(m)];
+    c = (uint32_t)(((gu + s) / tw - (gu - s) / tw + 1) *
+                   ((gv + s) / th - (gv - s) / th + 1));
+  }
+  count[i] = c;
 }
 
 // One thread per visibility writes one record per tile its footprint
@@ -192,11 +233,24 @@ cudaError_t launch_place(PlaceParams<Real> p, StackView view, TileGeom geom,
 cudaError_t launch_place_finalize(const double* blk_norm,
                                   const unsigned long long* blk_skip,
                                   const unsigned long long* blk_macs,
-                                  int num_blocks, double* d_norm,
+                                  int num_blocks, unsigned long long n,
+                                  int forced_shape, double* d_norm,
                                   unsigned long long* d_num_skipped,
-                                  unsigned long long* d_macs, cudaStream_t s) {
-  k_place_finalize<<<1, 32, 0, s>>>(blk_norm, blk_skip, blk_macs, num_blocks,
-                                    d_norm, d_num_skipped, d_macs);
+                                  unsigned long long* d_macs,
+                                  uint32_t* d_shape, cudaStream_t s) {
+  k_place_finalize<<<1, 1024, 0, s>>>(blk_norm, blk_skip, blk_macs,
+                                      num_blocks, n, forced_shape, d_norm,
+                                      d_num_skipped, d_macs, d_shape);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_count_records(const uint32_t* cell, const uint32_t* meta,
+                                 unsigned long long n, StackView view,
+                                 const uint32_t* d_shape, uint32_t* count,
+                                 cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  k_count<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(cell, meta, n, view,
+                                                     d_shape, count);
   return cudaGetLastError();
 }
 

@@ -48,14 +48,24 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x,
   return result;
 }
 
-__global__ void k_scan_reduce(const uint32_t* __restrict__ in, size_t n,
+// Scan input loader (a functor, so other input forms can reuse the
+// kernels).
+struct LoadU32 {
+  const uint32_t* in;
+  __device__ __forceinline__ uint32_t operator()(size_t i) const {
+    return in[i];
+  }
+};
+
+template <typename Load>
+__global__ void k_scan_reduce(Load in, size_t n,
                               uint32_t* __restrict__ block_sums) {
   const size_t base = (size_t)blockIdx.x * kScanTile;
   uint32_t s = 0;
 #pragma unroll
   for (int i = 0; i < kScanItems; ++i) {
     size_t idx = base + (size_t)i * kScanThreads + threadIdx.x;
-    if (idx < n) s += in[idx];
+    if (idx < n) s += in(idx);
   }
   uint32_t total;
   block_exclusive_scan(s, &total);
@@ -77,8 +87,8 @@ __global__ void k_scan_top(uint32_t* __restrict__ sums, size_t nb,
   if (threadIdx.x == 0 && d_total) *d_total = carry;
 }
 
-__global__ void k_scan_down(const uint32_t* __restrict__ in,
-                            uint32_t* __restrict__ out, size_t n,
+template <typename Load>
+__global__ void k_scan_down(Load in, uint32_t* __restrict__ out, size_t n,
                             const uint32_t* __restrict__ block_offsets) {
   __shared__ uint32_t tile[kScanTile];
   const size_t base = (size_t)blockIdx.x * kScanTile;
@@ -87,7 +97,7 @@ __global__ void k_scan_down(const uint32_t* __restrict__ in,
   for (int i = 0; i < kScanItems; ++i) {
     int t = i * kScanThreads + threadIdx.x;
     size_t idx = base + t;
-    tile[t] = idx < n ? in[idx] : 0;
+    tile[t] = idx < n ? in(idx) : 0;
   }
   __syncthreads();
   // Each thread scans its kScanItems consecutive entries.
@@ -200,8 +210,9 @@ size_t scan_temp_bytes(size_t n) {
   return align_up((nb + 1) * sizeof(uint32_t), 256);
 }
 
-cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n,
-                               uint32_t* d_total, void* tmp, cudaStream_t s) {
+template <typename Load>
+static cudaError_t scan_impl(Load in, uint32_t* out, size_t n,
+                             uint32_t* d_total, void* tmp, cudaStream_t s) {
   if (n == 0) {
     if (d_total) return cudaMemsetAsync(d_total, 0, sizeof(uint32_t), s);
     return cudaSuccess;
@@ -212,6 +223,11 @@ cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n,
   k_scan_top<<<1, 1024, 0, s>>>(sums, nb, d_total);
   k_scan_down<<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, sums);
   return cudaGetLastError();
+}
+
+cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n,
+                               uint32_t* d_total, void* tmp, cudaStream_t s) {
+  return scan_impl(LoadU32{in}, out, n, d_total, tmp, s);
 }
 
 size_t radix_temp_bytes(size_t n) {

@@ -246,10 +246,12 @@ def _fit_cell_size(u_max_lambda, grid_size, s_max):
 
 
 def config2(variant: str = "EL56-82", seed: int = 20242,
-            freq_hz: float = 100e6) -> Workload:
+            freq_hz: float = 100e6, num_times: int = 240) -> Workload:
     """SKA-LOW-shaped snapshot: 512 stations, 130,816 baselines x 240 times
     = 31,395,840 visibilities on an 8192^2 grid, unit weights.  Variant
-    "EL56-82": 601 planes, support 4..72; "EL82-70": 339 planes, 8..44."""
+    "EL56-82": 601 planes, support 4..72; "EL82-70": 339 planes, 8..44.
+    num_times < 240 samples the same 4 h track more coarsely (a smaller
+    problem with the same uv density structure)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     if variant == "EL56-82":
         planes, s_min, s_max = 601, 4, 72
@@ -258,7 +260,7 @@ def config2(variant: str = "EL56-82", seed: int = 20242,
     else:
         raise ValueError(variant)
     grid_size = 8192
-    u, v, w = ska_low_uvw_metres(rng)
+    u, v, w = ska_low_uvw_metres(rng, num_times=num_times)
     scale = freq_hz / SPEED_OF_LIGHT
     u *= scale; v *= scale; w *= scale
     u_max = float(max(np.abs(u).max(), np.abs(v).max()))
@@ -310,5 +312,6 @@ WORKLOADS = {
     "cfg1": config1,
     "cfg2": config2,
     "cfg2b": lambda: config2("EL82-70"),
+    "cfg2s": lambda: config2("EL56-82", num_times=60),
     "cfg4": config4,
 }

@@ -136,6 +136,13 @@ typedef struct
 
 GG_API int gg_plan_last_stats(const gg_plan* plan, gg_stats* stats);
 
+/* Tile shape of the gridding kernel for calls made with this plan.  Every
+ * tile holds 2048 cells: tile_u = 32 (32 x 64 cells), 16 (16 x 128) or 8
+ * (8 x 256); 0 (the default) lets each call choose from its mean footprint
+ * (narrow tiles for small supports).  The result of a call depends only on
+ * its inputs and this setting. */
+GG_API int gg_plan_set_tile_shape(gg_plan* plan, int tile_u);
+
 /* Phase timing.  With profiling enabled, every gridding call made with the
  * plan records CUDA events on its stream around five phases:
  *   0 placement (placement, skip/norm reduction, record offsets)

@@ -171,6 +171,42 @@ def test_device_entry_equals_drop_in_and_is_deterministic(pkg, synthetic,
     assert st["num_points"] == wl.num_points and st["num_macs"] > 0
 
 
+@pytest.mark.parametrize("which", ["cfg0", "skalow_small"])
+def test_every_tile_shape_matches_fp64_oracle(pkg, oracle_mod, synthetic,
+                                              torch, which):
+    """Each tile width (32, 16, 8) grids to within 1e-5 of the FP64 oracle;
+    the automatic choice equals one of them bit for bit."""
+    wl = synthetic.config0() if which == "cfg0" else _skalow_small(synthetic)
+    g64, ns64, nm64 = oracle_mod.grid_f_fp64acc(wl)
+    stack = pkg.KernelStack.from_workload(wl, "f")
+    plan = pkg.Plan()
+    grids = {}
+    for tu in (32, 16, 8, 0):
+        plan.set_tile_shape(tu)
+        grid = torch.zeros((wl.grid_size, wl.grid_size, 2),
+                           dtype=torch.float32, device="cuda")
+        norm = torch.zeros(1, dtype=torch.float64, device="cuda")
+        ns = torch.zeros(1, dtype=torch.int64, device="cuda")
+        pkg.grid_wproj_device(plan, stack, _dev(torch, wl.uu),
+                              _dev(torch, wl.vv), _dev(torch, wl.ww),
+                              _dev(torch, wl.vis), _dev(torch, wl.weight),
+                              np.float32(wl.cell_size_rad),
+                              np.float32(wl.w_scale), wl.grid_size, grid,
+                              norm, ns)
+        torch.cuda.synchronize()
+        st = plan.stats()
+        g = grid.cpu().numpy()
+        assert int(ns.item()) == ns64
+        assert abs(norm.item() - nm64) <= 1e-12 * abs(nm64)
+        if tu:
+            assert st["tile_u"] == tu and st["tile_u"] * st["tile_v"] == 2048
+            assert max_rel(g, g64) <= 1e-5, tu
+        grids[tu if tu else ("auto", st["tile_u"])] = g
+    auto_key = next(k for k in grids if isinstance(k, tuple))
+    assert np.array_equal(grids[auto_key].view(np.uint32),
+                          grids[auto_key[1]].view(np.uint32))
+
+
 def test_accumulate_semantics(pkg, synthetic, torch):
     """grid and norm accumulate across calls, num_skipped is set."""
     wl = synthetic.config0().subset(20_000)
