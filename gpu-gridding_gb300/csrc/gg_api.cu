@@ -166,7 +166,8 @@ struct gg_kernels {
   long long total_taps = 0;
   std::vector<int> h_support;
   std::vector<long long> h_base;
-  DevBuf support, base, taps, tap_sum;
+  size_t zero_half_bytes = 0;
+  DevBuf support, base, taps, tap_sum, zeros;
 
   StackView view() const {
     StackView v;
@@ -178,6 +179,7 @@ struct gg_kernels {
     v.base = base.as<long long>();
     v.taps = taps.p;
     v.tap_sum = tap_sum.as<double>();
+    v.zeros = zeros.as<char>() + zero_half_bytes;
     return v;
   }
 };
@@ -239,9 +241,8 @@ int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
   long long total = 0;
   const long long classes = (long long)(k->omax + 1) * (k->omax + 1);
   for (size_t p = 0; p < num_w_planes; ++p) {
-    const long long F = 2LL * support[p] + 1;
     base[p] = total;
-    total += classes * F * F;
+    total += classes * slice_taps(support[p]);
     k->support_max = std::max(k->support_max, support[p]);
   }
   if (total > 0x7fffffffLL)
@@ -250,13 +251,19 @@ int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
                           "indexes at most 2^31-1",
                           total));
   k->total_taps = total;
+  // Zero buffer for lanes outside a footprint: a lane reads kRows = 8 rows
+  // at a stride of up to 2*s_max+1 taps either way from its middle.
+  k->zero_half_bytes = (size_t)8 * (2 * k->support_max + 1) * 2 * sizeof(Real);
   int r;
   if ((r = k->support.ensure(num_w_planes * sizeof(int))) ||
       (r = k->base.ensure(num_w_planes * sizeof(long long))) ||
       (r = k->taps.ensure((size_t)total * 2 * sizeof(Real))) ||
+      (r = k->zeros.ensure(2 * k->zero_half_bytes + 256)) ||
       (r = k->tap_sum.ensure(num_w_planes * (2 * k->omax + 1) *
                              (2 * k->omax + 1) * sizeof(double))))
     return fail(r);
+  if (cudaMemsetAsync(k->zeros.p, 0, k->zeros.bytes, s) != cudaSuccess)
+    return fail(set_error(GG_ERR_CUDA, "zero buffer memset failed"));
   auto cu = [&](cudaError_t e, const char* what) -> int {
     if (e == cudaSuccess) return GG_OK;
     return set_error(GG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
@@ -336,6 +343,7 @@ enum Scalar {
   kNumSplit,
   kCounter,
   kShape,
+  kDeviceError,   // set by a kernel whose bounded wait ran out; sticky
   kScalarCount
 };
 // 64-bit device scalars live after the 32-bit ones.
@@ -349,7 +357,22 @@ unsigned long long* scalar64(gg_plan* p, int i) {
 int plan_init(gg_plan* p) {
   GG_TRY(current_device(&p->device));
   GG_TRY(p->scalars.ensure(kScalar64Offset + kScalar64Count * 8));
+  GG_CUDA(cudaMemset(p->scalars.p, 0, p->scalars.bytes));
   GG_CUDA(cudaMallocHost(&p->h_scalars, 64));
+  return GG_OK;
+}
+
+// The device error flag of a plan (set when a kernel's bounded wait ran
+// out; the call's results are then incomplete).  The stream must be idle.
+int check_device_error(gg_plan* p, cudaStream_t s) {
+  uint32_t flag = 0;
+  GG_CUDA(cudaMemcpyAsync(&flag, p->scalars.as<uint32_t>() + kDeviceError,
+                          4, cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  if (flag)
+    return set_error(GG_ERR_CUDA,
+                     "a gridding kernel's bounded wait ran out; the results "
+                     "of that call are incomplete");
   return GG_OK;
 }
 
@@ -476,6 +499,10 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   GG_CUDA(cudaMemcpyAsync((char*)plan->h_scalars + 32, scalar64(plan, kMacs),
                           8, cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaStreamSynchronize(s));
+  if (plan->h_scalars[kDeviceError])
+    return set_error(GG_ERR_CUDA,
+                     "an earlier call with this plan had a gridding kernel "
+                     "whose bounded wait ran out");
   const uint32_t total = plan->h_scalars[kTotalRecords];
   const int shape = (int)plan->h_scalars[kShape];
   plan->stats.num_records = total;
@@ -545,9 +572,9 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
                                total, chunk, ib, s));
     plan->mark(3, s);
     GG_CUDA(launch_grid_tiles<Real>(
-        ib.items, ib.num_items, ib.counter, vals, po.cell, po.meta, po.vw,
-        view, geom, grid_size, d_grid, 0, plan->partials.as<Real>(), num_ctas,
-        s));
+        ib.items, ib.num_items, ib.counter, sc + kDeviceError, vals, po.cell,
+        po.meta, po.vw, view, geom, grid_size, d_grid, 0,
+        plan->partials.as<Real>(), num_ctas, s));
     plan->mark(4, s);
     GG_CUDA(launch_reduce_partials<Real>(ib.split_tiles, ib.num_split,
                                          num_tiles, plan->partials.as<Real>(),
@@ -668,6 +695,7 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   GG_CUDA(cudaMemcpyAsync(&skip_out, d_skip, sizeof(unsigned long long),
                           cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaStreamSynchronize(s));
+  GG_TRY(check_device_error(plan, s));
   *norm = norm_out;
   *num_skipped = (size_t)skip_out;
   return GG_OK;

@@ -62,7 +62,12 @@ struct Vec2<double> { using type = double2; };
 // so the tap of (j, k) for offsets (ou, ov) is
 //   S_{|ou|,|ov|}[s + sgn(ov)*j][s + sgn(ou)*k].
 // Each slice is contiguous (one bulk copy stages it in shared memory) and a
-// warp whose lanes hold consecutive k reads consecutive words.
+// warp whose lanes hold consecutive k reads consecutive words.  Every slice
+// carries kSlicePad zero rows above and below, so a lane whose kRows
+// consecutive cells straddle the footprint's top or bottom edge reads zeros
+// there instead of testing each row.
+constexpr int kSlicePad = 7;
+
 struct StackView {
   int num_planes;
   int oversample;
@@ -72,14 +77,24 @@ struct StackView {
   const long long* base;    // [P] first tap of plane p (complex units)
   const void* taps;         // float2 or double2
   const double* tap_sum;    // [P][2*omax+1][2*omax+1] sum of Re(tap), FP64
+  const void* zeros;        // middle of a zero buffer that any lane's rows
+                            // (kRows rows of any slice stride) stay inside
 };
 
-// Offset of the slice of plane p for absolute offsets (cu, cv).
+// Taps one slice occupies, padding rows included.
+__host__ __device__ inline long long slice_taps(int s) {
+  const long long F = 2 * s + 1;
+  return (F + 2 * kSlicePad) * F;
+}
+
+// Index of tap S[0][0] of the slice of plane p for absolute offsets
+// (cu, cv) (the padding rows come before it).
 __host__ __device__ inline long long slice_offset(long long plane_base,
                                                   int s, int omax, int cu,
                                                   int cv) {
   const long long F = 2 * s + 1;
-  return plane_base + (long long)(cu * (omax + 1) + cv) * F * F;
+  return plane_base + (long long)(cu * (omax + 1) + cv) * slice_taps(s) +
+         kSlicePad * F;
 }
 
 // ---------------------------------------------------------------------------

@@ -33,11 +33,18 @@ namespace gg {
 
 namespace {
 
-constexpr int kRows = 8;       // rows per lane (registers)
-constexpr int kWarps = 8;      // warps per CTA
-constexpr int kThreads = kWarps * 32;
-constexpr int kCells = kThreads * kRows;   // 2048 cells per tile
-constexpr int kBatch = kThreads;           // records staged per round
+constexpr int kRows = 8;          // rows per lane (registers)
+constexpr int kWarps = 8;         // consumer warps per CTA
+constexpr int kConsumers = kWarps * 32;
+constexpr int kThreads = kConsumers + 32;  // + one producer warp
+constexpr int kCells = kConsumers * kRows; // 2048 cells per tile
+constexpr int kRing = 4;          // record buffers in flight
+constexpr int kBuf = 128;         // records per buffer
+constexpr int kPerLane = kBuf / 32;
+static_assert(kRows - 1 <= kSlicePad, "slices need kRows-1 padding rows");
+// Bound on every mbarrier wait (each failed probe sleeps ~100 ns): a wait
+// that runs out (> ~1 s) sets the error flag and the CTA returns.
+constexpr unsigned kWaitLimit = 1u << 24;
 
 template <int TW>
 struct WarpShape {
@@ -66,6 +73,7 @@ struct GridArgs {
   const WorkItem* items;
   const uint32_t* num_items;
   uint32_t* counter;
+  uint32_t* error;          // set to 1 when a bounded wait runs out
   const uint32_t* rec_vis;
   const uint32_t* cell;
   const uint32_t* meta;
@@ -78,195 +86,325 @@ struct GridArgs {
   typename Vec2<Real>::type* partials;
 };
 
-// Per-record data, staged in shared memory once per CTA (the first kBatch
-// threads each prepare one record) and read by every warp with broadcast
-// loads.  With tile-relative cell (row, col), the record's tap for that cell
-// is taps[org + row * rstep + col * su], valid when row is in [vlo, vhi]
-// and col in [ulo, ulo + s2].
-struct RecGeo {   // int4
-  int vlo, vhi;   // footprint rows (tile-relative)
-  int ulo, s2;    // first footprint column (tile-relative), 2 * support
-};
-struct RecAddr {  // int4
-  int org;        // tap index of tile cell (0, 0) on the record's slice
-  int rstep;      // +-(2s+1): slice rows per tile row (mirrored for ov < 0)
-  int su;         // +-1: slice columns per tile column (mirrored for ou < 0)
-  int pad;
-};
-
-template <typename Real, typename R2>
-__device__ __forceinline__ void load_taps(const R2* __restrict__ taps,
-                                          const int4 geo, const int4 adr,
-                                          int lx, int rowl, uint32_t& mask,
-                                          R2 (&t)[kRows]) {
-  const bool colok = (unsigned)(lx - geo.z) <= (unsigned)geo.w;
-  const int lo = max(geo.x - rowl, 0);
-  const int hi = min(geo.y - rowl, kRows - 1);
-  mask = (colok && lo <= hi) ? ((2u << hi) - (1u << lo)) : 0u;
-  const R2* __restrict__ p = taps + (adr.x + rowl * adr.y + lx * adr.z);
-#pragma unroll
-  for (int r = 0; r < kRows; ++r)
-    if (mask & (1u << r)) t[r] = __ldg(p + r * adr.y);
+// ---- mbarrier helpers (shared::cta) ----------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(count)
+               : "memory");
+}
+// Release-arrive: the caller's earlier shared-memory writes are visible to
+// a thread whose wait observes the phase completion.
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Acquire-wait for the completion of the phase with the given parity;
+// false when the bound runs out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (unsigned i = 0; i < kWaitLimit; ++i) {
+    if (mbar_test(bar, parity)) return true;
+    if (i >= 32) __nanosleep(64);
+  }
+  return false;
 }
 
-template <typename Real, typename R2>
-__device__ __forceinline__ void mac_taps(R2 (&acc)[kRows],
-                                         const R2 (&t)[kRows], uint32_t mask,
-                                         const Coef<Real> cf) {
-#pragma unroll
-  for (int r = 0; r < kRows; ++r) {
-    if (mask & (1u << r)) {
-      acc[r].x = fma(cf.b, t[r].y, fma(cf.a, t[r].x, acc[r].x));
-      acc[r].y = fma(cf.d, t[r].y, fma(cf.c, t[r].x, acc[r].y));
+// Record data in shared memory (int4 per record):
+//   x = org:   tap index of tile cell (0, 0) on the record's slice
+//   y = rstep: +-(2s+1), slice rows per tile row (mirrored for ov < 0)
+//   z = ulo:   first footprint column (tile-relative)
+//   w = su * (2s+1): column mirror sign and footprint width
+// so the record's tap for tile cell (row, col) is
+// taps[org + row * rstep + col * su]; lanes whose column lies outside
+// [ulo, ulo + 2s] read the zero buffer instead.
+//
+// The producer warp: takes work items from the queue and streams their
+// records, staged, through the ring.  Returns false if a wait ran out.
+template <typename Real, int TW>
+__device__ bool produce(const GridArgs<Real>& a, int4 (*s_rec)[kBuf],
+                        Coef<Real> (*s_cf)[kBuf], uint32_t (*s_band)[kBuf],
+                        int4* s_head, uint64_t* full, uint64_t* empty) {
+  using R2 = typename Vec2<Real>::type;
+  using WS = WarpShape<TW>;
+  const int lane = threadIdx.x & 31;
+  const int omax = a.view.omax;
+  const int tiles_per_grid = a.geom.tiles_u * a.geom.tiles_v;
+  const int num_items = (int)*a.num_items;
+  unsigned k = 0;
+  for (;;) {
+    int it = 0;
+    if (lane == 0) it = (int)atomicAdd(a.counter, 1u);
+    it = __shfl_sync(0xffffffffu, it, 0);
+    const bool done = it >= num_items;
+    WorkItem item{0, 0, 0, -1};
+    int u0 = 0, v0 = 0;
+    if (!done) {
+      item = a.items[it];
+      const int tl = item.tile % tiles_per_grid;
+      u0 = (tl % a.geom.tiles_u) * WS::kTileU;
+      v0 = (tl / a.geom.tiles_u) * WS::kTileV;
     }
+    int b0 = item.rec_begin;
+    do {
+      const int slot = (int)(k % kRing);
+      const unsigned use = k / kRing;
+      if (use > 0 && !mbar_wait(&empty[slot], (use - 1) & 1)) return false;
+      int nb = -1;
+      if (!done) {
+        nb = min(kBuf, item.rec_end - b0);
+        // Gather and prepare kPerLane records per lane; the loads of the
+        // records are independent, so they overlap.
+        uint32_t vid[kPerLane], ce[kPerLane], me[kPerLane];
+        R2 v[kPerLane];
+#pragma unroll
+        for (int q = 0; q < kPerLane; ++q) {
+          const int t = q * 32 + lane;
+          vid[q] = t < nb ? a.rec_vis[b0 + t] : 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < kPerLane; ++q) {
+          const int t = q * 32 + lane;
+          if (t < nb) {
+            ce[q] = a.cell[vid[q]];
+            me[q] = a.meta[vid[q]];
+            v[q] = a.vw[vid[q]];
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < kPerLane; ++q) {
+          const int t = q * 32 + lane;
+          if (t < nb) {
+            const uint32_t m = me[q];
+            const int plane = meta_plane(m);
+            const int ou = meta_ou(m), ov = meta_ov(m);
+            const int s = a.view.support[plane];
+            const int F = 2 * s + 1;
+            const int gu = cell_u(ce[q]) - u0, gv = cell_v(ce[q]) - v0;
+            const int su = ou < 0 ? -1 : 1, sv = ov < 0 ? -1 : 1;
+            const int slice = (int)slice_offset(a.view.base[plane], s, omax,
+                                                abs(ou), abs(ov));
+            s_rec[slot][t] = make_int4(
+                slice + (s - sv * gv) * F + (s - su * gu), sv * F, gu - s,
+                su * F);
+            // Bit (warp * kLanesY + lane row) = that lane row's kRows rows
+            // meet the footprint rows [gv - s, gv + s].
+            uint32_t band = 0;
+#pragma unroll
+            for (int g = 0; g < kWarps * WS::kLanesY; ++g) {
+              const int r0 = g * kRows;
+              if (gv - s <= r0 + kRows - 1 && gv + s >= r0) band |= 1u << g;
+            }
+            s_band[slot][t] = band;
+            Coef<Real> cf;
+            cf.a = v[q].x;
+            cf.c = v[q].y;
+            if (meta_conj(m)) { cf.b = v[q].y; cf.d = -v[q].x; }
+            else { cf.b = -v[q].y; cf.d = v[q].x; }
+            s_cf[slot][t] = cf;
+          }
+        }
+      }
+      if (lane == 0) {
+        // item index, record count (-1 = no more work), first/last flags
+        const int flags = done ? 0 : ((b0 == item.rec_begin ? 1 : 0) |
+                                      (b0 + kBuf >= item.rec_end ? 2 : 0));
+        s_head[slot] = make_int4(it, nb, flags, 0);
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&full[slot]);
+      ++k;
+      if (done) return true;
+      b0 += kBuf;
+    } while (b0 < item.rec_end);
   }
 }
 
 template <typename Real, bool kCompensate, int TW>
-__global__ void __launch_bounds__(kThreads, sizeof(Real) == 4 ? 3 : 2)
+__global__ void __launch_bounds__(kThreads, sizeof(Real) == 4 ? 2 : 1)
 k_grid_tiles(GridArgs<Real> a) {
   using R2 = typename Vec2<Real>::type;
   using WS = WarpShape<TW>;
-  __shared__ int4 s_geo[kBatch];
-  __shared__ Coef<Real> s_coef[kBatch];
-  __shared__ int4 s_adr[kBatch];
-  // Compensated running sums (hi, lo) of each thread's cells: the register
-  // accumulators hold one batch at a time and are folded in after it.
-  __shared__ R2 s_hi[kCompensate ? kRows : 1][kThreads];
-  __shared__ R2 s_lo[kCompensate ? kRows : 1][kThreads];
-  __shared__ int s_item;
+  constexpr int G = WS::kLanesY;
+  __shared__ int4 s_rec[kRing][kBuf];
+  __shared__ Coef<Real> s_cf[kRing][kBuf];
+  __shared__ uint32_t s_band[kRing][kBuf];
+  __shared__ int4 s_head[kRing];
+  __shared__ __align__(8) uint64_t s_full[kRing], s_empty[kRing];
+  // Compensated running sums (hi, lo) of each consumer thread's cells: the
+  // register accumulators hold one buffer of records at a time and are
+  // folded in after it.
+  __shared__ R2 s_hi[kCompensate ? kRows : 1][kConsumers];
+  __shared__ R2 s_lo[kCompensate ? kRows : 1][kConsumers];
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kRing; ++i) {
+      mbar_init(&s_full[i], 1);
+      mbar_init(&s_empty[i], kWarps);
+    }
+  }
+  __syncthreads();
+
+  if (warp == kWarps) {
+    if (!produce<Real, TW>(a, s_rec, s_cf, s_band, s_head, s_full, s_empty))
+      atomicExch(a.error, 1u);
+    return;
+  }
+
   const int lx = lane % TW, ly = lane / TW;
-  const int band0 = warp * WS::kBand;          // first row of the band
-  const int rowl = band0 + ly * kRows;         // this lane's row 0
-  const int G = a.grid_size;
-  const int omax = a.view.omax;
+  const int rowl = warp * WS::kBand + ly * kRows;   // this lane's row 0
+  const int G_size = a.grid_size;
   const R2* __restrict__ taps = (const R2*)a.view.taps;
+  const R2* __restrict__ zeros = (const R2*)a.view.zeros;
   const int tiles_per_grid = a.geom.tiles_u * a.geom.tiles_v;
+  const uint32_t my_bit = 1u << (warp * G + ly);
+  const uint32_t warp_bits = ((1u << G) - 1u) << (warp * G);
 
-  for (;;) {
-    if (threadIdx.x == 0) s_item = (int)atomicAdd(a.counter, 1u);
-    __syncthreads();
-    const int it = s_item;
-    if (it >= (int)*a.num_items) break;
-    const WorkItem item = a.items[it];
-    const int gi = item.tile / tiles_per_grid;
-    const int tl = item.tile - gi * tiles_per_grid;
-    const int u0 = (tl % a.geom.tiles_u) * WS::kTileU;
-    const int v0 = (tl / a.geom.tiles_u) * WS::kTileV;
+  R2 acc[kRows];
+#pragma unroll
+  for (int r = 0; r < kRows; ++r) acc[r].x = acc[r].y = 0;
 
-    R2 acc[kRows];
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) {
-      acc[r].x = acc[r].y = 0;
-      if constexpr (kCompensate) {
-        s_hi[r][threadIdx.x] = acc[r];
-        s_lo[r][threadIdx.x] = acc[r];
-      }
+  for (unsigned k = 0;; ++k) {
+    const int slot = (int)(k % kRing);
+    if (!mbar_wait(&s_full[slot], (k / kRing) & 1)) {
+      atomicExch(a.error, 1u);
+      return;
     }
-
-    for (int b0 = item.rec_begin; b0 < item.rec_end; b0 += kBatch) {
-      const int nb = min(kBatch, item.rec_end - b0);
-      // ---- stage the batch's records ------------------------------------
-      if (threadIdx.x < nb) {
-        const uint32_t vid = a.rec_vis[b0 + threadIdx.x];
-        const uint32_t c = a.cell[vid], m = a.meta[vid];
-        const R2 v = a.vw[vid];
-        const int plane = meta_plane(m);
-        const int ou = meta_ou(m), ov = meta_ov(m);
-        const int s = a.view.support[plane];
-        const int F = 2 * s + 1;
-        const int gu = cell_u(c) - u0, gv = cell_v(c) - v0;
-        const int su = ou < 0 ? -1 : 1, sv = ov < 0 ? -1 : 1;
-        const int slice = (int)slice_offset(a.view.base[plane], s, omax,
-                                            abs(ou), abs(ov));
-        s_geo[threadIdx.x] = make_int4(gv - s, gv + s, gu - s, 2 * s);
-        s_adr[threadIdx.x] = make_int4(
-            slice + (s - sv * gv) * F + (s - su * gu), sv * F, su, 0);
-        Coef<Real> cf;
-        cf.a = v.x;
-        cf.c = v.y;
-        if (meta_conj(m)) { cf.b = v.y; cf.d = -v.x; }
-        else { cf.b = -v.y; cf.d = v.x; }
-        s_coef[threadIdx.x] = cf;
-      }
-      __syncthreads();
-      // ---- this warp's records: those whose footprint meets its band ----
-      for (int c0 = 0; c0 < nb; c0 += 32) {
-        bool touch = false;
-        if (c0 + lane < nb) {
-          const int4 g = s_geo[c0 + lane];
-          touch = (g.x <= band0 + WS::kBand - 1) && (g.y >= band0);
-        }
-        uint32_t m = __ballot_sync(0xffffffffu, touch);
-        // Two records at a time: up to 2*kRows tap loads in flight.
-        while (m) {
-          const int tA = c0 + __ffs(m) - 1;
-          m &= m - 1;
-          const int tB = m ? c0 + __ffs(m) - 1 : -1;
-          if (m) m &= m - 1;
-          R2 ta[kRows], tb[kRows];
-          uint32_t ma, mb = 0;
-          load_taps<Real>(taps, s_geo[tA], s_adr[tA], lx, rowl, ma, ta);
-          if (tB >= 0)
-            load_taps<Real>(taps, s_geo[tB], s_adr[tB], lx, rowl, mb, tb);
-          mac_taps<Real>(acc, ta, ma, s_coef[tA]);
-          if (tB >= 0) mac_taps<Real>(acc, tb, mb, s_coef[tB]);
-        }
-      }
-      if constexpr (kCompensate) {
-#pragma unroll
-        for (int r = 0; r < kRows; ++r) {
-          R2 hi = s_hi[r][threadIdx.x], lo = s_lo[r][threadIdx.x];
-          float s, e;
-          two_sum(hi.x, acc[r].x, s, e); hi.x = s; lo.x += e;
-          two_sum(hi.y, acc[r].y, s, e); hi.y = s; lo.y += e;
-          s_hi[r][threadIdx.x] = hi;
-          s_lo[r][threadIdx.x] = lo;
-          acc[r].x = acc[r].y = 0;
-        }
-      }
-      __syncthreads();
-    }
-    // ---- flush ------------------------------------------------------------
-    R2 out[kRows];
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) {
-      if constexpr (kCompensate) {
-        const R2 hi = s_hi[r][threadIdx.x], lo = s_lo[r][threadIdx.x];
-        out[r].x = hi.x + lo.x;
-        out[r].y = hi.y + lo.y;
-      } else {
-        out[r] = acc[r];
-      }
-    }
-    const int col = u0 + lx;
-    if (item.slot < 0) {
-      R2* g = (R2*)(a.grid + (long long)gi * a.grid_stride);
+    const int4 head = s_head[slot];
+    const int nb = head.y;
+    if (nb < 0) break;
+    if (head.z & 1) {  // first buffer of a work item
 #pragma unroll
       for (int r = 0; r < kRows; ++r) {
-        const int row = v0 + rowl + r;
-        if (row < G && col < G) {
-          R2* p = g + (size_t)row * G + col;
-          R2 old = *p;
-          old.x += out[r].x;
-          old.y += out[r].y;
-          *p = old;
+        acc[r].x = acc[r].y = 0;
+        if constexpr (kCompensate) {
+          s_hi[r][threadIdx.x] = acc[r];
+          s_lo[r][threadIdx.x] = acc[r];
         }
       }
-    } else {
-      // Partial tile, thread-major: entry r * kThreads + thread.
-      R2* p = a.partials + (size_t)item.slot * kCells;
-#pragma unroll
-      for (int r = 0; r < kRows; ++r) p[r * kThreads + threadIdx.x] = out[r];
     }
+    // ---- this warp's records: those whose footprint meets its band ------
+    for (int c0 = 0; c0 < nb; c0 += 32) {
+      const bool touch =
+          c0 + lane < nb && (s_band[slot][c0 + lane] & warp_bits) != 0u;
+      uint32_t m = __ballot_sync(0xffffffffu, touch);
+      // Two records at a time: 2*kRows independent tap loads per lane.
+      while (m) {
+        const int tA = c0 + __ffs(m) - 1;
+        m &= m - 1;
+        const int tB = m ? c0 + __ffs(m) - 1 : -1;
+        if (m) m &= m - 1;
+        R2 ta[kRows], tb[kRows];
+        Coef<Real> ca, cb;
+        {
+          const int4 ra = s_rec[slot][tA];
+          const bool ok = (s_band[slot][tA] & my_bit) &&
+                          (unsigned)(lx - ra.z) <= (unsigned)(abs(ra.w) - 1);
+          const R2* p = ok ? taps + (ra.x + rowl * ra.y +
+                                     lx * (ra.w < 0 ? -1 : 1))
+                           : zeros;
+#pragma unroll
+          for (int r = 0; r < kRows; ++r) ta[r] = __ldg(p + r * ra.y);
+          ca = s_cf[slot][tA];
+        }
+        if (tB >= 0) {
+          const int4 rb = s_rec[slot][tB];
+          const bool ok = (s_band[slot][tB] & my_bit) &&
+                          (unsigned)(lx - rb.z) <= (unsigned)(abs(rb.w) - 1);
+          const R2* p = ok ? taps + (rb.x + rowl * rb.y +
+                                     lx * (rb.w < 0 ? -1 : 1))
+                           : zeros;
+#pragma unroll
+          for (int r = 0; r < kRows; ++r) tb[r] = __ldg(p + r * rb.y);
+          cb = s_cf[slot][tB];
+        } else {
+#pragma unroll
+          for (int r = 0; r < kRows; ++r) tb[r].x = tb[r].y = 0;
+          cb.a = cb.b = cb.c = cb.d = 0;
+        }
+#pragma unroll
+        for (int r = 0; r < kRows; ++r) {
+          acc[r].x = fma(ca.b, ta[r].y, fma(ca.a, ta[r].x, acc[r].x));
+          acc[r].y = fma(ca.d, ta[r].y, fma(ca.c, ta[r].x, acc[r].y));
+          acc[r].x = fma(cb.b, tb[r].y, fma(cb.a, tb[r].x, acc[r].x));
+          acc[r].y = fma(cb.d, tb[r].y, fma(cb.c, tb[r].x, acc[r].y));
+        }
+      }
+    }
+    if constexpr (kCompensate) {
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) {
+        R2 hi = s_hi[r][threadIdx.x], lo = s_lo[r][threadIdx.x];
+        float s, e;
+        two_sum(hi.x, acc[r].x, s, e); hi.x = s; lo.x += e;
+        two_sum(hi.y, acc[r].y, s, e); hi.y = s; lo.y += e;
+        s_hi[r][threadIdx.x] = hi;
+        s_lo[r][threadIdx.x] = lo;
+        acc[r].x = acc[r].y = 0;
+      }
+    }
+    if (head.z & 2) {  // last buffer of the work item: flush its tile
+      const WorkItem item = a.items[head.x];
+      const int gi = item.tile / tiles_per_grid;
+      const int tl = item.tile - gi * tiles_per_grid;
+      const int u0 = (tl % a.geom.tiles_u) * WS::kTileU;
+      const int v0 = (tl / a.geom.tiles_u) * WS::kTileV;
+      R2 out[kRows];
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) {
+        if constexpr (kCompensate) {
+          const R2 hi = s_hi[r][threadIdx.x], lo = s_lo[r][threadIdx.x];
+          out[r].x = hi.x + lo.x;
+          out[r].y = hi.y + lo.y;
+        } else {
+          out[r] = acc[r];
+        }
+      }
+      const int col = u0 + lx;
+      if (item.slot < 0) {
+        R2* g = (R2*)(a.grid + (long long)gi * a.grid_stride);
+#pragma unroll
+        for (int r = 0; r < kRows; ++r) {
+          const int row = v0 + rowl + r;
+          if (row < G_size && col < G_size) {
+            R2* p = g + (size_t)row * G_size + col;
+            R2 old = *p;
+            old.x += out[r].x;
+            old.y += out[r].y;
+            *p = old;
+          }
+        }
+      } else {
+        // Partial tile, thread-major: entry r * kConsumers + thread.
+        R2* p = a.partials + (size_t)item.slot * kCells;
+#pragma unroll
+        for (int r = 0; r < kRows; ++r)
+          p[r * kConsumers + threadIdx.x] = out[r];
+      }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&s_empty[slot]);
   }
 }
 
 // grid(tile) += sum of the tile's partials in chunk order, accumulated in
 // FP64 and rounded once.  The partial layout is the kernel's thread-major
-// one: entry e = r * kThreads + thread.
+// one: entry e = r * kConsumers + consumer thread.
 template <typename Real, int TW>
 __global__ void k_reduce_partials(const int4* __restrict__ split_tiles,
                                   const uint32_t* __restrict__ num_split,
@@ -285,7 +423,7 @@ __global__ void k_reduce_partials(const int4* __restrict__ split_tiles,
     const int v0 = (tl / g.tiles_u) * WS::kTileV;
     R2* gp = (R2*)(grid + (long long)gi * grid_stride);
     for (int e = threadIdx.x; e < kCells; e += blockDim.x) {
-      const int r = e / kThreads, t = e % kThreads;
+      const int r = e / kConsumers, t = e % kConsumers;
       const int w = t >> 5, ln = t & 31;
       const int row = v0 + w * WS::kBand + (ln / TW) * kRows + r;
       const int col = u0 + ln % TW;
@@ -424,7 +562,8 @@ int grid_tiles_ctas_per_sm(int tile_u) {
 
 template <typename Real>
 cudaError_t launch_grid_tiles(const WorkItem* items, const uint32_t* num_items,
-                              uint32_t* counter, const uint32_t* rec_vis,
+                              uint32_t* counter, uint32_t* error,
+                              const uint32_t* rec_vis,
                               const uint32_t* cell, const uint32_t* meta,
                               const void* vw, StackView view, TileGeom geom,
                               int grid_size, Real* grid, long long grid_stride,
@@ -433,6 +572,7 @@ cudaError_t launch_grid_tiles(const WorkItem* items, const uint32_t* num_items,
   a.items = items;
   a.num_items = num_items;
   a.counter = counter;
+  a.error = error;
   a.rec_vis = rec_vis;
   a.cell = cell;
   a.meta = meta;
@@ -480,11 +620,11 @@ cudaError_t launch_reduce_partials(const int4* split_tiles,
 template int grid_tiles_ctas_per_sm<float>(int);
 template int grid_tiles_ctas_per_sm<double>(int);
 template cudaError_t launch_grid_tiles<float>(
-    const WorkItem*, const uint32_t*, uint32_t*, const uint32_t*,
+    const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
     float*, long long, float*, int, cudaStream_t);
 template cudaError_t launch_grid_tiles<double>(
-    const WorkItem*, const uint32_t*, uint32_t*, const uint32_t*,
+    const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
     double*, long long, double*, int, cudaStream_t);
 template cudaError_t launch_reduce_partials<float>(const int4*,

@@ -109,7 +109,8 @@ cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
                                ItemBuffers b, cudaStream_t s);
 template <typename Real>
 cudaError_t launch_grid_tiles(const WorkItem* items, const uint32_t* num_items,
-                              uint32_t* counter, const uint32_t* rec_vis,
+                              uint32_t* counter, uint32_t* error,
+                              const uint32_t* rec_vis,
                               const uint32_t* cell, const uint32_t* meta,
                               const void* vw, StackView view, TileGeom geom,
                               int grid_size, Real* grid, long long grid_stride,
