@@ -38,6 +38,7 @@ EXPORTED_SYMBOLS = (
     "gg_plan_destroy", "gg_plan_last_stats", "gg_plan_set_tile_shape",
     "gg_plan_set_profiling",
     "gg_plan_phase_ms", "gg_measure_fp32_fma_tflops", "gg_grid_wproj_f_device",
+    "gg_grid_wproj_f_device_noalloc",
     "gg_grid_wproj_d_device", "gg_place_wproj_f_device",
     "gg_place_wproj_d_device", "gg_degrid_wproj_f_device",
     "gg_degrid_wproj_d_device",

@@ -725,6 +725,27 @@ int place_only(const gg_kernels* K, size_t num_points, const Real* uu,
 }  // namespace
 
 // ===========================================================================
+// Accessors for other translation units of the library (gg_internal.h).
+// ===========================================================================
+namespace gg {
+
+int record_error(int code, const char* message) {
+  return set_error(code, "%s", message);
+}
+
+bool kernels_info(const gg_kernels* k, StackView* view, int* device,
+                  bool* is_double, int* num_planes) {
+  if (!k) return false;
+  *view = k->view();
+  *device = k->device;
+  *is_double = k->is_double;
+  *num_planes = k->num_planes;
+  return true;
+}
+
+}  // namespace gg
+
+// ===========================================================================
 // C ABI
 // ===========================================================================
 extern "C" {

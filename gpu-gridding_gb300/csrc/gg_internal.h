@@ -7,6 +7,8 @@
 
 #include "gg_common.cuh"
 
+struct gg_kernels;  // kernel-stack handle of the C ABI (gg_api.cu)
+
 namespace gg {
 
 // ---- device-wide exclusive scan of uint32 (gg_sort.cu) --------------------
@@ -123,6 +125,13 @@ cudaError_t launch_reduce_partials(const int4* split_tiles,
                                    long long grid_stride, cudaStream_t s);
 template <typename Real>
 int grid_tiles_ctas_per_sm(int tile_u);
+
+// ---- accessors defined in gg_api.cu ---------------------------------------
+// Records a failure for gg_last_error() on this thread; returns code.
+int record_error(int code, const char* message);
+// The device view and properties of a kernel-stack handle.
+bool kernels_info(const gg_kernels* k, StackView* view, int* device,
+                  bool* is_double, int* num_planes);
 
 // ---- FP32 FMA throughput probe (gg_calib.cu) ------------------------------
 cudaError_t measure_fp32_fma(int num_sms, double* tflops_best, float* ms_out);

@@ -179,6 +179,28 @@ GG_API int gg_grid_wproj_d_device(gg_plan* plan, const gg_kernels* kernels,
         unsigned long long* d_num_skipped, double* d_norm, double* d_grid,
         void* stream);
 
+/* Allocation-free form of gg_grid_wproj_f_device, for callers that cannot
+ * allocate device memory while they grid (a real-time loop that must not
+ * stall on cudaMalloc, or code running under another framework's memory
+ * pool).  This entry point has no counterpart in the reference.  All scratch
+ * comes from one 32 MiB device array inside the library, held by every GPU
+ * that loads it until the process exits; nothing is allocated or freed by
+ * the call.  The kernel-stack handle is made beforehand (that step
+ * allocates).  Limits: num_points <= 131072, grid_size <= 8192, and at most
+ * 1048576 (visibility, tile) records; beyond them the call returns
+ * GG_ERR_CAPACITY.  All calls on a device share the array, so calls that
+ * overlap on the GPU race and must be serialised by the caller.  The first
+ * call on each device looks up the array's device address; make it with
+ * that device current and before any stream capture.  Same semantics and
+ * results as gg_grid_wproj_f_device otherwise (grid and *d_norm accumulated,
+ * *d_num_skipped set; one stream synchronisation per call). */
+GG_API int gg_grid_wproj_f_device_noalloc(const gg_kernels* kernels,
+        size_t num_points, const float* d_uu, const float* d_vv,
+        const float* d_ww, const float* d_vis, const float* d_weight,
+        float cell_size_rad, float w_scale, int grid_size,
+        unsigned long long* d_num_skipped, double* d_norm, float* d_grid,
+        void* stream);
+
 /* Placement only (diagnostic): writes, per visibility, six int32 --
  * cell u, cell v, off_u, off_v, w-plane (after the clamp to the last plane)
  * and flags (bit 0 skipped, bit 1 kernel conjugated because ww > 0) --
