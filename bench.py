@@ -70,6 +70,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tile-shape", type=int, default=0,
                     help="force the tile width (32, 16, 8); 0 = automatic")
+    ap.add_argument("--staging", type=int, default=-1,
+                    help="kernel-slice staging: -1 automatic, 0 off, 1 on")
     return ap.parse_args()
 
 
@@ -268,6 +270,7 @@ def run_ours(args):
     stack = pkg.KernelStack.from_workload(wl, "f")
     plan = pkg.Plan()
     plan.set_tile_shape(args.tile_shape)
+    plan.set_slice_staging(args.staging)
     uu, vv, ww = to_dev(wl.uu), to_dev(wl.vv), to_dev(wl.ww)
     vis, weight = to_dev(wl.vis), to_dev(wl.weight)
     G = wl.grid_size

@@ -36,7 +36,7 @@ EXPORTED_SYMBOLS = (
     "gg_grid_wproj_f", "gg_last_error", "gg_version", "gg_kernels_create_f",
     "gg_kernels_create_d", "gg_kernels_destroy", "gg_plan_create",
     "gg_plan_destroy", "gg_plan_last_stats", "gg_plan_set_tile_shape",
-    "gg_plan_set_profiling",
+    "gg_plan_set_slice_staging", "gg_plan_set_profiling",
     "gg_plan_phase_ms", "gg_measure_fp32_fma_tflops", "gg_grid_wproj_f_device",
     "gg_grid_wproj_f_device_noalloc",
     "gg_grid_wproj_d_device", "gg_place_wproj_f_device",
@@ -108,6 +108,8 @@ def _declare(L):
     L.gg_plan_last_stats.restype = ctypes.c_int
     L.gg_plan_set_tile_shape.argtypes = [_vp, ctypes.c_int]
     L.gg_plan_set_tile_shape.restype = ctypes.c_int
+    L.gg_plan_set_slice_staging.argtypes = [_vp, ctypes.c_int]
+    L.gg_plan_set_slice_staging.restype = ctypes.c_int
     L.gg_plan_set_profiling.argtypes = [_vp, ctypes.c_int]
     L.gg_plan_set_profiling.restype = ctypes.c_int
     L.gg_plan_phase_ms.argtypes = [_vp, ctypes.POINTER(ctypes.c_float),
@@ -298,6 +300,10 @@ class Plan:
     def set_tile_shape(self, tile_u: int = 0) -> None:
         """Force the tile width (32, 16 or 8); 0 = chosen per call."""
         _check(lib().gg_plan_set_tile_shape(self.handle, int(tile_u)))
+
+    def set_slice_staging(self, mode: int = -1) -> None:
+        """Kernel-slice staging in shared memory: -1 auto, 0 off, 1 on."""
+        _check(lib().gg_plan_set_slice_staging(self.handle, int(mode)))
 
     def set_profiling(self, enable: bool = True) -> None:
         _check(lib().gg_plan_set_profiling(self.handle, int(enable)))

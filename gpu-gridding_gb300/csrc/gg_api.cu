@@ -319,6 +319,7 @@ struct gg_plan {
   // Phase events (recorded only when profiling is enabled).
   static constexpr int kEvents = 6;
   int forced_shape = -1;  // tile shape index, -1 = chosen per call
+  int forced_stage = -1;  // slice staging 0/1, -1 = chosen per call
   bool profile = false;
   bool events_valid = false;
   cudaEvent_t ev[kEvents] = {};
@@ -504,7 +505,10 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
                      "an earlier call with this plan had a gridding kernel "
                      "whose bounded wait ran out");
   const uint32_t total = plan->h_scalars[kTotalRecords];
-  const int shape = (int)plan->h_scalars[kShape];
+  const int shape = (int)(plan->h_scalars[kShape] & 0xFFu);
+  const bool stage = plan->forced_stage >= 0
+                         ? plan->forced_stage != 0
+                         : ((plan->h_scalars[kShape] >> 8) & 1u) != 0;
   plan->stats.num_records = total;
   memcpy(&plan->stats.num_macs, (char*)plan->h_scalars + 32, 8);
   int key_bits = 0;
@@ -547,7 +551,8 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
 
     int sms = 0;
     GG_TRY(num_sms_of_current(&sms));
-    const int num_ctas = sms * grid_tiles_ctas_per_sm<Real>(geom.tile_u);
+    const int num_ctas =
+        sms * grid_tiles_ctas_per_sm<Real>(geom.tile_u, stage);
     const uint32_t chunk = (uint32_t)std::max<unsigned long long>(
         64, ((unsigned long long)total + 4ull * num_ctas - 1) / (4ull * num_ctas));
     const size_t item_cap = (size_t)num_tiles + 8 * (size_t)num_ctas + 16;
@@ -574,7 +579,7 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
     GG_CUDA(launch_grid_tiles<Real>(
         ib.items, ib.num_items, ib.counter, sc + kDeviceError, vals, po.cell,
         po.meta, po.vw, view, geom, grid_size, d_grid, 0,
-        plan->partials.as<Real>(), num_ctas, s));
+        plan->partials.as<Real>(), num_ctas, stage, s));
     plan->mark(4, s);
     GG_CUDA(launch_reduce_partials<Real>(ib.split_tiles, ib.num_split,
                                          num_tiles, plan->partials.as<Real>(),
@@ -881,6 +886,16 @@ GG_API int gg_plan_set_tile_shape(gg_plan* plan, int tile_u) {
   return set_error(GG_ERR_INVALID_ARG,
                    "tile_u = %d: supported tile widths are 32, 16, 8 (0 = "
                    "automatic)", tile_u);
+}
+
+GG_API int gg_plan_set_slice_staging(gg_plan* plan, int mode) {
+  t_last_error.clear();
+  if (!plan) return set_error(GG_ERR_INVALID_ARG, "plan is NULL");
+  if (mode < -1 || mode > 1)
+    return set_error(GG_ERR_INVALID_ARG,
+                     "mode = %d: -1 (automatic), 0 (off) or 1 (on)", mode);
+  plan->forced_stage = mode;
+  return GG_OK;
 }
 
 GG_API int gg_plan_set_profiling(gg_plan* plan, int enable) {

@@ -81,10 +81,11 @@ struct StackView {
                             // (kRows rows of any slice stride) stay inside
 };
 
-// Taps one slice occupies, padding rows included.
+// Taps one slice occupies: padding rows included, rounded up to an even
+// count so that every slice starts 16-byte aligned (bulk copies need it).
 __host__ __device__ inline long long slice_taps(int s) {
   const long long F = 2 * s + 1;
-  return (F + 2 * kSlicePad) * F;
+  return ((F + 2 * kSlicePad) * F + 1) & ~1LL;
 }
 
 // Index of tap S[0][0] of the slice of plane p for absolute offsets

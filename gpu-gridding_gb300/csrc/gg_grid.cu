@@ -4,14 +4,24 @@
 // tile's (visibility, tile) records are contiguous and ordered by (plane,
 // |offset| class); a tile's record range is cut into work items of at most
 // `chunk` records.  A persistent CTA takes work items from a queue and keeps
-// the item's whole tile in registers: lane (lx, ly) of warp w owns column lx
-// and R consecutive rows of the warp's band.  For every record, each warp
-// whose band meets the footprint multiplies the visibility by the kernel taps
-// of its own cells and accumulates -- no atomics, no shared-memory
-// read-modify-write.  A tile with one item is then added to the grid in place
-// with one coalesced read-modify-write; a tile split over several items
-// writes one partial tile per item and k_reduce_partials adds them to the
-// grid in item order, so the result does not depend on scheduling.
+// the item's whole tile in registers: lane (lx, ly) of consumer warp w owns
+// column lx and kRows consecutive rows of the warp's band.  For every record,
+// each warp whose band meets the footprint multiplies the visibility by the
+// kernel taps of its own cells and accumulates -- no atomics, no
+// shared-memory read-modify-write.  A tile with one item is then added to
+// the grid in place with one coalesced read-modify-write; a tile split over
+// several items writes one partial tile per item and k_reduce_partials adds
+// them to the grid in item order, so the result does not depend on
+// scheduling.
+//
+// The CTA is warp-specialised.  One producer warp takes work items, gathers
+// and prepares their records and streams them through a ring of kRing
+// shared-memory buffers guarded by mbarriers; when a buffer is dominated by
+// one (plane, |offset|) group that is long enough to pay for it, the producer
+// also stages that group's kernel slice into one of kSlots shared-memory
+// slots with a bulk asynchronous copy (cp.async.bulk, completion tracked by
+// the buffer's mbarrier), and those records read their taps from shared
+// memory instead of L2.  Eight consumer warps accumulate.
 //
 // Three warp shapes share the 2048-cell tile: TW = 32 (32 x 64 tiles, for
 // large footprints), 16 (16 x 128) and 8 (8 x 256, for small footprints,
@@ -21,7 +31,7 @@
 // (oskar_grid_wproj_gpu.cu:840-1309), a one-warp-per-32x16-tile kernel that
 // flushes with float atomics whenever its tile changes.
 //
-// FP32 accumulation is compensated: each batch of records is summed in
+// FP32 accumulation is compensated: each buffer of records is summed in
 // plain FP32 FMA, then folded into a (hi, lo) pair by Knuth's TwoSum, so
 // rounding error does not grow with the number of visibilities on a cell.
 #include <algorithm>
@@ -41,6 +51,9 @@ constexpr int kCells = kConsumers * kRows; // 2048 cells per tile
 constexpr int kRing = 4;          // record buffers in flight
 constexpr int kBuf = 128;         // records per buffer
 constexpr int kPerLane = kBuf / 32;
+constexpr int kSlots = 2;         // staged kernel slices
+constexpr int kSliceBytes = 26624;  // per slot: (2s+15)(2s+1) taps, s <= 25 (FP32)
+constexpr int kRunMin = 24;       // records of one group that pay for staging
 static_assert(kRows - 1 <= kSlicePad, "slices need kRows-1 padding rows");
 // Bound on every mbarrier wait (each failed probe sleeps ~100 ns): a wait
 // that runs out (> ~1 s) sets the error flag and the CTA returns.
@@ -86,7 +99,36 @@ struct GridArgs {
   typename Vec2<Real>::type* partials;
 };
 
-// ---- mbarrier helpers (shared::cta) ----------------------------------------
+// Shared-memory layout of one CTA (dynamic shared memory).  Without slice
+// staging the CTA needs about 50 KB, leaving the rest of the SM's unified
+// L1 / shared memory to cache the taps it reads from the global stack.
+template <typename Real, bool kStage>
+struct Smem {
+  using R2 = typename Vec2<Real>::type;
+  static constexpr int kNSlots = kStage ? kSlots : 1;
+  static constexpr int kSliceTaps = kStage ? kSliceBytes / (int)sizeof(R2) : 2;
+  // Largest staged slice width F: (F + 2*kSlicePad) * F <= kSliceTaps.
+  static constexpr int kMaxStagedF = sizeof(Real) == 4 ? 51 : 33;
+  // Zero region for lanes outside a footprint: kRows rows of up to
+  // kMaxStagedF taps either way from its middle.
+  static constexpr int kZeroTaps = kStage ? 2 * kRows * kMaxStagedF + 2 : 2;
+  static constexpr bool kComp = sizeof(Real) == 4;
+  R2 slice[kNSlots][kSliceTaps];
+  R2 zero[kZeroTaps];
+  R2 hi[kComp ? kRows : 1][kConsumers];
+  R2 lo[kComp ? kRows : 1][kConsumers];
+  int4 rec[kRing][kBuf];
+  Coef<Real> cf[kRing][kBuf];
+  uint32_t band[kRing][kBuf];
+  signed char src[kRing][kBuf];   // slice slot of the record, -1 = global
+  int4 head[kRing];
+  uint64_t full[kRing];
+  uint64_t empty[kRing];
+};
+static_assert((51 + 2 * kSlicePad) * 51 <= kSliceBytes / 8, "FP32 slot size");
+static_assert((33 + 2 * kSlicePad) * 33 <= kSliceBytes / 16, "FP64 slot size");
+
+// ---- mbarrier and bulk-copy helpers (shared::cta) --------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
@@ -101,6 +143,14 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile(
       "{\n\t.reg .b64 st;\n\t"
       "mbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar))
+      : "memory");
+}
+// Adds `bytes` of expected asynchronous transactions to the current phase.
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile(
+      "mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "r"(bytes)
       : "memory");
 }
 __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
@@ -123,28 +173,54 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   }
   return false;
 }
+// Bulk copy global -> shared (16-byte aligned, size a multiple of 16),
+// completing `bytes` transactions on `bar`.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src,
+                                              uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
 
 // Record data in shared memory (int4 per record):
-//   x = org:   tap index of tile cell (0, 0) on the record's slice
+//   x = org:   tap index of tile cell (0, 0) on the record's slice -- in the
+//              global stack, or in the slice slot when src >= 0
 //   y = rstep: +-(2s+1), slice rows per tile row (mirrored for ov < 0)
 //   z = ulo:   first footprint column (tile-relative)
 //   w = su * (2s+1): column mirror sign and footprint width
-// so the record's tap for tile cell (row, col) is
-// taps[org + row * rstep + col * su]; lanes whose column lies outside
-// [ulo, ulo + 2s] read the zero buffer instead.
+// so the record's tap for tile cell (row, col) is taps[org + row * rstep +
+// col * su]; lanes whose column lies outside [ulo, ulo + 2s] read zeros.
 //
+// Slice-slot bookkeeping of the producer (lane-uniform).
+struct SlotState {
+  int group[kSlots];       // (plane, |offset| class) held, -1 = none
+  unsigned last_k[kSlots]; // last ring buffer that referenced the slot
+  bool used[kSlots];
+};
+
+__device__ __forceinline__ int group_of(uint32_t meta) {
+  return meta_plane(meta) * 64 + abs(meta_ou(meta)) * 8 + abs(meta_ov(meta));
+}
+
 // The producer warp: takes work items from the queue and streams their
 // records, staged, through the ring.  Returns false if a wait ran out.
-template <typename Real, int TW>
-__device__ bool produce(const GridArgs<Real>& a, int4 (*s_rec)[kBuf],
-                        Coef<Real> (*s_cf)[kBuf], uint32_t (*s_band)[kBuf],
-                        int4* s_head, uint64_t* full, uint64_t* empty) {
+template <typename Real, int TW, bool kStage>
+__device__ bool produce(const GridArgs<Real>& a, Smem<Real, kStage>& sm) {
   using R2 = typename Vec2<Real>::type;
   using WS = WarpShape<TW>;
   const int lane = threadIdx.x & 31;
   const int omax = a.view.omax;
   const int tiles_per_grid = a.geom.tiles_u * a.geom.tiles_v;
   const int num_items = (int)*a.num_items;
+  const R2* __restrict__ taps = (const R2*)a.view.taps;
+  SlotState st;
+  for (int x = 0; x < kSlots; ++x) {
+    st.group[x] = -1;
+    st.last_k[x] = 0;
+    st.used[x] = false;
+  }
   unsigned k = 0;
   for (;;) {
     int it = 0;
@@ -163,14 +239,15 @@ __device__ bool produce(const GridArgs<Real>& a, int4 (*s_rec)[kBuf],
     do {
       const int slot = (int)(k % kRing);
       const unsigned use = k / kRing;
-      if (use > 0 && !mbar_wait(&empty[slot], (use - 1) & 1)) return false;
+      if (use > 0 && !mbar_wait(&sm.empty[slot], (use - 1) & 1)) return false;
       int nb = -1;
       if (!done) {
         nb = min(kBuf, item.rec_end - b0);
-        // Gather and prepare kPerLane records per lane; the loads of the
-        // records are independent, so they overlap.
+        // Gather kPerLane records per lane; their loads are independent,
+        // so they overlap.
         uint32_t vid[kPerLane], ce[kPerLane], me[kPerLane];
         R2 v[kPerLane];
+        int grp[kPerLane];
 #pragma unroll
         for (int q = 0; q < kPerLane; ++q) {
           const int t = q * 32 + lane;
@@ -179,15 +256,89 @@ __device__ bool produce(const GridArgs<Real>& a, int4 (*s_rec)[kBuf],
 #pragma unroll
         for (int q = 0; q < kPerLane; ++q) {
           const int t = q * 32 + lane;
+          ce[q] = 0; me[q] = 0; grp[q] = -2;
           if (t < nb) {
             ce[q] = a.cell[vid[q]];
             me[q] = a.meta[vid[q]];
             v[q] = a.vw[vid[q]];
+            grp[q] = group_of(me[q]);
           }
         }
+        // ---- stage the slices of the buffer's dominant groups ----------
+        // Candidates: the groups of the first and the last record (records
+        // are sorted by group within a tile, so a long run covers one end).
+        if constexpr (kStage) {
+        const int last = nb - 1;
+        int cand[2];
+        uint32_t cand_meta[2];
+        cand[0] = __shfl_sync(0xffffffffu, grp[0], 0);
+        cand_meta[0] = __shfl_sync(0xffffffffu, me[0], 0);
+        {
+          int gl = grp[0];
+          uint32_t ml = me[0];
+#pragma unroll
+          for (int q = 1; q < kPerLane; ++q)
+            if (q == last / 32) { gl = grp[q]; ml = me[q]; }
+          cand[1] = __shfl_sync(0xffffffffu, gl, last % 32);
+          cand_meta[1] = __shfl_sync(0xffffffffu, ml, last % 32);
+        }
+#pragma unroll
+        for (int ci = 0; ci < 2; ++ci) {
+          const int g = cand[ci];
+          if (ci == 1 && g == cand[0]) break;
+          int cnt = 0;
+#pragma unroll
+          for (int q = 0; q < kPerLane; ++q)
+            cnt += __popc(__ballot_sync(0xffffffffu, grp[q] == g));
+          const int plane = meta_plane(cand_meta[ci]);
+          const int s = a.view.support[plane];
+          const long long bytes = slice_taps(s) * (long long)sizeof(R2);
+          bool resident = false;
+          for (int x = 0; x < kSlots; ++x) resident |= st.group[x] == g;
+          if (resident || cnt < kRunMin || bytes > kSliceBytes) continue;
+          // Take the slot used longest ago that the other candidate does
+          // not hold.
+          int x = 0;
+          for (int y = 1; y < kSlots; ++y) {
+            const bool other = st.group[x] == cand[1 - ci];
+            if (other || (st.group[y] != cand[1 - ci] &&
+                          st.last_k[y] < st.last_k[x]))
+              x = y;
+          }
+          // The slot's previous contents may still be read by a buffer in
+          // flight: wait for the consumers to finish it.
+          if (st.used[x] && st.last_k[x] + kRing > k) {
+            const unsigned kk = st.last_k[x];
+            if (!mbar_wait(&sm.empty[kk % kRing], (kk / kRing) & 1))
+              return false;
+          }
+          const long long start =
+              a.view.base[plane] +
+              (long long)(abs(meta_ou(cand_meta[ci])) * (omax + 1) +
+                          abs(meta_ov(cand_meta[ci]))) * slice_taps(s);
+          if (lane == 0) {
+            mbar_expect_tx(&sm.full[slot], (uint32_t)bytes);
+            bulk_copy_g2s(&sm.slice[x][0], taps + start, (uint32_t)bytes,
+                          &sm.full[slot]);
+          }
+          st.group[x] = g;
+          st.used[x] = true;
+          st.last_k[x] = k;
+        }
+        }  // kStage
+        // ---- prepare the records ---------------------------------------
 #pragma unroll
         for (int q = 0; q < kPerLane; ++q) {
           const int t = q * 32 + lane;
+          int src = -1;
+          if constexpr (kStage) {
+            for (int x = 0; x < kSlots; ++x)
+              if (grp[q] == st.group[x]) src = x;
+            // Slots referenced by this buffer stay reserved until it is
+            // done.
+            for (int x = 0; x < kSlots; ++x)
+              if (__any_sync(0xffffffffu, src == x)) st.last_k[x] = k;
+          }
           if (t < nb) {
             const uint32_t m = me[q];
             const int plane = meta_plane(m);
@@ -196,26 +347,31 @@ __device__ bool produce(const GridArgs<Real>& a, int4 (*s_rec)[kBuf],
             const int F = 2 * s + 1;
             const int gu = cell_u(ce[q]) - u0, gv = cell_v(ce[q]) - v0;
             const int su = ou < 0 ? -1 : 1, sv = ov < 0 ? -1 : 1;
-            const int slice = (int)slice_offset(a.view.base[plane], s, omax,
-                                                abs(ou), abs(ov));
-            s_rec[slot][t] = make_int4(
-                slice + (s - sv * gv) * F + (s - su * gu), sv * F, gu - s,
-                su * F);
+            // Tap index of S[0][0] relative to the padded slice start.
+            const int org_rel = kSlicePad * F + (s - sv * gv) * F +
+                                (s - su * gu);
+            int org = org_rel;
+            if (src < 0)
+              org += (int)(a.view.base[plane] +
+                           (long long)(abs(ou) * (omax + 1) + abs(ov)) *
+                               slice_taps(s));
+            sm.rec[slot][t] = make_int4(org, sv * F, gu - s, su * F);
+            sm.src[slot][t] = (signed char)src;
             // Bit (warp * kLanesY + lane row) = that lane row's kRows rows
             // meet the footprint rows [gv - s, gv + s].
             uint32_t band = 0;
 #pragma unroll
-            for (int g = 0; g < kWarps * WS::kLanesY; ++g) {
-              const int r0 = g * kRows;
-              if (gv - s <= r0 + kRows - 1 && gv + s >= r0) band |= 1u << g;
+            for (int gg = 0; gg < kWarps * WS::kLanesY; ++gg) {
+              const int r0 = gg * kRows;
+              if (gv - s <= r0 + kRows - 1 && gv + s >= r0) band |= 1u << gg;
             }
-            s_band[slot][t] = band;
+            sm.band[slot][t] = band;
             Coef<Real> cf;
             cf.a = v[q].x;
             cf.c = v[q].y;
             if (meta_conj(m)) { cf.b = v[q].y; cf.d = -v[q].x; }
             else { cf.b = -v[q].y; cf.d = v[q].x; }
-            s_cf[slot][t] = cf;
+            sm.cf[slot][t] = cf;
           }
         }
       }
@@ -223,10 +379,10 @@ __device__ bool produce(const GridArgs<Real>& a, int4 (*s_rec)[kBuf],
         // item index, record count (-1 = no more work), first/last flags
         const int flags = done ? 0 : ((b0 == item.rec_begin ? 1 : 0) |
                                       (b0 + kBuf >= item.rec_end ? 2 : 0));
-        s_head[slot] = make_int4(it, nb, flags, 0);
+        sm.head[slot] = make_int4(it, nb, flags, 0);
       }
       __syncwarp();
-      if (lane == 0) mbar_arrive(&full[slot]);
+      if (lane == 0) mbar_arrive(&sm.full[slot]);
       ++k;
       if (done) return true;
       b0 += kBuf;
@@ -234,35 +390,60 @@ __device__ bool produce(const GridArgs<Real>& a, int4 (*s_rec)[kBuf],
   }
 }
 
-template <typename Real, bool kCompensate, int TW>
+// Loads the kRows taps of one record for this lane: from the record's
+// slice slot in shared memory, or from the global stack.
+template <typename Real, bool kStage, typename R2>
+__device__ __forceinline__ void load_record(const Smem<Real, kStage>& sm,
+                                            int slot,
+                                            int t, const R2* __restrict__ taps,
+                                            const R2* __restrict__ gzeros,
+                                            uint32_t my_bit, int lx, int rowl,
+                                            R2 (&out)[kRows]) {
+  const int4 ra = sm.rec[slot][t];
+  const int src = kStage ? sm.src[slot][t] : -1;
+  const bool ok = (sm.band[slot][t] & my_bit) &&
+                  (unsigned)(lx - ra.z) <= (unsigned)(abs(ra.w) - 1);
+  const int off = ra.x + rowl * ra.y + lx * (ra.w < 0 ? -1 : 1);
+  if (kStage && src >= 0) {
+    const R2* p = ok ? &sm.slice[src][0] + off
+                     : &sm.zero[Smem<Real, kStage>::kZeroTaps / 2];
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) out[r] = p[r * ra.y];
+  } else {
+    const R2* p = ok ? taps + off : gzeros;
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) out[r] = __ldg(p + r * ra.y);
+  }
+}
+
+template <typename Real, bool kCompensate, int TW, bool kStage>
 __global__ void __launch_bounds__(kThreads, sizeof(Real) == 4 ? 2 : 1)
 k_grid_tiles(GridArgs<Real> a) {
   using R2 = typename Vec2<Real>::type;
   using WS = WarpShape<TW>;
+  using SM = Smem<Real, kStage>;
   constexpr int G = WS::kLanesY;
-  __shared__ int4 s_rec[kRing][kBuf];
-  __shared__ Coef<Real> s_cf[kRing][kBuf];
-  __shared__ uint32_t s_band[kRing][kBuf];
-  __shared__ int4 s_head[kRing];
-  __shared__ __align__(8) uint64_t s_full[kRing], s_empty[kRing];
-  // Compensated running sums (hi, lo) of each consumer thread's cells: the
-  // register accumulators hold one buffer of records at a time and are
-  // folded in after it.
-  __shared__ R2 s_hi[kCompensate ? kRows : 1][kConsumers];
-  __shared__ R2 s_lo[kCompensate ? kRows : 1][kConsumers];
+  extern __shared__ __align__(16) unsigned char g_smem_raw[];
+  SM& sm = *reinterpret_cast<SM*>(g_smem_raw);
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < SM::kZeroTaps; i += blockDim.x) {
+    sm.zero[i].x = 0;
+    sm.zero[i].y = 0;
+  }
   if (threadIdx.x == 0) {
     for (int i = 0; i < kRing; ++i) {
-      mbar_init(&s_full[i], 1);
-      mbar_init(&s_empty[i], kWarps);
+      mbar_init(&sm.full[i], 1);
+      mbar_init(&sm.empty[i], kWarps);
     }
+    // Make the initialised barriers visible to the async proxy (bulk
+    // copies complete transactions on them).
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
 
   if (warp == kWarps) {
-    if (!produce<Real, TW>(a, s_rec, s_cf, s_band, s_head, s_full, s_empty))
-      atomicExch(a.error, 1u);
+    if (!produce<Real, TW, kStage>(a, sm)) atomicExch(a.error, 1u);
     return;
   }
 
@@ -270,7 +451,7 @@ k_grid_tiles(GridArgs<Real> a) {
   const int rowl = warp * WS::kBand + ly * kRows;   // this lane's row 0
   const int G_size = a.grid_size;
   const R2* __restrict__ taps = (const R2*)a.view.taps;
-  const R2* __restrict__ zeros = (const R2*)a.view.zeros;
+  const R2* __restrict__ gzeros = (const R2*)a.view.zeros;
   const int tiles_per_grid = a.geom.tiles_u * a.geom.tiles_v;
   const uint32_t my_bit = 1u << (warp * G + ly);
   const uint32_t warp_bits = ((1u << G) - 1u) << (warp * G);
@@ -281,11 +462,11 @@ k_grid_tiles(GridArgs<Real> a) {
 
   for (unsigned k = 0;; ++k) {
     const int slot = (int)(k % kRing);
-    if (!mbar_wait(&s_full[slot], (k / kRing) & 1)) {
+    if (!mbar_wait(&sm.full[slot], (k / kRing) & 1)) {
       atomicExch(a.error, 1u);
       return;
     }
-    const int4 head = s_head[slot];
+    const int4 head = sm.head[slot];
     const int nb = head.y;
     if (nb < 0) break;
     if (head.z & 1) {  // first buffer of a work item
@@ -293,15 +474,15 @@ k_grid_tiles(GridArgs<Real> a) {
       for (int r = 0; r < kRows; ++r) {
         acc[r].x = acc[r].y = 0;
         if constexpr (kCompensate) {
-          s_hi[r][threadIdx.x] = acc[r];
-          s_lo[r][threadIdx.x] = acc[r];
+          sm.hi[r][threadIdx.x] = acc[r];
+          sm.lo[r][threadIdx.x] = acc[r];
         }
       }
     }
     // ---- this warp's records: those whose footprint meets its band ------
     for (int c0 = 0; c0 < nb; c0 += 32) {
       const bool touch =
-          c0 + lane < nb && (s_band[slot][c0 + lane] & warp_bits) != 0u;
+          c0 + lane < nb && (sm.band[slot][c0 + lane] & warp_bits) != 0u;
       uint32_t m = __ballot_sync(0xffffffffu, touch);
       // Two records at a time: 2*kRows independent tap loads per lane.
       while (m) {
@@ -311,27 +492,13 @@ k_grid_tiles(GridArgs<Real> a) {
         if (m) m &= m - 1;
         R2 ta[kRows], tb[kRows];
         Coef<Real> ca, cb;
-        {
-          const int4 ra = s_rec[slot][tA];
-          const bool ok = (s_band[slot][tA] & my_bit) &&
-                          (unsigned)(lx - ra.z) <= (unsigned)(abs(ra.w) - 1);
-          const R2* p = ok ? taps + (ra.x + rowl * ra.y +
-                                     lx * (ra.w < 0 ? -1 : 1))
-                           : zeros;
-#pragma unroll
-          for (int r = 0; r < kRows; ++r) ta[r] = __ldg(p + r * ra.y);
-          ca = s_cf[slot][tA];
-        }
+        load_record<Real, kStage>(sm, slot, tA, taps, gzeros, my_bit, lx,
+                                  rowl, ta);
+        ca = sm.cf[slot][tA];
         if (tB >= 0) {
-          const int4 rb = s_rec[slot][tB];
-          const bool ok = (s_band[slot][tB] & my_bit) &&
-                          (unsigned)(lx - rb.z) <= (unsigned)(abs(rb.w) - 1);
-          const R2* p = ok ? taps + (rb.x + rowl * rb.y +
-                                     lx * (rb.w < 0 ? -1 : 1))
-                           : zeros;
-#pragma unroll
-          for (int r = 0; r < kRows; ++r) tb[r] = __ldg(p + r * rb.y);
-          cb = s_cf[slot][tB];
+          load_record<Real, kStage>(sm, slot, tB, taps, gzeros, my_bit, lx,
+                                    rowl, tb);
+          cb = sm.cf[slot][tB];
         } else {
 #pragma unroll
           for (int r = 0; r < kRows; ++r) tb[r].x = tb[r].y = 0;
@@ -349,12 +516,12 @@ k_grid_tiles(GridArgs<Real> a) {
     if constexpr (kCompensate) {
 #pragma unroll
       for (int r = 0; r < kRows; ++r) {
-        R2 hi = s_hi[r][threadIdx.x], lo = s_lo[r][threadIdx.x];
+        R2 hi = sm.hi[r][threadIdx.x], lo = sm.lo[r][threadIdx.x];
         float s, e;
         two_sum(hi.x, acc[r].x, s, e); hi.x = s; lo.x += e;
         two_sum(hi.y, acc[r].y, s, e); hi.y = s; lo.y += e;
-        s_hi[r][threadIdx.x] = hi;
-        s_lo[r][threadIdx.x] = lo;
+        sm.hi[r][threadIdx.x] = hi;
+        sm.lo[r][threadIdx.x] = lo;
         acc[r].x = acc[r].y = 0;
       }
     }
@@ -368,7 +535,7 @@ k_grid_tiles(GridArgs<Real> a) {
 #pragma unroll
       for (int r = 0; r < kRows; ++r) {
         if constexpr (kCompensate) {
-          const R2 hi = s_hi[r][threadIdx.x], lo = s_lo[r][threadIdx.x];
+          const R2 hi = sm.hi[r][threadIdx.x], lo = sm.lo[r][threadIdx.x];
           out[r].x = hi.x + lo.x;
           out[r].y = hi.y + lo.y;
         } else {
@@ -398,7 +565,7 @@ k_grid_tiles(GridArgs<Real> a) {
       }
     }
     __syncwarp();
-    if (lane == 0) mbar_arrive(&s_empty[slot]);
+    if (lane == 0) mbar_arrive(&sm.empty[slot]);
   }
 }
 
@@ -507,9 +674,33 @@ __global__ void k_item_emit(const uint32_t* __restrict__ tile_start,
   }
 }
 
-template <typename Real, int TW>
+template <typename Real, int TW, bool kStage>
 void* grid_kernel_ptr() {
-  return (void*)k_grid_tiles<Real, std::is_same<Real, float>::value, TW>;
+  return (void*)k_grid_tiles<Real, std::is_same<Real, float>::value, TW,
+                             kStage>;
+}
+
+// The kernels take more than 48 KB of dynamic shared memory: opt in before
+// querying occupancy or launching.
+template <typename Real, int TW, bool kStage>
+cudaError_t prepare_grid_kernel(void** fn, size_t* smem) {
+  *fn = grid_kernel_ptr<Real, TW, kStage>();
+  *smem = sizeof(Smem<Real, kStage>);
+  return cudaFuncSetAttribute(*fn,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)*smem);
+}
+
+template <typename Real>
+cudaError_t prepare_grid_kernel_for(int tile_u, bool stage, void** fn,
+                                    size_t* smem) {
+  if (stage)
+    return tile_u == 32   ? prepare_grid_kernel<Real, 32, true>(fn, smem)
+           : tile_u == 16 ? prepare_grid_kernel<Real, 16, true>(fn, smem)
+                          : prepare_grid_kernel<Real, 8, true>(fn, smem);
+  return tile_u == 32   ? prepare_grid_kernel<Real, 32, false>(fn, smem)
+         : tile_u == 16 ? prepare_grid_kernel<Real, 16, false>(fn, smem)
+                        : prepare_grid_kernel<Real, 8, false>(fn, smem);
 }
 
 }  // namespace
@@ -549,13 +740,14 @@ cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
 }
 
 template <typename Real>
-int grid_tiles_ctas_per_sm(int tile_u) {
-  void* fn = tile_u == 32   ? grid_kernel_ptr<Real, 32>()
-             : tile_u == 16 ? grid_kernel_ptr<Real, 16>()
-                            : grid_kernel_ptr<Real, 8>();
+int grid_tiles_ctas_per_sm(int tile_u, bool stage) {
+  void* fn = nullptr;
+  size_t smem = 0;
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kThreads, 0) !=
-      cudaSuccess)
+  if (prepare_grid_kernel_for<Real>(tile_u, stage, &fn, &smem) !=
+          cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kThreads,
+                                                    smem) != cudaSuccess)
     n = 1;
   return n < 1 ? 1 : n;
 }
@@ -567,7 +759,8 @@ cudaError_t launch_grid_tiles(const WorkItem* items, const uint32_t* num_items,
                               const uint32_t* cell, const uint32_t* meta,
                               const void* vw, StackView view, TileGeom geom,
                               int grid_size, Real* grid, long long grid_stride,
-                              Real* partials, int num_ctas, cudaStream_t s) {
+                              Real* partials, int num_ctas, bool stage,
+                              cudaStream_t s) {
   GridArgs<Real> a;
   a.items = items;
   a.num_items = num_items;
@@ -583,14 +776,15 @@ cudaError_t launch_grid_tiles(const WorkItem* items, const uint32_t* num_items,
   a.grid = grid;
   a.grid_stride = grid_stride;
   a.partials = (typename Vec2<Real>::type*)partials;
-  constexpr bool comp = std::is_same<Real, float>::value;
-  switch (geom.tile_u) {
-    case 32: k_grid_tiles<Real, comp, 32><<<num_ctas, kThreads, 0, s>>>(a); break;
-    case 16: k_grid_tiles<Real, comp, 16><<<num_ctas, kThreads, 0, s>>>(a); break;
-    case 8: k_grid_tiles<Real, comp, 8><<<num_ctas, kThreads, 0, s>>>(a); break;
-    default: return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
+  if (geom.tile_u != 32 && geom.tile_u != 16 && geom.tile_u != 8)
+    return cudaErrorInvalidValue;
+  void* fn = nullptr;
+  size_t smem = 0;
+  cudaError_t e = prepare_grid_kernel_for<Real>(geom.tile_u, stage, &fn,
+                                                &smem);
+  if (e != cudaSuccess) return e;
+  void* args[] = {&a};
+  return cudaLaunchKernel(fn, dim3(num_ctas), dim3(kThreads), args, smem, s);
 }
 
 template <typename Real>
@@ -617,16 +811,16 @@ cudaError_t launch_reduce_partials(const int4* split_tiles,
   return cudaGetLastError();
 }
 
-template int grid_tiles_ctas_per_sm<float>(int);
-template int grid_tiles_ctas_per_sm<double>(int);
+template int grid_tiles_ctas_per_sm<float>(int, bool);
+template int grid_tiles_ctas_per_sm<double>(int, bool);
 template cudaError_t launch_grid_tiles<float>(
     const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
-    float*, long long, float*, int, cudaStream_t);
+    float*, long long, float*, int, bool, cudaStream_t);
 template cudaError_t launch_grid_tiles<double>(
     const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
-    double*, long long, double*, int, cudaStream_t);
+    double*, long long, double*, int, bool, cudaStream_t);
 template cudaError_t launch_reduce_partials<float>(const int4*,
                                                    const uint32_t*, int,
                                                    const float*, TileGeom, int,

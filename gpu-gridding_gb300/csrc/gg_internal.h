@@ -116,15 +116,17 @@ cudaError_t launch_grid_tiles(const WorkItem* items, const uint32_t* num_items,
                               const uint32_t* cell, const uint32_t* meta,
                               const void* vw, StackView view, TileGeom geom,
                               int grid_size, Real* grid, long long grid_stride,
-                              Real* partials, int num_ctas, cudaStream_t s);
+                              Real* partials, int num_ctas, bool stage,
+                              cudaStream_t s);
 template <typename Real>
 cudaError_t launch_reduce_partials(const int4* split_tiles,
                                    const uint32_t* num_split, int max_split,
                                    const Real* partials, TileGeom geom,
                                    int grid_size, Real* grid,
                                    long long grid_stride, cudaStream_t s);
+// stage: the kernel variant that stages kernel slices in shared memory.
 template <typename Real>
-int grid_tiles_ctas_per_sm(int tile_u);
+int grid_tiles_ctas_per_sm(int tile_u, bool stage);
 
 // ---- accessors defined in gg_api.cu ---------------------------------------
 // Records a failure for gg_last_error() on this thread; returns code.

@@ -214,7 +214,7 @@ extern "C" GG_API int gg_grid_wproj_f_device_noalloc(
                         "its bounded wait; that call's grid is incomplete");
   }
   const uint32_t total = host_sc[0];
-  const int shape = (int)host_sc[5];
+  const int shape = (int)(host_sc[5] & 0xFFu);
   if (total > kNoAllocMaxRecords)
     return record_error(GG_ERR_CAPACITY,
                         "the call needs more (visibility, tile) records than "
@@ -252,7 +252,7 @@ extern "C" GG_API int gg_grid_wproj_f_device_noalloc(
                              s));
   int sms = 0;
   NA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int num_ctas = sms * grid_tiles_ctas_per_sm<float>(geom.tile_u);
+  const int num_ctas = sms * grid_tiles_ctas_per_sm<float>(geom.tile_u, false);
   // At most kNoAllocMaxSlots / 2 chunks' worth of split tiles: split
   // chunks <= 2 * total / chunk <= kNoAllocMaxSlots.
   const uint32_t chunk = (uint32_t)std::max<unsigned long long>(
@@ -271,7 +271,7 @@ extern "C" GG_API int gg_grid_wproj_f_device_noalloc(
   NA_CUDA(launch_build_items(tile_start, num_tiles, total, chunk, ib, s));
   NA_CUDA(launch_grid_tiles<float>(items, sc + 1, sc + 4, sc + 6, vals, cell,
                                    meta, vw, view, geom, grid_size, d_grid, 0,
-                                   (float*)partials, num_ctas, s));
+                                   (float*)partials, num_ctas, false, s));
   NA_CUDA(launch_reduce_partials<float>(split_tiles, sc + 3, num_tiles,
                                         (const float*)partials, geom,
                                         grid_size, d_grid, 0, s));

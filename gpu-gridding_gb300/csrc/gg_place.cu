@@ -108,15 +108,18 @@ __global__ void k_place_finalize(const double* __restrict__ blk_norm,
       if (d_norm) *d_norm += n;
       if (d_num_skipped) *d_num_skipped = s;
       if (d_macs) *d_macs = m;
-      // Tile shape: narrow tiles for small footprints, where a 32-wide
-      // warp would leave most lanes outside the footprint.
+      // Tile shape from the mean footprint side: narrow tiles only for tiny
+      // footprints, where a 32-wide warp would leave most lanes outside
+      // them.  Kernel slices are staged in shared memory (bit 8) when
+      // footprints are small enough for their slices to fit the slots;
+      // otherwise the kernel keeps its shared memory small so the L1 cache
+      // serves the tap loads.
+      const unsigned long long gridded = n_points - s;
+      const double side = gridded ? sqrt((double)m / (double)gridded) : 0.0;
       int shape = forced_shape;
-      if (shape < 0) {
-        const unsigned long long gridded = n_points - s;
-        const double side = gridded ? sqrt((double)m / (double)gridded) : 0.0;
-        shape = side >= 40.0 ? 0 : (side >= 18.0 ? 1 : 2);
-      }
-      *d_shape = (uint32_t)shape;
+      if (shape < 0) shape = side >= 16.0 ? 0 : (side >= 8.0 ? 1 : 2);
+      const uint32_t stage = side < 40.0 ? 1u : 0u;
+      *d_shape = (uint32_t)shape | (stage << 8);
     }
   }
 }
@@ -133,7 +136,7 @@ __global__ void k_count(const uint32_t* __restrict__ cell,
   const uint32_t m = meta[i];
   uint32_t c = 0;
   if (!meta_skipped(m)) {
-    const int shape = (int)*d_shape;
+    const int shape = (int)(*d_shape & 0xFFu);
     const int tw = tile_u_of_shape(shape), th = tile_v_of_shape(shape);
     const uint32_t ce = cell[i];
     const int gu = cell_u(ce), gv = cell_v(ce);

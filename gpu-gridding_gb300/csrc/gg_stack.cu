@@ -25,19 +25,21 @@ __global__ void k_relayout(const Real* __restrict__ conv, StackView v,
   const int s = v.support[p];
   const long long F = 2 * s + 1;
   const long long rows = F + 2 * kSlicePad;   // padded slice rows
+  const long long stride = slice_taps(s);     // >= rows * F, even
   const int classes = (v.omax + 1) * (v.omax + 1);
-  const long long n = (long long)classes * rows * F;
+  const long long n = (long long)classes * stride;
   const long long base = v.base[p];
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
        e += (long long)gridDim.x * blockDim.x) {
-    const int kk = (int)(e % F);
-    const int jj = (int)((e / F) % rows) - kSlicePad;
-    const int cls = (int)(e / (rows * F));
+    const long long rem = e % stride;
+    const int kk = (int)(rem % F);
+    const int jj = (int)(rem / F) - kSlicePad;
+    const int cls = (int)(e / stride);
     const int cu = cls / (v.omax + 1), cv = cls % (v.omax + 1);
     const int t = abs(cv + (jj - s) * os);   // row    = |off_v + j*os|
     const int c = abs(cu + (kk - s) * os);   // column = |off_u + k*os|
     R2 val;
-    if (jj >= 0 && jj < F && t < csh && c < csh) {
+    if (rem < rows * F && jj >= 0 && jj < F && t < csh && c < csh) {
       const size_t src = (((size_t)p * csh + t) * csh + c) * 2;
       val.x = conv[src];
       val.y = conv[src + 1];

@@ -143,6 +143,13 @@ GG_API int gg_plan_last_stats(const gg_plan* plan, gg_stats* stats);
  * its inputs and this setting. */
 GG_API int gg_plan_set_tile_shape(gg_plan* plan, int tile_u);
 
+/* Staging of kernel slices in shared memory by the gridding kernel (bulk
+ * asynchronous copies of a (plane, offset) slice shared by many records of
+ * a tile): -1 (default) decides per call from the mean footprint, 0 off,
+ * 1 on.  Results are bit-identical either way: only where the taps are
+ * read from changes, not the arithmetic or its order. */
+GG_API int gg_plan_set_slice_staging(gg_plan* plan, int mode);
+
 /* Phase timing.  With profiling enabled, every gridding call made with the
  * plan records CUDA events on its stream around five phases:
  *   0 placement (placement, skip/norm reduction, record offsets)

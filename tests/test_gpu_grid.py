@@ -207,6 +207,31 @@ def test_every_tile_shape_matches_fp64_oracle(pkg, oracle_mod, synthetic,
                           grids[auto_key[1]].view(np.uint32))
 
 
+@pytest.mark.parametrize("which", ["cfg0", "skalow_small"])
+def test_slice_staging_is_bit_identical(pkg, synthetic, torch, which):
+    """Staging kernel slices in shared memory changes only where taps are
+    read from: the grids with staging on and off are bit-identical."""
+    wl = synthetic.config0() if which == "cfg0" else _skalow_small(synthetic)
+    stack = pkg.KernelStack.from_workload(wl, "f")
+    plan = pkg.Plan()
+    out = []
+    for mode in (0, 1):
+        plan.set_slice_staging(mode)
+        grid = torch.zeros((wl.grid_size, wl.grid_size, 2),
+                           dtype=torch.float32, device="cuda")
+        norm = torch.zeros(1, dtype=torch.float64, device="cuda")
+        ns = torch.zeros(1, dtype=torch.int64, device="cuda")
+        pkg.grid_wproj_device(plan, stack, _dev(torch, wl.uu),
+                              _dev(torch, wl.vv), _dev(torch, wl.ww),
+                              _dev(torch, wl.vis), _dev(torch, wl.weight),
+                              np.float32(wl.cell_size_rad),
+                              np.float32(wl.w_scale), wl.grid_size, grid,
+                              norm, ns)
+        torch.cuda.synchronize()
+        out.append(grid.cpu().numpy())
+    assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32))
+
+
 def test_accumulate_semantics(pkg, synthetic, torch):
     """grid and norm accumulate across calls, num_skipped is set."""
     wl = synthetic.config0().subset(20_000)
