@@ -55,7 +55,66 @@ WORKLOAD_TEXT = {
              "w-planes, support 8..44",
     "cfg2s": "SKA-LOW EL56-82 array with 60 time samples (7,848,960 vis), "
              "8192^2 grid, 601 w-planes, support 4..72 (profiling size)",
+    "cfg4s": "64 channels (100-200 MHz, 0-60% flagged) of a 128-station "
+             "SKA-LOW-like array, 120 times, 64 grids of 4096^2, 339 "
+             "w-planes, support 8..44",
 }
+
+
+def measure_batched(pkg, torch, steps, warmup=2):
+    """Batched (one call for all channels) vs plain (one call per channel)
+    on the 64-channel workload; both device-resident, CUDA-event timed."""
+    wl = load_workload("cfg4s")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    uu, vv, ww, vis, weight = (to(wl.uu), to(wl.vv), to(wl.ww), to(wl.vis),
+                               to(wl.weight))
+    C, G = wl.num_grids, wl.grid_size
+    offs = [int(x) for x in wl.channel_offsets]
+    grids = torch.zeros((C, G, G, 2), dtype=torch.float32, device=dev)
+    norms = torch.zeros(C, dtype=torch.float64, device=dev)
+    skips = torch.zeros(C, dtype=torch.int64, device=dev)
+    stack = pkg.KernelStack.from_workload(wl, "f")
+    plan = pkg.Plan()
+    cell, wsc = np.float32(wl.cell_size_rad), np.float32(wl.w_scale)
+    stream = torch.cuda.current_stream()
+
+    def batched():
+        pkg.grid_wproj_batched_device(plan, stack, offs, uu, vv, ww, vis,
+                                      weight, cell, wsc, G, grids, norms,
+                                      skips, stream)
+
+    def plain():
+        for c in range(C):
+            a, b = offs[c], offs[c + 1]
+            pkg.grid_wproj_device(plan, stack, uu[a:b], vv[a:b], ww[a:b],
+                                  vis[a:b], weight[a:b], cell, wsc, G,
+                                  grids[c], norms[c:c + 1], skips[c:c + 1],
+                                  stream)
+
+    out = {}
+    for name, fn in (("plain", plain), ("batched", batched)):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(steps):
+            fn()
+        t1.record(stream)
+        torch.cuda.synchronize()
+        ms = t0.elapsed_time(t1) / steps
+        out[name] = {"ms_per_step": ms,
+                     "mvis_s": wl.num_points / (ms * 1e-3) / 1e6}
+    out["speedup"] = out["plain"]["ms_per_step"] / out["batched"]["ms_per_step"]
+    out["workload"] = f"cfg4s: {WORKLOAD_TEXT['cfg4s']}"
+    out["num_vis"] = wl.num_points
+    out["macs_per_step"] = plan.stats()["num_macs"]
+    out["gflops_batched"] = 8.0 * out["macs_per_step"] / (
+        out["batched"]["ms_per_step"] * 1e-3) / 1e9
+    del grids
+    return out
 
 
 def parse_args():
@@ -72,6 +131,9 @@ def parse_args():
                     help="force the tile width (32, 16, 8); 0 = automatic")
     ap.add_argument("--staging", type=int, default=-1,
                     help="kernel-slice staging: -1 automatic, 0 off, 1 on")
+    ap.add_argument("--batched-steps", type=int, default=3,
+                    help="steps of the batched-vs-plain comparison on the "
+                         "64-channel workload (0 = skip)")
     return ap.parse_args()
 
 
@@ -387,6 +449,10 @@ def run_ours(args):
                                       wl.support.nbytes + 8 * G * G + 8),
                "d2h_bytes_per_step": 8 * G * G + 16}
 
+    batched = None
+    if args.batched_steps > 0 and world == 1:
+        batched = measure_batched(pkg, torch, args.batched_steps)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -428,6 +494,7 @@ def run_ours(args):
             "gpu_launches": args.steps * stats["num_launches"],
             "clocks": clk,
             "published_p100_mvis": PUBLISHED_P100_MVIS.get(args.workload),
+            "batched_vs_plain": batched,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -38,7 +38,8 @@ EXPORTED_SYMBOLS = (
     "gg_plan_destroy", "gg_plan_last_stats", "gg_plan_set_tile_shape",
     "gg_plan_set_slice_staging", "gg_plan_set_profiling",
     "gg_plan_phase_ms", "gg_measure_fp32_fma_tflops", "gg_grid_wproj_f_device",
-    "gg_grid_wproj_f_device_noalloc",
+    "gg_grid_wproj_f_device_noalloc", "gg_grid_wproj_f_batched_device",
+    "gg_grid_wproj_d_batched_device",
     "gg_grid_wproj_d_device", "gg_place_wproj_f_device",
     "gg_place_wproj_d_device", "gg_degrid_wproj_f_device",
     "gg_degrid_wproj_d_device",
@@ -85,6 +86,10 @@ def _declare(L):
         fn = getattr(L, f"gg_grid_wproj_{suffix}_device")
         fn.argtypes = [_vp, _vp, _sz, _vp, _vp, _vp, _vp, _vp, real, real,
                        ctypes.c_int, _vp, _vp, _vp, _vp]
+        fn.restype = ctypes.c_int
+        fn = getattr(L, f"gg_grid_wproj_{suffix}_batched_device")
+        fn.argtypes = [_vp, _vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp,
+                       real, real, ctypes.c_int, _vp, _vp, _vp, _vp]
         fn.restype = ctypes.c_int
         fn = getattr(L, f"gg_place_wproj_{suffix}_device")
         fn.argtypes = [_vp, _sz, _vp, _vp, _vp, real, real, ctypes.c_int,
@@ -355,6 +360,26 @@ def grid_wproj_device(plan, stack, uu, vv, ww, vis, weight, cell_size_rad,
     _check(fn(plan.handle, stack.handle, n, _ptr(uu), _ptr(vv), _ptr(ww),
               _ptr(vis), _ptr(weight), cell_size_rad, w_scale, grid_size,
               _ptr(num_skipped), _ptr(norm), _ptr(grid), _stream_ptr(stream)))
+
+
+def grid_wproj_batched_device(plan, stack, offsets, uu, vv, ww, vis, weight,
+                              cell_size_rad, w_scale, grid_size, grids, norms,
+                              num_skipped, stream=None):
+    """Grid several channels in one call.  offsets: int sequence of
+    num_grids + 1 (channel g = visibilities offsets[g]:offsets[g+1] of the
+    concatenated uu, vv, ww, vis, weight); grids: [num_grids, G, G, 2]
+    (accumulated); norms: float64 [num_grids] (accumulated); num_skipped:
+    int64 [num_grids] (set)."""
+    _require_cuda(uu, vv, ww, vis, weight, grids, norms, num_skipped)
+    offs = np.ascontiguousarray(offsets, dtype=np.uint64)
+    num_grids = int(offs.shape[0] - 1)
+    if grids.shape[0] != num_grids or norms.shape[0] != num_grids:
+        raise ValueError("grids and norms need one entry per channel")
+    fn = getattr(lib(), f"gg_grid_wproj_{stack.precision}_batched_device")
+    _check(fn(plan.handle, stack.handle, num_grids, _ptr(offs), _ptr(uu),
+              _ptr(vv), _ptr(ww), _ptr(vis), _ptr(weight), cell_size_rad,
+              w_scale, grid_size, _ptr(num_skipped), _ptr(norms), _ptr(grids),
+              _stream_ptr(stream)))
 
 
 def place_wproj_device(stack, uu, vv, ww, cell_size_rad, w_scale, grid_size,

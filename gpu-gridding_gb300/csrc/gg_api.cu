@@ -323,6 +323,9 @@ struct gg_plan {
   bool profile = false;
   bool events_valid = false;
   cudaEvent_t ev[kEvents] = {};
+  // Batched calls: per-visibility norm terms, chunk table, chunk totals,
+  // per-grid visibility offsets.
+  DevBuf nterm, chunk_begin, grid_chunk0, chunk_part, grid_offsets;
   // Staging of the host-pointer entry points.
   DevBuf in_uu, in_vv, in_ww, in_vis, in_weight, in_grid, in_misc;
   ~gg_plan() {
@@ -410,6 +413,12 @@ int max_tiles(int grid_size, int num_grids) {
   }
   return m * num_grids;
 }
+
+template <typename Real>
+int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
+                 const PlaceOut& po, int grid_size, int num_grids,
+                 const unsigned long long* d_grid_offsets, Real* d_grid,
+                 long long grid_stride, cudaStream_t s);
 
 template <typename Real>
 int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
@@ -500,6 +509,22 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   GG_CUDA(cudaMemcpyAsync((char*)plan->h_scalars + 32, scalar64(plan, kMacs),
                           8, cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaStreamSynchronize(s));
+  return bin_and_grid<Real>(plan, K, n, po, grid_size, 1, nullptr, d_grid, 0,
+                            s);
+}
+
+// The second half of a gridding call, after the host has read back the
+// record total and the tile shape: record emission, sort, work items, the
+// tile-gridding kernel and the partial reduction.  Batched calls pass the
+// device array of per-grid visibility offsets and the stride between grids.
+template <typename Real>
+int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
+                 const PlaceOut& po, int grid_size, int num_grids,
+                 const unsigned long long* d_grid_offsets, Real* d_grid,
+                 long long grid_stride, cudaStream_t s) {
+  using R2 = typename Vec2<Real>::type;
+  const StackView view = K->view();
+  uint32_t* sc = plan->scalars.as<uint32_t>();
   if (plan->h_scalars[kDeviceError])
     return set_error(GG_ERR_CUDA,
                      "an earlier call with this plan had a gridding kernel "
@@ -512,8 +537,8 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   plan->stats.num_records = total;
   memcpy(&plan->stats.num_macs, (char*)plan->h_scalars + 32, 8);
   int key_bits = 0;
-  const TileGeom geom = make_geom(shape, grid_size, 1, K, &key_bits);
-  const int num_tiles = geom.tiles_u * geom.tiles_v;
+  const TileGeom geom = make_geom(shape, grid_size, num_grids, K, &key_bits);
+  const int num_tiles = num_grids * geom.tiles_u * geom.tiles_v;
   const int low_bits = geom.plane_bits + geom.phase_bits;
   plan->stats.tile_u = geom.tile_u;
   plan->stats.tile_v = geom.tile_v;
@@ -531,7 +556,8 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
     GG_CUDA(launch_emit_records(po.cell, po.meta,
                                 plan->rec_offset.as<uint32_t>(), n, view, geom,
                                 0, 0, plan->keys0.as<uint32_t>(),
-                                plan->vals0.as<uint32_t>(), s));
+                                plan->vals0.as<uint32_t>(), s, d_grid_offsets,
+                                num_grids));
     bool in_alt = false;
     GG_CUDA(radix_sort_pairs(plan->keys0.as<uint32_t>(),
                              plan->vals0.as<uint32_t>(),
@@ -578,18 +604,152 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
     plan->mark(3, s);
     GG_CUDA(launch_grid_tiles<Real>(
         ib.items, ib.num_items, ib.counter, sc + kDeviceError, vals, po.cell,
-        po.meta, po.vw, view, geom, grid_size, d_grid, 0,
+        po.meta, po.vw, view, geom, grid_size, d_grid, grid_stride,
         plan->partials.as<Real>(), num_ctas, stage, s));
     plan->mark(4, s);
     GG_CUDA(launch_reduce_partials<Real>(ib.split_tiles, ib.num_split,
                                          num_tiles, plan->partials.as<Real>(),
-                                         geom, grid_size, d_grid, 0, s));
+                                         geom, grid_size, d_grid, grid_stride,
+                                         s));
     plan->mark(5, s);
     // tile bounds, item counts, 2 scans, item emit, gridding, reduction
     plan->stats.num_launches += 1 + 1 + 6 + 1 + 1 + 1;
     plan->events_valid = plan->profile;
   }
   return GG_OK;
+}
+
+// Many grids in one call: the visibilities of grid g are
+// [h_offsets[g], h_offsets[g+1]) of the concatenated input arrays and its
+// grid is d_grids + g * grid_size^2 * 2.  One placement pass, one sort and
+// one persistent tile-gridding launch cover every grid.
+template <typename Real>
+int batched_pipeline(gg_plan* plan, const gg_kernels* K, int num_grids,
+                     const unsigned long long* h_offsets, const Real* uu,
+                     const Real* vv, const Real* ww, const Real* vis,
+                     const Real* weight, Real cell_size_rad, Real w_scale,
+                     int grid_size, unsigned long long* d_num_skipped,
+                     double* d_norm, Real* d_grids, cudaStream_t s) {
+  using R2 = typename Vec2<Real>::type;
+  if (!plan || !K) return set_error(GG_ERR_INVALID_ARG, "plan or kernels is NULL");
+  if (K->is_double != (sizeof(Real) == 8))
+    return set_error(GG_ERR_INVALID_ARG,
+                     "kernel stack precision does not match the call");
+  if (num_grids < 1 || !h_offsets)
+    return set_error(GG_ERR_INVALID_ARG, "need num_grids >= 1 and offsets");
+  if (grid_size < 1 || grid_size > kMaxGridSize)
+    return set_error(GG_ERR_UNSUPPORTED, "grid_size = %d outside [1, %d]",
+                     grid_size, kMaxGridSize);
+  if (h_offsets[0] != 0)
+    return set_error(GG_ERR_INVALID_ARG, "offsets[0] must be 0");
+  for (int g = 0; g < num_grids; ++g)
+    if (h_offsets[g + 1] < h_offsets[g])
+      return set_error(GG_ERR_INVALID_ARG,
+                       "offsets must not decrease (grid %d)", g);
+  const unsigned long long n = h_offsets[num_grids];
+  if (n > 0xFFFFFFF0ull)
+    return set_error(GG_ERR_UNSUPPORTED,
+                     "%llu visibilities exceed 2^32-16 per call", n);
+  if (n > 0 && (!uu || !vv || !ww || !vis || !weight))
+    return set_error(GG_ERR_INVALID_ARG, "an input array is NULL");
+  if (!d_grids || !d_norm || !d_num_skipped)
+    return set_error(GG_ERR_INVALID_ARG, "an output pointer is NULL");
+  const long long grid_stride = 2LL * grid_size * grid_size;
+  int key_bits = 0;
+  make_geom(0, grid_size, num_grids, K, &key_bits);
+  if (ceil_log2((unsigned long long)max_tiles(grid_size, num_grids)) > 32)
+    return set_error(GG_ERR_UNSUPPORTED, "too many tiles for 32-bit keys");
+  int dev;
+  GG_TRY(current_device(&dev));
+  if (dev != K->device || dev != plan->device)
+    return set_error(GG_ERR_INVALID_ARG,
+                     "plan, kernel stack and current device differ");
+
+  plan->stats = gg_stats{};
+  plan->stats.num_points = n;
+  plan->events_valid = false;
+  const StackView view = K->view();
+  const int tiles_cap = max_tiles(grid_size, num_grids);
+
+  // Chunk table of the per-grid reductions (chunks never straddle grids).
+  constexpr unsigned long long kChunk = 1ull << 16;
+  std::vector<unsigned long long> chunk_begin;
+  std::vector<int> grid_chunk0(num_grids + 1);
+  for (int g = 0; g < num_grids; ++g) {
+    grid_chunk0[g] = (int)chunk_begin.size();
+    for (unsigned long long b = h_offsets[g]; b < h_offsets[g + 1];
+         b += kChunk)
+      chunk_begin.push_back(b);
+  }
+  grid_chunk0[num_grids] = (int)chunk_begin.size();
+  const int num_chunks = (int)chunk_begin.size();
+  chunk_begin.push_back(n);
+
+  GG_TRY(plan->cell.ensure(n * 4 + 4));
+  GG_TRY(plan->meta.ensure(n * 4 + 4));
+  GG_TRY(plan->vw.ensure(n * sizeof(R2) + sizeof(R2)));
+  GG_TRY(plan->rec_count.ensure(n * 4 + 4));
+  GG_TRY(plan->rec_offset.ensure(n * 4 + 4));
+  GG_TRY(plan->nterm.ensure(n * 8 + 8));
+  GG_TRY(plan->chunk_begin.ensure(chunk_begin.size() * 8));
+  GG_TRY(plan->grid_chunk0.ensure(grid_chunk0.size() * 4));
+  GG_TRY(plan->chunk_part.ensure((size_t)(num_chunks + 1) * 24));
+  GG_TRY(plan->grid_offsets.ensure((size_t)(num_grids + 1) * 8));
+  GG_TRY(plan->scan_tmp.ensure(
+      scan_temp_bytes(std::max<size_t>(n, (size_t)tiles_cap))));
+  GG_CUDA(cudaMemcpyAsync(plan->chunk_begin.p, chunk_begin.data(),
+                          chunk_begin.size() * 8, cudaMemcpyHostToDevice, s));
+  GG_CUDA(cudaMemcpyAsync(plan->grid_chunk0.p, grid_chunk0.data(),
+                          grid_chunk0.size() * 4, cudaMemcpyHostToDevice, s));
+  GG_CUDA(cudaMemcpyAsync(plan->grid_offsets.p, h_offsets,
+                          (size_t)(num_grids + 1) * 8, cudaMemcpyHostToDevice,
+                          s));
+
+  uint32_t* sc = plan->scalars.as<uint32_t>();
+  PlaceParams<Real> pp;
+  pp.uu = uu; pp.vv = vv; pp.ww = ww; pp.vis = vis; pp.weight = weight;
+  pp.grid_scale = (Real)grid_size * cell_size_rad;
+  pp.w_scale = w_scale;
+  pp.grid_size = grid_size;
+  pp.grid_centre = grid_size / 2;
+  pp.num_points = n;
+  PlaceOut po;
+  po.cell = plan->cell.as<uint32_t>();
+  po.meta = plan->meta.as<uint32_t>();
+  po.vw = plan->vw.p;
+  po.rec_count = plan->rec_count.as<uint32_t>();
+  po.blk_norm = nullptr;
+  po.blk_skip = nullptr;
+  po.blk_macs = nullptr;
+  double* chunk_norm = plan->chunk_part.as<double>();
+  unsigned long long* chunk_skip =
+      (unsigned long long*)(chunk_norm + num_chunks + 1);
+  unsigned long long* chunk_macs = chunk_skip + num_chunks + 1;
+
+  plan->mark(0, s);
+  GG_CUDA(launch_place_batched<Real>(pp, view, po, plan->nterm.as<double>(),
+                                     s));
+  GG_CUDA(launch_batch_totals(
+      po.meta, plan->nterm.as<double>(), view, num_chunks,
+      plan->chunk_begin.as<unsigned long long>(), num_grids,
+      plan->grid_chunk0.as<int>(), chunk_norm, chunk_skip, chunk_macs,
+      plan->forced_shape, d_norm, d_num_skipped, scalar64(plan, kMacs),
+      sc + kShape, s));
+  GG_CUDA(launch_count_records(po.cell, po.meta, n, view, sc + kShape,
+                               po.rec_count, s));
+  GG_CUDA(exclusive_scan_u32(po.rec_count, plan->rec_offset.as<uint32_t>(), n,
+                             sc + kTotalRecords, plan->scan_tmp.p, s));
+  // place, chunk totals, finalize, count, 3-kernel scan
+  plan->stats.num_launches = (num_chunks > 0 ? 7 : 6);
+  plan->mark(1, s);
+  GG_CUDA(cudaMemcpyAsync(plan->h_scalars, sc, 4 * kScalarCount,
+                          cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaMemcpyAsync((char*)plan->h_scalars + 32, scalar64(plan, kMacs),
+                          8, cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  return bin_and_grid<Real>(plan, K, n, po, grid_size, num_grids,
+                            plan->grid_offsets.as<unsigned long long>(),
+                            d_grids, grid_stride, s);
 }
 
 template <typename Real>
@@ -961,6 +1121,34 @@ GG_API int gg_grid_wproj_d_device(gg_plan* plan, const gg_kernels* kernels,
                                d_vis, d_weight, cell_size_rad, w_scale,
                                grid_size, d_num_skipped, d_norm, d_grid,
                                (cudaStream_t)stream);
+}
+
+GG_API int gg_grid_wproj_f_batched_device(
+    gg_plan* plan, const gg_kernels* kernels, int num_grids,
+    const unsigned long long* offsets, const float* d_uu, const float* d_vv,
+    const float* d_ww, const float* d_vis, const float* d_weight,
+    float cell_size_rad, float w_scale, int grid_size,
+    unsigned long long* d_num_skipped, double* d_norm, float* d_grids,
+    void* stream) {
+  t_last_error.clear();
+  return batched_pipeline<float>(plan, kernels, num_grids, offsets, d_uu,
+                                 d_vv, d_ww, d_vis, d_weight, cell_size_rad,
+                                 w_scale, grid_size, d_num_skipped, d_norm,
+                                 d_grids, (cudaStream_t)stream);
+}
+
+GG_API int gg_grid_wproj_d_batched_device(
+    gg_plan* plan, const gg_kernels* kernels, int num_grids,
+    const unsigned long long* offsets, const double* d_uu,
+    const double* d_vv, const double* d_ww, const double* d_vis,
+    const double* d_weight, double cell_size_rad, double w_scale,
+    int grid_size, unsigned long long* d_num_skipped, double* d_norm,
+    double* d_grids, void* stream) {
+  t_last_error.clear();
+  return batched_pipeline<double>(plan, kernels, num_grids, offsets, d_uu,
+                                  d_vv, d_ww, d_vis, d_weight, cell_size_rad,
+                                  w_scale, grid_size, d_num_skipped, d_norm,
+                                  d_grids, (cudaStream_t)stream);
 }
 
 GG_API int gg_place_wproj_f_device(const gg_kernels* kernels,

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 #include <stddef.h>
 
@@ -50,6 +51,22 @@ __host__ __device__ inline int tile_v_of_shape(int shape) {
   return 2048 / (32 >> shape);
 }
 
+// Tile shape and slice staging for a call, from its mean footprint side
+// sqrt(macs / gridded points): narrow tiles only for tiny footprints (a
+// 32-wide warp would leave most lanes outside them); kernel slices staged in
+// shared memory (bit 8) when footprints are small enough for their slices to
+// fit the slots, otherwise the kernel keeps its shared memory small so the
+// L1 cache serves the tap loads.  forced_shape >= 0 overrides the shape.
+__host__ __device__ inline uint32_t choose_shape(unsigned long long macs,
+                                                 unsigned long long gridded,
+                                                 int forced_shape) {
+  const double side = gridded ? sqrt((double)macs / (double)gridded) : 0.0;
+  int shape = forced_shape;
+  if (shape < 0) shape = side >= 16.0 ? 0 : (side >= 8.0 ? 1 : 2);
+  const uint32_t stage = side < 40.0 ? 1u : 0u;
+  return (uint32_t)shape | (stage << 8);
+}
+
 struct PlaceOut {
   uint32_t* cell;             // [N]
   uint32_t* meta;             // [N]
@@ -89,7 +106,36 @@ cudaError_t launch_emit_records(const uint32_t* cell, const uint32_t* meta,
                                 unsigned long long n, StackView view,
                                 TileGeom geom, int grid_index,
                                 unsigned long long vis_offset, uint32_t* keys,
-                                uint32_t* vals, cudaStream_t s);
+                                uint32_t* vals, cudaStream_t s,
+                                const unsigned long long* grid_offsets =
+                                    nullptr,
+                                int num_grids = 1);
+// grid_offsets (device, num_grids + 1): batched calls, where visibility i
+// belongs to the grid g with grid_offsets[g] <= i < grid_offsets[g + 1].
+
+// ---- batched calls (gg_batch.cu) ------------------------------------------
+// Per-visibility placement for a batched call: like launch_place, but the
+// FP64 norm term of every visibility goes to nterm[i] (0 if skipped) so the
+// norm can be reduced per grid.
+template <typename Real>
+cudaError_t launch_place_batched(PlaceParams<Real> p, StackView view,
+                                 PlaceOut out, double* nterm, cudaStream_t s);
+// Deterministic per-grid totals over a chunk table (chunk c covers
+// visibilities [chunk_begin[c], chunk_begin[c+1]) of grid chunk_grid[c];
+// grid g owns chunks [grid_chunk0[g], grid_chunk0[g+1])):
+// d_norm[g] += sum of nterm, d_num_skipped[g] = skips, *d_macs = total
+// MACs, *d_shape = choose_shape(total MACs, gridded, forced_shape).
+cudaError_t launch_batch_totals(const uint32_t* meta, const double* nterm,
+                                StackView view, int num_chunks,
+                                const unsigned long long* chunk_begin,
+                                int num_grids, const int* grid_chunk0,
+                                double* chunk_norm,
+                                unsigned long long* chunk_skip,
+                                unsigned long long* chunk_macs,
+                                int forced_shape, double* d_norm,
+                                unsigned long long* d_num_skipped,
+                                unsigned long long* d_macs, uint32_t* d_shape,
+                                cudaStream_t s);
 
 // ---- work decomposition and gridding (gg_grid.cu) -------------------------
 cudaError_t launch_tile_bounds(const uint32_t* keys, uint32_t n, int shift,

@@ -108,18 +108,7 @@ __global__ void k_place_finalize(const double* __restrict__ blk_norm,
       if (d_norm) *d_norm += n;
       if (d_num_skipped) *d_num_skipped = s;
       if (d_macs) *d_macs = m;
-      // Tile shape from the mean footprint side: narrow tiles only for tiny
-      // footprints, where a 32-wide warp would leave most lanes outside
-      // them.  Kernel slices are staged in shared memory (bit 8) when
-      // footprints are small enough for their slices to fit the slots;
-      // otherwise the kernel keeps its shared memory small so the L1 cache
-      // serves the tap loads.
-      const unsigned long long gridded = n_points - s;
-      const double side = gridded ? sqrt((double)m / (double)gridded) : 0.0;
-      int shape = forced_shape;
-      if (shape < 0) shape = side >= 16.0 ? 0 : (side >= 8.0 ? 1 : 2);
-      const uint32_t stage = side < 40.0 ? 1u : 0u;
-      *d_shape = (uint32_t)shape | (stage << 8);
+      *d_shape = choose_shape(m, n_points - s, forced_shape);
     }
   }
 }
@@ -157,12 +146,24 @@ __global__ void k_emit(const uint32_t* __restrict__ cell,
                        unsigned long long n, StackView v, TileGeom g,
                        int grid_index, unsigned long long vis_offset,
                        uint32_t* __restrict__ keys,
-                       uint32_t* __restrict__ vals) {
+                       uint32_t* __restrict__ vals,
+                       const unsigned long long* __restrict__ grid_offsets,
+                       int num_grids) {
   const unsigned long long i =
       (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint32_t m = meta[i];
   if (meta_skipped(m)) return;
+  if (grid_offsets) {
+    // Batched call: the grid of visibility i is the channel whose range
+    // [grid_offsets[g], grid_offsets[g+1]) holds it.
+    int lo = 0, hi = num_grids - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (grid_offsets[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    grid_index = lo;
+  }
   const uint32_t c = cell[i];
   const int gu = cell_u(c), gv = cell_v(c);
   const int plane = meta_plane(m);
@@ -262,11 +263,14 @@ cudaError_t launch_emit_records(const uint32_t* cell, const uint32_t* meta,
                                 unsigned long long n, StackView view,
                                 TileGeom geom, int grid_index,
                                 unsigned long long vis_offset, uint32_t* keys,
-                                uint32_t* vals, cudaStream_t s) {
+                                uint32_t* vals, cudaStream_t s,
+                                const unsigned long long* grid_offsets,
+                                int num_grids) {
   if (n == 0) return cudaSuccess;
   const unsigned nb = (unsigned)((n + 255) / 256);
   k_emit<<<nb, 256, 0, s>>>(cell, meta, rec_offset, n, view, geom,
-                            grid_index, vis_offset, keys, vals);
+                            grid_index, vis_offset, keys, vals, grid_offsets,
+                            num_grids);
   return cudaGetLastError();
 }
 

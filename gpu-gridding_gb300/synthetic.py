@@ -314,4 +314,8 @@ WORKLOADS = {
     "cfg2b": lambda: config2("EL82-70"),
     "cfg2s": lambda: config2("EL56-82", num_times=60),
     "cfg4": config4,
+    # Config-4 structure at a size a benchmark step can hold: 64 channels
+    # (100-200 MHz, 0-60% flagged) of a 128-station array, 120 times.
+    "cfg4s": lambda: config4(num_channels=64, grid_size=4096, times=120,
+                             stations=128),
 }

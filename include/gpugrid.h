@@ -186,6 +186,33 @@ GG_API int gg_grid_wproj_d_device(gg_plan* plan, const gg_kernels* kernels,
         unsigned long long* d_num_skipped, double* d_norm, double* d_grid,
         void* stream);
 
+/* Batched gridding: num_grids independent grids (frequency channels or
+ * snapshots, each with its own number of visibilities) in one call -- one
+ * placement pass, one sort and one persistent tile-gridding launch over all
+ * of them.  Grid g takes visibilities [offsets[g], offsets[g+1]) of the
+ * concatenated device arrays d_uu ... d_weight (offsets: host, num_grids+1
+ * entries, offsets[0] = 0) and accumulates into d_grids + g * grid_size^2 *
+ * 2; d_norm[g] is accumulated and d_num_skipped[g] set (device arrays of
+ * num_grids).  The kernel stack, cell size and w_scale are shared.  Each
+ * grid's result equals that of gg_grid_wproj_f_device on its own
+ * visibilities (same placement, norm and num_skipped; grid within FP32
+ * rounding).  The reference grids one channel per call (its main.cpp
+ * loops over visibility blocks and calls oskar_grid_wproj_f for each). */
+GG_API int gg_grid_wproj_f_batched_device(gg_plan* plan,
+        const gg_kernels* kernels, int num_grids,
+        const unsigned long long* offsets, const float* d_uu,
+        const float* d_vv, const float* d_ww, const float* d_vis,
+        const float* d_weight, float cell_size_rad, float w_scale,
+        int grid_size, unsigned long long* d_num_skipped, double* d_norm,
+        float* d_grids, void* stream);
+GG_API int gg_grid_wproj_d_batched_device(gg_plan* plan,
+        const gg_kernels* kernels, int num_grids,
+        const unsigned long long* offsets, const double* d_uu,
+        const double* d_vv, const double* d_ww, const double* d_vis,
+        const double* d_weight, double cell_size_rad, double w_scale,
+        int grid_size, unsigned long long* d_num_skipped, double* d_norm,
+        double* d_grids, void* stream);
+
 /* Allocation-free form of gg_grid_wproj_f_device, for callers that cannot
  * allocate device memory while they grid (a real-time loop that must not
  * stall on cudaMalloc, or code running under another framework's memory
