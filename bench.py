@@ -61,9 +61,11 @@ WORKLOAD_TEXT = {
 }
 
 
-def measure_batched(pkg, torch, steps, warmup=2):
+def measure_batched(pkg, torch, steps, warmup=2, tune=None):
     """Batched (one call for all channels) vs plain (one call per channel)
-    on the 64-channel workload; both device-resident, CUDA-event timed."""
+    on the 64-channel workload; both device-resident, CUDA-event timed.
+    tune: a TuningCache -- both plans are autotuned first (the plain plan on
+    channel 0's single calls) -- or None for the per-call heuristics."""
     wl = load_workload("cfg4s")
     dev = torch.device("cuda", torch.cuda.current_device())
     to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
@@ -76,8 +78,20 @@ def measure_batched(pkg, torch, steps, warmup=2):
     skips = torch.zeros(C, dtype=torch.int64, device=dev)
     stack = pkg.KernelStack.from_workload(wl, "f")
     plan = pkg.Plan()
+    plain_plan = pkg.Plan()
     cell, wsc = np.float32(wl.cell_size_rad), np.float32(wl.w_scale)
     stream = torch.cuda.current_stream()
+    tuning = None
+    if tune is not None:
+        from importlib import import_module
+        at = import_module(pkg.__name__ + ".autotune")
+        a, b = offs[0], offs[1]
+        tuning = {
+            "batched": at.autotune(pkg, plan, stack, uu, vv, ww, vis, weight,
+                                   cell, wsc, G, offsets=offs, cache=tune),
+            "plain": at.autotune(pkg, plain_plan, stack, uu[a:b], vv[a:b],
+                                 ww[a:b], vis[a:b], weight[a:b], cell, wsc,
+                                 G, cache=tune)}
 
     def batched():
         pkg.grid_wproj_batched_device(plan, stack, offs, uu, vv, ww, vis,
@@ -87,7 +101,7 @@ def measure_batched(pkg, torch, steps, warmup=2):
     def plain():
         for c in range(C):
             a, b = offs[c], offs[c + 1]
-            pkg.grid_wproj_device(plan, stack, uu[a:b], vv[a:b], ww[a:b],
+            pkg.grid_wproj_device(plain_plan, stack, uu[a:b], vv[a:b], ww[a:b],
                                   vis[a:b], weight[a:b], cell, wsc, G,
                                   grids[c], norms[c:c + 1], skips[c:c + 1],
                                   stream)
@@ -113,6 +127,30 @@ def measure_batched(pkg, torch, steps, warmup=2):
     out["macs_per_step"] = plan.stats()["num_macs"]
     out["gflops_batched"] = 8.0 * out["macs_per_step"] / (
         out["batched"]["ms_per_step"] * 1e-3) / 1e9
+
+    # Replay of the kept geometry (fixed uvw, new amplitudes each major
+    # cycle) captured once in a CUDA graph and launched per step.
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        pkg.grid_wproj_batched_replay(plan, stack, vis, weight, grids, norms,
+                                      skips)
+    for _ in range(warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(steps):
+        graph.replay()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    pkg.check_plan(plan)
+    ms = t0.elapsed_time(t1) / steps
+    out["replay_graph"] = {"ms_per_step": ms,
+                           "mvis_s": wl.num_points / (ms * 1e-3) / 1e6}
+    out["replay_speedup_vs_plain"] = out["plain"]["ms_per_step"] / ms
+    out["tuning"] = tuning
+    del graph
     del grids
     return out
 
@@ -131,6 +169,12 @@ def parse_args():
                     help="force the tile width (32, 16, 8); 0 = automatic")
     ap.add_argument("--staging", type=int, default=-1,
                     help="kernel-slice staging: -1 automatic, 0 off, 1 on")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="use the per-call heuristics instead of tuning the "
+                         "plans (tuning runs before the timed region)")
+    ap.add_argument("--tune-cache", default=None,
+                    help="autotuner cache file (default: $GPUGRID_TUNE_CACHE "
+                         "or ~/.cache/gpugrid/tuning.json)")
     ap.add_argument("--batched-steps", type=int, default=3,
                     help="steps of the batched-vs-plain comparison on the "
                          "64-channel workload (0 = skip)")
@@ -331,11 +375,19 @@ def run_ours(args):
 
     stack = pkg.KernelStack.from_workload(wl, "f")
     plan = pkg.Plan()
-    plan.set_tile_shape(args.tile_shape)
-    plan.set_slice_staging(args.staging)
     uu, vv, ww = to_dev(wl.uu), to_dev(wl.vv), to_dev(wl.ww)
     vis, weight = to_dev(wl.vis), to_dev(wl.weight)
     G = wl.grid_size
+    tune_cache, tuning = None, None
+    if args.no_autotune or args.tile_shape or args.staging >= 0:
+        plan.set_tile_shape(args.tile_shape)
+        plan.set_slice_staging(args.staging)
+    else:
+        at = importlib.import_module(pkg.__name__ + ".autotune")
+        tune_cache = at.TuningCache(args.tune_cache)
+        tuning = at.autotune(pkg, plan, stack, uu, vv, ww, vis, weight,
+                             np.float32(wl.cell_size_rad),
+                             np.float32(wl.w_scale), G, cache=tune_cache)
     grid = torch.zeros((G, G, 2), dtype=torch.float32, device=dev)
     norm = torch.zeros(1, dtype=torch.float64, device=dev)
     nskip = torch.zeros(1, dtype=torch.int64, device=dev)
@@ -451,7 +503,8 @@ def run_ours(args):
 
     batched = None
     if args.batched_steps > 0 and world == 1:
-        batched = measure_batched(pkg, torch, args.batched_steps)
+        batched = measure_batched(pkg, torch, args.batched_steps,
+                                  tune=tune_cache)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -475,7 +528,11 @@ def run_ours(args):
             "config": workload_config(args.workload, wl, {
                 "macs_per_step": macs, "records_per_step":
                     stats["num_records"], "tile": [stats["tile_u"],
-                                                    stats["tile_v"]]}),
+                                                    stats["tile_v"]],
+                "slice_staging": stats["slice_staging"],
+                "gridding_ctas": stats["num_ctas"],
+                "chunk_records": stats["chunk_records"],
+                "tuning": tuning or plan.tuning()}),
             "gflops": gflops,
             "phase_ms": phase_ms,
             "roofline": {

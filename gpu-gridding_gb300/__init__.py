@@ -36,10 +36,12 @@ EXPORTED_SYMBOLS = (
     "gg_grid_wproj_f", "gg_last_error", "gg_version", "gg_kernels_create_f",
     "gg_kernels_create_d", "gg_kernels_destroy", "gg_plan_create",
     "gg_plan_destroy", "gg_plan_last_stats", "gg_plan_set_tile_shape",
-    "gg_plan_set_slice_staging", "gg_plan_set_profiling",
+    "gg_plan_set_slice_staging", "gg_plan_set_tuning", "gg_plan_get_tuning",
+    "gg_plan_set_profiling",
     "gg_plan_phase_ms", "gg_measure_fp32_fma_tflops", "gg_grid_wproj_f_device",
     "gg_grid_wproj_f_device_noalloc", "gg_grid_wproj_f_batched_device",
-    "gg_grid_wproj_d_batched_device",
+    "gg_grid_wproj_d_batched_device", "gg_grid_wproj_f_batched_replay",
+    "gg_grid_wproj_d_batched_replay", "gg_plan_check",
     "gg_grid_wproj_d_device", "gg_place_wproj_f_device",
     "gg_place_wproj_d_device", "gg_degrid_wproj_f_device",
     "gg_degrid_wproj_d_device",
@@ -60,7 +62,27 @@ class Stats(ctypes.Structure):
                 ("num_records", ctypes.c_ulonglong),
                 ("num_macs", ctypes.c_ulonglong),
                 ("num_launches", ctypes.c_ulonglong),
-                ("tile_u", ctypes.c_int), ("tile_v", ctypes.c_int)]
+                ("tile_u", ctypes.c_int), ("tile_v", ctypes.c_int),
+                ("slice_staging", ctypes.c_int), ("num_ctas", ctypes.c_int),
+                ("chunk_records", ctypes.c_ulonglong)]
+
+
+class Tuning(ctypes.Structure):
+    """gg_tuning: launch and decomposition parameters of a plan."""
+    _fields_ = [("tile_u", ctypes.c_int), ("slice_staging", ctypes.c_int),
+                ("items_per_cta", ctypes.c_int), ("sort_detail", ctypes.c_int),
+                ("ctas_per_sm", ctypes.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "Tuning":
+        t = cls(0, -1, 4, 2, 0)
+        for k, _ in cls._fields_:
+            if k in d:
+                setattr(t, k, int(d[k]))
+        return t
 
 
 _lib = None
@@ -91,6 +113,9 @@ def _declare(L):
         fn.argtypes = [_vp, _vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp,
                        real, real, ctypes.c_int, _vp, _vp, _vp, _vp]
         fn.restype = ctypes.c_int
+        fn = getattr(L, f"gg_grid_wproj_{suffix}_batched_replay")
+        fn.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
+        fn.restype = ctypes.c_int
         fn = getattr(L, f"gg_place_wproj_{suffix}_device")
         fn.argtypes = [_vp, _sz, _vp, _vp, _vp, real, real, ctypes.c_int,
                        _vp, _vp]
@@ -115,6 +140,12 @@ def _declare(L):
     L.gg_plan_set_tile_shape.restype = ctypes.c_int
     L.gg_plan_set_slice_staging.argtypes = [_vp, ctypes.c_int]
     L.gg_plan_set_slice_staging.restype = ctypes.c_int
+    L.gg_plan_set_tuning.argtypes = [_vp, ctypes.POINTER(Tuning)]
+    L.gg_plan_set_tuning.restype = ctypes.c_int
+    L.gg_plan_get_tuning.argtypes = [_vp, ctypes.POINTER(Tuning)]
+    L.gg_plan_get_tuning.restype = ctypes.c_int
+    L.gg_plan_check.argtypes = [_vp, _vp]
+    L.gg_plan_check.restype = ctypes.c_int
     L.gg_plan_set_profiling.argtypes = [_vp, ctypes.c_int]
     L.gg_plan_set_profiling.restype = ctypes.c_int
     L.gg_plan_phase_ms.argtypes = [_vp, ctypes.POINTER(ctypes.c_float),
@@ -310,6 +341,17 @@ class Plan:
         """Kernel-slice staging in shared memory: -1 auto, 0 off, 1 on."""
         _check(lib().gg_plan_set_slice_staging(self.handle, int(mode)))
 
+    def set_tuning(self, tuning) -> None:
+        """Apply a Tuning (or a dict of its fields; missing fields take the
+        defaults)."""
+        t = tuning if isinstance(tuning, Tuning) else Tuning.from_dict(tuning)
+        _check(lib().gg_plan_set_tuning(self.handle, ctypes.byref(t)))
+
+    def tuning(self) -> dict:
+        t = Tuning()
+        _check(lib().gg_plan_get_tuning(self.handle, ctypes.byref(t)))
+        return t.as_dict()
+
     def set_profiling(self, enable: bool = True) -> None:
         _check(lib().gg_plan_set_profiling(self.handle, int(enable)))
 
@@ -380,6 +422,26 @@ def grid_wproj_batched_device(plan, stack, offsets, uu, vv, ww, vis, weight,
               _ptr(vv), _ptr(ww), _ptr(vis), _ptr(weight), cell_size_rad,
               w_scale, grid_size, _ptr(num_skipped), _ptr(norms), _ptr(grids),
               _stream_ptr(stream)))
+
+
+def grid_wproj_batched_replay(plan, stack, vis, weight, grids, norms,
+                              num_skipped, stream=None):
+    """Grid new amplitudes and weights on the geometry kept by the plan's
+    last batched call (same channel layout and visibility count).  Enqueues
+    kernels only -- no allocation, no host synchronisation -- so it can be
+    captured in a CUDA graph (pass the capturing stream, or call it inside
+    ``torch.cuda.graph``, whose stream is then the current one)."""
+    _require_cuda(vis, weight, grids, norms, num_skipped)
+    fn = getattr(lib(), f"gg_grid_wproj_{stack.precision}_batched_replay")
+    _check(fn(plan.handle, stack.handle, _ptr(vis), _ptr(weight),
+              _ptr(num_skipped), _ptr(norms), _ptr(grids),
+              _stream_ptr(stream)))
+
+
+def check_plan(plan, stream=None):
+    """Synchronise the stream and raise GridError if a gridding kernel of
+    the plan flagged a failure (for replays, which do not check)."""
+    _check(lib().gg_plan_check(plan.handle, _stream_ptr(stream)))
 
 
 def place_wproj_device(stack, uu, vv, ww, cell_size_rad, w_scale, grid_size,

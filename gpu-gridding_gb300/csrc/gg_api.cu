@@ -320,6 +320,9 @@ struct gg_plan {
   static constexpr int kEvents = 6;
   int forced_shape = -1;  // tile shape index, -1 = chosen per call
   int forced_stage = -1;  // slice staging 0/1, -1 = chosen per call
+  int items_per_cta = 4;  // work-item granularity of heavy-tile splits
+  int sort_detail = 2;    // low sort-key fields: 2 plane+class, 1 plane, 0
+  int ctas_per_sm = 0;    // cap on resident gridding CTAs, 0 = none
   bool profile = false;
   bool events_valid = false;
   cudaEvent_t ev[kEvents] = {};
@@ -328,6 +331,20 @@ struct gg_plan {
   DevBuf nterm, chunk_begin, grid_chunk0, chunk_part, grid_offsets;
   // Staging of the host-pointer entry points.
   DevBuf in_uu, in_vv, in_ww, in_vis, in_weight, in_grid, in_misc;
+  // Geometry kept by the last batched call for replays on new amplitudes:
+  // placement (cell, meta), sorted records, work items and launch shape.
+  struct Kept {
+    bool valid = false;
+    const gg_kernels* kernels = nullptr;
+    bool is_double = false;
+    unsigned long long num_points = 0;
+    int num_grids = 0, grid_size = 0, num_chunks = 0, num_tiles = 0;
+    int num_ctas = 0, shape = 0;
+    bool stage = false;
+    uint32_t num_records = 0;
+    TileGeom geom{};
+    const uint32_t* rec_vis = nullptr;
+  } kept;
   ~gg_plan() {
     if (h_scalars) cudaFreeHost(h_scalars);
     for (auto& e : ev)
@@ -384,7 +401,7 @@ int check_device_error(gg_plan* p, cudaStream_t s) {
 // Key = tile | plane | |offset| class in 32 bits; the low fields shrink
 // (ordering within a tile gets coarser) if the grids have many tiles.
 TileGeom make_geom(int shape, int grid_size, int num_grids,
-                   const gg_kernels* K, int* key_bits) {
+                   const gg_kernels* K, int* key_bits, int sort_detail = 2) {
   TileGeom g{};
   g.tile_u = tile_u_of_shape(shape);
   g.tile_v = tile_v_of_shape(shape);
@@ -396,6 +413,8 @@ TileGeom make_geom(int shape, int grid_size, int num_grids,
   int plane_bits = ceil_log2((unsigned long long)K->num_planes);
   int phase_bits =
       ceil_log2((unsigned long long)(K->omax + 1) * (K->omax + 1));
+  if (sort_detail < 2) phase_bits = 0;
+  if (sort_detail < 1) plane_bits = 0;
   if (tile_bits + plane_bits + phase_bits > 32) phase_bits = 0;
   if (tile_bits + plane_bits + phase_bits > 32) plane_bits = 0;
   g.plane_bits = plane_bits;
@@ -419,6 +438,21 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
                  const PlaceOut& po, int grid_size, int num_grids,
                  const unsigned long long* d_grid_offsets, Real* d_grid,
                  long long grid_stride, cudaStream_t s);
+
+// Per-chunk partial sums of a batched call live in one buffer: norm, skip
+// and MAC count arrays of num_chunks + 1 entries each.
+struct ChunkParts {
+  double* norm;
+  unsigned long long* skip;
+  unsigned long long* macs;
+};
+ChunkParts chunk_parts(gg_plan* p, int num_chunks) {
+  ChunkParts c;
+  c.norm = p->chunk_part.as<double>();
+  c.skip = (unsigned long long*)(c.norm + num_chunks + 1);
+  c.macs = c.skip + num_chunks + 1;
+  return c;
+}
 
 template <typename Real>
 int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
@@ -451,6 +485,7 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   plan->stats = gg_stats{};
   plan->stats.num_points = num_points;
   plan->events_valid = false;
+  plan->kept.valid = false;
 
   const StackView view = K->view();
   const int tiles_cap = max_tiles(grid_size, 1);
@@ -537,7 +572,8 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
   plan->stats.num_records = total;
   memcpy(&plan->stats.num_macs, (char*)plan->h_scalars + 32, 8);
   int key_bits = 0;
-  const TileGeom geom = make_geom(shape, grid_size, num_grids, K, &key_bits);
+  const TileGeom geom = make_geom(shape, grid_size, num_grids, K, &key_bits,
+                                  plan->sort_detail);
   const int num_tiles = num_grids * geom.tiles_u * geom.tiles_v;
   const int low_bits = geom.plane_bits + geom.phase_bits;
   plan->stats.tile_u = geom.tile_u;
@@ -546,6 +582,11 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
   // can only wrap for inputs far beyond the per-call limit; guard anyway.
   if ((unsigned long long)total > 0xFFFFFFF0ull)
     return set_error(GG_ERR_UNSUPPORTED, "record count overflow");
+  plan->kept.num_records = total;
+  plan->kept.geom = geom;
+  plan->kept.shape = shape;
+  plan->kept.stage = stage;
+  plan->kept.num_tiles = num_tiles;
 
   if (total > 0) {
     GG_TRY(plan->keys0.ensure((size_t)total * 4));
@@ -577,12 +618,21 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
 
     int sms = 0;
     GG_TRY(num_sms_of_current(&sms));
-    const int num_ctas =
-        sms * grid_tiles_ctas_per_sm<Real>(geom.tile_u, stage);
+    int per_sm = grid_tiles_ctas_per_sm<Real>(geom.tile_u, stage);
+    if (plan->ctas_per_sm > 0) per_sm = std::min(per_sm, plan->ctas_per_sm);
+    const int num_ctas = sms * per_sm;
+    // Heavy tiles are split into work items of `chunk` records so that the
+    // call has about items_per_cta items per CTA.  Items: at most one more
+    // per tile than total / chunk; partial-tile slots (split tiles only):
+    // at most 2 * total / chunk.
+    const unsigned long long f = (unsigned long long)plan->items_per_cta;
     const uint32_t chunk = (uint32_t)std::max<unsigned long long>(
-        64, ((unsigned long long)total + 4ull * num_ctas - 1) / (4ull * num_ctas));
-    const size_t item_cap = (size_t)num_tiles + 8 * (size_t)num_ctas + 16;
-    const size_t slot_cap = 8 * (size_t)num_ctas + 16;
+        64, ((unsigned long long)total + f * num_ctas - 1) / (f * num_ctas));
+    const size_t item_cap = (size_t)num_tiles + 2 * f * (size_t)num_ctas + 16;
+    const size_t slot_cap = 2 * f * (size_t)num_ctas + 16;
+    plan->stats.slice_staging = stage ? 1 : 0;
+    plan->stats.num_ctas = num_ctas;
+    plan->stats.chunk_records = chunk;
     GG_TRY(plan->item_a.ensure((size_t)num_tiles * 4 + 4));
     GG_TRY(plan->item_b.ensure((size_t)num_tiles * 4 + 4));
     GG_TRY(plan->items.ensure(item_cap * sizeof(WorkItem)));
@@ -601,6 +651,8 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
     ib.scan_tmp = plan->scan_tmp.p;
     GG_CUDA(launch_build_items(plan->tile_start.as<uint32_t>(), num_tiles,
                                total, chunk, ib, s));
+    plan->kept.rec_vis = vals;
+    plan->kept.num_ctas = num_ctas;
     plan->mark(3, s);
     GG_CUDA(launch_grid_tiles<Real>(
         ib.items, ib.num_items, ib.counter, sc + kDeviceError, vals, po.cell,
@@ -668,6 +720,7 @@ int batched_pipeline(gg_plan* plan, const gg_kernels* K, int num_grids,
   plan->stats = gg_stats{};
   plan->stats.num_points = n;
   plan->events_valid = false;
+  plan->kept.valid = false;
   const StackView view = K->view();
   const int tiles_cap = max_tiles(grid_size, num_grids);
 
@@ -721,10 +774,7 @@ int batched_pipeline(gg_plan* plan, const gg_kernels* K, int num_grids,
   po.blk_norm = nullptr;
   po.blk_skip = nullptr;
   po.blk_macs = nullptr;
-  double* chunk_norm = plan->chunk_part.as<double>();
-  unsigned long long* chunk_skip =
-      (unsigned long long*)(chunk_norm + num_chunks + 1);
-  unsigned long long* chunk_macs = chunk_skip + num_chunks + 1;
+  const ChunkParts cp = chunk_parts(plan, num_chunks);
 
   plan->mark(0, s);
   GG_CUDA(launch_place_batched<Real>(pp, view, po, plan->nterm.as<double>(),
@@ -732,7 +782,7 @@ int batched_pipeline(gg_plan* plan, const gg_kernels* K, int num_grids,
   GG_CUDA(launch_batch_totals(
       po.meta, plan->nterm.as<double>(), view, num_chunks,
       plan->chunk_begin.as<unsigned long long>(), num_grids,
-      plan->grid_chunk0.as<int>(), chunk_norm, chunk_skip, chunk_macs,
+      plan->grid_chunk0.as<int>(), cp.norm, cp.skip, cp.macs,
       plan->forced_shape, d_norm, d_num_skipped, scalar64(plan, kMacs),
       sc + kShape, s));
   GG_CUDA(launch_count_records(po.cell, po.meta, n, view, sc + kShape,
@@ -747,9 +797,68 @@ int batched_pipeline(gg_plan* plan, const gg_kernels* K, int num_grids,
   GG_CUDA(cudaMemcpyAsync((char*)plan->h_scalars + 32, scalar64(plan, kMacs),
                           8, cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaStreamSynchronize(s));
-  return bin_and_grid<Real>(plan, K, n, po, grid_size, num_grids,
+  GG_TRY(bin_and_grid<Real>(plan, K, n, po, grid_size, num_grids,
                             plan->grid_offsets.as<unsigned long long>(),
-                            d_grids, grid_stride, s);
+                            d_grids, grid_stride, s));
+  gg_plan::Kept& kp = plan->kept;
+  kp.kernels = K;
+  kp.is_double = sizeof(Real) == 8;
+  kp.num_points = n;
+  kp.num_grids = num_grids;
+  kp.grid_size = grid_size;
+  kp.num_chunks = num_chunks;
+  kp.valid = true;
+  return GG_OK;
+}
+
+// Grids new amplitudes and weights on the geometry kept by the plan's last
+// batched call: weighted visibilities and norm terms, per-grid totals, the
+// persistent tile-gridding launch and the partial reduction.  Kernel
+// launches and one memset only -- no host synchronisation, no allocation --
+// so the call can be captured in a CUDA graph and replayed.
+template <typename Real>
+int replay_pipeline(gg_plan* plan, const gg_kernels* K, const Real* vis,
+                    const Real* weight, unsigned long long* d_num_skipped,
+                    double* d_norm, Real* d_grids, cudaStream_t s) {
+  if (!plan || !K) return set_error(GG_ERR_INVALID_ARG, "plan or kernels is NULL");
+  const gg_plan::Kept& kp = plan->kept;
+  if (!kp.valid)
+    return set_error(GG_ERR_INVALID_ARG,
+                     "the plan holds no batched-call geometry to replay");
+  if (kp.kernels != K || kp.is_double != (sizeof(Real) == 8))
+    return set_error(GG_ERR_INVALID_ARG,
+                     "replay needs the kernel stack and precision of the "
+                     "batched call that made the geometry");
+  if (kp.num_points > 0 && (!vis || !weight))
+    return set_error(GG_ERR_INVALID_ARG, "an input array is NULL");
+  if (!d_grids || !d_norm || !d_num_skipped)
+    return set_error(GG_ERR_INVALID_ARG, "an output pointer is NULL");
+  const StackView view = K->view();
+  uint32_t* sc = plan->scalars.as<uint32_t>();
+  const ChunkParts cp = chunk_parts(plan, kp.num_chunks);
+  GG_CUDA(launch_revalue<Real>(vis, weight, plan->meta.as<uint32_t>(), view,
+                               kp.num_points, plan->vw.p,
+                               plan->nterm.as<double>(), s));
+  GG_CUDA(launch_batch_totals(
+      plan->meta.as<uint32_t>(), plan->nterm.as<double>(), view,
+      kp.num_chunks, plan->chunk_begin.as<unsigned long long>(),
+      kp.num_grids, plan->grid_chunk0.as<int>(), cp.norm, cp.skip, cp.macs,
+      kp.shape, d_norm, d_num_skipped, scalar64(plan, kMacs), sc + kShape,
+      s));
+  if (kp.num_records == 0) return GG_OK;
+  const long long grid_stride = 2LL * kp.grid_size * kp.grid_size;
+  GG_CUDA(cudaMemsetAsync(sc + kCounter, 0, sizeof(uint32_t), s));
+  GG_CUDA(launch_grid_tiles<Real>(
+      plan->items.as<WorkItem>(), sc + kNumItems, sc + kCounter,
+      sc + kDeviceError, kp.rec_vis, plan->cell.as<uint32_t>(),
+      plan->meta.as<uint32_t>(), plan->vw.p, view, kp.geom, kp.grid_size,
+      d_grids, grid_stride, plan->partials.as<Real>(), kp.num_ctas, kp.stage,
+      s));
+  GG_CUDA(launch_reduce_partials<Real>(
+      plan->split_tiles.as<int4>(), sc + kNumSplit, kp.num_tiles,
+      plan->partials.as<Real>(), kp.geom, kp.grid_size, d_grids, grid_stride,
+      s));
+  return GG_OK;
 }
 
 template <typename Real>
@@ -1058,6 +1167,42 @@ GG_API int gg_plan_set_slice_staging(gg_plan* plan, int mode) {
   return GG_OK;
 }
 
+GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* t) {
+  t_last_error.clear();
+  if (!plan || !t) return set_error(GG_ERR_INVALID_ARG, "plan or tuning is NULL");
+  if (t->items_per_cta < 1 || t->items_per_cta > 64)
+    return set_error(GG_ERR_INVALID_ARG, "items_per_cta = %d outside [1, 64]",
+                     t->items_per_cta);
+  if (t->sort_detail < 0 || t->sort_detail > 2)
+    return set_error(GG_ERR_INVALID_ARG, "sort_detail = %d: 0, 1 or 2",
+                     t->sort_detail);
+  if (t->ctas_per_sm < 0 || t->ctas_per_sm > 32)
+    return set_error(GG_ERR_INVALID_ARG, "ctas_per_sm = %d outside [0, 32]",
+                     t->ctas_per_sm);
+  const int old_shape = plan->forced_shape;
+  GG_TRY(gg_plan_set_tile_shape(plan, t->tile_u));
+  const int r = gg_plan_set_slice_staging(plan, t->slice_staging);
+  if (r != GG_OK) {
+    plan->forced_shape = old_shape;
+    return r;
+  }
+  plan->items_per_cta = t->items_per_cta;
+  plan->sort_detail = t->sort_detail;
+  plan->ctas_per_sm = t->ctas_per_sm;
+  return GG_OK;
+}
+
+GG_API int gg_plan_get_tuning(const gg_plan* plan, gg_tuning* t) {
+  t_last_error.clear();
+  if (!plan || !t) return set_error(GG_ERR_INVALID_ARG, "plan or tuning is NULL");
+  t->tile_u = plan->forced_shape < 0 ? 0 : tile_u_of_shape(plan->forced_shape);
+  t->slice_staging = plan->forced_stage;
+  t->items_per_cta = plan->items_per_cta;
+  t->sort_detail = plan->sort_detail;
+  t->ctas_per_sm = plan->ctas_per_sm;
+  return GG_OK;
+}
+
 GG_API int gg_plan_set_profiling(gg_plan* plan, int enable) {
   t_last_error.clear();
   if (!plan) return set_error(GG_ERR_INVALID_ARG, "plan is NULL");
@@ -1149,6 +1294,38 @@ GG_API int gg_grid_wproj_d_batched_device(
                                   d_vv, d_ww, d_vis, d_weight, cell_size_rad,
                                   w_scale, grid_size, d_num_skipped, d_norm,
                                   d_grids, (cudaStream_t)stream);
+}
+
+GG_API int gg_grid_wproj_f_batched_replay(gg_plan* plan,
+                                          const gg_kernels* kernels,
+                                          const float* d_vis,
+                                          const float* d_weight,
+                                          unsigned long long* d_num_skipped,
+                                          double* d_norm, float* d_grids,
+                                          void* stream) {
+  t_last_error.clear();
+  return replay_pipeline<float>(plan, kernels, d_vis, d_weight,
+                                d_num_skipped, d_norm, d_grids,
+                                (cudaStream_t)stream);
+}
+
+GG_API int gg_grid_wproj_d_batched_replay(gg_plan* plan,
+                                          const gg_kernels* kernels,
+                                          const double* d_vis,
+                                          const double* d_weight,
+                                          unsigned long long* d_num_skipped,
+                                          double* d_norm, double* d_grids,
+                                          void* stream) {
+  t_last_error.clear();
+  return replay_pipeline<double>(plan, kernels, d_vis, d_weight,
+                                 d_num_skipped, d_norm, d_grids,
+                                 (cudaStream_t)stream);
+}
+
+GG_API int gg_plan_check(gg_plan* plan, void* stream) {
+  t_last_error.clear();
+  if (!plan) return set_error(GG_ERR_INVALID_ARG, "plan is NULL");
+  return check_device_error(plan, (cudaStream_t)stream);
 }
 
 GG_API int gg_place_wproj_f_device(const gg_kernels* kernels,

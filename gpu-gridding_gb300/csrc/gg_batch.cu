@@ -66,6 +66,35 @@ k_place_batched(PlaceParams<Real> p, StackView v, PlaceOut out,
   nterm[i] = t;
 }
 
+// New amplitudes and weights on a kept geometry: weighted visibilities and
+// FP64 norm terms from the stored placement (meta), no re-placement.
+template <typename Real>
+__global__ void __launch_bounds__(kThreads)
+k_revalue(const Real* __restrict__ vis, const Real* __restrict__ weight,
+          const uint32_t* __restrict__ meta, StackView v,
+          unsigned long long n, typename Vec2<Real>::type* __restrict__ vw,
+          double* __restrict__ nterm) {
+  using R2 = typename Vec2<Real>::type;
+  const unsigned long long i =
+      (unsigned long long)blockIdx.x * kThreads + threadIdx.x;
+  if (i >= n) return;
+  const Real w = weight[i];
+  R2 o;
+  o.x = rmul(w, vis[2 * i]);
+  o.y = rmul(w, vis[2 * i + 1]);
+  vw[i] = o;
+  const uint32_t m = meta[i];
+  double t = 0.0;
+  if (!meta_skipped(m)) {
+    const int side = 2 * v.omax + 1;
+    const double ts =
+        v.tap_sum[((size_t)meta_plane(m) * side + (meta_ou(m) + v.omax)) *
+                      side + (meta_ov(m) + v.omax)];
+    t = __dmul_rn(ts, (double)w);
+  }
+  nterm[i] = t;
+}
+
 // One block per chunk of one grid.
 __global__ void __launch_bounds__(kThreads)
 k_chunk_totals(const uint32_t* __restrict__ meta,
@@ -162,6 +191,26 @@ cudaError_t launch_batch_totals(const uint32_t* meta, const double* nterm,
       chunk_macs, forced_shape, d_norm, d_num_skipped, d_macs, d_shape);
   return cudaGetLastError();
 }
+
+template <typename Real>
+cudaError_t launch_revalue(const Real* vis, const Real* weight,
+                           const uint32_t* meta, StackView view,
+                           unsigned long long n, void* vw, double* nterm,
+                           cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const unsigned nb = (unsigned)((n + kThreads - 1) / kThreads);
+  k_revalue<Real><<<nb, kThreads, 0, s>>>(
+      vis, weight, meta, view, n, (typename Vec2<Real>::type*)vw, nterm);
+  return cudaGetLastError();
+}
+template cudaError_t launch_revalue<float>(const float*, const float*,
+                                           const uint32_t*, StackView,
+                                           unsigned long long, void*, double*,
+                                           cudaStream_t);
+template cudaError_t launch_revalue<double>(const double*, const double*,
+                                            const uint32_t*, StackView,
+                                            unsigned long long, void*,
+                                            double*, cudaStream_t);
 
 template cudaError_t launch_place_batched<float>(PlaceParams<float>,
                                                  StackView, PlaceOut, double*,

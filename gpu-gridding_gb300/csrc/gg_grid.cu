@@ -35,6 +35,7 @@
 // plain FP32 FMA, then folded into a (hi, lo) pair by Knuth's TwoSum, so
 // rounding error does not grow with the number of visibilities on a cell.
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 
 #include "gg_internal.h"
@@ -681,14 +682,23 @@ void* grid_kernel_ptr() {
 }
 
 // The kernels take more than 48 KB of dynamic shared memory: opt in before
-// querying occupancy or launching.
+// querying occupancy or launching.  The opt-in is made once per device, so
+// later launches (replays captured in a CUDA graph among them) make no
+// attribute call.
 template <typename Real, int TW, bool kStage>
 cudaError_t prepare_grid_kernel(void** fn, size_t* smem) {
+  static std::atomic<unsigned long long> opted_in{0};
   *fn = grid_kernel_ptr<Real, TW, kStage>();
   *smem = sizeof(Smem<Real, kStage>);
-  return cudaFuncSetAttribute(*fn,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)*smem);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (dev < 64 && (opted_in.load() & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(*fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)*smem);
+  if (e == cudaSuccess && dev < 64) opted_in.fetch_or(bit);
+  return e;
 }
 
 template <typename Real>

@@ -120,6 +120,13 @@ cudaError_t launch_emit_records(const uint32_t* cell, const uint32_t* meta,
 template <typename Real>
 cudaError_t launch_place_batched(PlaceParams<Real> p, StackView view,
                                  PlaceOut out, double* nterm, cudaStream_t s);
+// Weighted visibilities and norm terms for new amplitudes and weights on
+// an existing placement (meta).
+template <typename Real>
+cudaError_t launch_revalue(const Real* vis, const Real* weight,
+                           const uint32_t* meta, StackView view,
+                           unsigned long long n, void* vw, double* nterm,
+                           cudaStream_t s);
 // Deterministic per-grid totals over a chunk table (chunk c covers
 // visibilities [chunk_begin[c], chunk_begin[c+1]) of grid chunk_grid[c];
 // grid g owns chunks [grid_chunk0[g], grid_chunk0[g+1])):

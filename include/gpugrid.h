@@ -132,6 +132,9 @@ typedef struct
     unsigned long long num_macs;        /* complex multiply-adds performed */
     unsigned long long num_launches;    /* kernels this library launched */
     int tile_u, tile_v;                 /* tile shape used */
+    int slice_staging;                  /* 1 if slices were staged */
+    int num_ctas;                       /* persistent gridding CTAs */
+    unsigned long long chunk_records;   /* records per work item (max) */
 } gg_stats;
 
 GG_API int gg_plan_last_stats(const gg_plan* plan, gg_stats* stats);
@@ -149,6 +152,34 @@ GG_API int gg_plan_set_tile_shape(gg_plan* plan, int tile_u);
  * 1 on.  Results are bit-identical either way: only where the taps are
  * read from changes, not the arithmetic or its order. */
 GG_API int gg_plan_set_slice_staging(gg_plan* plan, int mode);
+
+/* Launch and decomposition parameters of a plan's gridding calls, as set
+ * by an autotuner (or by hand).  Every setting changes speed only; tile_u
+ * and sort_detail also change the order in which contributions to a cell
+ * are added (results then differ by FP32 rounding, not in placement, norm
+ * or num_skipped).
+ *   tile_u         32, 16 or 8 (cells across a tile); 0 = chosen per call
+ *   slice_staging  -1 chosen per call, 0 off, 1 on (bit-identical results)
+ *   items_per_cta  work items per persistent CTA that the split of heavy
+ *                  tiles aims for, 1..64 (default 4): more items balance
+ *                  the load better but write more partial tiles
+ *   sort_detail    order of a tile's records: 2 (default) by w-plane then
+ *                  kernel-offset class, 1 by w-plane, 0 visibility order
+ *   ctas_per_sm    resident gridding CTAs per SM, 0 (default) = as many as
+ *                  fit, else min(that, what fits), 1..32
+ * gg_plan_set_tile_shape and gg_plan_set_slice_staging set the first two
+ * fields alone. */
+typedef struct
+{
+    int tile_u;
+    int slice_staging;
+    int items_per_cta;
+    int sort_detail;
+    int ctas_per_sm;
+} gg_tuning;
+
+GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* tuning);
+GG_API int gg_plan_get_tuning(const gg_plan* plan, gg_tuning* tuning);
 
 /* Phase timing.  With profiling enabled, every gridding call made with the
  * plan records CUDA events on its stream around five phases:
@@ -212,6 +243,34 @@ GG_API int gg_grid_wproj_d_batched_device(gg_plan* plan,
         const double* d_weight, double cell_size_rad, double w_scale,
         int grid_size, unsigned long long* d_num_skipped, double* d_norm,
         double* d_grids, void* stream);
+
+/* Replay of a plan's last batched call on new amplitudes and weights.  The
+ * plan keeps the geometry of its last successful batched call (placement,
+ * sorted records, work items, tile shape); a replay grids d_vis and
+ * d_weight -- laid out like that call's inputs, same number of
+ * visibilities -- with it, for imaging loops whose (u, v, w) coordinates
+ * stay fixed while the amplitudes change between major cycles.  Outputs as
+ * in the batched call (grids and d_norm accumulated, d_num_skipped set);
+ * with the original amplitudes and weights the results are bit-identical
+ * to the batched call's.  A replay only enqueues kernel launches and a
+ * memset on the stream -- no allocation, no host synchronisation -- so it
+ * may be captured in a CUDA graph.  Any other gridding call on the plan
+ * discards the kept geometry (GG_ERR_INVALID_ARG on the next replay).  The
+ * kernels argument must be the batched call's.  A failure inside the
+ * gridding kernel (a bounded wait that ran out) is reported by the next
+ * gg_plan_check or the next non-replay call. */
+GG_API int gg_grid_wproj_f_batched_replay(gg_plan* plan,
+        const gg_kernels* kernels, const float* d_vis, const float* d_weight,
+        unsigned long long* d_num_skipped, double* d_norm, float* d_grids,
+        void* stream);
+GG_API int gg_grid_wproj_d_batched_replay(gg_plan* plan,
+        const gg_kernels* kernels, const double* d_vis,
+        const double* d_weight, unsigned long long* d_num_skipped,
+        double* d_norm, double* d_grids, void* stream);
+
+/* Synchronises the stream and returns GG_ERR_CUDA if a gridding kernel of
+ * this plan flagged a failure (a bounded wait that ran out). */
+GG_API int gg_plan_check(gg_plan* plan, void* stream);
 
 /* Allocation-free form of gg_grid_wproj_f_device, for callers that cannot
  * allocate device memory while they grid (a real-time loop that must not

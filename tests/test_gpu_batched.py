@@ -95,3 +95,101 @@ def test_batched_rejects_bad_offsets(pkg, torch, batch):
             torch.zeros((2, 64, 64, 2), device="cuda"),
             torch.zeros(2, dtype=torch.float64, device="cuda"),
             torch.zeros(2, dtype=torch.int64, device="cuda"))
+
+
+def _replay(pkg, torch, plan, stack, vis, weight, C, G):
+    grids = torch.zeros((C, G, G, 2), dtype=torch.float32, device="cuda")
+    norms = torch.zeros(C, dtype=torch.float64, device="cuda")
+    skips = torch.full((C,), -1, dtype=torch.int64, device="cuda")
+    pkg.grid_wproj_batched_replay(plan, stack, vis, weight, grids, norms,
+                                  skips)
+    pkg.check_plan(plan)
+    return grids.cpu().numpy(), norms.cpu().numpy(), skips.cpu().numpy()
+
+
+def _same(a, b):
+    assert np.array_equal(a[0].view(np.uint32), b[0].view(np.uint32))
+    assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+
+
+def _new_values(wl, seed):
+    rng = np.random.default_rng(seed)
+    vis = rng.standard_normal(wl.vis.shape).astype(np.float32)
+    weight = rng.uniform(0.5, 2.0, wl.num_points).astype(np.float32)
+    return vis, weight
+
+
+def test_replay_matches_batched_calls(pkg, torch, batch):
+    """A replay with the original amplitudes reproduces the batched call bit
+    for bit; with new amplitudes and weights it matches a fresh batched call
+    on them bit for bit (the geometry depends on (u, v, w) only)."""
+    import copy
+    wl = batch
+    C, G = wl.num_grids, wl.grid_size
+    stack = pkg.KernelStack.from_workload(wl, "f")
+    plan = pkg.Plan()
+    ref = _run_batched(pkg, torch, wl, plan, stack)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    _same(_replay(pkg, torch, plan, stack, dev(wl.vis), dev(wl.weight), C, G),
+          ref)
+    vis2, w2 = _new_values(wl, 5)
+    got = _replay(pkg, torch, plan, stack, dev(vis2), dev(w2), C, G)
+    wl2 = copy.copy(wl)
+    wl2.vis, wl2.weight = vis2, w2
+    _same(got, _run_batched(pkg, torch, wl2, pkg.Plan(), stack))
+
+
+def test_replay_in_cuda_graph(pkg, torch, batch):
+    """The replay captured in a CUDA graph: launching the graph after the
+    inputs change in place gives the direct replay's results."""
+    wl = batch
+    C, G = wl.num_grids, wl.grid_size
+    stack = pkg.KernelStack.from_workload(wl, "f")
+    plan = pkg.Plan()
+    _run_batched(pkg, torch, wl, plan, stack)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    vis, weight = dev(wl.vis), dev(wl.weight)
+    grids = torch.zeros((C, G, G, 2), dtype=torch.float32, device="cuda")
+    norms = torch.zeros(C, dtype=torch.float64, device="cuda")
+    skips = torch.full((C,), -1, dtype=torch.int64, device="cuda")
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        grids.zero_()
+        norms.zero_()
+        pkg.grid_wproj_batched_replay(plan, stack, vis, weight, grids, norms,
+                                      skips)
+    for seed in (11, 12):
+        v2, w2 = _new_values(wl, seed)
+        vis.copy_(dev(v2))
+        weight.copy_(dev(w2))
+        graph.replay()
+        pkg.check_plan(plan)
+        got = (grids.cpu().numpy(), norms.cpu().numpy(), skips.cpu().numpy())
+        _same(got, _replay(pkg, torch, plan, stack, dev(v2), dev(w2), C, G))
+    del graph
+
+
+def test_replay_needs_kept_geometry(pkg, torch, batch):
+    wl = batch
+    C, G = wl.num_grids, wl.grid_size
+    stack = pkg.KernelStack.from_workload(wl, "f")
+    other = pkg.KernelStack.from_workload(wl, "f")
+    plan = pkg.Plan()
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    vis, weight = dev(wl.vis), dev(wl.weight)
+    with pytest.raises(pkg.GridError):   # nothing kept yet
+        _replay(pkg, torch, plan, stack, vis, weight, C, G)
+    _run_batched(pkg, torch, wl, plan, stack)
+    with pytest.raises(pkg.GridError):   # another kernel stack
+        _replay(pkg, torch, plan, other, vis, weight, C, G)
+    ch = wl.channel(0)
+    g = torch.zeros((G, G, 2), dtype=torch.float32, device="cuda")
+    pkg.grid_wproj_device(plan, stack, dev(ch.uu), dev(ch.vv), dev(ch.ww),
+                          dev(ch.vis), dev(ch.weight),
+                          np.float32(ch.cell_size_rad), np.float32(ch.w_scale),
+                          G, g, torch.zeros(1, dtype=torch.float64,
+                                            device="cuda"),
+                          torch.zeros(1, dtype=torch.int64, device="cuda"))
+    with pytest.raises(pkg.GridError):   # a single call discarded it
+        _replay(pkg, torch, plan, stack, vis, weight, C, G)
