@@ -8,7 +8,8 @@ no placement, norm or skip count (gg_tuning in the C header):
 * ``items_per_cta`` -- how finely heavy tiles are split into work items,
 * ``sort_detail``   -- record order within a tile (plane + offset class,
   plane only, or visibility order),
-* ``ctas_per_sm``   -- resident gridding CTAs per SM (0 = as many as fit).
+* ``ctas_per_sm``   -- resident gridding CTAs per SM (0 = as many as fit),
+* ``plane_group_mb`` -- kernel bytes per gridding pass (0 = a quarter of L2).
 
 :func:`search` runs a coordinate search over them with a caller-supplied
 timing function; :func:`autotune` times real gridding calls of a workload
@@ -32,11 +33,11 @@ from typing import Callable, Dict, Iterable, Optional
 import numpy as np
 
 CACHE_ENV = "GPUGRID_TUNE_CACHE"
-CACHE_VERSION = 1
+CACHE_VERSION = 2
 
 #: The plan's settings before any tuning (each call chooses shape/staging).
 DEFAULT_TUNING = {"tile_u": 0, "slice_staging": -1, "items_per_cta": 4,
-                  "sort_detail": 2, "ctas_per_sm": 0}
+                  "sort_detail": 2, "ctas_per_sm": 0, "plane_group_mb": 0}
 
 #: Values tried per setting, in search order.
 SEARCH_SPACE = (
@@ -45,6 +46,7 @@ SEARCH_SPACE = (
     (("items_per_cta",), [(2,), (4,), (8,), (16,)]),
     (("sort_detail",), [(2,), (1,), (0,)]),
     (("ctas_per_sm",), [(0,), (1,)]),
+    (("plane_group_mb",), [(0,), (16,), (64,), (1 << 20,)]),
 )
 
 
@@ -76,7 +78,7 @@ def tuning_key(grid_size: int, num_w_planes: int, max_support: int,
 
 
 class TuningCache:
-    """JSON file of tuned settings: {"version": 1, "devices": {name: {key:
+    """JSON file of tuned settings: {"version": 2, "devices": {name: {key:
     {setting: value, ..., "ms": t}}}}."""
 
     def __init__(self, path: Optional[str] = None):

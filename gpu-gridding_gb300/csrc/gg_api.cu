@@ -13,6 +13,7 @@
 //   8. reduce          split tiles: grid += partials, in chunk order
 // The host synchronises once, after step 2, to size the sort buffers.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -159,15 +160,17 @@ int num_sms_of_current(int* sms) {
 // Kernel stacks
 // ===========================================================================
 struct gg_kernels {
+  unsigned long long id = 0;   // unique per handle (plans cache by it)
   int device = 0;
   bool is_double = false;
   int num_planes = 0, oversample = 0, omax = 0, conv_size_half = 0;
   int support_max = 0;
   long long total_taps = 0;
   std::vector<int> h_support;
-  std::vector<long long> h_base;
+  std::vector<long long> h_base, h_sbase;
+  long long total_slab_taps = 0;
   size_t zero_half_bytes = 0;
-  DevBuf support, base, taps, tap_sum, zeros;
+  DevBuf support, base, taps, tap_sum, zeros, sbase, slabs;
 
   StackView view() const {
     StackView v;
@@ -180,6 +183,8 @@ struct gg_kernels {
     v.taps = taps.p;
     v.tap_sum = tap_sum.as<double>();
     v.zeros = zeros.as<char>() + zero_half_bytes;
+    v.sbase = sbase.as<long long>();
+    v.slabs = slabs.p;
     return v;
   }
 };
@@ -225,6 +230,8 @@ int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
   GG_TRY(validate_stack(num_w_planes, support, oversample, conv_size_half,
                         conv_func));
   gg_kernels* k = new gg_kernels();
+  static std::atomic<unsigned long long> next_id{1};
+  k->id = next_id.fetch_add(1);
   auto fail = [&](int code) {
     delete k;
     return code;
@@ -245,12 +252,28 @@ int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
     total += classes * slice_taps(support[p]);
     k->support_max = std::max(k->support_max, support[p]);
   }
-  if (total > 0x7fffffffLL)
+  k->h_sbase.resize(num_w_planes);
+  long long qtotal = 0;
+  for (size_t p = 0; p < num_w_planes; ++p) {
+    k->h_sbase[p] = qtotal;
+    qtotal += (k->omax + 1) * slab_taps(support[p], oversample, k->omax);
+  }
+  // Slab row pitch and column bases are 16-bit fields of the gridding
+  // kernel's record descriptors.
+  if ((long long)oversample * (k->support_max + 2) + k->support_max + 64 >
+      32767)
+    return fail(set_error(GG_ERR_UNSUPPORTED,
+                          "oversample * (support + 2) = %lld exceeds this "
+                          "build's slab row limit",
+                          (long long)oversample * (k->support_max + 2)));
+  // Record descriptors hold slab offsets plus column bases in 32 bits.
+  if (total > 0x7fffffffLL || qtotal > 0x7fffffffLL - (1LL << 24))
     return fail(set_error(GG_ERR_UNSUPPORTED,
                           "re-laid kernel stack has %lld taps; this build "
                           "indexes at most 2^31-1",
-                          total));
+                          std::max(total, qtotal)));
   k->total_taps = total;
+  k->total_slab_taps = qtotal;
   // Zero buffer for lanes outside a footprint: a lane reads kRows = 8 rows
   // at a stride of up to 2*s_max+1 taps either way from its middle.
   k->zero_half_bytes = (size_t)8 * (2 * k->support_max + 1) * 2 * sizeof(Real);
@@ -259,6 +282,8 @@ int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
       (r = k->base.ensure(num_w_planes * sizeof(long long))) ||
       (r = k->taps.ensure((size_t)total * 2 * sizeof(Real))) ||
       (r = k->zeros.ensure(2 * k->zero_half_bytes + 256)) ||
+      (r = k->sbase.ensure(num_w_planes * sizeof(long long))) ||
+      (r = k->slabs.ensure((size_t)qtotal * 2 * sizeof(Real) + 16)) ||
       (r = k->tap_sum.ensure(num_w_planes * (2 * k->omax + 1) *
                              (2 * k->omax + 1) * sizeof(double))))
     return fail(r);
@@ -273,7 +298,10 @@ int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
                               cudaMemcpyHostToDevice, s), "support H2D")) ||
       (r = cu(cudaMemcpyAsync(k->base.p, base.data(),
                               num_w_planes * sizeof(long long),
-                              cudaMemcpyHostToDevice, s), "base H2D")))
+                              cudaMemcpyHostToDevice, s), "base H2D")) ||
+      (r = cu(cudaMemcpyAsync(k->sbase.p, k->h_sbase.data(),
+                              num_w_planes * sizeof(long long),
+                              cudaMemcpyHostToDevice, s), "sbase H2D")))
     return fail(r);
   const size_t cube = num_w_planes * (size_t)conv_size_half * conv_size_half *
                       2 * sizeof(Real);
@@ -289,6 +317,9 @@ int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
   StackView v = k->view();
   if ((r = cu(launch_stack_relayout<Real>(d_conv, v, k->taps.p, total, s),
               "relayout")))
+    return fail(r);
+  if ((r = cu(launch_stack_relayout_slabs<Real>(d_conv, v, k->slabs.p, s),
+              "slab relayout")))
     return fail(r);
   StackView raw = v;
   raw.taps = d_conv;
@@ -323,6 +354,15 @@ struct gg_plan {
   int items_per_cta = 4;  // work-item granularity of heavy-tile splits
   int sort_detail = 2;    // low sort-key fields: 2 plane+class, 1 plane, 0
   int ctas_per_sm = 0;    // cap on resident gridding CTAs, 0 = none
+  int plane_group_mb = 0; // slab bytes per plane group, 0 = L2 size / 4
+  // Plane groups of the last call (see TileGeom): table, and what it was
+  // computed for.
+  DevBuf plane_group, group_items;
+  std::vector<int> h_plane_group;
+  unsigned long long pg_kernels = 0;   // id of the kernel stack
+  long long pg_budget = -1;           // requested budget (bytes)
+  int pg_max_groups = 0;
+  int pg_groups = 1;
   bool profile = false;
   bool events_valid = false;
   cudaEvent_t ev[kEvents] = {};
@@ -401,15 +441,19 @@ int check_device_error(gg_plan* p, cudaStream_t s) {
 // Key = tile | plane | |offset| class in 32 bits; the low fields shrink
 // (ordering within a tile gets coarser) if the grids have many tiles.
 TileGeom make_geom(int shape, int grid_size, int num_grids,
-                   const gg_kernels* K, int* key_bits, int sort_detail = 2) {
+                   const gg_kernels* K, int* key_bits, int sort_detail = 2,
+                   int num_groups = 1, const int* plane_group = nullptr) {
   TileGeom g{};
   g.tile_u = tile_u_of_shape(shape);
   g.tile_v = tile_v_of_shape(shape);
   g.tiles_u = (grid_size + g.tile_u - 1) / g.tile_u;
   g.tiles_v = (grid_size + g.tile_v - 1) / g.tile_v;
   g.num_grids = num_grids;
-  const int tile_bits = ceil_log2((unsigned long long)num_grids *
-                                  g.tiles_u * g.tiles_v);
+  g.tiles_total = num_grids * g.tiles_u * g.tiles_v;
+  g.num_groups = num_groups;
+  g.plane_group = num_groups > 1 ? plane_group : nullptr;
+  const int tile_bits = ceil_log2((unsigned long long)num_groups *
+                                  g.tiles_total);
   int plane_bits = ceil_log2((unsigned long long)K->num_planes);
   int phase_bits =
       ceil_log2((unsigned long long)(K->omax + 1) * (K->omax + 1));
@@ -422,6 +466,66 @@ TileGeom make_geom(int shape, int grid_size, int num_grids,
   g.phase_side = K->omax + 1;
   *key_bits = tile_bits + plane_bits + phase_bits;
   return g;
+}
+
+// Plane groups for a call: consecutive w-planes whose slabs together stay
+// within the byte budget (plan->plane_group_mb, or a quarter of the L2
+// cache), so that each gridding pass reads a stack slice that stays
+// resident in L2.  At most max_groups groups (the sort key's spare bits).
+// Uploads the plane -> group table when it changes; returns the number of
+// groups in *num_groups.
+int plane_groups(gg_plan* plan, const gg_kernels* K, int max_groups,
+                 cudaStream_t s, int* num_groups) {
+  long long budget = (long long)plan->plane_group_mb << 20;
+  const long long requested = budget;
+  if (budget <= 0) {
+    int l2 = 0;
+    GG_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, K->device));
+    budget = std::max<long long>((long long)l2 / 4, 1 << 20);
+  }
+  max_groups = std::max(1, std::min(max_groups, 64));
+  if (plan->pg_kernels == K->id && plan->pg_budget == requested &&
+      plan->pg_max_groups == max_groups) {
+    *num_groups = plan->pg_groups;
+    return GG_OK;
+  }
+  const long long tap_bytes = K->is_double ? 16 : 8;
+  std::vector<long long> bytes(K->num_planes);
+  long long total = 0;
+  for (int p = 0; p < K->num_planes; ++p) {
+    bytes[p] = (K->omax + 1) *
+               slab_taps(K->h_support[p], K->oversample, K->omax) * tap_bytes;
+    total += bytes[p];
+  }
+  // More groups than allowed: widen the budget until they fit.
+  budget = std::max(budget, (total + max_groups - 1) / max_groups);
+  std::vector<int>& grp = plan->h_plane_group;
+  grp.assign(K->num_planes, 0);
+  int g = 0;
+  long long acc = 0;
+  for (int p = 0; p < K->num_planes; ++p) {
+    if (acc > 0 && acc + bytes[p] > budget) {
+      ++g;
+      acc = 0;
+    }
+    grp[p] = g;
+    acc += bytes[p];
+  }
+  int groups = g + 1;
+  if (groups > max_groups) {   // rounding left one group too many: merge
+    for (int& x : grp) x = std::min(x, max_groups - 1);
+    groups = max_groups;
+  }
+  GG_TRY(plan->plane_group.ensure((size_t)K->num_planes * sizeof(int)));
+  GG_CUDA(cudaMemcpyAsync(plan->plane_group.p, grp.data(),
+                          (size_t)K->num_planes * sizeof(int),
+                          cudaMemcpyHostToDevice, s));
+  plan->pg_kernels = K->id;
+  plan->pg_budget = requested;
+  plan->pg_max_groups = max_groups;
+  plan->pg_groups = groups;
+  *num_groups = groups;
+  return GG_OK;
 }
 
 int max_tiles(int grid_size, int num_grids) {
@@ -572,9 +676,23 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
   plan->stats.num_records = total;
   memcpy(&plan->stats.num_macs, (char*)plan->h_scalars + 32, 8);
   int key_bits = 0;
+  // Plane groups: as many as the key's spare bits above the tile index
+  // allow (at most 64).
+  const int base_bits = ceil_log2((unsigned long long)num_grids *
+                                  ((grid_size + tile_u_of_shape(shape) - 1) /
+                                   tile_u_of_shape(shape)) *
+                                  ((grid_size + tile_v_of_shape(shape) - 1) /
+                                   tile_v_of_shape(shape)));
+  int num_groups = 1;
+  GG_TRY(plane_groups(plan, K, base_bits >= 32 ? 1 : 1 << std::min(6, 32 - base_bits),
+                      s, &num_groups));
   const TileGeom geom = make_geom(shape, grid_size, num_grids, K, &key_bits,
-                                  plan->sort_detail);
-  const int num_tiles = num_grids * geom.tiles_u * geom.tiles_v;
+                                  plan->sort_detail, num_groups,
+                                  plan->plane_group.as<int>());
+  const int num_tiles = num_groups * geom.tiles_total;
+  plan->stats.num_plane_groups = num_groups;
+  // The work-item scans run over every virtual tile (group, tile).
+  GG_TRY(plan->scan_tmp.ensure(scan_temp_bytes((size_t)num_tiles)));
   const int low_bits = geom.plane_bits + geom.phase_bits;
   plan->stats.tile_u = geom.tile_u;
   plan->stats.tile_v = geom.tile_v;
@@ -639,9 +757,12 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
     GG_TRY(plan->split_tiles.ensure((size_t)num_tiles * sizeof(int4) + 16));
     GG_TRY(plan->partials.ensure(slot_cap * geom.tile_u * geom.tile_v *
                                  sizeof(R2)));
+    GG_TRY(plan->group_items.ensure((size_t)(num_groups + 1) * 4));
     ItemBuffers ib;
     ib.chunks = plan->item_a.as<uint32_t>();
     ib.split_chunks = plan->item_b.as<uint32_t>();
+    ib.group_items = plan->group_items.as<uint32_t>();
+    ib.num_groups = num_groups;
     ib.num_items = sc + kNumItems;
     ib.num_slots = sc + kNumSlots;
     ib.items = plan->items.as<WorkItem>();
@@ -655,17 +776,15 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
     plan->kept.num_ctas = num_ctas;
     plan->mark(3, s);
     GG_CUDA(launch_grid_tiles<Real>(
-        ib.items, ib.num_items, ib.counter, sc + kDeviceError, vals, po.cell,
+        ib.items, ib.group_items, ib.counter, sc + kDeviceError, vals, po.cell,
         po.meta, po.vw, view, geom, grid_size, d_grid, grid_stride,
-        plan->partials.as<Real>(), num_ctas, stage, s));
+        plan->partials.as<Real>(), ib.split_tiles, ib.num_split, num_tiles,
+        num_ctas, stage, s));
     plan->mark(4, s);
-    GG_CUDA(launch_reduce_partials<Real>(ib.split_tiles, ib.num_split,
-                                         num_tiles, plan->partials.as<Real>(),
-                                         geom, grid_size, d_grid, grid_stride,
-                                         s));
     plan->mark(5, s);
-    // tile bounds, item counts, 2 scans, item emit, gridding, reduction
-    plan->stats.num_launches += 1 + 1 + 6 + 1 + 1 + 1;
+    // tile bounds, item counts, 2 scans, item emit, then per plane group
+    // the gridding pass and its partial reduction
+    plan->stats.num_launches += 1 + 1 + 6 + 1 + 2 * num_groups;
     plan->events_valid = plan->profile;
   }
   return GG_OK;
@@ -847,17 +966,14 @@ int replay_pipeline(gg_plan* plan, const gg_kernels* K, const Real* vis,
       s));
   if (kp.num_records == 0) return GG_OK;
   const long long grid_stride = 2LL * kp.grid_size * kp.grid_size;
-  GG_CUDA(cudaMemsetAsync(sc + kCounter, 0, sizeof(uint32_t), s));
   GG_CUDA(launch_grid_tiles<Real>(
-      plan->items.as<WorkItem>(), sc + kNumItems, sc + kCounter,
+      plan->items.as<WorkItem>(), plan->group_items.as<uint32_t>(),
+      sc + kCounter,
       sc + kDeviceError, kp.rec_vis, plan->cell.as<uint32_t>(),
       plan->meta.as<uint32_t>(), plan->vw.p, view, kp.geom, kp.grid_size,
-      d_grids, grid_stride, plan->partials.as<Real>(), kp.num_ctas, kp.stage,
-      s));
-  GG_CUDA(launch_reduce_partials<Real>(
-      plan->split_tiles.as<int4>(), sc + kNumSplit, kp.num_tiles,
-      plan->partials.as<Real>(), kp.geom, kp.grid_size, d_grids, grid_stride,
-      s));
+      d_grids, grid_stride, plan->partials.as<Real>(),
+      plan->split_tiles.as<int4>(), sc + kNumSplit, kp.num_tiles, kp.num_ctas,
+      kp.stage, s));
   return GG_OK;
 }
 
@@ -1179,6 +1295,10 @@ GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* t) {
   if (t->ctas_per_sm < 0 || t->ctas_per_sm > 32)
     return set_error(GG_ERR_INVALID_ARG, "ctas_per_sm = %d outside [0, 32]",
                      t->ctas_per_sm);
+  if (t->plane_group_mb < 0 || t->plane_group_mb > (1 << 20))
+    return set_error(GG_ERR_INVALID_ARG,
+                     "plane_group_mb = %d outside [0, 1048576]",
+                     t->plane_group_mb);
   const int old_shape = plan->forced_shape;
   GG_TRY(gg_plan_set_tile_shape(plan, t->tile_u));
   const int r = gg_plan_set_slice_staging(plan, t->slice_staging);
@@ -1189,6 +1309,7 @@ GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* t) {
   plan->items_per_cta = t->items_per_cta;
   plan->sort_detail = t->sort_detail;
   plan->ctas_per_sm = t->ctas_per_sm;
+  plan->plane_group_mb = t->plane_group_mb;
   return GG_OK;
 }
 
@@ -1200,6 +1321,7 @@ GG_API int gg_plan_get_tuning(const gg_plan* plan, gg_tuning* t) {
   t->items_per_cta = plan->items_per_cta;
   t->sort_detail = plan->sort_detail;
   t->ctas_per_sm = plan->ctas_per_sm;
+  t->plane_group_mb = plan->plane_group_mb;
   return GG_OK;
 }
 

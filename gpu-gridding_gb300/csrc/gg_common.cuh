@@ -79,7 +79,36 @@ struct StackView {
   const double* tap_sum;    // [P][2*omax+1][2*omax+1] sum of Re(tap), FP64
   const void* zeros;        // middle of a zero buffer that any lane's rows
                             // (kRows rows of any slice stride) stay inside
+  const long long* sbase;   // [P] first tap of plane p in the slab stack
+  const void* slabs;        // slab stack (see below)
 };
+
+// ---------------------------------------------------------------------------
+// Slab stack: footprint rows in order, columns residue-major.
+// ---------------------------------------------------------------------------
+// For plane p and row class c = |off_v| in [0, omax] a slab holds the
+// footprint's rows j = -s..s in order, each the quadrant row
+// t = |c + j*os|, with kSlicePad zero rows before and after:
+//   slab_{p,c}[kSlicePad + j + s][r][m] = K_p[|c + j*os|][r + m*os]
+// for residues r in [0, os) and lattice indices m in [0, M), M = s + 1
+// (+1 when omax >= os, i.e. os = 1).  A negative off_v reads the slab's
+// rows in reverse (|-c + j*os| = |c + (-j)*os|).  Rows are stored by column
+// residue: the tap of footprint column k for offset ou is
+// K[.][|ou + k*os|], and on either side of the fold ou + k*os = 0 that
+// column has one residue and a lattice index that moves by one per column,
+// so a warp's lanes (consecutive k) read at most two contiguous runs of a
+// row, and a lane's rows are evenly spaced.  Each quadrant row appears in
+// the slabs of a plane about 1.5 times (against (omax + 1) times plus the
+// column mirror in the per-offset slices above), which keeps the whole
+// stack of a large W-projection setup in L2.
+__host__ __device__ inline int slab_cols_m(int s, int os, int omax) {
+  return s + 1 + (omax >= os ? 1 : 0);
+}
+// Taps of one slab, rounded up to an even count (16-byte aligned slabs).
+__host__ __device__ inline long long slab_taps(int s, int os, int omax) {
+  return ((long long)(2 * s + 1 + 2 * kSlicePad) * os *
+              slab_cols_m(s, os, omax) + 1) & ~1LL;
+}
 
 // Taps one slice occupies: padding rows included, rounded up to an even
 // count so that every slice starts 16-byte aligned (bulk copies need it).
@@ -116,12 +145,19 @@ struct PlaceParams {
 };
 
 // Tile geometry shared by the binning and gridding kernels.
+// With plane groups (num_groups > 1) the records of a call are gridded in
+// one pass per group of consecutive w-planes, each group's kernel slabs
+// small enough to stay in L2 during its pass; the sort key's tile field is
+// then the virtual tile group * tiles_total + tile.
 struct TileGeom {
   int tile_u, tile_v;        // cells per tile
   int tiles_u, tiles_v;      // tiles per grid side
   int num_grids;
   int plane_bits, phase_bits;  // low key fields below the tile index
   int phase_side;            // 2*omax+1... stored as omax+1 (|off| classes)
+  int num_groups;            // plane groups (passes), >= 1
+  int tiles_total;           // num_grids * tiles_u * tiles_v
+  const int* plane_group;    // [P] group of each plane (num_groups > 1)
 };
 
 // Work item of the gridding kernel: a range of sorted records of one tile.

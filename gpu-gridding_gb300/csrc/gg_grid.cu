@@ -69,10 +69,13 @@ struct WarpShape {
 };
 
 // Visibility coefficients of one record with the conjugation folded in:
-// re += a*t.re + b*t.im, im += c*t.re + d*t.im.
+// re += a*t.re + b*t.im, im += c*t.re + d*t.im.  Stored as (a, d, c, b) so
+// that the FP32 kernel can accumulate two packed pairs per cell with FP32x2
+// FMAs, P += (a, d) * (t.re, t.im) and Q += (c, b) * (t.re, t.im), and
+// recover re = P.x + Q.y, im = Q.x + P.y when it folds a buffer.
 template <typename Real>
 struct alignas(4 * sizeof(Real)) Coef {
-  Real a, b, c, d;
+  Real a, d, c, b;
 };
 
 // Knuth's TwoSum: s + e == a + b exactly.
@@ -85,7 +88,8 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 template <typename Real>
 struct GridArgs {
   const WorkItem* items;
-  const uint32_t* num_items;
+  const uint32_t* group_items;  // queue range of this launch's plane group
+  int group;
   uint32_t* counter;
   uint32_t* error;          // set to 1 when a bounded wait runs out
   const uint32_t* rec_vis;
@@ -185,13 +189,23 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src,
       : "memory");
 }
 
-// Record data in shared memory (int4 per record):
-//   x = org:   tap index of tile cell (0, 0) on the record's slice -- in the
-//              global stack, or in the slice slot when src >= 0
+// Record data in shared memory (int4 per record).  A record whose taps are
+// read from the slab stack in global memory (src < 0) holds
+//   x = A + Cp, y = A + Cn, z = B,
+//   w = Lf | c0 << 8 | (c1 - c0) << 16
+// where A is the slab tap index of tile row 0 for a column offset of 0, B
+// the slab taps per tile row (+-row pitch), Cp + col and Cn - col the
+// column offsets on the non-negative and the negative side of the column
+// fold (which begins at lane column Lf), and [c0, c1] the footprint's
+// columns in the tile; so the tap of tile cell (row, col) is
+// slabs[(col >= Lf ? x + col : y - col) + row * B] for c0 <= col <= c1,
+// zero elsewhere.  A record whose slice is staged in a shared-memory slot
+// (src >= 0) holds
+//   x = org:   tap index of tile cell (0, 0) on the staged slice
 //   y = rstep: +-(2s+1), slice rows per tile row (mirrored for ov < 0)
 //   z = ulo:   first footprint column (tile-relative)
 //   w = su * (2s+1): column mirror sign and footprint width
-// so the record's tap for tile cell (row, col) is taps[org + row * rstep +
+// so its tap for tile cell (row, col) is slice[org + row * rstep +
 // col * su]; lanes whose column lies outside [ulo, ulo + 2s] read zeros.
 //
 // Slice-slot bookkeeping of the producer (lane-uniform).
@@ -214,7 +228,8 @@ __device__ bool produce(const GridArgs<Real>& a, Smem<Real, kStage>& sm) {
   const int lane = threadIdx.x & 31;
   const int omax = a.view.omax;
   const int tiles_per_grid = a.geom.tiles_u * a.geom.tiles_v;
-  const int num_items = (int)*a.num_items;
+  const int first_item = (int)a.group_items[a.group];
+  const int end_item = (int)a.group_items[a.group + 1];
   const R2* __restrict__ taps = (const R2*)a.view.taps;
   SlotState st;
   for (int x = 0; x < kSlots; ++x) {
@@ -225,9 +240,9 @@ __device__ bool produce(const GridArgs<Real>& a, Smem<Real, kStage>& sm) {
   unsigned k = 0;
   for (;;) {
     int it = 0;
-    if (lane == 0) it = (int)atomicAdd(a.counter, 1u);
+    if (lane == 0) it = first_item + (int)atomicAdd(a.counter, 1u);
     it = __shfl_sync(0xffffffffu, it, 0);
-    const bool done = it >= num_items;
+    const bool done = it >= end_item;
     WorkItem item{0, 0, 0, -1};
     int u0 = 0, v0 = 0;
     if (!done) {
@@ -348,15 +363,32 @@ __device__ bool produce(const GridArgs<Real>& a, Smem<Real, kStage>& sm) {
             const int F = 2 * s + 1;
             const int gu = cell_u(ce[q]) - u0, gv = cell_v(ce[q]) - v0;
             const int su = ou < 0 ? -1 : 1, sv = ov < 0 ? -1 : 1;
-            // Tap index of S[0][0] relative to the padded slice start.
-            const int org_rel = kSlicePad * F + (s - sv * gv) * F +
-                                (s - su * gu);
-            int org = org_rel;
-            if (src < 0)
-              org += (int)(a.view.base[plane] +
-                           (long long)(abs(ou) * (omax + 1) + abs(ov)) *
-                               slice_taps(s));
-            sm.rec[slot][t] = make_int4(org, sv * F, gu - s, su * F);
+            if (src < 0) {
+              // Slab of (plane, |ov|); rows mirrored for ov < 0, columns by
+              // residue on either side of the fold ou + k*os = 0.
+              const int os = a.view.oversample;
+              const int M = slab_cols_m(s, os, omax);
+              const int pitch = os * M;
+              const int sb = (int)(a.view.sbase[plane] +
+                                   abs(ov) * slab_taps(s, os, omax));
+              const int A = ov >= 0 ? sb + (s + kSlicePad - gv) * pitch
+                                    : sb + (s + kSlicePad + gv) * pitch;
+              const int B = ov >= 0 ? pitch : -pitch;
+              const int ap = ((ou % os) + os) % os, an = ((-ou % os) + os) % os;
+              const int bp = (ou - ap) / os, bn = (-ou - an) / os;
+              const int Cp = ap * M + bp - gu, Cn = an * M + bn + gu;
+              // floor(ou / os); the fold lane is gu - floor(ou / os).
+              const int fl = ou >= 0 ? ou / os : -((-ou + os - 1) / os);
+              const int Lf = min(max(gu - fl, 0), WS::kTileU);
+              const int c0 = max(gu - s, 0), c1 = min(gu + s, WS::kTileU - 1);
+              sm.rec[slot][t] =
+                  make_int4(A + Cp, A + Cn, B, Lf | (c0 << 8) | ((c1 - c0) << 16));
+            } else {
+              // Tap index of S[0][0] relative to the padded slice start.
+              const int org = kSlicePad * F + (s - sv * gv) * F +
+                              (s - su * gu);
+              sm.rec[slot][t] = make_int4(org, sv * F, gu - s, su * F);
+            }
             sm.src[slot][t] = (signed char)src;
             // Bit (warp * kLanesY + lane row) = that lane row's kRows rows
             // meet the footprint rows [gv - s, gv + s].
@@ -391,29 +423,84 @@ __device__ bool produce(const GridArgs<Real>& a, Smem<Real, kStage>& sm) {
   }
 }
 
+// Read-only tap load that asks L2 to keep the line (evict_last policy):
+// the compact stack is re-read by every tile while the grid streams past.
+__device__ __forceinline__ float2 ld_tap(const float2* p, uint64_t pol) {
+  float2 v;
+  asm("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
+      : "=f"(v.x), "=f"(v.y)
+      : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double2 ld_tap(const double2* p, uint64_t pol) {
+  double2 v;
+  asm("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+      : "=d"(v.x), "=d"(v.y)
+      : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ uint64_t evict_last_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;"
+               : "=l"(pol));
+  return pol;
+}
+
 // Loads the kRows taps of one record for this lane: from the record's
-// slice slot in shared memory, or from the global stack.
-template <typename Real, bool kStage, typename R2>
+// slice slot in shared memory, or from the slab stack (see the record
+// layout above).  Lanes outside the footprint's columns, or outside the
+// warp rows the record meets, read zeros.
+template <typename Real, int TW, bool kStage, typename R2>
 __device__ __forceinline__ void load_record(const Smem<Real, kStage>& sm,
-                                            int slot,
-                                            int t, const R2* __restrict__ taps,
+                                            int slot, int t,
+                                            const R2* __restrict__ slabs,
                                             const R2* __restrict__ gzeros,
                                             uint32_t my_bit, int lx, int rowl,
-                                            R2 (&out)[kRows]) {
+                                            uint64_t pol, R2 (&out)[kRows]) {
   const int4 ra = sm.rec[slot][t];
-  const int src = kStage ? sm.src[slot][t] : -1;
-  const bool ok = (sm.band[slot][t] & my_bit) &&
-                  (unsigned)(lx - ra.z) <= (unsigned)(abs(ra.w) - 1);
-  const int off = ra.x + rowl * ra.y + lx * (ra.w < 0 ? -1 : 1);
-  if (kStage && src >= 0) {
+  // With one lane row per warp (TW = 32) a warp only takes records that
+  // meet its rows; narrower tiles check the lane's own row group.
+  const bool inband = TW == 32 || (sm.band[slot][t] & my_bit) != 0u;
+  if (kStage && sm.src[slot][t] >= 0) {
+    const int src = sm.src[slot][t];
+    const bool ok =
+        inband && (unsigned)(lx - ra.z) <= (unsigned)(abs(ra.w) - 1);
+    const int off = ra.x + rowl * ra.y + lx * (ra.w < 0 ? -1 : 1);
     const R2* p = ok ? &sm.slice[src][0] + off
                      : &sm.zero[Smem<Real, kStage>::kZeroTaps / 2];
 #pragma unroll
     for (int r = 0; r < kRows; ++r) out[r] = p[r * ra.y];
-  } else {
-    const R2* p = ok ? taps + off : gzeros;
+    return;
+  }
+  const int c0 = (ra.w >> 8) & 0xFF, cw = (int)((unsigned)ra.w >> 16);
+  const bool ok = inband && (unsigned)(lx - c0) <= (unsigned)cw;
+  const int off = (lx >= (ra.w & 0xFF) ? ra.x + lx : ra.y - lx) + rowl * ra.z;
+  const R2* p = ok ? slabs + off : gzeros;
+  const int step = ok ? ra.z : 0;
 #pragma unroll
-    for (int r = 0; r < kRows; ++r) out[r] = __ldg(p + r * ra.y);
+  for (int r = 0; r < kRows; ++r) out[r] = ld_tap(p + r * step, pol);
+}
+
+// Adds one record's contribution to the lane's cells.  FP32: packed FP32x2
+// FMAs into the (P, Q) pairs (see Coef); FP64: plain FMAs into (re, im).
+template <typename Real, typename R2>
+__device__ __forceinline__ void accumulate(const Coef<Real>& c,
+                                           const R2 (&tp)[kRows],
+                                           R2 (&acc)[kRows],
+                                           R2 (&acq)[kRows]) {
+  if constexpr (sizeof(Real) == 4) {
+    const float2 cp = make_float2(c.a, c.d), cq = make_float2(c.c, c.b);
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+      acc[r] = __ffma2_rn(cp, tp[r], acc[r]);
+      acq[r] = __ffma2_rn(cq, tp[r], acq[r]);
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+      acc[r].x = fma(c.b, tp[r].y, fma(c.a, tp[r].x, acc[r].x));
+      acc[r].y = fma(c.d, tp[r].y, fma(c.c, tp[r].x, acc[r].y));
+    }
   }
 }
 
@@ -451,15 +538,17 @@ k_grid_tiles(GridArgs<Real> a) {
   const int lx = lane % TW, ly = lane / TW;
   const int rowl = warp * WS::kBand + ly * kRows;   // this lane's row 0
   const int G_size = a.grid_size;
-  const R2* __restrict__ taps = (const R2*)a.view.taps;
+  const R2* __restrict__ slabs = (const R2*)a.view.slabs;
   const R2* __restrict__ gzeros = (const R2*)a.view.zeros;
   const int tiles_per_grid = a.geom.tiles_u * a.geom.tiles_v;
+  const uint64_t pol = evict_last_policy();
   const uint32_t my_bit = 1u << (warp * G + ly);
   const uint32_t warp_bits = ((1u << G) - 1u) << (warp * G);
 
-  R2 acc[kRows];
+  // FP32: (P, Q) pairs of every cell (see Coef); FP64: (re, im) in acc.
+  R2 acc[kRows], acq[kRows];
 #pragma unroll
-  for (int r = 0; r < kRows; ++r) acc[r].x = acc[r].y = 0;
+  for (int r = 0; r < kRows; ++r) acc[r].x = acc[r].y = acq[r].x = acq[r].y = 0;
 
   for (unsigned k = 0;; ++k) {
     const int slot = (int)(k % kRing);
@@ -473,7 +562,7 @@ k_grid_tiles(GridArgs<Real> a) {
     if (head.z & 1) {  // first buffer of a work item
 #pragma unroll
       for (int r = 0; r < kRows; ++r) {
-        acc[r].x = acc[r].y = 0;
+        acc[r].x = acc[r].y = acq[r].x = acq[r].y = 0;
         if constexpr (kCompensate) {
           sm.hi[r][threadIdx.x] = acc[r];
           sm.lo[r][threadIdx.x] = acc[r];
@@ -485,32 +574,24 @@ k_grid_tiles(GridArgs<Real> a) {
       const bool touch =
           c0 + lane < nb && (sm.band[slot][c0 + lane] & warp_bits) != 0u;
       uint32_t m = __ballot_sync(0xffffffffu, touch);
-      // Two records at a time: 2*kRows independent tap loads per lane.
+      // Two records at a time: 2 * kRows independent tap loads per lane in
+      // flight.  Each cell takes the records in queue order.
       while (m) {
         const int tA = c0 + __ffs(m) - 1;
         m &= m - 1;
-        const int tB = m ? c0 + __ffs(m) - 1 : -1;
-        if (m) m &= m - 1;
-        R2 ta[kRows], tb[kRows];
-        Coef<Real> ca, cb;
-        load_record<Real, kStage>(sm, slot, tA, taps, gzeros, my_bit, lx,
-                                  rowl, ta);
-        ca = sm.cf[slot][tA];
-        if (tB >= 0) {
-          load_record<Real, kStage>(sm, slot, tB, taps, gzeros, my_bit, lx,
-                                    rowl, tb);
-          cb = sm.cf[slot][tB];
+        R2 ta[kRows];
+        load_record<Real, TW, kStage>(sm, slot, tA, slabs, gzeros, my_bit,
+                                      lx, rowl, pol, ta);
+        if (m) {
+          const int tB = c0 + __ffs(m) - 1;
+          m &= m - 1;
+          R2 tb[kRows];
+          load_record<Real, TW, kStage>(sm, slot, tB, slabs, gzeros, my_bit,
+                                        lx, rowl, pol, tb);
+          accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
+          accumulate<Real>(sm.cf[slot][tB], tb, acc, acq);
         } else {
-#pragma unroll
-          for (int r = 0; r < kRows; ++r) tb[r].x = tb[r].y = 0;
-          cb.a = cb.b = cb.c = cb.d = 0;
-        }
-#pragma unroll
-        for (int r = 0; r < kRows; ++r) {
-          acc[r].x = fma(ca.b, ta[r].y, fma(ca.a, ta[r].x, acc[r].x));
-          acc[r].y = fma(ca.d, ta[r].y, fma(ca.c, ta[r].x, acc[r].y));
-          acc[r].x = fma(cb.b, tb[r].y, fma(cb.a, tb[r].x, acc[r].x));
-          acc[r].y = fma(cb.d, tb[r].y, fma(cb.c, tb[r].x, acc[r].y));
+          accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
         }
       }
     }
@@ -518,18 +599,21 @@ k_grid_tiles(GridArgs<Real> a) {
 #pragma unroll
       for (int r = 0; r < kRows; ++r) {
         R2 hi = sm.hi[r][threadIdx.x], lo = sm.lo[r][threadIdx.x];
+        const float re = __fadd_rn(acc[r].x, acq[r].y);
+        const float im = __fadd_rn(acq[r].x, acc[r].y);
         float s, e;
-        two_sum(hi.x, acc[r].x, s, e); hi.x = s; lo.x += e;
-        two_sum(hi.y, acc[r].y, s, e); hi.y = s; lo.y += e;
+        two_sum(hi.x, re, s, e); hi.x = s; lo.x += e;
+        two_sum(hi.y, im, s, e); hi.y = s; lo.y += e;
         sm.hi[r][threadIdx.x] = hi;
         sm.lo[r][threadIdx.x] = lo;
-        acc[r].x = acc[r].y = 0;
+        acc[r].x = acc[r].y = acq[r].x = acq[r].y = 0;
       }
     }
     if (head.z & 2) {  // last buffer of the work item: flush its tile
       const WorkItem item = a.items[head.x];
-      const int gi = item.tile / tiles_per_grid;
-      const int tl = item.tile - gi * tiles_per_grid;
+      const int rt = item.tile % a.geom.tiles_total;   // real tile
+      const int gi = rt / tiles_per_grid;
+      const int tl = rt - gi * tiles_per_grid;
       const int u0 = (tl % a.geom.tiles_u) * WS::kTileU;
       const int v0 = (tl / a.geom.tiles_u) * WS::kTileV;
       R2 out[kRows];
@@ -551,10 +635,10 @@ k_grid_tiles(GridArgs<Real> a) {
           const int row = v0 + rowl + r;
           if (row < G_size && col < G_size) {
             R2* p = g + (size_t)row * G_size + col;
-            R2 old = *p;
+            R2 old = __ldcs(p);
             old.x += out[r].x;
             old.y += out[r].y;
-            *p = old;
+            __stcs(p, old);
           }
         }
       } else {
@@ -562,7 +646,7 @@ k_grid_tiles(GridArgs<Real> a) {
         R2* p = a.partials + (size_t)item.slot * kCells;
 #pragma unroll
         for (int r = 0; r < kRows; ++r)
-          p[r * kConsumers + threadIdx.x] = out[r];
+          __stcs(p + r * kConsumers + threadIdx.x, out[r]);
       }
     }
     __syncwarp();
@@ -571,22 +655,26 @@ k_grid_tiles(GridArgs<Real> a) {
 }
 
 // grid(tile) += sum of the tile's partials in chunk order, accumulated in
-// FP64 and rounded once.  The partial layout is the kernel's thread-major
-// one: entry e = r * kConsumers + consumer thread.
+// FP64 and rounded once, for the split tiles of one plane group (a real
+// tile is split at most once per group, so the blocks of one launch never
+// share a tile).  The partial layout is the kernel's thread-major one:
+// entry e = r * kConsumers + consumer thread.
 template <typename Real, int TW>
 __global__ void k_reduce_partials(const int4* __restrict__ split_tiles,
                                   const uint32_t* __restrict__ num_split,
                                   const typename Vec2<Real>::type* __restrict__ partials,
-                                  TileGeom g, int G, Real* grid,
+                                  TileGeom g, int group, int G, Real* grid,
                                   long long grid_stride) {
   using R2 = typename Vec2<Real>::type;
   using WS = WarpShape<TW>;
   const int tiles_per_grid = g.tiles_u * g.tiles_v;
   const int n = (int)*num_split;
   for (int st = blockIdx.x; st < n; st += gridDim.x) {
-    const int4 d = split_tiles[st];  // tile, first slot, chunks
-    const int gi = d.x / tiles_per_grid;
-    const int tl = d.x - gi * tiles_per_grid;
+    const int4 d = split_tiles[st];  // virtual tile, first slot, chunks
+    if (d.x / g.tiles_total != group) continue;
+    const int rt = d.x % g.tiles_total;
+    const int gi = rt / tiles_per_grid;
+    const int tl = rt - gi * tiles_per_grid;
     const int u0 = (tl % g.tiles_u) * WS::kTileU;
     const int v0 = (tl / g.tiles_u) * WS::kTileV;
     R2* gp = (R2*)(grid + (long long)gi * grid_stride);
@@ -637,10 +725,15 @@ __global__ void k_item_counts(const uint32_t* __restrict__ tile_start,
   B[t] = chunks == 1 ? 1 : 0;
 }
 
-// Split-tile chunks come first in the queue (they are the largest items),
-// then the single-chunk tiles.  Partial slot = queue position of the chunk.
+// The queue is group-major (see ItemBuffers); within plane group g the
+// chunks of split tiles come first (they are the largest items), then the
+// single-chunk tiles.  With exclusive scans sA (split chunks) and sB
+// (single-chunk tiles) over the virtual tiles, group g starts at
+// sA[gT] + sB[gT] (T = tiles per group), split chunk j of virtual tile t
+// sits at sA[t] + sB[gT] + j and single tile t at sA[(g+1)T] + sB[t].
+// Partial slot of a split chunk = sA[t] + j.
 __global__ void k_item_emit(const uint32_t* __restrict__ tile_start,
-                            int num_tiles, uint32_t chunk,
+                            int num_tiles, int num_groups, uint32_t chunk,
                             const uint32_t* __restrict__ sA,
                             const uint32_t* __restrict__ sB,
                             const uint32_t* __restrict__ totA,
@@ -648,10 +741,16 @@ __global__ void k_item_emit(const uint32_t* __restrict__ tile_start,
                             WorkItem* __restrict__ items,
                             int4* __restrict__ split_tiles,
                             uint32_t* __restrict__ num_split,
-                            uint32_t* __restrict__ num_items) {
+                            uint32_t* __restrict__ num_items,
+                            uint32_t* __restrict__ group_items) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int T = num_tiles / num_groups;
+  auto scanA = [&](int i) { return i < num_tiles ? sA[i] : *totA; };
+  auto scanB = [&](int i) { return i < num_tiles ? sB[i] : *totB; };
   if (t == 0) *num_items = *totA + *totB;
+  if (t <= num_groups) group_items[t] = scanA(t * T) + scanB(t * T);
   if (t >= num_tiles) return;
+  const int g = t / T;
   const uint32_t s0 = tile_start[t], s1 = tile_start[t + 1];
   const uint32_t c = s1 - s0;
   if (c == 0) return;
@@ -659,16 +758,17 @@ __global__ void k_item_emit(const uint32_t* __restrict__ tile_start,
   if (chunks == 1) {
     WorkItem w;
     w.tile = t; w.rec_begin = (int)s0; w.rec_end = (int)s1; w.slot = -1;
-    items[*totA + sB[t]] = w;
+    items[scanA((g + 1) * T) + sB[t]] = w;
   } else {
     const uint32_t first = sA[t];
+    const uint32_t pos = first + scanB(g * T);
     for (uint32_t j = 0; j < chunks; ++j) {
       WorkItem w;
       w.tile = t;
       w.rec_begin = (int)(s0 + j * chunk);
       w.rec_end = (int)min(s1, s0 + (j + 1) * chunk);
       w.slot = (int)(first + j);
-      items[first + j] = w;
+      items[pos + j] = w;
     }
     const uint32_t k = atomicAdd(num_split, 1u);
     split_tiles[k] = make_int4(t, (int)first, (int)chunks, 0);
@@ -730,7 +830,7 @@ cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
   (void)num_records;
   uint32_t* A = b.chunks;
   uint32_t* B = b.split_chunks;
-  const int blocks = (num_tiles + 255) / 256;
+  const int blocks = (num_tiles + 256) / 256;   // one more thread: bounds
   k_item_counts<<<blocks, 256, 0, s>>>(tile_start, num_tiles, chunk, A, B);
   cudaError_t e;
   e = exclusive_scan_u32(A, A, num_tiles, b.num_slots, b.scan_tmp, s);
@@ -740,9 +840,10 @@ cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(b.num_split, 0, sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
-  k_item_emit<<<blocks, 256, 0, s>>>(tile_start, num_tiles, chunk, A, B,
-                                     b.num_slots, b.counter, b.items,
-                                     b.split_tiles, b.num_split, b.num_items);
+  k_item_emit<<<blocks, 256, 0, s>>>(tile_start, num_tiles, b.num_groups,
+                                     chunk, A, B, b.num_slots, b.counter,
+                                     b.items, b.split_tiles, b.num_split,
+                                     b.num_items, b.group_items);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   // The persistent kernel's work counter starts at zero.
@@ -763,17 +864,44 @@ int grid_tiles_ctas_per_sm(int tile_u, bool stage) {
 }
 
 template <typename Real>
-cudaError_t launch_grid_tiles(const WorkItem* items, const uint32_t* num_items,
+cudaError_t launch_reduce_group(const int4* split_tiles,
+                                const uint32_t* num_split, int max_split,
+                                const Real* partials, TileGeom geom, int group,
+                                int grid_size, Real* grid,
+                                long long grid_stride, cudaStream_t s) {
+  if (max_split <= 0) return cudaSuccess;
+  const int blocks = std::min(max_split, 4096);
+  using P2 = const typename Vec2<Real>::type*;
+  switch (geom.tile_u) {
+    case 32: k_reduce_partials<Real, 32><<<blocks, 256, 0, s>>>(
+        split_tiles, num_split, (P2)partials, geom, group, grid_size, grid,
+        grid_stride); break;
+    case 16: k_reduce_partials<Real, 16><<<blocks, 256, 0, s>>>(
+        split_tiles, num_split, (P2)partials, geom, group, grid_size, grid,
+        grid_stride); break;
+    case 8: k_reduce_partials<Real, 8><<<blocks, 256, 0, s>>>(
+        split_tiles, num_split, (P2)partials, geom, group, grid_size, grid,
+        grid_stride); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+template <typename Real>
+cudaError_t launch_grid_tiles(const WorkItem* items,
+                              const uint32_t* group_items,
                               uint32_t* counter, uint32_t* error,
                               const uint32_t* rec_vis,
                               const uint32_t* cell, const uint32_t* meta,
                               const void* vw, StackView view, TileGeom geom,
                               int grid_size, Real* grid, long long grid_stride,
-                              Real* partials, int num_ctas, bool stage,
-                              cudaStream_t s) {
+                              Real* partials, const int4* split_tiles,
+                              const uint32_t* num_split, int max_split,
+                              int num_ctas, bool stage, cudaStream_t s) {
   GridArgs<Real> a;
   a.items = items;
-  a.num_items = num_items;
+  a.group_items = group_items;
+  a.group = 0;
   a.counter = counter;
   a.error = error;
   a.rec_vis = rec_vis;
@@ -794,31 +922,18 @@ cudaError_t launch_grid_tiles(const WorkItem* items, const uint32_t* num_items,
                                                 &smem);
   if (e != cudaSuccess) return e;
   void* args[] = {&a};
-  return cudaLaunchKernel(fn, dim3(num_ctas), dim3(kThreads), args, smem, s);
-}
-
-template <typename Real>
-cudaError_t launch_reduce_partials(const int4* split_tiles,
-                                   const uint32_t* num_split, int max_split,
-                                   const Real* partials, TileGeom geom,
-                                   int grid_size, Real* grid,
-                                   long long grid_stride, cudaStream_t s) {
-  if (max_split <= 0) return cudaSuccess;
-  const int blocks = std::min(max_split, 4096);
-  using P2 = const typename Vec2<Real>::type*;
-  switch (geom.tile_u) {
-    case 32: k_reduce_partials<Real, 32><<<blocks, 256, 0, s>>>(
-        split_tiles, num_split, (P2)partials, geom, grid_size, grid,
-        grid_stride); break;
-    case 16: k_reduce_partials<Real, 16><<<blocks, 256, 0, s>>>(
-        split_tiles, num_split, (P2)partials, geom, grid_size, grid,
-        grid_stride); break;
-    case 8: k_reduce_partials<Real, 8><<<blocks, 256, 0, s>>>(
-        split_tiles, num_split, (P2)partials, geom, grid_size, grid,
-        grid_stride); break;
-    default: return cudaErrorInvalidValue;
+  for (int g = 0; g < geom.num_groups; ++g) {
+    a.group = g;
+    e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    e = cudaLaunchKernel(fn, dim3(num_ctas), dim3(kThreads), args, smem, s);
+    if (e != cudaSuccess) return e;
+    e = launch_reduce_group<Real>(split_tiles, num_split, max_split,
+                                  partials, geom, g, grid_size, grid,
+                                  grid_stride, s);
+    if (e != cudaSuccess) return e;
   }
-  return cudaGetLastError();
+  return cudaSuccess;
 }
 
 template int grid_tiles_ctas_per_sm<float>(int, bool);
@@ -826,20 +941,12 @@ template int grid_tiles_ctas_per_sm<double>(int, bool);
 template cudaError_t launch_grid_tiles<float>(
     const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
-    float*, long long, float*, int, bool, cudaStream_t);
+    float*, long long, float*, const int4*, const uint32_t*, int, int, bool,
+    cudaStream_t);
 template cudaError_t launch_grid_tiles<double>(
     const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
-    double*, long long, double*, int, bool, cudaStream_t);
-template cudaError_t launch_reduce_partials<float>(const int4*,
-                                                   const uint32_t*, int,
-                                                   const float*, TileGeom, int,
-                                                   float*, long long,
-                                                   cudaStream_t);
-template cudaError_t launch_reduce_partials<double>(const int4*,
-                                                    const uint32_t*, int,
-                                                    const double*, TileGeom,
-                                                    int, double*, long long,
-                                                    cudaStream_t);
+    double*, long long, double*, const int4*, const uint32_t*, int, int, bool,
+    cudaStream_t);
 
 }  // namespace gg

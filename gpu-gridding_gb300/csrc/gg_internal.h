@@ -36,6 +36,11 @@ template <typename Real>
 cudaError_t launch_stack_relayout(const Real* d_conv_func, StackView view,
                                   void* d_taps_out, long long total_taps,
                                   cudaStream_t s);
+// Fills the slab stack (view.slabs layout, planes at view.sbase).
+template <typename Real>
+cudaError_t launch_stack_relayout_slabs(const Real* d_conv_func,
+                                        StackView view, void* d_out,
+                                        cudaStream_t s);
 template <typename Real>
 cudaError_t launch_tap_sums(StackView view, double* d_tap_sum,
                             cudaStream_t s);
@@ -148,9 +153,15 @@ cudaError_t launch_batch_totals(const uint32_t* meta, const double* nterm,
 cudaError_t launch_tile_bounds(const uint32_t* keys, uint32_t n, int shift,
                                int num_tiles, uint32_t* tile_start,
                                cudaStream_t s);
+// Work-item queue of a call.  Tiles are virtual tiles (group * tiles_total
+// + tile, see TileGeom); the queue is group-major, and within a group the
+// chunks of split tiles come first.  group_items[g] .. group_items[g+1] is
+// the queue range of plane group g (num_groups + 1 entries).
 struct ItemBuffers {
   uint32_t* chunks;       // [num_tiles] chunks per tile (then offsets)
   uint32_t* split_chunks; // [num_tiles] chunks of split tiles (then slots)
+  uint32_t* group_items;  // [num_groups + 1]
+  int num_groups;
   uint32_t* num_items;    // [1]
   uint32_t* num_slots;    // [1]
   WorkItem* items;        // [capacity]
@@ -162,21 +173,20 @@ struct ItemBuffers {
 cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
                                uint32_t num_records, uint32_t chunk,
                                ItemBuffers b, cudaStream_t s);
+// One persistent launch per plane group, in group order, each followed by
+// the reduction of that group's split tiles (grid += their partials in
+// chunk order, FP64): the grid takes the groups' contributions in order.
 template <typename Real>
-cudaError_t launch_grid_tiles(const WorkItem* items, const uint32_t* num_items,
+cudaError_t launch_grid_tiles(const WorkItem* items,
+                              const uint32_t* group_items,
                               uint32_t* counter, uint32_t* error,
                               const uint32_t* rec_vis,
                               const uint32_t* cell, const uint32_t* meta,
                               const void* vw, StackView view, TileGeom geom,
                               int grid_size, Real* grid, long long grid_stride,
-                              Real* partials, int num_ctas, bool stage,
-                              cudaStream_t s);
-template <typename Real>
-cudaError_t launch_reduce_partials(const int4* split_tiles,
-                                   const uint32_t* num_split, int max_split,
-                                   const Real* partials, TileGeom geom,
-                                   int grid_size, Real* grid,
-                                   long long grid_stride, cudaStream_t s);
+                              Real* partials, const int4* split_tiles,
+                              const uint32_t* num_split, int max_split,
+                              int num_ctas, bool stage, cudaStream_t s);
 // stage: the kernel variant that stages kernel slices in shared memory.
 template <typename Real>
 int grid_tiles_ctas_per_sm(int tile_u, bool stage);

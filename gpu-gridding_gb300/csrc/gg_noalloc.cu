@@ -229,6 +229,9 @@ extern "C" GG_API int gg_grid_wproj_f_device_noalloc(
   geom.tiles_u = (grid_size + geom.tile_u - 1) / geom.tile_u;
   geom.tiles_v = (grid_size + geom.tile_v - 1) / geom.tile_v;
   geom.num_grids = 1;
+  geom.num_groups = 1;
+  geom.tiles_total = geom.tiles_u * geom.tiles_v;
+  geom.plane_group = nullptr;
   const int num_tiles = geom.tiles_u * geom.tiles_v;
   const int tile_bits = ceil_log2_u((unsigned long long)num_tiles);
   int plane_bits = ceil_log2_u((unsigned long long)num_planes);
@@ -267,13 +270,13 @@ extern "C" GG_API int gg_grid_wproj_f_device_noalloc(
   ib.split_tiles = split_tiles;
   ib.num_split = sc + 3;
   ib.counter = sc + 4;
+  ib.group_items = sc + 8;   // two entries: one plane group
+  ib.num_groups = 1;
   ib.scan_tmp = scan_tmp;
   NA_CUDA(launch_build_items(tile_start, num_tiles, total, chunk, ib, s));
-  NA_CUDA(launch_grid_tiles<float>(items, sc + 1, sc + 4, sc + 6, vals, cell,
+  NA_CUDA(launch_grid_tiles<float>(items, sc + 8, sc + 4, sc + 6, vals, cell,
                                    meta, vw, view, geom, grid_size, d_grid, 0,
-                                   (float*)partials, num_ctas, false, s));
-  NA_CUDA(launch_reduce_partials<float>(split_tiles, sc + 3, num_tiles,
-                                        (const float*)partials, geom,
-                                        grid_size, d_grid, 0, s));
+                                   (float*)partials, split_tiles, sc + 3,
+                                   num_tiles, num_ctas, false, s));
   return GG_OK;
 }

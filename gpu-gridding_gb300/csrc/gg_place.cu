@@ -180,8 +180,10 @@ __global__ void k_emit(const uint32_t* __restrict__ cell,
   const uint32_t vid = (uint32_t)(vis_offset + i);
   for (int tv = tv0; tv <= tv1; ++tv) {
     for (int tu = tu0; tu <= tu1; ++tu) {
-      const uint32_t tile = (uint32_t)grid_index * tiles_per_grid +
-                            (uint32_t)tv * g.tiles_u + (uint32_t)tu;
+      uint32_t tile = (uint32_t)grid_index * tiles_per_grid +
+                      (uint32_t)tv * g.tiles_u + (uint32_t)tu;
+      if (g.num_groups > 1)
+        tile += (uint32_t)g.plane_group[plane] * (uint32_t)g.tiles_total;
       keys[pos] = low_bits >= 32 ? low : ((tile << low_bits) | low);
       vals[pos] = vid;
       ++pos;

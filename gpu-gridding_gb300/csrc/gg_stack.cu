@@ -52,6 +52,42 @@ __global__ void k_relayout(const Real* __restrict__ conv, StackView v,
   }
 }
 
+// One thread per output tap of the slab stack; blockIdx.y is the plane.
+// slab_{p,c}[kSlicePad + j + s][r][m] = K_p[|c + j*os|][r + m*os]; padding
+// rows, and taps beyond the cube, are zero.
+template <typename Real>
+__global__ void k_relayout_slabs(const Real* __restrict__ conv, StackView v,
+                                 typename Vec2<Real>::type* __restrict__ out) {
+  using R2 = typename Vec2<Real>::type;
+  const int p = blockIdx.y;
+  const int os = v.oversample, csh = v.conv_size_half;
+  const int s = v.support[p];
+  const int F = 2 * s + 1;
+  const int M = slab_cols_m(s, os, v.omax);
+  const long long row_taps = (long long)os * M;
+  const long long stride = slab_taps(s, os, v.omax);
+  const long long n = (long long)(v.omax + 1) * stride;
+  const long long base = v.sbase[p];
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(e / stride);
+    const long long rem = e - c * stride;
+    const int jp = (int)(rem / row_taps) - kSlicePad;
+    const int in_row = (int)(rem % row_taps);
+    const int col = (in_row / M) + (in_row % M) * os;   // r + m*os
+    const int t = abs(c + (jp - s) * os);
+    R2 val;
+    if (jp >= 0 && jp < F && t < csh && col < csh) {
+      const size_t src = (((size_t)p * csh + t) * csh + col) * 2;
+      val.x = conv[src];
+      val.y = conv[src + 1];
+    } else {
+      val.x = 0; val.y = 0;
+    }
+    out[base + e] = val;
+  }
+}
+
 // Sum of the real parts of every tap a footprint uses, for one (plane,
 // off_u, off_v), accumulated in FP64 in the reference's order: rows j
 // outer, columns k inner (oskar_grid_wproj.c:190-208, sum += c_re).  A
@@ -97,6 +133,16 @@ cudaError_t launch_stack_relayout(const Real* d_conv_func, StackView view,
 }
 
 template <typename Real>
+cudaError_t launch_stack_relayout_slabs(const Real* d_conv_func,
+                                        StackView view, void* d_out,
+                                        cudaStream_t s) {
+  dim3 grid(64, view.num_planes);
+  k_relayout_slabs<Real><<<grid, 256, 0, s>>>(
+      d_conv_func, view, (typename Vec2<Real>::type*)d_out);
+  return cudaGetLastError();
+}
+
+template <typename Real>
 cudaError_t launch_tap_sums(StackView view, double* d_tap_sum,
                             cudaStream_t s) {
   // The raw cube is needed for the reference-order sums; it is passed in
@@ -114,6 +160,12 @@ template cudaError_t launch_stack_relayout<float>(const float*, StackView,
 template cudaError_t launch_stack_relayout<double>(const double*, StackView,
                                                    void*, long long,
                                                    cudaStream_t);
+template cudaError_t launch_stack_relayout_slabs<float>(const float*,
+                                                        StackView, void*,
+                                                        cudaStream_t);
+template cudaError_t launch_stack_relayout_slabs<double>(const double*,
+                                                         StackView, void*,
+                                                         cudaStream_t);
 template cudaError_t launch_tap_sums<float>(StackView, double*, cudaStream_t);
 template cudaError_t launch_tap_sums<double>(StackView, double*,
                                              cudaStream_t);

@@ -135,6 +135,7 @@ typedef struct
     int slice_staging;                  /* 1 if slices were staged */
     int num_ctas;                       /* persistent gridding CTAs */
     unsigned long long chunk_records;   /* records per work item (max) */
+    int num_plane_groups;               /* gridding passes (plane groups) */
 } gg_stats;
 
 GG_API int gg_plan_last_stats(const gg_plan* plan, gg_stats* stats);
@@ -167,6 +168,11 @@ GG_API int gg_plan_set_slice_staging(gg_plan* plan, int mode);
  *                  kernel-offset class, 1 by w-plane, 0 visibility order
  *   ctas_per_sm    resident gridding CTAs per SM, 0 (default) = as many as
  *                  fit, else min(that, what fits), 1..32
+ *   plane_group_mb kernel bytes per gridding pass: the w-planes are cut
+ *                  into groups of consecutive planes whose re-laid kernels
+ *                  fit this many MiB and each group is gridded in its own
+ *                  pass, so that a pass's kernels stay in L2; 0 (default) =
+ *                  a quarter of the device's L2 cache, 0..1048576
  * gg_plan_set_tile_shape and gg_plan_set_slice_staging set the first two
  * fields alone. */
 typedef struct
@@ -176,6 +182,7 @@ typedef struct
     int items_per_cta;
     int sort_detail;
     int ctas_per_sm;
+    int plane_group_mb;
 } gg_tuning;
 
 GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* tuning);
@@ -186,8 +193,9 @@ GG_API int gg_plan_get_tuning(const gg_plan* plan, gg_tuning* tuning);
  *   0 placement (placement, skip/norm reduction, record offsets)
  *   1 binning (record emission and radix sort)
  *   2 work decomposition (tile ranges and work items)
- *   3 the tile-gridding kernel
- *   4 the partial-tile reduction
+ *   3 the tile-gridding passes (one per plane group, each with the
+ *     reduction of its split tiles' partials)
+ *   4 reserved (0; the reductions are timed within phase 3)
  * gg_plan_phase_ms fills ms[0..n-1] for the last call; the call's stream
  * must have been synchronised.  Off by default (no events recorded). */
 GG_API int gg_plan_set_profiling(gg_plan* plan, int enable);

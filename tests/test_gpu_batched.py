@@ -56,10 +56,12 @@ def _run_batched(pkg, torch, wl, plan, stack):
     return grids.cpu().numpy(), norms.cpu().numpy(), skips.cpu().numpy()
 
 
-def test_batched_equals_single_calls(pkg, oracle_mod, torch, batch):
+@pytest.mark.parametrize("group_mb", [1 << 20, 1])
+def test_batched_equals_single_calls(pkg, oracle_mod, torch, batch, group_mb):
     wl = batch
     stack = pkg.KernelStack.from_workload(wl, "f")
     plan = pkg.Plan()
+    plan.set_tuning({"plane_group_mb": group_mb})
     grids, norms, skips = _run_batched(pkg, torch, wl, plan, stack)
     assert wl.num_grids == 6
     for c in range(wl.num_grids):
@@ -119,7 +121,8 @@ def _new_values(wl, seed):
     return vis, weight
 
 
-def test_replay_matches_batched_calls(pkg, torch, batch):
+@pytest.mark.parametrize("group_mb", [1 << 20, 1])
+def test_replay_matches_batched_calls(pkg, torch, batch, group_mb):
     """A replay with the original amplitudes reproduces the batched call bit
     for bit; with new amplitudes and weights it matches a fresh batched call
     on them bit for bit (the geometry depends on (u, v, w) only)."""
@@ -128,7 +131,10 @@ def test_replay_matches_batched_calls(pkg, torch, batch):
     C, G = wl.num_grids, wl.grid_size
     stack = pkg.KernelStack.from_workload(wl, "f")
     plan = pkg.Plan()
+    plan.set_tuning({"plane_group_mb": group_mb})
     ref = _run_batched(pkg, torch, wl, plan, stack)
+    # 1 MiB per pass: several plane groups; 1 TiB: a single pass.
+    assert (plan.stats()["num_plane_groups"] > 1) == (group_mb == 1)
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     _same(_replay(pkg, torch, plan, stack, dev(wl.vis), dev(wl.weight), C, G),
           ref)
@@ -136,7 +142,9 @@ def test_replay_matches_batched_calls(pkg, torch, batch):
     got = _replay(pkg, torch, plan, stack, dev(vis2), dev(w2), C, G)
     wl2 = copy.copy(wl)
     wl2.vis, wl2.weight = vis2, w2
-    _same(got, _run_batched(pkg, torch, wl2, pkg.Plan(), stack))
+    plan2 = pkg.Plan()
+    plan2.set_tuning({"plane_group_mb": group_mb})
+    _same(got, _run_batched(pkg, torch, wl2, plan2, stack))
 
 
 def test_replay_in_cuda_graph(pkg, torch, batch):

@@ -55,6 +55,8 @@ TUNINGS = [
     {"tile_u": 16, "slice_staging": 0, "items_per_cta": 16, "sort_detail": 1},
     {"tile_u": 8, "slice_staging": 1, "items_per_cta": 64, "sort_detail": 0},
     {"tile_u": 0, "slice_staging": -1, "items_per_cta": 8, "ctas_per_sm": 1},
+    {"tile_u": 32, "slice_staging": 0, "items_per_cta": 4, "plane_group_mb": 1},
+    {"tile_u": 8, "slice_staging": 1, "items_per_cta": 2, "plane_group_mb": 1},
 ]
 
 
@@ -68,6 +70,10 @@ def test_tuning_changes_speed_only(pkg, torch, wl, fp64, tuning):
     st = plan.stats()
     if tuning["tile_u"]:
         assert st["tile_u"] == tuning["tile_u"]
+    if tuning.get("plane_group_mb") == 1:
+        assert st["num_plane_groups"] > 1
+    else:
+        assert st["num_plane_groups"] == 1
     if tuning.get("ctas_per_sm") == 1:
         assert st["num_ctas"] == torch.cuda.get_device_properties(
             0).multi_processor_count
@@ -106,3 +112,14 @@ def test_autotune_applies_and_caches(pkg, torch, wl, fp64, tmp_path):
     r2 = at.autotune(pkg, plan2, stack, *args,
                      cache=at.TuningCache(cache.path))
     assert r2["cached"] is True and plan2.tuning() == applied
+
+
+def test_plane_groups_deterministic(pkg, torch, wl):
+    """Gridding in several plane-group passes is reproducible bit for bit."""
+    stack = pkg.KernelStack.from_workload(wl, "f")
+    plan = pkg.Plan()
+    plan.set_tuning({"plane_group_mb": 1})
+    a = _grid(pkg, torch, wl, plan, stack)
+    b = _grid(pkg, torch, wl, plan, stack)
+    assert plan.stats()["num_plane_groups"] > 1
+    assert np.array_equal(a[0].view(np.uint32), b[0].view(np.uint32))
