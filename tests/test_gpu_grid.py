@@ -298,3 +298,21 @@ def test_empty_and_all_skipped_device(pkg, synthetic, torch):
     wl.uu = np.full(100, 1e9, np.float32)
     g, ns, nm = pkg.grid_f(wl, norm=1.0)
     assert ns == 100 and nm == 1.0 and not g.any()
+
+
+def test_nonfinite_kernel_tap_stays_in_its_footprints(pkg, oracle_mod,
+                                                      synthetic, torch):
+    """A NaN kernel tap reaches exactly the grid cells whose footprints use
+    it, as in the reference: the kernel never reads a tap for a lane
+    outside a footprint when the stack holds a non-finite value."""
+    wl = synthetic.config0().subset(50_000)
+    cf = wl.conv_func.copy()
+    cf[3, 2, 1, 0] = np.nan     # plane 3, quadrant row 2, column 1, real
+    wl.conv_func = cf
+    g, ns, _ = pkg.grid_f(wl)
+    gr, nsr, _ = oracle_mod.grid_f(wl)
+    assert ns == nsr
+    assert np.isnan(gr).any()
+    assert np.array_equal(np.isnan(g), np.isnan(gr))
+    fin = ~np.isnan(gr)
+    assert max_rel(np.where(fin, g, 0), np.where(fin, gr, 0)) <= 1e-5
