@@ -172,6 +172,9 @@ def parse_args():
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the per-call heuristics instead of tuning the "
                          "plans (tuning runs before the timed region)")
+    ap.add_argument("--tuning", default=None,
+                    help="plan settings as JSON (gg_tuning fields), applied "
+                         "instead of tuning")
     ap.add_argument("--tune-cache", default=None,
                     help="autotuner cache file (default: $GPUGRID_TUNE_CACHE "
                          "or ~/.cache/gpugrid/tuning.json)")
@@ -331,13 +334,14 @@ def run_reference(args):
 # GPU run
 # ---------------------------------------------------------------------------
 def read_traffic(kernel, workload):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary
-    (profiles/<kernel>_<workload>.txt, line 'dram_bytes_per_launch: X')."""
+    """DRAM bytes of `kernel` per gridding step (all its plane-group passes)
+    from the committed ncu summary (profiles/<kernel>_<workload>.txt, line
+    'dram_bytes_per_step: X')."""
     path = os.path.join(HERE, "profiles", f"{kernel}_{workload}.txt")
     if not os.path.isfile(path):
         return None
     for line in open(path):
-        if line.startswith("dram_bytes_per_launch:"):
+        if line.startswith("dram_bytes_per_step:"):
             try:
                 return float(line.split(":", 1)[1])
             except ValueError:
@@ -379,7 +383,9 @@ def run_ours(args):
     vis, weight = to_dev(wl.vis), to_dev(wl.weight)
     G = wl.grid_size
     tune_cache, tuning = None, None
-    if args.no_autotune or args.tile_shape or args.staging >= 0:
+    if args.tuning:
+        plan.set_tuning(json.loads(args.tuning))
+    elif args.no_autotune or args.tile_shape or args.staging >= 0:
         plan.set_tile_shape(args.tile_shape)
         plan.set_slice_staging(args.staging)
     else:

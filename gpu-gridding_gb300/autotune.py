@@ -9,7 +9,7 @@ no placement, norm or skip count (gg_tuning in the C header):
 * ``sort_detail``   -- record order within a tile (plane + offset class,
   plane only, or visibility order),
 * ``ctas_per_sm``   -- resident gridding CTAs per SM (0 = as many as fit),
-* ``plane_group_mb`` -- kernel bytes per gridding pass (0 = a quarter of L2).
+* ``plane_group_mb`` -- kernel bytes per gridding pass (0 = half of L2).
 
 :func:`search` runs a coordinate search over them with a caller-supplied
 timing function; :func:`autotune` times real gridding calls of a workload

@@ -354,7 +354,7 @@ struct gg_plan {
   int items_per_cta = 4;  // work-item granularity of heavy-tile splits
   int sort_detail = 2;    // low sort-key fields: 2 plane+class, 1 plane, 0
   int ctas_per_sm = 0;    // cap on resident gridding CTAs, 0 = none
-  int plane_group_mb = 0; // slab bytes per plane group, 0 = L2 size / 4
+  int plane_group_mb = 0; // slab bytes per plane group, 0 = L2 size / 2
   // Plane groups of the last call (see TileGeom): table, and what it was
   // computed for.
   DevBuf plane_group, group_items;
@@ -469,8 +469,7 @@ TileGeom make_geom(int shape, int grid_size, int num_grids,
 }
 
 // Plane groups for a call: consecutive w-planes whose slabs together stay
-// within the byte budget (plan->plane_group_mb, or a quarter of the L2
-// cache), so that each gridding pass reads a stack slice that stays
+// within the byte budget (plan->plane_group_mb, or half the L2 cache), so that each gridding pass reads a stack slice that stays
 // resident in L2.  At most max_groups groups (the sort key's spare bits).
 // Uploads the plane -> group table when it changes; returns the number of
 // groups in *num_groups.
@@ -481,7 +480,7 @@ int plane_groups(gg_plan* plan, const gg_kernels* K, int max_groups,
   if (budget <= 0) {
     int l2 = 0;
     GG_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, K->device));
-    budget = std::max<long long>((long long)l2 / 4, 1 << 20);
+    budget = std::max<long long>((long long)l2 / 2, 1 << 20);
   }
   max_groups = std::max(1, std::min(max_groups, 64));
   if (plan->pg_kernels == K->id && plan->pg_budget == requested &&

@@ -172,7 +172,7 @@ GG_API int gg_plan_set_slice_staging(gg_plan* plan, int mode);
  *                  into groups of consecutive planes whose re-laid kernels
  *                  fit this many MiB and each group is gridded in its own
  *                  pass, so that a pass's kernels stay in L2; 0 (default) =
- *                  a quarter of the device's L2 cache, 0..1048576
+ *                  half the device's L2 cache, 0..1048576
  * gg_plan_set_tile_shape and gg_plan_set_slice_staging set the first two
  * fields alone. */
 typedef struct
