@@ -44,7 +44,14 @@ EXPORTED_SYMBOLS = (
     "gg_grid_wproj_d_batched_replay", "gg_plan_check",
     "gg_grid_wproj_d_device", "gg_place_wproj_f_device",
     "gg_place_wproj_d_device", "gg_degrid_wproj_f_device",
-    "gg_degrid_wproj_d_device",
+    "gg_degrid_wproj_d_device", "gg_degrid_wproj_f", "gg_degrid_wproj_d",
+    "oskar_degrid_wproj_f", "oskar_degrid_wproj_d",
+    "oskar_grid_weights_write_f", "oskar_grid_weights_write_d",
+    "oskar_grid_weights_read_f", "oskar_grid_weights_read_d",
+    "gg_grid_weights_write_f", "gg_grid_weights_write_d",
+    "gg_grid_weights_read_f", "gg_grid_weights_read_d",
+    "gg_grid_weights_write_f_device", "gg_grid_weights_write_d_device",
+    "gg_grid_weights_read_f_device", "gg_grid_weights_read_d_device",
 )
 
 
@@ -119,6 +126,31 @@ def _declare(L):
         fn.restype = ctypes.c_int
         fn = getattr(L, f"gg_place_wproj_{suffix}_device")
         fn.argtypes = [_vp, _sz, _vp, _vp, _vp, real, real, ctypes.c_int,
+                       _vp, _vp]
+        fn.restype = ctypes.c_int
+        degrid_args = [_sz, _vp, ctypes.c_int, ctypes.c_int, _vp, _sz, _vp,
+                       _vp, _vp, real, real, ctypes.c_int, _vp, _vp]
+        fn = getattr(L, f"gg_degrid_wproj_{suffix}")
+        fn.argtypes = degrid_args
+        fn.restype = ctypes.c_int
+        fn = getattr(L, f"oskar_degrid_wproj_{suffix}")
+        fn.argtypes = degrid_args
+        fn.restype = None
+        w_args = [_sz, _vp, _vp, _vp, real, ctypes.c_int, _vp, _vp]
+        r_args = [_sz, _vp, _vp, _vp, _vp, real, ctypes.c_int, _vp, _vp]
+        for name, args in (("write", w_args), ("read", r_args)):
+            fn = getattr(L, f"gg_grid_weights_{name}_{suffix}")
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+            fn = getattr(L, f"oskar_grid_weights_{name}_{suffix}")
+            fn.argtypes = args
+            fn.restype = None
+        fn = getattr(L, f"gg_grid_weights_write_{suffix}_device")
+        fn.argtypes = [_vp, _sz, _vp, _vp, _vp, real, ctypes.c_int, _vp, _vp,
+                       _vp]
+        fn.restype = ctypes.c_int
+        fn = getattr(L, f"gg_grid_weights_read_{suffix}_device")
+        fn.argtypes = [_vp, _sz, _vp, _vp, _vp, _vp, real, ctypes.c_int, _vp,
                        _vp, _vp]
         fn.restype = ctypes.c_int
         fn = getattr(L, f"gg_degrid_wproj_{suffix}_device")
@@ -469,6 +501,115 @@ def degrid_wproj_device(plan, stack, uu, vv, ww, cell_size_rad, w_scale,
     _check(fn(plan.handle, stack.handle, n, _ptr(uu), _ptr(vv), _ptr(ww),
               cell_size_rad, w_scale, grid_size, _ptr(grid), _ptr(out_vis),
               _stream_ptr(stream)))
+
+
+def _suffix(a):
+    dt = np.asarray(a).dtype if not hasattr(a, "dtype") else a.dtype
+    name = str(dt).replace("torch.", "")
+    if name == "float32":
+        return "f", np.float32
+    if name == "float64":
+        return "d", np.float64
+    raise TypeError(f"float32 or float64 arrays expected, got {dt}")
+
+
+# ---------------------------------------------------------------------------
+# Uniform weighting (reference utils/oskar_grid_weights.c)
+# ---------------------------------------------------------------------------
+def grid_weights_write(uu, vv, weight, cell_size_rad, grid_size, grid=None):
+    """Density grid of uniform weighting (oskar_grid_weights_write_{f,d}):
+    grid[gv, gu] += weight for every point on the grid.  float32 or float64
+    host arrays; grid ([G, G], accumulated) is created when None.  Returns
+    (grid, num_skipped)."""
+    suffix, dt = _suffix(uu)
+    if grid is None:
+        grid = np.zeros((grid_size, grid_size), dt)
+    if not (isinstance(grid, np.ndarray) and grid.dtype == dt and
+            grid.flags.c_contiguous and grid.size == grid_size * grid_size):
+        raise TypeError("grid must be a C-contiguous [G, G] array of the "
+                        "coordinates' dtype")
+    a = [_host(uu, dt), _host(vv, dt), _host(weight, dt)]
+    ns = ctypes.c_size_t(0)
+    _check(getattr(lib(), f"gg_grid_weights_write_{suffix}")(
+        a[0].shape[0], _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), cell_size_rad,
+        grid_size, ctypes.addressof(ns), _ptr(grid)))
+    return grid, int(ns.value)
+
+
+def grid_weights_read(uu, vv, weight_in, weight_out, cell_size_rad,
+                      grid_size, grid):
+    """Uniform re-weighting (oskar_grid_weights_read_{f,d}): weight_out =
+    weight_in / density for points on the grid (0 where the density is 0);
+    other entries of weight_out (updated in place) are left alone.  Returns
+    num_skipped."""
+    suffix, dt = _suffix(uu)
+    if not (isinstance(weight_out, np.ndarray) and weight_out.dtype == dt and
+            weight_out.flags.c_contiguous):
+        raise TypeError("weight_out must be a C-contiguous array of the "
+                        "coordinates' dtype")
+    a = [_host(uu, dt), _host(vv, dt), _host(weight_in, dt), _host(grid, dt)]
+    ns = ctypes.c_size_t(0)
+    _check(getattr(lib(), f"gg_grid_weights_read_{suffix}")(
+        a[0].shape[0], _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), _ptr(weight_out),
+        cell_size_rad, grid_size, ctypes.addressof(ns), _ptr(a[3])))
+    return int(ns.value)
+
+
+def grid_weights_write_device(plan, uu, vv, weight, cell_size_rad, grid_size,
+                              grid, num_skipped, stream=None):
+    """Device form of grid_weights_write: torch CUDA tensors; grid [G, G]
+    accumulated, num_skipped int64 [1] set."""
+    _require_cuda(uu, vv, weight, grid, num_skipped)
+    suffix, _ = _suffix(uu)
+    _check(getattr(lib(), f"gg_grid_weights_write_{suffix}_device")(
+        plan.handle, int(uu.shape[0]), _ptr(uu), _ptr(vv), _ptr(weight),
+        cell_size_rad, grid_size, _ptr(num_skipped), _ptr(grid),
+        _stream_ptr(stream)))
+
+
+def grid_weights_read_device(plan, uu, vv, weight_in, weight_out,
+                             cell_size_rad, grid_size, grid, num_skipped,
+                             stream=None):
+    """Device form of grid_weights_read."""
+    _require_cuda(uu, vv, weight_in, weight_out, grid, num_skipped)
+    suffix, _ = _suffix(uu)
+    _check(getattr(lib(), f"gg_grid_weights_read_{suffix}_device")(
+        plan.handle, int(uu.shape[0]), _ptr(uu), _ptr(vv), _ptr(weight_in),
+        _ptr(weight_out), cell_size_rad, grid_size, _ptr(num_skipped),
+        _ptr(grid), _stream_ptr(stream)))
+
+
+# ---------------------------------------------------------------------------
+# Degridding with host arrays
+# ---------------------------------------------------------------------------
+def degrid_wproj(num_w_planes, support, oversample, conv_size_half,
+                 conv_func, uu, vv, ww, cell_size_rad, w_scale, grid_size,
+                 grid):
+    """Host form of the adjoint (gg_degrid_wproj_{f,d}): returns the
+    [N, 2] visibilities G^H grid, in the coordinates' precision."""
+    suffix, dt = _suffix(uu)
+    a = [_host(support, np.int32), _host(conv_func, dt), _host(uu, dt),
+         _host(vv, dt), _host(ww, dt), _host(grid, dt)]
+    if a[5].size != 2 * grid_size * grid_size:
+        raise ValueError("grid must hold grid_size^2 complex values")
+    n = a[2].shape[0]
+    out = np.zeros((n, 2), dt)
+    _check(getattr(lib(), f"gg_degrid_wproj_{suffix}")(
+        num_w_planes, _ptr(a[0]), oversample, conv_size_half, _ptr(a[1]), n,
+        _ptr(a[2]), _ptr(a[3]), _ptr(a[4]), cell_size_rad, w_scale,
+        grid_size, _ptr(a[5]), _ptr(out)))
+    return out
+
+
+def degrid_f(wl, grid):
+    """degrid_wproj on a Workload in FP32."""
+    return degrid_wproj(wl.num_w_planes, wl.support, wl.oversample,
+                        wl.conv_size_half, wl.conv_func,
+                        np.asarray(wl.uu, np.float32),
+                        np.asarray(wl.vv, np.float32),
+                        np.asarray(wl.ww, np.float32),
+                        np.float32(wl.cell_size_rad), np.float32(wl.w_scale),
+                        wl.grid_size, np.asarray(grid, np.float32))
 
 
 from .autograd import GridWproj  # noqa: E402,F401

@@ -1002,6 +1002,20 @@ int degrid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
 }
 
 // Host-pointer drop-in: stage inputs, grid on the device, copy back.
+// The workspace plan of a device's host-pointer calls (made on first use;
+// the caller holds the device lock).
+int ensure_device_plan(DeviceState* st) {
+  if (st->plan) return GG_OK;
+  gg_plan* p = new gg_plan();
+  const int r = plan_init(p);
+  if (r != GG_OK) {
+    delete p;
+    return r;
+  }
+  st->plan = p;
+  return GG_OK;
+}
+
 template <typename Real>
 int dropin(size_t num_w_planes, const int* support, int oversample,
            int conv_size_half, const Real* conv_func, size_t num_points,
@@ -1023,15 +1037,7 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   GG_TRY(device_state(dev, &st));
   std::lock_guard<std::mutex> lk(st->mu);
   cudaStream_t s = st->stream;
-  if (!st->plan) {
-    gg_plan* p = new gg_plan();
-    int r = plan_init(p);
-    if (r != GG_OK) {
-      delete p;
-      return r;
-    }
-    st->plan = p;
-  }
+  GG_TRY(ensure_device_plan(st));
   gg_plan* plan = st->plan;
   gg_kernels* K = nullptr;
   GG_TRY(kernels_create<Real>(&K, num_w_planes, support, oversample,
@@ -1087,6 +1093,242 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   GG_TRY(check_device_error(plan, s));
   *norm = norm_out;
   *num_skipped = (size_t)skip_out;
+  return GG_OK;
+}
+
+// ---- uniform weighting --------------------------------------------------
+int weights_checks(gg_plan* plan, size_t n, int grid_size) {
+  if (!plan) return set_error(GG_ERR_INVALID_ARG, "plan is NULL");
+  if (grid_size < 1 || grid_size > kMaxGridSize)
+    return set_error(GG_ERR_UNSUPPORTED, "grid_size = %d outside [1, %d]",
+                     grid_size, kMaxGridSize);
+  if (n > 0xFFFFFFF0ull)
+    return set_error(GG_ERR_UNSUPPORTED,
+                     "num_points = %zu exceeds 2^32-16 per call", n);
+  int dev;
+  GG_TRY(current_device(&dev));
+  if (dev != plan->device)
+    return set_error(GG_ERR_INVALID_ARG, "plan and current device differ");
+  return GG_OK;
+}
+
+// Density grid: grid[cell] += weights of the cell's points, in point order
+// (see gg_weights.cu).  Uses the plan's sort buffers.
+template <typename Real>
+int weights_write_pipeline(gg_plan* plan, size_t n, const Real* uu,
+                           const Real* vv, const Real* weight,
+                           Real cell_size_rad, int grid_size,
+                           unsigned long long* d_num_skipped, Real* d_grid,
+                           cudaStream_t s) {
+  GG_TRY(weights_checks(plan, n, grid_size));
+  if (n > 0 && (!uu || !vv || !weight))
+    return set_error(GG_ERR_INVALID_ARG, "an input array is NULL");
+  if (!d_grid || !d_num_skipped)
+    return set_error(GG_ERR_INVALID_ARG, "an output pointer is NULL");
+  plan->kept.valid = false;   // the sort buffers are reused below
+  GG_CUDA(cudaMemsetAsync(d_num_skipped, 0, sizeof(unsigned long long), s));
+  if (n == 0) return GG_OK;
+  GG_TRY(plan->keys0.ensure(n * 4));
+  GG_TRY(plan->vals0.ensure(n * 4));
+  GG_TRY(plan->keys1.ensure(n * 4));
+  GG_TRY(plan->vals1.ensure(n * 4));
+  GG_TRY(plan->sort_tmp.ensure(radix_temp_bytes(n)));
+  GG_CUDA(launch_weight_keys<Real>(uu, vv, n, cell_size_rad, grid_size,
+                                   plan->keys0.as<uint32_t>(),
+                                   plan->vals0.as<uint32_t>(), d_num_skipped,
+                                   s));
+  const int key_bits =
+      ceil_log2((unsigned long long)grid_size * grid_size + 1);
+  bool in_alt = false;
+  GG_CUDA(radix_sort_pairs(plan->keys0.as<uint32_t>(),
+                           plan->vals0.as<uint32_t>(),
+                           plan->keys1.as<uint32_t>(),
+                           plan->vals1.as<uint32_t>(), n, key_bits,
+                           plan->sort_tmp.p, s, &in_alt));
+  GG_CUDA(launch_weight_runs<Real>(
+      in_alt ? plan->keys1.as<uint32_t>() : plan->keys0.as<uint32_t>(),
+      in_alt ? plan->vals1.as<uint32_t>() : plan->vals0.as<uint32_t>(), n,
+      weight, grid_size, d_grid, s));
+  return GG_OK;
+}
+
+template <typename Real>
+int weights_read_pipeline(gg_plan* plan, size_t n, const Real* uu,
+                          const Real* vv, const Real* w_in, Real* w_out,
+                          Real cell_size_rad, int grid_size,
+                          unsigned long long* d_num_skipped,
+                          const Real* d_grid, cudaStream_t s) {
+  GG_TRY(weights_checks(plan, n, grid_size));
+  if (n > 0 && (!uu || !vv || !w_in || !w_out))
+    return set_error(GG_ERR_INVALID_ARG, "an input or output array is NULL");
+  if (!d_grid || !d_num_skipped)
+    return set_error(GG_ERR_INVALID_ARG, "grid or num_skipped is NULL");
+  GG_CUDA(cudaMemsetAsync(d_num_skipped, 0, sizeof(unsigned long long), s));
+  GG_CUDA(launch_weights_read<Real>(uu, vv, w_in, w_out, n, cell_size_rad,
+                                    grid_size, d_grid, d_num_skipped, s));
+  return GG_OK;
+}
+
+template <typename Real>
+int weights_write_host(size_t n, const Real* uu, const Real* vv,
+                       const Real* weight, Real cell_size_rad, int grid_size,
+                       size_t* num_skipped, Real* grid) {
+  if (!num_skipped || !grid)
+    return set_error(GG_ERR_INVALID_ARG, "num_skipped or grid is NULL");
+  if (grid_size < 1 || grid_size > kMaxGridSize)
+    return set_error(GG_ERR_UNSUPPORTED, "grid_size = %d outside [1, %d]",
+                     grid_size, kMaxGridSize);
+  if (n > 0 && (!uu || !vv || !weight))
+    return set_error(GG_ERR_INVALID_ARG, "an input array is NULL");
+  int dev;
+  GG_TRY(current_device(&dev));
+  DeviceState* st;
+  GG_TRY(device_state(dev, &st));
+  std::lock_guard<std::mutex> lk(st->mu);
+  cudaStream_t s = st->stream;
+  GG_TRY(ensure_device_plan(st));
+  gg_plan* plan = st->plan;
+  const size_t grid_bytes = (size_t)grid_size * grid_size * sizeof(Real);
+  GG_TRY(plan->in_uu.ensure(n * sizeof(Real) + 16));
+  GG_TRY(plan->in_vv.ensure(n * sizeof(Real) + 16));
+  GG_TRY(plan->in_weight.ensure(n * sizeof(Real) + 16));
+  GG_TRY(plan->in_grid.ensure(grid_bytes));
+  GG_TRY(plan->in_misc.ensure(64));
+  unsigned long long* d_skip = plan->in_misc.as<unsigned long long>();
+  if (n) {
+    GG_CUDA(cudaMemcpyAsync(plan->in_uu.p, uu, n * sizeof(Real),
+                            cudaMemcpyHostToDevice, s));
+    GG_CUDA(cudaMemcpyAsync(plan->in_vv.p, vv, n * sizeof(Real),
+                            cudaMemcpyHostToDevice, s));
+    GG_CUDA(cudaMemcpyAsync(plan->in_weight.p, weight, n * sizeof(Real),
+                            cudaMemcpyHostToDevice, s));
+  }
+  GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, grid_bytes,
+                          cudaMemcpyHostToDevice, s));
+  GG_TRY(weights_write_pipeline<Real>(
+      plan, n, plan->in_uu.as<Real>(), plan->in_vv.as<Real>(),
+      plan->in_weight.as<Real>(), cell_size_rad, grid_size, d_skip,
+      plan->in_grid.as<Real>(), s));
+  unsigned long long skip_out = 0;
+  GG_CUDA(cudaMemcpyAsync(grid, plan->in_grid.p, grid_bytes,
+                          cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaMemcpyAsync(&skip_out, d_skip, 8, cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  *num_skipped = (size_t)skip_out;
+  return GG_OK;
+}
+
+template <typename Real>
+int weights_read_host(size_t n, const Real* uu, const Real* vv,
+                      const Real* w_in, Real* w_out, Real cell_size_rad,
+                      int grid_size, size_t* num_skipped, const Real* grid) {
+  if (!num_skipped || !grid)
+    return set_error(GG_ERR_INVALID_ARG, "num_skipped or grid is NULL");
+  if (grid_size < 1 || grid_size > kMaxGridSize)
+    return set_error(GG_ERR_UNSUPPORTED, "grid_size = %d outside [1, %d]",
+                     grid_size, kMaxGridSize);
+  if (n > 0 && (!uu || !vv || !w_in || !w_out))
+    return set_error(GG_ERR_INVALID_ARG, "an input or output array is NULL");
+  int dev;
+  GG_TRY(current_device(&dev));
+  DeviceState* st;
+  GG_TRY(device_state(dev, &st));
+  std::lock_guard<std::mutex> lk(st->mu);
+  cudaStream_t s = st->stream;
+  GG_TRY(ensure_device_plan(st));
+  gg_plan* plan = st->plan;
+  const size_t grid_bytes = (size_t)grid_size * grid_size * sizeof(Real);
+  GG_TRY(plan->in_uu.ensure(n * sizeof(Real) + 16));
+  GG_TRY(plan->in_vv.ensure(n * sizeof(Real) + 16));
+  GG_TRY(plan->in_weight.ensure(n * sizeof(Real) + 16));
+  GG_TRY(plan->in_vis.ensure(n * sizeof(Real) + 16));
+  GG_TRY(plan->in_grid.ensure(grid_bytes));
+  GG_TRY(plan->in_misc.ensure(64));
+  unsigned long long* d_skip = plan->in_misc.as<unsigned long long>();
+  if (n) {
+    GG_CUDA(cudaMemcpyAsync(plan->in_uu.p, uu, n * sizeof(Real),
+                            cudaMemcpyHostToDevice, s));
+    GG_CUDA(cudaMemcpyAsync(plan->in_vv.p, vv, n * sizeof(Real),
+                            cudaMemcpyHostToDevice, s));
+    GG_CUDA(cudaMemcpyAsync(plan->in_weight.p, w_in, n * sizeof(Real),
+                            cudaMemcpyHostToDevice, s));
+    // Skipped points keep the caller's weight_out values.
+    GG_CUDA(cudaMemcpyAsync(plan->in_vis.p, w_out, n * sizeof(Real),
+                            cudaMemcpyHostToDevice, s));
+  }
+  GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, grid_bytes,
+                          cudaMemcpyHostToDevice, s));
+  GG_TRY(weights_read_pipeline<Real>(
+      plan, n, plan->in_uu.as<Real>(), plan->in_vv.as<Real>(),
+      plan->in_weight.as<Real>(), plan->in_vis.as<Real>(), cell_size_rad,
+      grid_size, d_skip, plan->in_grid.as<Real>(), s));
+  unsigned long long skip_out = 0;
+  if (n)
+    GG_CUDA(cudaMemcpyAsync(w_out, plan->in_vis.p, n * sizeof(Real),
+                            cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaMemcpyAsync(&skip_out, d_skip, 8, cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  *num_skipped = (size_t)skip_out;
+  return GG_OK;
+}
+
+// ---- degridding with host pointers ------------------------------------------
+template <typename Real>
+int degrid_host(size_t num_w_planes, const int* support, int oversample,
+                int conv_size_half, const Real* conv_func, size_t num_points,
+                const Real* uu, const Real* vv, const Real* ww,
+                Real cell_size_rad, Real w_scale, int grid_size,
+                const Real* grid, Real* vis) {
+  if (!grid || (num_points > 0 && !vis))
+    return set_error(GG_ERR_INVALID_ARG, "grid or vis is NULL");
+  if (grid_size < 1 || grid_size > kMaxGridSize)
+    return set_error(GG_ERR_UNSUPPORTED, "grid_size = %d outside [1, %d]",
+                     grid_size, kMaxGridSize);
+  if (num_points > 0 && (!uu || !vv || !ww))
+    return set_error(GG_ERR_INVALID_ARG, "an input array is NULL");
+  GG_TRY(validate_stack(num_w_planes, support, oversample, conv_size_half,
+                        conv_func));
+  int dev;
+  GG_TRY(current_device(&dev));
+  DeviceState* st;
+  GG_TRY(device_state(dev, &st));
+  std::lock_guard<std::mutex> lk(st->mu);
+  cudaStream_t s = st->stream;
+  GG_TRY(ensure_device_plan(st));
+  gg_plan* plan = st->plan;
+  gg_kernels* K = nullptr;
+  GG_TRY(kernels_create<Real>(&K, num_w_planes, support, oversample,
+                              conv_size_half, conv_func, 0, s));
+  struct KGuard {
+    gg_kernels* k;
+    ~KGuard() { delete k; }
+  } kguard{K};
+  const size_t n = num_points;
+  const size_t grid_bytes = (size_t)grid_size * grid_size * 2 * sizeof(Real);
+  GG_TRY(plan->in_uu.ensure(n * sizeof(Real) + 16));
+  GG_TRY(plan->in_vv.ensure(n * sizeof(Real) + 16));
+  GG_TRY(plan->in_ww.ensure(n * sizeof(Real) + 16));
+  GG_TRY(plan->in_vis.ensure(2 * n * sizeof(Real) + 16));
+  GG_TRY(plan->in_grid.ensure(grid_bytes));
+  if (n) {
+    GG_CUDA(cudaMemcpyAsync(plan->in_uu.p, uu, n * sizeof(Real),
+                            cudaMemcpyHostToDevice, s));
+    GG_CUDA(cudaMemcpyAsync(plan->in_vv.p, vv, n * sizeof(Real),
+                            cudaMemcpyHostToDevice, s));
+    GG_CUDA(cudaMemcpyAsync(plan->in_ww.p, ww, n * sizeof(Real),
+                            cudaMemcpyHostToDevice, s));
+  }
+  GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, grid_bytes,
+                          cudaMemcpyHostToDevice, s));
+  GG_TRY(degrid_pipeline<Real>(plan, K, n, plan->in_uu.as<Real>(),
+                               plan->in_vv.as<Real>(), plan->in_ww.as<Real>(),
+                               cell_size_rad, w_scale, grid_size,
+                               plan->in_grid.as<Real>(),
+                               plan->in_vis.as<Real>(), s));
+  if (n)
+    GG_CUDA(cudaMemcpyAsync(vis, plan->in_vis.p, 2 * n * sizeof(Real),
+                            cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
   return GG_OK;
 }
 
@@ -1441,6 +1683,215 @@ GG_API int gg_grid_wproj_d_batched_replay(gg_plan* plan,
   return replay_pipeline<double>(plan, kernels, d_vis, d_weight,
                                  d_num_skipped, d_norm, d_grids,
                                  (cudaStream_t)stream);
+}
+
+GG_API int gg_grid_weights_write_f_device(gg_plan* plan, size_t num_points,
+                                          const float* d_uu, const float* d_vv,
+                                          const float* d_weight,
+                                          float cell_size_rad, int grid_size,
+                                          unsigned long long* d_num_skipped,
+                                          float* d_grid, void* stream) {
+  t_last_error.clear();
+  return weights_write_pipeline<float>(plan, num_points, d_uu, d_vv, d_weight,
+                                       cell_size_rad, grid_size, d_num_skipped,
+                                       d_grid, (cudaStream_t)stream);
+}
+
+GG_API int gg_grid_weights_write_d_device(gg_plan* plan, size_t num_points,
+                                          const double* d_uu,
+                                          const double* d_vv,
+                                          const double* d_weight,
+                                          double cell_size_rad, int grid_size,
+                                          unsigned long long* d_num_skipped,
+                                          double* d_grid, void* stream) {
+  t_last_error.clear();
+  return weights_write_pipeline<double>(plan, num_points, d_uu, d_vv,
+                                        d_weight, cell_size_rad, grid_size,
+                                        d_num_skipped, d_grid,
+                                        (cudaStream_t)stream);
+}
+
+GG_API int gg_grid_weights_read_f_device(gg_plan* plan, size_t num_points,
+                                         const float* d_uu, const float* d_vv,
+                                         const float* d_weight_in,
+                                         float* d_weight_out,
+                                         float cell_size_rad, int grid_size,
+                                         unsigned long long* d_num_skipped,
+                                         const float* d_grid, void* stream) {
+  t_last_error.clear();
+  return weights_read_pipeline<float>(plan, num_points, d_uu, d_vv,
+                                      d_weight_in, d_weight_out, cell_size_rad,
+                                      grid_size, d_num_skipped, d_grid,
+                                      (cudaStream_t)stream);
+}
+
+GG_API int gg_grid_weights_read_d_device(gg_plan* plan, size_t num_points,
+                                         const double* d_uu,
+                                         const double* d_vv,
+                                         const double* d_weight_in,
+                                         double* d_weight_out,
+                                         double cell_size_rad, int grid_size,
+                                         unsigned long long* d_num_skipped,
+                                         const double* d_grid, void* stream) {
+  t_last_error.clear();
+  return weights_read_pipeline<double>(plan, num_points, d_uu, d_vv,
+                                       d_weight_in, d_weight_out,
+                                       cell_size_rad, grid_size,
+                                       d_num_skipped, d_grid,
+                                       (cudaStream_t)stream);
+}
+
+GG_API int gg_grid_weights_write_f(size_t num_points, const float* uu,
+                                   const float* vv, const float* weight,
+                                   float cell_size_rad, int grid_size,
+                                   size_t* num_skipped, float* grid) {
+  t_last_error.clear();
+  return weights_write_host<float>(num_points, uu, vv, weight, cell_size_rad,
+                                   grid_size, num_skipped, grid);
+}
+
+GG_API int gg_grid_weights_write_d(size_t num_points, const double* uu,
+                                   const double* vv, const double* weight,
+                                   double cell_size_rad, int grid_size,
+                                   size_t* num_skipped, double* grid) {
+  t_last_error.clear();
+  return weights_write_host<double>(num_points, uu, vv, weight,
+                                    cell_size_rad, grid_size, num_skipped,
+                                    grid);
+}
+
+GG_API int gg_grid_weights_read_f(size_t num_points, const float* uu,
+                                  const float* vv, const float* weight_in,
+                                  float* weight_out, float cell_size_rad,
+                                  int grid_size, size_t* num_skipped,
+                                  const float* grid) {
+  t_last_error.clear();
+  return weights_read_host<float>(num_points, uu, vv, weight_in, weight_out,
+                                  cell_size_rad, grid_size, num_skipped,
+                                  grid);
+}
+
+GG_API int gg_grid_weights_read_d(size_t num_points, const double* uu,
+                                  const double* vv, const double* weight_in,
+                                  double* weight_out, double cell_size_rad,
+                                  int grid_size, size_t* num_skipped,
+                                  const double* grid) {
+  t_last_error.clear();
+  return weights_read_host<double>(num_points, uu, vv, weight_in, weight_out,
+                                   cell_size_rad, grid_size, num_skipped,
+                                   grid);
+}
+
+GG_API void oskar_grid_weights_write_f(const size_t num_points,
+                                       const float* uu, const float* vv,
+                                       const float* weight,
+                                       const float cell_size_rad,
+                                       const int grid_size,
+                                       size_t* num_skipped, float* grid) {
+  if (gg_grid_weights_write_f(num_points, uu, vv, weight, cell_size_rad,
+                              grid_size, num_skipped, grid) != GG_OK)
+    fprintf(stderr, "oskar_grid_weights_write_f (gpugrid): %s\n",
+            gg_last_error());
+}
+
+GG_API void oskar_grid_weights_write_d(const size_t num_points,
+                                       const double* uu, const double* vv,
+                                       const double* weight,
+                                       const double cell_size_rad,
+                                       const int grid_size,
+                                       size_t* num_skipped, double* grid) {
+  if (gg_grid_weights_write_d(num_points, uu, vv, weight, cell_size_rad,
+                              grid_size, num_skipped, grid) != GG_OK)
+    fprintf(stderr, "oskar_grid_weights_write_d (gpugrid): %s\n",
+            gg_last_error());
+}
+
+GG_API void oskar_grid_weights_read_f(const size_t num_points,
+                                      const float* uu, const float* vv,
+                                      const float* weight_in,
+                                      float* weight_out,
+                                      const float cell_size_rad,
+                                      const int grid_size,
+                                      size_t* num_skipped, const float* grid) {
+  if (gg_grid_weights_read_f(num_points, uu, vv, weight_in, weight_out,
+                             cell_size_rad, grid_size, num_skipped,
+                             grid) != GG_OK)
+    fprintf(stderr, "oskar_grid_weights_read_f (gpugrid): %s\n",
+            gg_last_error());
+}
+
+GG_API void oskar_grid_weights_read_d(const size_t num_points,
+                                      const double* uu, const double* vv,
+                                      const double* weight_in,
+                                      double* weight_out,
+                                      const double cell_size_rad,
+                                      const int grid_size,
+                                      size_t* num_skipped,
+                                      const double* grid) {
+  if (gg_grid_weights_read_d(num_points, uu, vv, weight_in, weight_out,
+                             cell_size_rad, grid_size, num_skipped,
+                             grid) != GG_OK)
+    fprintf(stderr, "oskar_grid_weights_read_d (gpugrid): %s\n",
+            gg_last_error());
+}
+
+GG_API int gg_degrid_wproj_f(size_t num_w_planes, const int* support,
+                             int oversample, int conv_size_half,
+                             const float* conv_func, size_t num_points,
+                             const float* uu, const float* vv,
+                             const float* ww, float cell_size_rad,
+                             float w_scale, int grid_size, const float* grid,
+                             float* vis) {
+  t_last_error.clear();
+  return degrid_host<float>(num_w_planes, support, oversample,
+                            conv_size_half, conv_func, num_points, uu, vv, ww,
+                            cell_size_rad, w_scale, grid_size, grid, vis);
+}
+
+GG_API int gg_degrid_wproj_d(size_t num_w_planes, const int* support,
+                             int oversample, int conv_size_half,
+                             const double* conv_func, size_t num_points,
+                             const double* uu, const double* vv,
+                             const double* ww, double cell_size_rad,
+                             double w_scale, int grid_size,
+                             const double* grid, double* vis) {
+  t_last_error.clear();
+  return degrid_host<double>(num_w_planes, support, oversample,
+                             conv_size_half, conv_func, num_points, uu, vv,
+                             ww, cell_size_rad, w_scale, grid_size, grid,
+                             vis);
+}
+
+GG_API void oskar_degrid_wproj_f(const size_t num_w_planes,
+                                 const int* support, const int oversample,
+                                 const int conv_size_half,
+                                 const float* conv_func,
+                                 const size_t num_points, const float* uu,
+                                 const float* vv, const float* ww,
+                                 const float cell_size_rad,
+                                 const float w_scale, const int grid_size,
+                                 const float* grid, float* vis) {
+  if (gg_degrid_wproj_f(num_w_planes, support, oversample, conv_size_half,
+                        conv_func, num_points, uu, vv, ww, cell_size_rad,
+                        w_scale, grid_size, grid, vis) != GG_OK)
+    fprintf(stderr, "oskar_degrid_wproj_f (gpugrid): %s\n",
+            gg_last_error());
+}
+
+GG_API void oskar_degrid_wproj_d(const size_t num_w_planes,
+                                 const int* support, const int oversample,
+                                 const int conv_size_half,
+                                 const double* conv_func,
+                                 const size_t num_points, const double* uu,
+                                 const double* vv, const double* ww,
+                                 const double cell_size_rad,
+                                 const double w_scale, const int grid_size,
+                                 const double* grid, double* vis) {
+  if (gg_degrid_wproj_d(num_w_planes, support, oversample, conv_size_half,
+                        conv_func, num_points, uu, vv, ww, cell_size_rad,
+                        w_scale, grid_size, grid, vis) != GG_OK)
+    fprintf(stderr, "oskar_degrid_wproj_d (gpugrid): %s\n",
+            gg_last_error());
 }
 
 GG_API int gg_plan_check(gg_plan* plan, void* stream) {

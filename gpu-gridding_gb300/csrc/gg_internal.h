@@ -198,6 +198,29 @@ int record_error(int code, const char* message);
 bool kernels_info(const gg_kernels* k, StackView* view, int* device,
                   bool* is_double, int* num_planes);
 
+// ---- uniform weighting (gg_weights.cu) -------------------------------------
+// Keys each point by its density cell (grid_size^2 when off the grid) and
+// counts the off-grid points into *d_num_skipped (which must start at 0).
+template <typename Real>
+cudaError_t launch_weight_keys(const Real* uu, const Real* vv,
+                               unsigned long long n, Real cell_size_rad,
+                               int grid_size, uint32_t* keys, uint32_t* vals,
+                               unsigned long long* d_num_skipped,
+                               cudaStream_t s);
+// grid[cell] += the weights of the cell's points, in the order of the
+// stably sorted (keys, vals).
+template <typename Real>
+cudaError_t launch_weight_runs(const uint32_t* keys, const uint32_t* vals,
+                               unsigned long long n, const Real* weight,
+                               int grid_size, Real* grid, cudaStream_t s);
+template <typename Real>
+cudaError_t launch_weights_read(const Real* uu, const Real* vv,
+                                const Real* w_in, Real* w_out,
+                                unsigned long long n, Real cell_size_rad,
+                                int grid_size, const Real* grid,
+                                unsigned long long* d_num_skipped,
+                                cudaStream_t s);
+
 // ---- FP32 FMA throughput probe (gg_calib.cu) ------------------------------
 cudaError_t measure_fp32_fma(int num_sms, double* tflops_best, float* ms_out);
 

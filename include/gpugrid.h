@@ -337,6 +337,103 @@ GG_API int gg_degrid_wproj_d_device(gg_plan* plan, const gg_kernels* kernels,
         const double* d_ww, double cell_size_rad, double w_scale,
         int grid_size, const double* d_grid, double* d_out_vis, void* stream);
 
+/* Host-pointer degridding, the sibling of oskar_grid_wproj_f/_d (the
+ * reference has no degridder): the same kernel stack, coordinates and
+ * placement rules; vis (complex interleaved, num_points entries) is
+ * overwritten with the adjoint map above applied to grid.  Synchronous. */
+GG_API int gg_degrid_wproj_f(size_t num_w_planes, const int* support,
+        int oversample, int conv_size_half, const float* conv_func,
+        size_t num_points, const float* uu, const float* vv, const float* ww,
+        float cell_size_rad, float w_scale, int grid_size, const float* grid,
+        float* vis);
+GG_API int gg_degrid_wproj_d(size_t num_w_planes, const int* support,
+        int oversample, int conv_size_half, const double* conv_func,
+        size_t num_points, const double* uu, const double* vv,
+        const double* ww, double cell_size_rad, double w_scale,
+        int grid_size, const double* grid, double* vis);
+/* void forms (failures are reported on stderr and by gg_last_error). */
+GG_API void oskar_degrid_wproj_f(const size_t num_w_planes,
+        const int* support, const int oversample, const int conv_size_half,
+        const float* conv_func, const size_t num_points, const float* uu,
+        const float* vv, const float* ww, const float cell_size_rad,
+        const float w_scale, const int grid_size, const float* grid,
+        float* vis);
+GG_API void oskar_degrid_wproj_d(const size_t num_w_planes,
+        const int* support, const int oversample, const int conv_size_half,
+        const double* conv_func, const size_t num_points, const double* uu,
+        const double* vv, const double* ww, const double cell_size_rad,
+        const double w_scale, const int grid_size, const double* grid,
+        double* vis);
+
+/* ---------------------------------------------------------------------- */
+/* Uniform weighting                                                      */
+/* ---------------------------------------------------------------------- */
+
+/* Same prototypes and semantics as the reference's uniform-weighting
+ * functions (utils/oskar_grid_weights.h:60-144, oskar_grid_weights.c:
+ * 38-172), which the reference runs before gridding (main.cpp:230-286):
+ *   write: grid[gv][gu] += weight[i] for every point on the grid (a real
+ *          grid_size^2 density grid, accumulated), *num_skipped = points
+ *          off the grid;
+ *   read:  weight_out[i] = weight_in[i] / grid[gv][gu] (0 where the
+ *          density is 0) for points on the grid; off-grid points leave
+ *          weight_out untouched; *num_skipped set.
+ * with gu = (int)round(-uu * grid_size * cell_size_rad) + grid_size / 2
+ * and gv likewise from vv, in the call's precision.  Results are
+ * bit-identical to the reference's serial code: each cell's weights are
+ * added in point order.  Host pointers, synchronous. */
+GG_API void oskar_grid_weights_write_f(const size_t num_points,
+        const float* uu, const float* vv, const float* weight,
+        const float cell_size_rad, const int grid_size, size_t* num_skipped,
+        float* grid);
+GG_API void oskar_grid_weights_write_d(const size_t num_points,
+        const double* uu, const double* vv, const double* weight,
+        const double cell_size_rad, const int grid_size, size_t* num_skipped,
+        double* grid);
+GG_API void oskar_grid_weights_read_f(const size_t num_points,
+        const float* uu, const float* vv, const float* weight_in,
+        float* weight_out, const float cell_size_rad, const int grid_size,
+        size_t* num_skipped, const float* grid);
+GG_API void oskar_grid_weights_read_d(const size_t num_points,
+        const double* uu, const double* vv, const double* weight_in,
+        double* weight_out, const double cell_size_rad, const int grid_size,
+        size_t* num_skipped, const double* grid);
+/* Status-returning forms (same arguments). */
+GG_API int gg_grid_weights_write_f(size_t num_points, const float* uu,
+        const float* vv, const float* weight, float cell_size_rad,
+        int grid_size, size_t* num_skipped, float* grid);
+GG_API int gg_grid_weights_write_d(size_t num_points, const double* uu,
+        const double* vv, const double* weight, double cell_size_rad,
+        int grid_size, size_t* num_skipped, double* grid);
+GG_API int gg_grid_weights_read_f(size_t num_points, const float* uu,
+        const float* vv, const float* weight_in, float* weight_out,
+        float cell_size_rad, int grid_size, size_t* num_skipped,
+        const float* grid);
+GG_API int gg_grid_weights_read_d(size_t num_points, const double* uu,
+        const double* vv, const double* weight_in, double* weight_out,
+        double cell_size_rad, int grid_size, size_t* num_skipped,
+        const double* grid);
+/* Device-pointer forms on a stream: *d_num_skipped (64-bit) is set, the
+ * density grid accumulated.  The write form uses the plan's sort
+ * workspace (and discards geometry kept for a batched replay). */
+GG_API int gg_grid_weights_write_f_device(gg_plan* plan, size_t num_points,
+        const float* d_uu, const float* d_vv, const float* d_weight,
+        float cell_size_rad, int grid_size, unsigned long long* d_num_skipped,
+        float* d_grid, void* stream);
+GG_API int gg_grid_weights_write_d_device(gg_plan* plan, size_t num_points,
+        const double* d_uu, const double* d_vv, const double* d_weight,
+        double cell_size_rad, int grid_size,
+        unsigned long long* d_num_skipped, double* d_grid, void* stream);
+GG_API int gg_grid_weights_read_f_device(gg_plan* plan, size_t num_points,
+        const float* d_uu, const float* d_vv, const float* d_weight_in,
+        float* d_weight_out, float cell_size_rad, int grid_size,
+        unsigned long long* d_num_skipped, const float* d_grid, void* stream);
+GG_API int gg_grid_weights_read_d_device(gg_plan* plan, size_t num_points,
+        const double* d_uu, const double* d_vv, const double* d_weight_in,
+        double* d_weight_out, double cell_size_rad, int grid_size,
+        unsigned long long* d_num_skipped, const double* d_grid,
+        void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -209,6 +209,34 @@ def degrid_fp64(wl, grid):
     return out
 
 
+def weights_write(uu, vv, weight, cell_size_rad, grid_size, grid=None):
+    """Serial uniform-weighting density (oskar_grid_weights_write_{f,d}
+    semantics, precision from uu's dtype); grid [G, G] in/out.  Returns
+    (grid, num_skipped)."""
+    real = np.asarray(uu).dtype.type
+    sfx = "f" if real == np.float32 else "d"
+    grid = np.zeros((grid_size, grid_size), real) if grid is None else grid
+    ns = ctypes.c_size_t(0)
+    getattr(lib(), f"oracle_grid_weights_write_{sfx}")(
+        len(uu), _c(uu, real), _c(vv, real), _c(weight, real),
+        real(cell_size_rad), grid_size, ctypes.byref(ns), grid.reshape(-1))
+    return grid, int(ns.value)
+
+
+def weights_read(uu, vv, weight_in, weight_out, cell_size_rad, grid_size,
+                 grid):
+    """Serial uniform re-weighting (oskar_grid_weights_read_{f,d});
+    weight_out updated in place.  Returns num_skipped."""
+    real = np.asarray(uu).dtype.type
+    sfx = "f" if real == np.float32 else "d"
+    ns = ctypes.c_size_t(0)
+    getattr(lib(), f"oracle_grid_weights_read_{sfx}")(
+        len(uu), _c(uu, real), _c(vv, real), _c(weight_in, real), weight_out,
+        real(cell_size_rad), grid_size, ctypes.byref(ns),
+        _c(grid, real).reshape(-1))
+    return int(ns.value)
+
+
 def mac_count(wl, precision="f"):
     """Algorithmic complex MACs: sum of (2 s + 1)^2 over gridded points."""
     p = place(wl, precision)
