@@ -109,6 +109,15 @@ struct DeviceState {
   cudaStream_t stream = nullptr;
   int num_sms = 0;
   gg_plan* plan = nullptr;  // workspace of the host-pointer entry points
+  // Kernel stack the host-pointer entry points rebuild on every call (the
+  // caller may change its cube between calls), with its buffers and the
+  // cube's staging copy kept from call to call.
+  gg_kernels* host_kernels = nullptr;
+  DevBuf host_cube;
+  // Side stream and event that upload a host grid while the call's other
+  // work runs.
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t grid_ready = nullptr;
 };
 
 std::mutex g_devices_mu;
@@ -221,21 +230,23 @@ int validate_stack(size_t num_w_planes, const int* support, int oversample,
   return GG_OK;
 }
 
+// (Re)builds kernel stack k from a cube: sizes, tables, the re-laid slice
+// and slab stacks and the tap sums, enqueued on s.  k's device buffers are
+// reused when large enough, so rebuilding one object for every call (the
+// host-pointer entry points do) allocates nothing after the first call.  A
+// host cube is copied through *stage (a local buffer when stage is NULL).
+// With sync = false the caller must synchronise s before the host cube or
+// *stage may change.
 template <typename Real>
-int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
-                   int oversample, int conv_size_half, const Real* conv_func,
-                   int on_device, cudaStream_t s) {
-  if (!out) return set_error(GG_ERR_INVALID_ARG, "out is NULL");
-  *out = nullptr;
+int kernels_fill(gg_kernels* k, size_t num_w_planes, const int* support,
+                 int oversample, int conv_size_half, const Real* conv_func,
+                 int on_device, cudaStream_t s, DevBuf* stage, bool sync) {
   GG_TRY(validate_stack(num_w_planes, support, oversample, conv_size_half,
                         conv_func));
-  gg_kernels* k = new gg_kernels();
   static std::atomic<unsigned long long> next_id{1};
   k->id = next_id.fetch_add(1);
-  auto fail = [&](int code) {
-    delete k;
-    return code;
-  };
+  k->support_max = 0;
+  auto fail = [&](int code) { return code; };
   if (current_device(&k->device) != GG_OK) return fail(GG_ERR_CUDA);
   k->is_double = sizeof(Real) == 8;
   k->num_planes = (int)num_w_planes;
@@ -305,7 +316,8 @@ int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
     return fail(r);
   const size_t cube = num_w_planes * (size_t)conv_size_half * conv_size_half *
                       2 * sizeof(Real);
-  DevBuf staged;
+  DevBuf local;
+  DevBuf& staged = stage ? *stage : local;
   const Real* d_conv = conv_func;
   if (!on_device) {
     if ((r = staged.ensure(cube))) return fail(r);
@@ -328,7 +340,26 @@ int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
     return fail(r);
   // The staging copy (and the caller's host array) must outlive the
   // kernels that read it.
-  if ((r = cu(cudaStreamSynchronize(s), "kernel stack sync"))) return fail(r);
+  if (sync || !stage)
+    if ((r = cu(cudaStreamSynchronize(s), "kernel stack sync")))
+      return fail(r);
+  return GG_OK;
+}
+
+template <typename Real>
+int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
+                   int oversample, int conv_size_half, const Real* conv_func,
+                   int on_device, cudaStream_t s) {
+  if (!out) return set_error(GG_ERR_INVALID_ARG, "out is NULL");
+  *out = nullptr;
+  gg_kernels* k = new gg_kernels();
+  const int r = kernels_fill<Real>(k, num_w_planes, support, oversample,
+                                   conv_size_half, conv_func, on_device, s,
+                                   nullptr, true);
+  if (r != GG_OK) {
+    delete k;
+    return r;
+  }
   *out = k;
   return GG_OK;
 }
@@ -355,6 +386,9 @@ struct gg_plan {
   int sort_detail = 2;    // low sort-key fields: 2 plane+class, 1 plane, 0
   int ctas_per_sm = 0;    // cap on resident gridding CTAs, 0 = none
   int plane_group_mb = 0; // slab bytes per plane group, 0 = L2 size / 2
+  // Event the gridding passes wait for (a grid upload on another stream),
+  // or null.
+  cudaEvent_t grid_wait = nullptr;
   // Plane groups of the last call (see TileGeom): table, and what it was
   // computed for.
   DevBuf plane_group, group_items;
@@ -773,6 +807,7 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
                                total, chunk, ib, s));
     plan->kept.rec_vis = vals;
     plan->kept.num_ctas = num_ctas;
+    if (plan->grid_wait) GG_CUDA(cudaStreamWaitEvent(s, plan->grid_wait, 0));
     plan->mark(3, s);
     GG_CUDA(launch_grid_tiles<Real>(
         ib.items, ib.group_items, ib.counter, sc + kDeviceError, vals, po.cell,
@@ -1002,6 +1037,31 @@ int degrid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
 }
 
 // Host-pointer drop-in: stage inputs, grid on the device, copy back.
+// The kernel stack of a host-pointer call, rebuilt from the caller's cube
+// into the device's reused stack object (the caller holds the device lock
+// and synchronises s before returning).
+template <typename Real>
+int host_kernels(DeviceState* st, size_t num_w_planes, const int* support,
+                 int oversample, int conv_size_half, const Real* conv_func,
+                 cudaStream_t s, gg_kernels** out) {
+  if (!st->host_kernels) st->host_kernels = new gg_kernels();
+  GG_TRY(kernels_fill<Real>(st->host_kernels, num_w_planes, support,
+                            oversample, conv_size_half, conv_func, 0, s,
+                            &st->host_cube, false));
+  *out = st->host_kernels;
+  return GG_OK;
+}
+
+int ensure_copy_stream(DeviceState* st) {
+  if (!st->copy_stream)
+    GG_CUDA(cudaStreamCreateWithFlags(&st->copy_stream,
+                                      cudaStreamNonBlocking));
+  if (!st->grid_ready)
+    GG_CUDA(cudaEventCreateWithFlags(&st->grid_ready,
+                                     cudaEventDisableTiming));
+  return GG_OK;
+}
+
 // The workspace plan of a device's host-pointer calls (made on first use;
 // the caller holds the device lock).
 int ensure_device_plan(DeviceState* st) {
@@ -1039,22 +1099,28 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   cudaStream_t s = st->stream;
   GG_TRY(ensure_device_plan(st));
   gg_plan* plan = st->plan;
-  gg_kernels* K = nullptr;
-  GG_TRY(kernels_create<Real>(&K, num_w_planes, support, oversample,
-                              conv_size_half, conv_func, 0, s));
-  struct KGuard {
-    gg_kernels* k;
-    ~KGuard() { delete k; }
-  } kguard{K};
-
   const size_t n = num_points;
   const size_t grid_bytes = (size_t)grid_size * grid_size * 2 * sizeof(Real);
+  // The grid is needed only by the gridding passes: upload it on a side
+  // stream while the kernel stack, placement and sort run.
+  GG_TRY(plan->in_grid.ensure(grid_bytes));
+  GG_TRY(ensure_copy_stream(st));
+  struct CopyGuard {   // the upload reads the caller's grid: finish it
+    cudaStream_t s;
+    ~CopyGuard() { cudaStreamSynchronize(s); }
+  } copy_guard{st->copy_stream};
+  GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, grid_bytes,
+                          cudaMemcpyHostToDevice, st->copy_stream));
+  GG_CUDA(cudaEventRecord(st->grid_ready, st->copy_stream));
+  gg_kernels* K = nullptr;
+  GG_TRY(host_kernels<Real>(st, num_w_planes, support, oversample,
+                            conv_size_half, conv_func, s, &K));
+
   GG_TRY(plan->in_uu.ensure(n * sizeof(Real) + 16));
   GG_TRY(plan->in_vv.ensure(n * sizeof(Real) + 16));
   GG_TRY(plan->in_ww.ensure(n * sizeof(Real) + 16));
   GG_TRY(plan->in_vis.ensure(2 * n * sizeof(Real) + 16));
   GG_TRY(plan->in_weight.ensure(n * sizeof(Real) + 16));
-  GG_TRY(plan->in_grid.ensure(grid_bytes));
   GG_TRY(plan->in_misc.ensure(64));
   double* d_norm = plan->in_misc.as<double>();
   unsigned long long* d_skip = (unsigned long long*)(plan->in_misc.as<char>() + 8);
@@ -1070,17 +1136,22 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
     GG_CUDA(cudaMemcpyAsync(plan->in_weight.p, weight, n * sizeof(Real),
                             cudaMemcpyHostToDevice, s));
   }
-  GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, grid_bytes,
-                          cudaMemcpyHostToDevice, s));
   const double norm_in = *norm;
   GG_CUDA(cudaMemcpyAsync(d_norm, &norm_in, sizeof(double),
                           cudaMemcpyHostToDevice, s));
-  GG_TRY(grid_pipeline<Real>(plan, K, n, plan->in_uu.as<Real>(),
-                             plan->in_vv.as<Real>(), plan->in_ww.as<Real>(),
-                             plan->in_vis.as<Real>(),
-                             plan->in_weight.as<Real>(), cell_size_rad,
-                             w_scale, grid_size, d_skip, d_norm,
-                             plan->in_grid.as<Real>(), s));
+  plan->grid_wait = st->grid_ready;
+  const int rc = grid_pipeline<Real>(plan, K, n, plan->in_uu.as<Real>(),
+                                     plan->in_vv.as<Real>(),
+                                     plan->in_ww.as<Real>(),
+                                     plan->in_vis.as<Real>(),
+                                     plan->in_weight.as<Real>(),
+                                     cell_size_rad, w_scale, grid_size,
+                                     d_skip, d_norm, plan->in_grid.as<Real>(),
+                                     s);
+  plan->grid_wait = nullptr;
+  GG_TRY(rc);
+  // (A call with nothing to grid never waited for the upload.)
+  GG_CUDA(cudaStreamWaitEvent(s, st->grid_ready, 0));
   double norm_out = 0.0;
   unsigned long long skip_out = 0;
   GG_CUDA(cudaMemcpyAsync(grid, plan->in_grid.p, grid_bytes,
@@ -1297,12 +1368,8 @@ int degrid_host(size_t num_w_planes, const int* support, int oversample,
   GG_TRY(ensure_device_plan(st));
   gg_plan* plan = st->plan;
   gg_kernels* K = nullptr;
-  GG_TRY(kernels_create<Real>(&K, num_w_planes, support, oversample,
-                              conv_size_half, conv_func, 0, s));
-  struct KGuard {
-    gg_kernels* k;
-    ~KGuard() { delete k; }
-  } kguard{K};
+  GG_TRY(host_kernels<Real>(st, num_w_planes, support, oversample,
+                            conv_size_half, conv_func, s, &K));
   const size_t n = num_points;
   const size_t grid_bytes = (size_t)grid_size * grid_size * 2 * sizeof(Real);
   GG_TRY(plan->in_uu.ensure(n * sizeof(Real) + 16));

@@ -105,15 +105,27 @@ __global__ void k_tap_sums(const Real* __restrict__ conv, StackView v,
   const int s = v.support[p];
   const int os = v.oversample, csh = v.conv_size_half;
   const size_t kstart = (size_t)p * csh * csh;
+  // The additions stay in the reference's order; the loads of 8 taps are
+  // issued together so their latencies overlap.
   double sum = 0.0;
   for (int j = -s; j <= s; ++j) {
     const int t = abs(ov + j * os);
-    for (int k = -s; k <= s; ++k) {
+    const Real* row = conv + (kstart + (size_t)t * csh) * 2;
+    int k = -s;
+    for (; k + 7 <= s; k += 8) {
+      double re[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int c = abs(ou + (k + q) * os);
+        re[q] = (t < csh && c < csh) ? (double)row[(size_t)c * 2] : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) sum = __dadd_rn(sum, re[q]);
+    }
+    for (; k <= s; ++k) {
       const int c = abs(ou + k * os);
-      const double re = (t < csh && c < csh)
-                            ? (double)conv[(kstart + (size_t)t * csh + c) * 2]
-                            : 0.0;
-      sum += re;
+      sum = __dadd_rn(sum, (t < csh && c < csh) ? (double)row[(size_t)c * 2]
+                                                : 0.0);
     }
   }
   tap_sum[idx] = sum;
