@@ -507,6 +507,41 @@ def run_ours(args):
                                       wl.support.nbytes + 8 * G * G + 8),
                "d2h_bytes_per_step": 8 * G * G + 16}
 
+    # The operations either side of the gridder on the same workload: the
+    # adjoint (degridding) and the uniform-weighting pair (density grid,
+    # re-weighting), device-resident, CUDA-event timed.
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    out_vis = torch.empty((num_vis, 2), dtype=torch.float32, device=dev)
+    dens = torch.zeros((G, G), dtype=torch.float32, device=dev)
+    w_out = torch.empty_like(weight)
+    ms_degrid = timed(lambda: pkg.degrid_wproj_device(
+        plan, stack, uu, vv, ww, cell, wsc, G, grid, out_vis, stream))
+    ms_wwrite = timed(lambda: pkg.grid_weights_write_device(
+        plan, uu, vv, weight, cell, G, dens, nskip, stream))
+    ms_wread = timed(lambda: pkg.grid_weights_read_device(
+        plan, uu, vv, weight, w_out, cell, G, dens, nskip, stream))
+    neighbours = {
+        "degrid": {"ms_per_step": ms_degrid,
+                   "mvis_s": num_vis / (ms_degrid * 1e-3) / 1e6,
+                   "gflops": 8.0 * macs / (ms_degrid * 1e-3) / 1e9},
+        "weights_write": {"ms_per_step": ms_wwrite,
+                          "mvis_s": num_vis / (ms_wwrite * 1e-3) / 1e6},
+        "weights_read": {"ms_per_step": ms_wread,
+                         "mvis_s": num_vis / (ms_wread * 1e-3) / 1e6},
+    }
+    del out_vis, dens, w_out
+
     batched = None
     if args.batched_steps > 0 and world == 1:
         batched = measure_batched(pkg, torch, args.batched_steps,
@@ -558,6 +593,7 @@ def run_ours(args):
             "clocks": clk,
             "published_p100_mvis": PUBLISHED_P100_MVIS.get(args.workload),
             "batched_vs_plain": batched,
+            "neighbours": neighbours,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
