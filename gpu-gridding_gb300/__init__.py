@@ -34,7 +34,8 @@ _ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory",
 EXPORTED_SYMBOLS = (
     "oskar_grid_wproj_d", "oskar_grid_wproj_f", "gg_grid_wproj_d",
     "gg_grid_wproj_f", "gg_last_error", "gg_version", "gg_kernels_create_f",
-    "gg_kernels_create_d", "gg_kernels_destroy", "gg_plan_create",
+    "gg_kernels_create_d", "gg_kernels_generate_f", "gg_kernels_generate_d",
+    "gg_kernels_destroy", "gg_plan_create",
     "gg_plan_destroy", "gg_plan_last_stats", "gg_plan_set_tile_shape",
     "gg_plan_set_slice_staging", "gg_plan_set_tuning", "gg_plan_get_tuning",
     "gg_plan_set_profiling",
@@ -112,6 +113,10 @@ def _declare(L):
         fn = getattr(L, f"gg_kernels_create_{suffix}")
         fn.argtypes = [ctypes.POINTER(_vp), _sz, _vp, ctypes.c_int,
                        ctypes.c_int, _vp, ctypes.c_int, _vp]
+        fn.restype = ctypes.c_int
+        fn = getattr(L, f"gg_kernels_generate_{suffix}")
+        fn.argtypes = [ctypes.POINTER(_vp), _sz, _vp, ctypes.c_int,
+                       ctypes.c_int, _vp, _vp, _vp]
         fn.restype = ctypes.c_int
         fn = getattr(L, f"gg_grid_wproj_{suffix}_device")
         fn.argtypes = [_vp, _vp, _sz, _vp, _vp, _vp, _vp, _vp, real, real,
@@ -332,6 +337,32 @@ class KernelStack:
             _stream_ptr(stream) if on_device else None))
         self._keep = None
         self.handle = h
+
+    @classmethod
+    def generate(cls, num_w_planes, support, oversample, conv_size_half,
+                 w_planes, precision="f", cube_out=None, stream=None):
+        """Kernel stack generated on the device (gg_kernels_generate_*):
+        the taper x chirp recipe with chirp parameters w_planes[p]; the
+        cube also goes to cube_out (a CUDA tensor [P, csh, csh, 2]) when
+        given."""
+        self = cls.__new__(cls)
+        self.precision = precision
+        self.num_w_planes = int(num_w_planes)
+        self.oversample = int(oversample)
+        self.conv_size_half = int(conv_size_half)
+        self.support = _host(support, np.int32)
+        self._keep = None
+        w = _host(w_planes, np.float64)
+        if w.shape[0] != self.num_w_planes:
+            raise ValueError("w_planes needs one value per plane")
+        h = ctypes.c_void_p(0)
+        _check(getattr(lib(), f"gg_kernels_generate_{precision}")(
+            ctypes.byref(h), self.num_w_planes, _ptr(self.support),
+            self.oversample, self.conv_size_half, _ptr(w),
+            _ptr(cube_out) if cube_out is not None else None,
+            _stream_ptr(stream)))
+        self.handle = h
+        return self
 
     @classmethod
     def from_workload(cls, wl, precision="f", stream=None):

@@ -21,7 +21,7 @@ LIB = os.path.join(BUILD, "libgpugrid.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["gg_api.cu", "gg_sort.cu", "gg_stack.cu", "gg_place.cu",
            "gg_grid.cu", "gg_degrid.cu", "gg_calib.cu", "gg_noalloc.cu",
-           "gg_batch.cu", "gg_weights.cu"]
+           "gg_batch.cu", "gg_weights.cu", "gg_kgen.cu"]
 
 
 def nvcc() -> str:

@@ -349,6 +349,47 @@ int kernels_fill(gg_kernels* k, size_t num_w_planes, const int* support,
 template <typename Real>
 int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
                    int oversample, int conv_size_half, const Real* conv_func,
+                   int on_device, cudaStream_t s);
+
+// Generates the taper x chirp cube on the device (gg_kgen.cu) and builds a
+// kernel stack from it; the cube also goes to d_cube_out when given.
+template <typename Real>
+int kernels_generate(gg_kernels** out, size_t num_w_planes, const int* support,
+                     int oversample, int conv_size_half,
+                     const double* w_planes, Real* d_cube_out,
+                     cudaStream_t s) {
+  if (!out) return set_error(GG_ERR_INVALID_ARG, "out is NULL");
+  *out = nullptr;
+  if (!w_planes) return set_error(GG_ERR_INVALID_ARG, "w_planes is NULL");
+  // Same checks as a caller's cube (the cube pointer is not needed yet).
+  GG_TRY(validate_stack(num_w_planes, support, oversample, conv_size_half,
+                        w_planes));
+  DevBuf d_support, d_w, d_total, cube;
+  GG_TRY(d_support.ensure(num_w_planes * sizeof(int)));
+  GG_TRY(d_w.ensure(num_w_planes * sizeof(double)));
+  GG_TRY(d_total.ensure(num_w_planes * 16));
+  Real* d_cube = d_cube_out;
+  if (!d_cube) {
+    GG_TRY(cube.ensure(num_w_planes * (size_t)conv_size_half *
+                       conv_size_half * 2 * sizeof(Real)));
+    d_cube = cube.as<Real>();
+  }
+  GG_CUDA(cudaMemcpyAsync(d_support.p, support, num_w_planes * sizeof(int),
+                          cudaMemcpyHostToDevice, s));
+  GG_CUDA(cudaMemcpyAsync(d_w.p, w_planes, num_w_planes * sizeof(double),
+                          cudaMemcpyHostToDevice, s));
+  GG_CUDA(launch_kernel_generate<Real>((int)num_w_planes, d_support.as<int>(),
+                                       d_w.as<double>(), oversample,
+                                       conv_size_half, d_total.p, d_cube, s));
+  // kernels_create synchronises s before returning, so the temporaries
+  // above outlive the kernels that read them.
+  return kernels_create<Real>(out, num_w_planes, support, oversample,
+                              conv_size_half, d_cube, 1, s);
+}
+
+template <typename Real>
+int kernels_create(gg_kernels** out, size_t num_w_planes, const int* support,
+                   int oversample, int conv_size_half, const Real* conv_func,
                    int on_device, cudaStream_t s) {
   if (!out) return set_error(GG_ERR_INVALID_ARG, "out is NULL");
   *out = nullptr;
@@ -1532,6 +1573,26 @@ GG_API int gg_kernels_create_d(gg_kernels** out, size_t num_w_planes,
   return kernels_create<double>(out, num_w_planes, support, oversample,
                                 conv_size_half, conv_func,
                                 conv_func_on_device, (cudaStream_t)stream);
+}
+
+GG_API int gg_kernels_generate_f(gg_kernels** out, size_t num_w_planes,
+                                 const int* support, int oversample,
+                                 int conv_size_half, const double* w_planes,
+                                 float* d_conv_func_out, void* stream) {
+  t_last_error.clear();
+  return kernels_generate<float>(out, num_w_planes, support, oversample,
+                                 conv_size_half, w_planes, d_conv_func_out,
+                                 (cudaStream_t)stream);
+}
+
+GG_API int gg_kernels_generate_d(gg_kernels** out, size_t num_w_planes,
+                                 const int* support, int oversample,
+                                 int conv_size_half, const double* w_planes,
+                                 double* d_conv_func_out, void* stream) {
+  t_last_error.clear();
+  return kernels_generate<double>(out, num_w_planes, support, oversample,
+                                  conv_size_half, w_planes, d_conv_func_out,
+                                  (cudaStream_t)stream);
 }
 
 GG_API int gg_kernels_destroy(gg_kernels* k) {

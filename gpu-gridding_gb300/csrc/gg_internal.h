@@ -221,6 +221,15 @@ cudaError_t launch_weights_read(const Real* uu, const Real* vv,
                                 unsigned long long* d_num_skipped,
                                 cudaStream_t s);
 
+// ---- W-kernel generation (gg_kgen.cu) -------------------------------------
+// Writes the taper x chirp cube [P][csh][csh] complex into d_cube; d_total
+// holds P complex FP64 normalisation sums (16 B each).
+template <typename Real>
+cudaError_t launch_kernel_generate(int num_planes, const int* d_support,
+                                   const double* d_w_planes, int oversample,
+                                   int conv_size_half, void* d_total,
+                                   Real* d_cube, cudaStream_t s);
+
 // ---- FP32 FMA throughput probe (gg_calib.cu) ------------------------------
 cudaError_t measure_fp32_fma(int num_sms, double* tflops_best, float* ms_out);
 

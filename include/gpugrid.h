@@ -108,6 +108,23 @@ GG_API int gg_kernels_create_f(gg_kernels** out, size_t num_w_planes,
 GG_API int gg_kernels_create_d(gg_kernels** out, size_t num_w_planes,
         const int* support, int oversample, int conv_size_half,
         const double* conv_func, int conv_func_on_device, void* stream);
+/* A kernel stack generated on the device, so that no cube crosses the host
+ * link: plane p of the cube is the taper x chirp kernel the synthetic
+ * workloads of this project use,
+ *   k(iv, iu) = exp(-2 (r2 / os^2) / s_p^2) * exp(i pi w_p r2 / csh^2),
+ *   r2 = iv^2 + iu^2 (oversampled pixels), s_p = max(support[p], 1),
+ * divided by the complex sum of the taps a visibility at zero offset uses
+ * (k[|j| os][|l| os], |j|, |l| <= s_p, inside the cube), computed in FP64
+ * and rounded once.  w_planes: host array of the P chirp parameters w_p.
+ * d_conv_func_out (device, [P][csh][csh] complex) receives the cube when
+ * not NULL.  The reference reads its kernels from FITS files instead
+ * (utils/read_kernel.c:36-118). */
+GG_API int gg_kernels_generate_f(gg_kernels** out, size_t num_w_planes,
+        const int* support, int oversample, int conv_size_half,
+        const double* w_planes, float* d_conv_func_out, void* stream);
+GG_API int gg_kernels_generate_d(gg_kernels** out, size_t num_w_planes,
+        const int* support, int oversample, int conv_size_half,
+        const double* w_planes, double* d_conv_func_out, void* stream);
 GG_API int gg_kernels_destroy(gg_kernels* k);
 
 /* ---------------------------------------------------------------------- */
