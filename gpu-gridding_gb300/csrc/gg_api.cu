@@ -1073,7 +1073,43 @@ int degrid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   pp.grid_size = grid_size;
   pp.grid_centre = grid_size / 2;
   pp.num_points = num_points;
-  GG_CUDA(launch_degrid<Real>(pp, K->view(), d_grid, d_out, s));
+  if (num_points == 0) return GG_OK;
+  if (num_points > 0xFFFFFFF0ull)
+    return set_error(GG_ERR_UNSUPPORTED,
+                     "num_points = %zu exceeds 2^32-16 per call", num_points);
+  int dev;
+  GG_TRY(current_device(&dev));
+  if (dev != K->device || dev != plan->device)
+    return set_error(GG_ERR_INVALID_ARG,
+                     "plan, kernel stack and current device differ");
+  // Gather order: by 32 x 32-cell block, then w-plane (plan's sort buffers;
+  // geometry kept for a batched replay is discarded).
+  plan->kept.valid = false;
+  const size_t n = num_points;
+  GG_TRY(plan->keys0.ensure(n * 4));
+  GG_TRY(plan->vals0.ensure(n * 4));
+  GG_TRY(plan->keys1.ensure(n * 4));
+  GG_TRY(plan->vals1.ensure(n * 4));
+  GG_TRY(plan->sort_tmp.ensure(radix_temp_bytes(n)));
+  const int blocks_u = (grid_size + 31) / 32;
+  const int block_bits =
+      ceil_log2((unsigned long long)blocks_u * blocks_u + 1);
+  int plane_bits = ceil_log2((unsigned long long)K->num_planes);
+  if (block_bits + plane_bits > 32) plane_bits = 0;
+  const StackView view = K->view();
+  GG_CUDA(launch_degrid_keys<Real>(pp, view, blocks_u, plane_bits,
+                                   plan->keys0.as<uint32_t>(),
+                                   plan->vals0.as<uint32_t>(), s));
+  bool in_alt = false;
+  GG_CUDA(radix_sort_pairs(plan->keys0.as<uint32_t>(),
+                           plan->vals0.as<uint32_t>(),
+                           plan->keys1.as<uint32_t>(),
+                           plan->vals1.as<uint32_t>(), n, 32,
+                           plan->sort_tmp.p, s, &in_alt));
+  GG_CUDA(launch_degrid<Real>(
+      pp, view,
+      in_alt ? plan->vals1.as<uint32_t>() : plan->vals0.as<uint32_t>(),
+      d_grid, d_out, s));
   return GG_OK;
 }
 

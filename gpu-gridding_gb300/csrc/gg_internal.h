@@ -234,8 +234,16 @@ cudaError_t launch_kernel_generate(int num_planes, const int* d_support,
 cudaError_t measure_fp32_fma(int num_sms, double* tflops_best, float* ms_out);
 
 // ---- adjoint (gg_degrid.cu) -----------------------------------------------
+// Sort keys (32 x 32-cell block, then w-plane in plane_bits bits; skipped
+// points last) and identity values of the degridding order.
+template <typename Real>
+cudaError_t launch_degrid_keys(PlaceParams<Real> p, StackView view,
+                               int blocks_u, int plane_bits, uint32_t* keys,
+                               uint32_t* vals, cudaStream_t s);
+// out_vis[order[w]] for every w (one warp each).
 template <typename Real>
 cudaError_t launch_degrid(PlaceParams<Real> p, StackView view,
-                          const Real* grid, Real* out_vis, cudaStream_t s);
+                          const uint32_t* order, const Real* grid,
+                          Real* out_vis, cudaStream_t s);
 
 }  // namespace gg
