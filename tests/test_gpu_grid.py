@@ -316,3 +316,27 @@ def test_nonfinite_kernel_tap_stays_in_its_footprints(pkg, oracle_mod,
     assert np.array_equal(np.isnan(g), np.isnan(gr))
     fin = ~np.isnan(gr)
     assert max_rel(np.where(fin, g, 0), np.where(fin, gr, 0)) <= 1e-5
+
+
+@pytest.mark.parametrize("os_,G,s_min,s_max", [(5, 255, 0, 6), (14, 301, 1, 5),
+                                                (1, 128, 0, 9), (2, 97, 0, 3)])
+def test_unusual_parameters_vs_oracle(pkg, oracle_mod, synthetic, torch, os_,
+                                      G, s_min, s_max):
+    """Odd and extreme oversampling (the column-residue split of the slab
+    stack, offsets up to (os+1)/2), zero supports and odd grid sizes:
+    skips and norm as the reference, FP32 grid within 1e-5 of the FP64
+    oracle, FP64 grid within 1e-12 of the reference _d."""
+    wl = synthetic.random_uniform_workload(
+        f"odd_os{os_}", 6000, G, 7, s_min, s_max, oversample=os_, seed=os_,
+        cell_size_rad=4.0 / (G * 300.0), w_max=400.0, sigma_frac=0.2,
+        clip_frac=0.48)
+    g, ns, nm = pkg.grid_f(wl)
+    g64, ns64, nm64 = oracle_mod.grid_f_fp64acc(wl)
+    _, nsr, nmr = oracle_mod.grid_f(wl)
+    assert ns == ns64 == nsr
+    assert abs(nm - nmr) <= 1e-12 * max(abs(nmr), 1.0)
+    assert max_rel(g, g64) <= 1e-5
+    gd, nsd, nmd = pkg.grid_d(wl)
+    gr, nsdr, nmdr = oracle_mod.grid_d(wl)
+    assert nsd == nsdr
+    assert max_rel(gd, gr) <= 1e-12
