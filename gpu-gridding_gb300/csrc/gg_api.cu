@@ -114,10 +114,16 @@ struct DeviceState {
   // cube's staging copy kept from call to call.
   gg_kernels* host_kernels = nullptr;
   DevBuf host_cube;
-  // Side stream and event that upload a host grid while the call's other
-  // work runs.
+  // Side stream that uploads a host call's visibilities and grid while the
+  // kernel stack is rebuilt (vis_ready, grid_ready mark the two uploads),
+  // and the pinned tile-row spans of the grid cells a call touched
+  // (spans_ready marks their arrival).
   cudaStream_t copy_stream = nullptr;
+  cudaEvent_t vis_ready = nullptr;
   cudaEvent_t grid_ready = nullptr;
+  cudaEvent_t spans_ready = nullptr;
+  uint32_t* h_spans = nullptr;
+  static constexpr int kSpanCap = 2 * (kMaxGridSize / 64 + 2);
 };
 
 std::mutex g_devices_mu;
@@ -430,6 +436,17 @@ struct gg_plan {
   // Event the gridding passes wait for (a grid upload on another stream),
   // or null.
   cudaEvent_t grid_wait = nullptr;
+  // Touched spans (single-grid calls, when h_spans is set): per tile row
+  // tv, the tile columns [lo[tv], hi[tv]) that hold records, lo at
+  // h_spans[0..tiles_v) and hi after it (hi = 0: no records in the row).
+  // spans_written says they were produced for the last call; spans_ready
+  // (when spans_async) is recorded once they have reached h_spans.
+  uint32_t* h_spans = nullptr;
+  int h_spans_cap = 0;
+  cudaEvent_t spans_ready = nullptr;
+  bool spans_written = false, spans_async = false;
+  int spans_tiles_v = 0, spans_tile_u = 0, spans_tile_v = 0;
+  DevBuf spans;
   // Plane groups of the last call (see TileGeom): table, and what it was
   // computed for.
   DevBuf plane_group, group_items;
@@ -779,6 +796,17 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
   plan->kept.shape = shape;
   plan->kept.stage = stage;
   plan->kept.num_tiles = num_tiles;
+  const bool want_spans = plan->h_spans && num_grids == 1 &&
+                          2 * geom.tiles_v <= plan->h_spans_cap;
+  if (want_spans) {
+    plan->spans_tiles_v = geom.tiles_v;
+    plan->spans_tile_u = geom.tile_u;
+    plan->spans_tile_v = geom.tile_v;
+    plan->spans_async = total > 0;
+    plan->spans_written = true;
+    if (total == 0)   // nothing is gridded: no row is touched
+      memset(plan->h_spans + geom.tiles_v, 0, geom.tiles_v * sizeof(uint32_t));
+  }
 
   if (total > 0) {
     GG_TRY(plan->keys0.ensure((size_t)total * 4));
@@ -807,6 +835,21 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
     GG_TRY(plan->tile_start.ensure((size_t)(num_tiles + 1) * 4));
     GG_CUDA(launch_tile_bounds(keys, total, low_bits, num_tiles,
                                plan->tile_start.as<uint32_t>(), s));
+    if (want_spans) {
+      const size_t half = (size_t)geom.tiles_v * sizeof(uint32_t);
+      GG_TRY(plan->spans.ensure(2 * half));
+      GG_CUDA(cudaMemsetAsync(plan->spans.p, 0xFF, half, s));
+      GG_CUDA(cudaMemsetAsync(plan->spans.as<char>() + half, 0, half, s));
+      GG_CUDA(launch_touched_spans(plan->tile_start.as<uint32_t>(), num_tiles,
+                                   geom.tiles_total, geom.tiles_u,
+                                   plan->spans.as<uint32_t>(),
+                                   plan->spans.as<uint32_t>() + geom.tiles_v,
+                                   s));
+      GG_CUDA(cudaMemcpyAsync(plan->h_spans, plan->spans.p, 2 * half,
+                              cudaMemcpyDeviceToHost, s));
+      GG_CUDA(cudaEventRecord(plan->spans_ready, s));
+      plan->stats.num_launches += 1;
+    }
 
     int sms = 0;
     GG_TRY(num_sms_of_current(&sms));
@@ -1133,9 +1176,11 @@ int ensure_copy_stream(DeviceState* st) {
   if (!st->copy_stream)
     GG_CUDA(cudaStreamCreateWithFlags(&st->copy_stream,
                                       cudaStreamNonBlocking));
-  if (!st->grid_ready)
-    GG_CUDA(cudaEventCreateWithFlags(&st->grid_ready,
-                                     cudaEventDisableTiming));
+  for (cudaEvent_t* e : {&st->vis_ready, &st->grid_ready, &st->spans_ready})
+    if (!*e) GG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  if (!st->h_spans)
+    GG_CUDA(cudaMallocHost(&st->h_spans,
+                           DeviceState::kSpanCap * sizeof(uint32_t)));
   return GG_OK;
 }
 
@@ -1178,21 +1223,8 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   gg_plan* plan = st->plan;
   const size_t n = num_points;
   const size_t grid_bytes = (size_t)grid_size * grid_size * 2 * sizeof(Real);
-  // The grid is needed only by the gridding passes: upload it on a side
-  // stream while the kernel stack, placement and sort run.
+  const size_t row_bytes = (size_t)grid_size * 2 * sizeof(Real);
   GG_TRY(plan->in_grid.ensure(grid_bytes));
-  GG_TRY(ensure_copy_stream(st));
-  struct CopyGuard {   // the upload reads the caller's grid: finish it
-    cudaStream_t s;
-    ~CopyGuard() { cudaStreamSynchronize(s); }
-  } copy_guard{st->copy_stream};
-  GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, grid_bytes,
-                          cudaMemcpyHostToDevice, st->copy_stream));
-  GG_CUDA(cudaEventRecord(st->grid_ready, st->copy_stream));
-  gg_kernels* K = nullptr;
-  GG_TRY(host_kernels<Real>(st, num_w_planes, support, oversample,
-                            conv_size_half, conv_func, s, &K));
-
   GG_TRY(plan->in_uu.ensure(n * sizeof(Real) + 16));
   GG_TRY(plan->in_vv.ensure(n * sizeof(Real) + 16));
   GG_TRY(plan->in_ww.ensure(n * sizeof(Real) + 16));
@@ -1201,22 +1233,47 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   GG_TRY(plan->in_misc.ensure(64));
   double* d_norm = plan->in_misc.as<double>();
   unsigned long long* d_skip = (unsigned long long*)(plan->in_misc.as<char>() + 8);
+  GG_TRY(ensure_copy_stream(st));
+  struct CopyGuard {   // the side stream reads the caller's arrays
+    cudaStream_t s;
+    ~CopyGuard() { cudaStreamSynchronize(s); }
+  } copy_guard{st->copy_stream};
+  // Host-to-device copies run one after another in the order they are
+  // issued, so the kernel stack's cube goes first (the stack is rebuilt
+  // from it on the call's stream), then the visibilities and the grid on
+  // the side stream: placement waits for the visibilities only, and the
+  // grid upload runs under the stack rebuild, placement and sort; only the
+  // gridding passes wait for it.
+  gg_kernels* K = nullptr;
+  GG_TRY(host_kernels<Real>(st, num_w_planes, support, oversample,
+                            conv_size_half, conv_func, s, &K));
+  cudaStream_t cs = st->copy_stream;
   if (n) {
     GG_CUDA(cudaMemcpyAsync(plan->in_uu.p, uu, n * sizeof(Real),
-                            cudaMemcpyHostToDevice, s));
+                            cudaMemcpyHostToDevice, cs));
     GG_CUDA(cudaMemcpyAsync(plan->in_vv.p, vv, n * sizeof(Real),
-                            cudaMemcpyHostToDevice, s));
+                            cudaMemcpyHostToDevice, cs));
     GG_CUDA(cudaMemcpyAsync(plan->in_ww.p, ww, n * sizeof(Real),
-                            cudaMemcpyHostToDevice, s));
+                            cudaMemcpyHostToDevice, cs));
     GG_CUDA(cudaMemcpyAsync(plan->in_vis.p, vis, 2 * n * sizeof(Real),
-                            cudaMemcpyHostToDevice, s));
+                            cudaMemcpyHostToDevice, cs));
     GG_CUDA(cudaMemcpyAsync(plan->in_weight.p, weight, n * sizeof(Real),
-                            cudaMemcpyHostToDevice, s));
+                            cudaMemcpyHostToDevice, cs));
   }
+  GG_CUDA(cudaEventRecord(st->vis_ready, cs));
+  if (n)
+    GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, grid_bytes,
+                            cudaMemcpyHostToDevice, cs));
+  GG_CUDA(cudaEventRecord(st->grid_ready, cs));
+  GG_CUDA(cudaStreamWaitEvent(s, st->vis_ready, 0));
   const double norm_in = *norm;
   GG_CUDA(cudaMemcpyAsync(d_norm, &norm_in, sizeof(double),
                           cudaMemcpyHostToDevice, s));
   plan->grid_wait = st->grid_ready;
+  plan->h_spans = st->h_spans;
+  plan->h_spans_cap = DeviceState::kSpanCap;
+  plan->spans_ready = st->spans_ready;
+  plan->spans_written = false;
   const int rc = grid_pipeline<Real>(plan, K, n, plan->in_uu.as<Real>(),
                                      plan->in_vv.as<Real>(),
                                      plan->in_ww.as<Real>(),
@@ -1226,13 +1283,49 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
                                      d_skip, d_norm, plan->in_grid.as<Real>(),
                                      s);
   plan->grid_wait = nullptr;
+  plan->h_spans = nullptr;
+  plan->spans_ready = nullptr;
   GG_TRY(rc);
-  // (A call with nothing to grid never waited for the upload.)
-  GG_CUDA(cudaStreamWaitEvent(s, st->grid_ready, 0));
+  // Copy back only what the call can have changed: cells outside every tile
+  // that holds records were neither read nor written on the device, so the
+  // caller's grid already holds them.  One 2-D copy per run of tile rows
+  // with the same column span; the whole grid when the spans are unknown;
+  // nothing when there were no visibilities.
+  if (n) {
+    GG_CUDA(cudaStreamWaitEvent(s, st->grid_ready, 0));
+    if (plan->spans_written) {
+      if (plan->spans_async) GG_CUDA(cudaEventSynchronize(st->spans_ready));
+      const int tiles_v = plan->spans_tiles_v;
+      const uint32_t* lo = st->h_spans;
+      const uint32_t* hi = st->h_spans + tiles_v;
+      const size_t cell_bytes = 2 * sizeof(Real);
+      for (int tv = 0; tv < tiles_v;) {
+        if (hi[tv] == 0) {
+          ++tv;
+          continue;
+        }
+        int te = tv + 1;
+        while (te < tiles_v && lo[te] == lo[tv] && hi[te] == hi[tv]) ++te;
+        const size_t r0 = (size_t)tv * plan->spans_tile_v;
+        const size_t r1 =
+            std::min((size_t)grid_size, (size_t)te * plan->spans_tile_v);
+        const size_t c0 = (size_t)lo[tv] * plan->spans_tile_u;
+        const size_t c1 =
+            std::min((size_t)grid_size, (size_t)hi[tv] * plan->spans_tile_u);
+        const size_t off = r0 * row_bytes + c0 * cell_bytes;
+        GG_CUDA(cudaMemcpy2DAsync((char*)grid + off, row_bytes,
+                                  plan->in_grid.as<char>() + off, row_bytes,
+                                  (c1 - c0) * cell_bytes, r1 - r0,
+                                  cudaMemcpyDeviceToHost, s));
+        tv = te;
+      }
+    } else {
+      GG_CUDA(cudaMemcpyAsync(grid, plan->in_grid.p, grid_bytes,
+                              cudaMemcpyDeviceToHost, s));
+    }
+  }
   double norm_out = 0.0;
   unsigned long long skip_out = 0;
-  GG_CUDA(cudaMemcpyAsync(grid, plan->in_grid.p, grid_bytes,
-                          cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaMemcpyAsync(&norm_out, d_norm, sizeof(double),
                           cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaMemcpyAsync(&skip_out, d_skip, sizeof(unsigned long long),

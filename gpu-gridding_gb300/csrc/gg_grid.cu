@@ -711,6 +711,19 @@ __global__ void k_tile_bounds(const uint32_t* __restrict__ keys, uint32_t n,
   }
 }
 
+__global__ void k_touched_spans(const uint32_t* __restrict__ tile_start,
+                                int num_tiles, int tiles_total, int tiles_u,
+                                uint32_t* __restrict__ lo,
+                                uint32_t* __restrict__ hi) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < num_tiles;
+       t += gridDim.x * blockDim.x) {
+    if (tile_start[t + 1] == tile_start[t]) continue;
+    const int r = t % tiles_total;
+    atomicMin(&lo[r / tiles_u], (uint32_t)(r % tiles_u));
+    atomicMax(&hi[r / tiles_u], (uint32_t)(r % tiles_u) + 1u);
+  }
+}
+
 // A[t] = chunks of tile t if it is split (more than one chunk), else 0;
 // B[t] = 1 if tile t has exactly one chunk.
 __global__ void k_item_counts(const uint32_t* __restrict__ tile_start,
@@ -821,6 +834,15 @@ cudaError_t launch_tile_bounds(const uint32_t* keys, uint32_t n, int shift,
   const long long work = (long long)n + 1;
   const int blocks = (int)std::min<long long>((work + 255) / 256, 65536);
   k_tile_bounds<<<blocks, 256, 0, s>>>(keys, n, shift, num_tiles, tile_start);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_touched_spans(const uint32_t* tile_start, int num_tiles,
+                                 int tiles_total, int tiles_u, uint32_t* lo,
+                                 uint32_t* hi, cudaStream_t s) {
+  const int blocks = std::max(1, std::min((num_tiles + 255) / 256, 4096));
+  k_touched_spans<<<blocks, 256, 0, s>>>(tile_start, num_tiles, tiles_total,
+                                         tiles_u, lo, hi);
   return cudaGetLastError();
 }
 

@@ -153,6 +153,14 @@ cudaError_t launch_batch_totals(const uint32_t* meta, const double* nterm,
 cudaError_t launch_tile_bounds(const uint32_t* keys, uint32_t n, int shift,
                                int num_tiles, uint32_t* tile_start,
                                cudaStream_t s);
+// Touched spans of a single-grid call: for every virtual tile t holding
+// records (tile_start[t + 1] > tile_start[t]), with real tile r = t mod
+// tiles_total at row r / tiles_u and column r mod tiles_u, lo[row] takes the
+// minimum column and hi[row] the maximum column + 1.  lo must start at
+// 0xFFFFFFFF and hi at 0.
+cudaError_t launch_touched_spans(const uint32_t* tile_start, int num_tiles,
+                                 int tiles_total, int tiles_u, uint32_t* lo,
+                                 uint32_t* hi, cudaStream_t s);
 // Work-item queue of a call.  Tiles are virtual tiles (group * tiles_total
 // + tile, see TileGeom); the queue is group-major, and within a group the
 // chunks of split tiles come first.  group_items[g] .. group_items[g+1] is

@@ -11,6 +11,8 @@ Bars (the tolerances are written in each assertion):
 """
 from __future__ import annotations
 
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -110,7 +112,6 @@ def test_placement_bit_exact_synthetic(pkg, oracle_mod, synthetic, torch,
 
 def _skalow_small(synthetic):
     """SKA-LOW-shaped array at reduced size (64 stations, 60 times)."""
-    import dataclasses
     rng = np.random.Generator(np.random.PCG64(3))
     u, v, w = synthetic.ska_low_uvw_metres(rng, num_stations=64,
                                            num_times=60)
@@ -340,3 +341,62 @@ def test_unusual_parameters_vs_oracle(pkg, oracle_mod, synthetic, torch, os_,
     gr, nsdr, nmdr = oracle_mod.grid_d(wl)
     assert nsd == nsdr
     assert max_rel(gd, gr) <= 1e-12
+
+
+def _start_grid(G, seed):
+    return np.random.default_rng(seed).standard_normal(
+        (G, G, 2)).astype(np.float32)
+
+
+@pytest.mark.parametrize("where", ["disk", "patch_centre", "patch_corner"])
+def test_dropin_copies_back_touched_spans(pkg, oracle_mod, synthetic, torch,
+                                          where):
+    """The host-pointer call copies back only the tile rows' spans that
+    hold records.  With a random starting grid the result must be start +
+    the contributions everywhere, and bit-for-bit the start wherever
+    nothing was added (cells outside every footprint)."""
+    G = 1800
+    if where == "disk":
+        wl = synthetic.random_uniform_workload(
+            "spans_disk", 40_000, G, 32, 2, 12, seed=17, cell_size_rad=3e-5)
+    else:
+        wl = synthetic.random_uniform_workload(
+            "spans_patch", 20_000, G, 32, 2, 12, seed=18, cell_size_rad=3e-5,
+            sigma_frac=0.01, clip_frac=0.03)
+        if where == "patch_corner":   # shift the patch towards a corner
+            extent = 1.0 / wl.cell_size_rad
+            wl = dataclasses.replace(
+                wl, uu=(wl.uu + np.float32(0.4 * extent)).astype(np.float32),
+                vv=(wl.vv - np.float32(0.4 * extent)).astype(np.float32))
+    start = _start_grid(G, 3)
+    g0, ns0, nm0 = pkg.grid_f(wl)
+    g1, ns1, nm1 = pkg.grid_f(wl, start.copy(), 2.0)
+    assert ns1 == ns0 < wl.num_points
+    assert abs(nm1 - (nm0 + 2.0)) <= 1e-12 * abs(nm1)
+    assert max_rel(g1, start + g0) <= 1e-6
+    untouched = g0 == 0
+    assert untouched.any()
+    assert np.array_equal(g1[untouched], start[untouched])
+    gr, nsr, _ = oracle_mod.grid_f(wl)
+    assert ns0 == nsr
+    assert max_rel(g0, gr) <= 1e-5
+
+
+def test_dropin_nothing_gridded_leaves_grid(pkg, synthetic, torch):
+    """Every visibility off the grid (all skipped), and no visibilities at
+    all: the grid comes back bit-for-bit unchanged and the norm as given."""
+    G = 512
+    wl = synthetic.random_uniform_workload("off_grid", 5_000, G, 8, 2, 6,
+                                           seed=5)
+    far = np.float32(10.0 / wl.cell_size_rad)
+    wl = dataclasses.replace(wl, uu=(wl.uu + far).astype(np.float32))
+    start = _start_grid(G, 4)
+    g, ns, nm = pkg.grid_f(wl, start.copy(), 3.5)
+    assert ns == wl.num_points
+    assert nm == 3.5
+    assert np.array_equal(g, start)
+    empty = dataclasses.replace(wl, uu=wl.uu[:0], vv=wl.vv[:0], ww=wl.ww[:0],
+                                vis=wl.vis[:0], weight=wl.weight[:0])
+    g, ns, nm = pkg.grid_f(empty, start.copy(), 1.25)
+    assert ns == 0 and nm == 1.25
+    assert np.array_equal(g, start)
