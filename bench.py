@@ -394,6 +394,9 @@ def run_ours(args):
         tuning = at.autotune(pkg, plan, stack, uu, vv, ww, vis, weight,
                              np.float32(wl.cell_size_rad),
                              np.float32(wl.w_scale), G, cache=tune_cache)
+    # The host-pointer entry points (the e2e leg) grid with the same
+    # settings as the device-pointer plan.
+    pkg.set_host_tuning(plan.tuning())
     grid = torch.zeros((G, G, 2), dtype=torch.float32, device=dev)
     norm = torch.zeros(1, dtype=torch.float64, device=dev)
     nskip = torch.zeros(1, dtype=torch.int64, device=dev)

@@ -38,6 +38,7 @@ EXPORTED_SYMBOLS = (
     "gg_kernels_destroy", "gg_plan_create",
     "gg_plan_destroy", "gg_plan_last_stats", "gg_plan_set_tile_shape",
     "gg_plan_set_slice_staging", "gg_plan_set_tuning", "gg_plan_get_tuning",
+    "gg_host_set_tuning", "gg_host_get_tuning",
     "gg_plan_set_profiling",
     "gg_plan_phase_ms", "gg_measure_fp32_fma_tflops", "gg_grid_wproj_f_device",
     "gg_grid_wproj_f_device_noalloc", "gg_grid_wproj_f_batched_device",
@@ -182,6 +183,10 @@ def _declare(L):
     L.gg_plan_set_tuning.restype = ctypes.c_int
     L.gg_plan_get_tuning.argtypes = [_vp, ctypes.POINTER(Tuning)]
     L.gg_plan_get_tuning.restype = ctypes.c_int
+    L.gg_host_set_tuning.argtypes = [ctypes.POINTER(Tuning)]
+    L.gg_host_set_tuning.restype = ctypes.c_int
+    L.gg_host_get_tuning.argtypes = [ctypes.POINTER(Tuning)]
+    L.gg_host_get_tuning.restype = ctypes.c_int
     L.gg_plan_check.argtypes = [_vp, _vp]
     L.gg_plan_check.restype = ctypes.c_int
     L.gg_plan_set_profiling.argtypes = [_vp, ctypes.c_int]
@@ -449,6 +454,22 @@ def _require_cuda(*tensors):
     for t in tensors:
         if not t.is_cuda or not t.is_contiguous():
             raise TypeError("device entry points take contiguous CUDA tensors")
+
+
+def set_host_tuning(tuning=None) -> None:
+    """Tuning of the host-pointer entry points on the current device (a
+    Tuning or a dict of its fields; None restores the defaults)."""
+    if tuning is None:
+        _check(lib().gg_host_set_tuning(None))
+        return
+    t = tuning if isinstance(tuning, Tuning) else Tuning.from_dict(tuning)
+    _check(lib().gg_host_set_tuning(ctypes.byref(t)))
+
+
+def host_tuning() -> dict:
+    t = Tuning()
+    _check(lib().gg_host_get_tuning(ctypes.byref(t)))
+    return t.as_dict()
 
 
 def grid_wproj_device(plan, stack, uu, vv, ww, vis, weight, cell_size_rad,

@@ -205,6 +205,14 @@ typedef struct
 GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* tuning);
 GG_API int gg_plan_get_tuning(const gg_plan* plan, gg_tuning* tuning);
 
+/* Tuning of the host-pointer entry points (oskar_grid_wproj_f/_d and
+ * gg_grid_wproj_f/_d) on the current device: they keep one workspace plan
+ * per device, and this sets its gg_tuning (NULL restores the defaults).
+ * An integrator sets it once, e.g. from an autotuned plan for the
+ * production grid; results are the same under every tuning. */
+GG_API int gg_host_set_tuning(const gg_tuning* tuning);
+GG_API int gg_host_get_tuning(gg_tuning* tuning);
+
 /* Phase timing.  With profiling enabled, every gridding call made with the
  * plan records CUDA events on its stream around five phases:
  *   0 placement (placement, skip/norm reduction, record offsets)

@@ -123,3 +123,26 @@ def test_plane_groups_deterministic(pkg, torch, wl):
     b = _grid(pkg, torch, wl, plan, stack)
     assert plan.stats()["num_plane_groups"] > 1
     assert np.array_equal(a[0].view(np.uint32), b[0].view(np.uint32))
+
+
+def test_host_tuning_applies_to_dropin(pkg, torch, wl, fp64):
+    """The host-pointer entry points take a tuning like a plan does: the
+    getter returns it, results stay within the bars, and None restores the
+    defaults."""
+    default = pkg.host_tuning()
+    tuned = {"tile_u": 16, "slice_staging": 0, "items_per_cta": 8,
+             "sort_detail": 1, "ctas_per_sm": 0, "plane_group_mb": 1}
+    try:
+        pkg.set_host_tuning(tuned)
+        assert pkg.host_tuning() == tuned
+        g, ns, nm = pkg.grid_f(wl)
+        assert ns == fp64[1]
+        assert max_rel(g, fp64[0]) <= 1e-5
+        with pytest.raises(pkg.GridError):
+            pkg.set_host_tuning({"items_per_cta": 0})
+        assert pkg.host_tuning() == tuned
+    finally:
+        pkg.set_host_tuning(None)
+    assert pkg.host_tuning() == default
+    g2, ns2, nm2 = pkg.grid_f(wl)
+    assert ns2 == ns and nm2 == nm
