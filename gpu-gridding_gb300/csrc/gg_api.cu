@@ -23,39 +23,6 @@
 #include <vector>
 
 #include "gg_internal.h"
-
-#include <chrono>
-#include <cstdlib>
-struct DTrace {
-  bool on = getenv("GG_TRACE_DROPIN") != nullptr;
-  cudaEvent_t ev[48];
-  const char* name[48];
-  int n = 0;
-  std::chrono::steady_clock::time_point h0 = std::chrono::steady_clock::now();
-  double hts[48]; const char* hname[48]; int hn = 0;
-  void rec(const char* nm, cudaStream_t s) {
-    if (!on || n >= 48) return;
-    cudaEventCreate(&ev[n]);
-    cudaEventRecord(ev[n], s);
-    name[n++] = nm;
-  }
-  void host(const char* nm) {
-    if (!on || hn >= 48) return;
-    hts[hn] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count();
-    hname[hn++] = nm;
-  }
-  ~DTrace() {
-    if (!on) return;
-    cudaDeviceSynchronize();
-    for (int i = 0; i < n; ++i) {
-      float ms = 0; cudaEventElapsedTime(&ms, ev[0], ev[i]);
-      fprintf(stderr, "TRACE dev %-24s %8.3f\n", name[i], ms);
-    }
-    for (int i = 0; i < n; ++i) cudaEventDestroy(ev[i]);
-    for (int i = 0; i < hn; ++i) fprintf(stderr, "TRACE host %-24s %8.3f\n", hname[i], hts[i]);
-  }
-};
-thread_local DTrace* g_tr = nullptr;
 #include "../../include/gpugrid.h"
 
 using namespace gg;
@@ -771,9 +738,7 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
                           cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaMemcpyAsync((char*)plan->h_scalars + 32, scalar64(plan, kMacs),
                           8, cudaMemcpyDeviceToHost, s));
-  if (g_tr) { g_tr->rec("placed", s); g_tr->host("pre-sync"); }
   GG_CUDA(cudaStreamSynchronize(s));
-  if (g_tr) g_tr->host("post-sync");
   return bin_and_grid<Real>(plan, K, n, po, grid_size, 1, nullptr, d_grid, 0,
                             s);
 }
@@ -926,9 +891,7 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
                                total, chunk, ib, s));
     plan->kept.rec_vis = vals;
     plan->kept.num_ctas = num_ctas;
-    if (g_tr) g_tr->rec("items built", s);
     if (plan->grid_wait) GG_CUDA(cudaStreamWaitEvent(s, plan->grid_wait, 0));
-    if (g_tr) g_tr->rec("grid wait done", s);
     plan->mark(3, s);
     GG_CUDA(launch_grid_tiles<Real>(
         ib.items, ib.group_items, ib.counter, sc + kDeviceError, vals, po.cell,
@@ -1271,11 +1234,6 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   double* d_norm = plan->in_misc.as<double>();
   unsigned long long* d_skip = (unsigned long long*)(plan->in_misc.as<char>() + 8);
   GG_TRY(ensure_copy_stream(st));
-  DTrace tr;
-  g_tr = &tr;
-  struct TrReset { ~TrReset() { g_tr = nullptr; } } tr_reset;
-  tr.rec("start", s);
-  tr.host("start");
   struct CopyGuard {   // the side stream reads the caller's arrays
     cudaStream_t s;
     ~CopyGuard() { cudaStreamSynchronize(s); }
@@ -1289,8 +1247,6 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   gg_kernels* K = nullptr;
   GG_TRY(host_kernels<Real>(st, num_w_planes, support, oversample,
                             conv_size_half, conv_func, s, &K));
-  tr.rec("stack built", s);
-  tr.host("stack enqueued");
   cudaStream_t cs = st->copy_stream;
   if (n) {
     GG_CUDA(cudaMemcpyAsync(plan->in_uu.p, uu, n * sizeof(Real),
@@ -1305,12 +1261,10 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
                             cudaMemcpyHostToDevice, cs));
   }
   GG_CUDA(cudaEventRecord(st->vis_ready, cs));
-  tr.rec("vis up", cs);
   if (n)
     GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, grid_bytes,
                             cudaMemcpyHostToDevice, cs));
   GG_CUDA(cudaEventRecord(st->grid_ready, cs));
-  tr.rec("grid up", cs);
   GG_CUDA(cudaStreamWaitEvent(s, st->vis_ready, 0));
   const double norm_in = *norm;
   GG_CUDA(cudaMemcpyAsync(d_norm, &norm_in, sizeof(double),
@@ -1328,8 +1282,6 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
                                      cell_size_rad, w_scale, grid_size,
                                      d_skip, d_norm, plan->in_grid.as<Real>(),
                                      s);
-  tr.rec("grid end", s);
-  tr.host("grid enqueued");
   plan->grid_wait = nullptr;
   plan->h_spans = nullptr;
   plan->spans_ready = nullptr;
@@ -1343,7 +1295,6 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
     GG_CUDA(cudaStreamWaitEvent(s, st->grid_ready, 0));
     if (plan->spans_written) {
       if (plan->spans_async) GG_CUDA(cudaEventSynchronize(st->spans_ready));
-      tr.host("spans read");
       const int tiles_v = plan->spans_tiles_v;
       const uint32_t* lo = st->h_spans;
       const uint32_t* hi = st->h_spans + tiles_v;
@@ -1373,8 +1324,6 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
                               cudaMemcpyDeviceToHost, s));
     }
   }
-  tr.rec("d2h end", s);
-  tr.host("d2h enqueued");
   double norm_out = 0.0;
   unsigned long long skip_out = 0;
   GG_CUDA(cudaMemcpyAsync(&norm_out, d_norm, sizeof(double),
@@ -1382,7 +1331,6 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   GG_CUDA(cudaMemcpyAsync(&skip_out, d_skip, sizeof(unsigned long long),
                           cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaStreamSynchronize(s));
-  tr.host("synced");
   GG_TRY(check_device_error(plan, s));
   *norm = norm_out;
   *num_skipped = (size_t)skip_out;
