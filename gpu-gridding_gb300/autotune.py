@@ -33,7 +33,7 @@ from typing import Callable, Dict, Iterable, Optional
 import numpy as np
 
 CACHE_ENV = "GPUGRID_TUNE_CACHE"
-CACHE_VERSION = 2
+CACHE_VERSION = 3
 
 #: The plan's settings before any tuning (each call chooses shape/staging).
 DEFAULT_TUNING = {"tile_u": 0, "slice_staging": -1, "items_per_cta": 4,
@@ -46,7 +46,8 @@ SEARCH_SPACE = (
     (("items_per_cta",), [(2,), (4,), (8,), (16,)]),
     (("sort_detail",), [(2,), (1,), (0,)]),
     (("ctas_per_sm",), [(0,), (1,)]),
-    (("plane_group_mb",), [(0,), (16,), (64,), (1 << 20,)]),
+    (("plane_group_mb",), [(0,), (16,), (32,), (48,), (64,), (96,),
+                           (1 << 20,)]),
 )
 
 
