@@ -461,6 +461,8 @@ struct gg_plan {
   // Batched calls: per-visibility norm terms, chunk table, chunk totals,
   // per-grid visibility offsets.
   DevBuf nterm, chunk_begin, grid_chunk0, chunk_part, grid_offsets;
+  // Degridding: partial result of every record, at its emission slot.
+  DevBuf rec_out;
   // Staging of the host-pointer entry points.
   DevBuf in_uu, in_vv, in_ww, in_vis, in_weight, in_grid, in_misc;
   // Geometry kept by the last batched call for replays on new amplitudes:
@@ -499,6 +501,8 @@ enum Scalar {
   kDeviceError,   // set by a kernel whose bounded wait ran out; sticky
   kScalarCount
 };
+// Tile shape of the degridding kernel (32 x 64 cells).
+constexpr int kDegridShape = 0;
 // 64-bit device scalars live after the 32-bit ones.
 constexpr size_t kScalar64Offset = 64;
 enum Scalar64 { kMacs = 0, kSkipScratch, kScalar64Count };
@@ -629,6 +633,11 @@ int max_tiles(int grid_size, int num_grids) {
 }
 
 template <typename Real>
+int place_and_count(gg_plan* plan, const gg_kernels* K,
+                    const PlaceParams<Real>& pp, int forced_shape,
+                    double* d_norm, unsigned long long* d_num_skipped,
+                    cudaStream_t s, PlaceOut* po_out);
+template <typename Real>
 int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
                  const PlaceOut& po, int grid_size, int num_grids,
                  const unsigned long long* d_grid_offsets, Real* d_grid,
@@ -682,22 +691,7 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   plan->events_valid = false;
   plan->kept.valid = false;
 
-  const StackView view = K->view();
-  const int tiles_cap = max_tiles(grid_size, 1);
-
   const size_t n = num_points;
-  const int nblk = place_num_blocks(n);
-  GG_TRY(plan->cell.ensure(n * 4 + 4));
-  GG_TRY(plan->meta.ensure(n * 4 + 4));
-  GG_TRY(plan->vw.ensure(n * sizeof(R2) + sizeof(R2)));
-  GG_TRY(plan->rec_count.ensure(n * 4 + 4));
-  GG_TRY(plan->rec_offset.ensure(n * 4 + 4));
-  GG_TRY(plan->blk_norm.ensure(nblk * sizeof(double)));
-  GG_TRY(plan->blk_skip.ensure(nblk * 8));
-  GG_TRY(plan->blk_macs.ensure(nblk * 8));
-  GG_TRY(plan->scan_tmp.ensure(scan_temp_bytes(std::max<size_t>(n, tiles_cap))));
-
-  uint32_t* sc = plan->scalars.as<uint32_t>();
   PlaceParams<Real> pp;
   pp.uu = uu; pp.vv = vv; pp.ww = ww; pp.vis = vis; pp.weight = weight;
   // oskar_grid_wproj.c:148 (and :59): grid_scale = grid_size * cell_size
@@ -712,19 +706,51 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
     GG_CUDA(cudaMemsetAsync(d_num_skipped, 0, sizeof(unsigned long long), s));
     return GG_OK;
   }
+  PlaceOut po;
+  GG_TRY(place_and_count<Real>(plan, K, pp, plan->forced_shape, d_norm,
+                               d_num_skipped, s, &po));
+  return bin_and_grid<Real>(plan, K, n, po, grid_size, 1, nullptr, d_grid, 0,
+                            s);
+}
+
+// The first half of a single-grid call, shared by gridding and degridding:
+// placement (skip count, norm and MAC totals), records per visibility and
+// their offsets, then the call's one host synchronisation (the record total
+// sizes the sort buffers and the tile shape picks the kernel).  pp.vis and
+// pp.weight are null for degridding, which places coordinates only.
+template <typename Real>
+int place_and_count(gg_plan* plan, const gg_kernels* K,
+                    const PlaceParams<Real>& pp, int forced_shape,
+                    double* d_norm, unsigned long long* d_num_skipped,
+                    cudaStream_t s, PlaceOut* po_out) {
+  using R2 = typename Vec2<Real>::type;
+  const StackView view = K->view();
+  const size_t n = pp.num_points;
+  const int tiles_cap = max_tiles(pp.grid_size, 1);
+  const int nblk = place_num_blocks(n);
+  GG_TRY(plan->cell.ensure(n * 4 + 4));
+  GG_TRY(plan->meta.ensure(n * 4 + 4));
+  if (pp.vis) GG_TRY(plan->vw.ensure(n * sizeof(R2) + sizeof(R2)));
+  GG_TRY(plan->rec_count.ensure(n * 4 + 4));
+  GG_TRY(plan->rec_offset.ensure(n * 4 + 4));
+  GG_TRY(plan->blk_norm.ensure(nblk * sizeof(double)));
+  GG_TRY(plan->blk_skip.ensure(nblk * 8));
+  GG_TRY(plan->blk_macs.ensure(nblk * 8));
+  GG_TRY(plan->scan_tmp.ensure(scan_temp_bytes(std::max<size_t>(n, tiles_cap))));
+  uint32_t* sc = plan->scalars.as<uint32_t>();
 
   plan->mark(0, s);
   PlaceOut po;
   po.cell = plan->cell.as<uint32_t>();
   po.meta = plan->meta.as<uint32_t>();
-  po.vw = plan->vw.p;
+  po.vw = pp.vis ? plan->vw.p : nullptr;
   po.rec_count = plan->rec_count.as<uint32_t>();
   po.blk_norm = plan->blk_norm.as<double>();
   po.blk_skip = plan->blk_skip.as<unsigned long long>();
   po.blk_macs = plan->blk_macs.as<unsigned long long>();
   GG_CUDA(launch_place<Real>(pp, view, TileGeom{}, 0, 0, po, s));
   GG_CUDA(launch_place_finalize(po.blk_norm, po.blk_skip, po.blk_macs, nblk,
-                                n, plan->forced_shape, d_norm, d_num_skipped,
+                                n, forced_shape, d_norm, d_num_skipped,
                                 scalar64(plan, kMacs), sc + kShape, s));
   GG_CUDA(launch_count_records(po.cell, po.meta, n, view, sc + kShape,
                                po.rec_count, s));
@@ -732,29 +758,37 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
                              sc + kTotalRecords, plan->scan_tmp.p, s));
   plan->stats.num_launches = 6;  // place, finalize, count, 3-kernel scan
   plan->mark(1, s);
-  // The one host synchronisation: the record total sizes the sort buffers
-  // and the tile shape picks the kernel.
   GG_CUDA(cudaMemcpyAsync(plan->h_scalars, sc, 4 * kScalarCount,
                           cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaMemcpyAsync((char*)plan->h_scalars + 32, scalar64(plan, kMacs),
                           8, cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaStreamSynchronize(s));
-  return bin_and_grid<Real>(plan, K, n, po, grid_size, 1, nullptr, d_grid, 0,
-                            s);
+  *po_out = po;
+  return GG_OK;
 }
 
-// The second half of a gridding call, after the host has read back the
-// record total and the tile shape: record emission, sort, work items, the
-// tile-gridding kernel and the partial reduction.  Batched calls pass the
-// device array of per-grid visibility offsets and the stride between grids.
+// Records binned by tile (bin_records): the sorted (key, visibility)
+// pairs, the tile geometry and each virtual tile's record range
+// (plan->tile_start).
+struct Bins {
+  uint32_t total = 0;
+  int shape = 0;
+  bool stage = false;
+  int num_groups = 1, num_tiles = 0;
+  TileGeom geom{};
+  const uint32_t* keys = nullptr;
+  const uint32_t* vals = nullptr;
+};
+
+// After the host has read back the record total and the tile shape: plane
+// groups, tile geometry, record emission, the sort and the tile bounds.
+// Batched calls pass the device array of per-grid visibility offsets.
 template <typename Real>
-int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
-                 const PlaceOut& po, int grid_size, int num_grids,
-                 const unsigned long long* d_grid_offsets, Real* d_grid,
-                 long long grid_stride, cudaStream_t s) {
-  using R2 = typename Vec2<Real>::type;
+int bin_records(gg_plan* plan, const gg_kernels* K, size_t n,
+                const PlaceOut& po, int grid_size, int num_grids,
+                const unsigned long long* d_grid_offsets, cudaStream_t s,
+                Bins* b) {
   const StackView view = K->view();
-  uint32_t* sc = plan->scalars.as<uint32_t>();
   if (plan->h_scalars[kDeviceError])
     return set_error(GG_ERR_CUDA,
                      "an earlier call with this plan had a gridding kernel "
@@ -796,115 +830,152 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
   plan->kept.shape = shape;
   plan->kept.stage = stage;
   plan->kept.num_tiles = num_tiles;
+  b->total = total;
+  b->shape = shape;
+  b->stage = stage;
+  b->num_groups = num_groups;
+  b->num_tiles = num_tiles;
+  b->geom = geom;
+  if (total == 0) return GG_OK;
+
+  GG_TRY(plan->keys0.ensure((size_t)total * 4));
+  GG_TRY(plan->vals0.ensure((size_t)total * 4));
+  GG_TRY(plan->keys1.ensure((size_t)total * 4));
+  GG_TRY(plan->vals1.ensure((size_t)total * 4));
+  GG_TRY(plan->sort_tmp.ensure(radix_temp_bytes(total)));
+  GG_CUDA(launch_emit_records(po.cell, po.meta,
+                              plan->rec_offset.as<uint32_t>(), n, view, geom,
+                              0, 0, plan->keys0.as<uint32_t>(),
+                              plan->vals0.as<uint32_t>(), s, d_grid_offsets,
+                              num_grids));
+  bool in_alt = false;
+  GG_CUDA(radix_sort_pairs(plan->keys0.as<uint32_t>(),
+                           plan->vals0.as<uint32_t>(),
+                           plan->keys1.as<uint32_t>(),
+                           plan->vals1.as<uint32_t>(), total, key_bits,
+                           plan->sort_tmp.p, s, &in_alt));
+  b->keys = in_alt ? plan->keys1.as<uint32_t>() : plan->keys0.as<uint32_t>();
+  b->vals = in_alt ? plan->vals1.as<uint32_t>() : plan->vals0.as<uint32_t>();
+  plan->stats.num_launches += 1 + 5 * (unsigned)((key_bits + 7) / 8);
+  plan->mark(2, s);
+
+  GG_TRY(plan->tile_start.ensure((size_t)(num_tiles + 1) * 4));
+  GG_CUDA(launch_tile_bounds(b->keys, total, low_bits, num_tiles,
+                             plan->tile_start.as<uint32_t>(), s));
+  plan->stats.num_launches += 1;
+  return GG_OK;
+}
+
+// The work-item queue of binned records for num_ctas persistent CTAs: heavy
+// tiles are split into items of `chunk` records so that the call has about
+// items_per_cta items per CTA.  Items: at most one more per tile than
+// total / chunk; partial-tile slots (split tiles only): at most
+// 2 * total / chunk, each a tile of partial sums when partial_tiles is set
+// (gridding; the degridder's items write no tile).
+template <typename Real>
+int build_work_items(gg_plan* plan, const Bins& b, int num_ctas,
+                     bool partial_tiles, cudaStream_t s, ItemBuffers* ib) {
+  using R2 = typename Vec2<Real>::type;
+  uint32_t* sc = plan->scalars.as<uint32_t>();
+  const int num_tiles = b.num_tiles;
+  const unsigned long long f = (unsigned long long)plan->items_per_cta;
+  const uint32_t chunk = (uint32_t)std::max<unsigned long long>(
+      64, ((unsigned long long)b.total + f * num_ctas - 1) / (f * num_ctas));
+  const size_t item_cap = (size_t)num_tiles + 2 * f * (size_t)num_ctas + 16;
+  const size_t slot_cap = 2 * f * (size_t)num_ctas + 16;
+  plan->stats.num_ctas = num_ctas;
+  plan->stats.chunk_records = chunk;
+  GG_TRY(plan->item_a.ensure((size_t)num_tiles * 4 + 4));
+  GG_TRY(plan->item_b.ensure((size_t)num_tiles * 4 + 4));
+  GG_TRY(plan->items.ensure(item_cap * sizeof(WorkItem)));
+  GG_TRY(plan->split_tiles.ensure((size_t)num_tiles * sizeof(int4) + 16));
+  if (partial_tiles)
+    GG_TRY(plan->partials.ensure(slot_cap * b.geom.tile_u * b.geom.tile_v *
+                                 sizeof(R2)));
+  GG_TRY(plan->group_items.ensure((size_t)(b.num_groups + 1) * 4));
+  ib->chunks = plan->item_a.as<uint32_t>();
+  ib->split_chunks = plan->item_b.as<uint32_t>();
+  ib->group_items = plan->group_items.as<uint32_t>();
+  ib->num_groups = b.num_groups;
+  ib->num_items = sc + kNumItems;
+  ib->num_slots = sc + kNumSlots;
+  ib->items = plan->items.as<WorkItem>();
+  ib->split_tiles = plan->split_tiles.as<int4>();
+  ib->num_split = sc + kNumSplit;
+  ib->counter = sc + kCounter;
+  ib->scan_tmp = plan->scan_tmp.p;
+  GG_CUDA(launch_build_items(plan->tile_start.as<uint32_t>(), num_tiles,
+                             b.total, chunk, *ib, s));
+  // item counts, 2 scans, item emit
+  plan->stats.num_launches += 1 + 6 + 1;
+  return GG_OK;
+}
+
+// The second half of a gridding call: binning, work items, the
+// tile-gridding kernel and the partial reductions.  Batched calls pass the
+// device array of per-grid visibility offsets and the stride between grids.
+template <typename Real>
+int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
+                 const PlaceOut& po, int grid_size, int num_grids,
+                 const unsigned long long* d_grid_offsets, Real* d_grid,
+                 long long grid_stride, cudaStream_t s) {
+  const StackView view = K->view();
+  uint32_t* sc = plan->scalars.as<uint32_t>();
+  Bins b;
+  GG_TRY(bin_records<Real>(plan, K, n, po, grid_size, num_grids,
+                           d_grid_offsets, s, &b));
+  const TileGeom& geom = b.geom;
   const bool want_spans = plan->h_spans && num_grids == 1 &&
                           2 * geom.tiles_v <= plan->h_spans_cap;
   if (want_spans) {
     plan->spans_tiles_v = geom.tiles_v;
     plan->spans_tile_u = geom.tile_u;
     plan->spans_tile_v = geom.tile_v;
-    plan->spans_async = total > 0;
+    plan->spans_async = b.total > 0;
     plan->spans_written = true;
-    if (total == 0)   // nothing is gridded: no row is touched
+    if (b.total == 0)   // nothing is gridded: no row is touched
       memset(plan->h_spans + geom.tiles_v, 0, geom.tiles_v * sizeof(uint32_t));
   }
+  if (b.total == 0) return GG_OK;
 
-  if (total > 0) {
-    GG_TRY(plan->keys0.ensure((size_t)total * 4));
-    GG_TRY(plan->vals0.ensure((size_t)total * 4));
-    GG_TRY(plan->keys1.ensure((size_t)total * 4));
-    GG_TRY(plan->vals1.ensure((size_t)total * 4));
-    GG_TRY(plan->sort_tmp.ensure(radix_temp_bytes(total)));
-    GG_CUDA(launch_emit_records(po.cell, po.meta,
-                                plan->rec_offset.as<uint32_t>(), n, view, geom,
-                                0, 0, plan->keys0.as<uint32_t>(),
-                                plan->vals0.as<uint32_t>(), s, d_grid_offsets,
-                                num_grids));
-    bool in_alt = false;
-    GG_CUDA(radix_sort_pairs(plan->keys0.as<uint32_t>(),
-                             plan->vals0.as<uint32_t>(),
-                             plan->keys1.as<uint32_t>(),
-                             plan->vals1.as<uint32_t>(), total, key_bits,
-                             plan->sort_tmp.p, s, &in_alt));
-    const uint32_t* keys = in_alt ? plan->keys1.as<uint32_t>()
-                                  : plan->keys0.as<uint32_t>();
-    const uint32_t* vals = in_alt ? plan->vals1.as<uint32_t>()
-                                  : plan->vals0.as<uint32_t>();
-    plan->stats.num_launches += 1 + 5 * (unsigned)((key_bits + 7) / 8);
-    plan->mark(2, s);
-
-    GG_TRY(plan->tile_start.ensure((size_t)(num_tiles + 1) * 4));
-    GG_CUDA(launch_tile_bounds(keys, total, low_bits, num_tiles,
-                               plan->tile_start.as<uint32_t>(), s));
-    if (want_spans) {
-      const size_t half = (size_t)geom.tiles_v * sizeof(uint32_t);
-      GG_TRY(plan->spans.ensure(2 * half));
-      GG_CUDA(cudaMemsetAsync(plan->spans.p, 0xFF, half, s));
-      GG_CUDA(cudaMemsetAsync(plan->spans.as<char>() + half, 0, half, s));
-      GG_CUDA(launch_touched_spans(plan->tile_start.as<uint32_t>(), num_tiles,
-                                   geom.tiles_total, geom.tiles_u,
-                                   plan->spans.as<uint32_t>(),
-                                   plan->spans.as<uint32_t>() + geom.tiles_v,
-                                   s));
-      GG_CUDA(cudaMemcpyAsync(plan->h_spans, plan->spans.p, 2 * half,
-                              cudaMemcpyDeviceToHost, s));
-      GG_CUDA(cudaEventRecord(plan->spans_ready, s));
-      plan->stats.num_launches += 1;
-    }
-
-    int sms = 0;
-    GG_TRY(num_sms_of_current(&sms));
-    int per_sm = grid_tiles_ctas_per_sm<Real>(geom.tile_u, stage);
-    if (plan->ctas_per_sm > 0) per_sm = std::min(per_sm, plan->ctas_per_sm);
-    const int num_ctas = sms * per_sm;
-    // Heavy tiles are split into work items of `chunk` records so that the
-    // call has about items_per_cta items per CTA.  Items: at most one more
-    // per tile than total / chunk; partial-tile slots (split tiles only):
-    // at most 2 * total / chunk.
-    const unsigned long long f = (unsigned long long)plan->items_per_cta;
-    const uint32_t chunk = (uint32_t)std::max<unsigned long long>(
-        64, ((unsigned long long)total + f * num_ctas - 1) / (f * num_ctas));
-    const size_t item_cap = (size_t)num_tiles + 2 * f * (size_t)num_ctas + 16;
-    const size_t slot_cap = 2 * f * (size_t)num_ctas + 16;
-    plan->stats.slice_staging = stage ? 1 : 0;
-    plan->stats.num_ctas = num_ctas;
-    plan->stats.chunk_records = chunk;
-    GG_TRY(plan->item_a.ensure((size_t)num_tiles * 4 + 4));
-    GG_TRY(plan->item_b.ensure((size_t)num_tiles * 4 + 4));
-    GG_TRY(plan->items.ensure(item_cap * sizeof(WorkItem)));
-    GG_TRY(plan->split_tiles.ensure((size_t)num_tiles * sizeof(int4) + 16));
-    GG_TRY(plan->partials.ensure(slot_cap * geom.tile_u * geom.tile_v *
-                                 sizeof(R2)));
-    GG_TRY(plan->group_items.ensure((size_t)(num_groups + 1) * 4));
-    ItemBuffers ib;
-    ib.chunks = plan->item_a.as<uint32_t>();
-    ib.split_chunks = plan->item_b.as<uint32_t>();
-    ib.group_items = plan->group_items.as<uint32_t>();
-    ib.num_groups = num_groups;
-    ib.num_items = sc + kNumItems;
-    ib.num_slots = sc + kNumSlots;
-    ib.items = plan->items.as<WorkItem>();
-    ib.split_tiles = plan->split_tiles.as<int4>();
-    ib.num_split = sc + kNumSplit;
-    ib.counter = sc + kCounter;
-    ib.scan_tmp = plan->scan_tmp.p;
-    GG_CUDA(launch_build_items(plan->tile_start.as<uint32_t>(), num_tiles,
-                               total, chunk, ib, s));
-    plan->kept.rec_vis = vals;
-    plan->kept.num_ctas = num_ctas;
-    if (plan->grid_wait) GG_CUDA(cudaStreamWaitEvent(s, plan->grid_wait, 0));
-    plan->mark(3, s);
-    GG_CUDA(launch_grid_tiles<Real>(
-        ib.items, ib.group_items, ib.counter, sc + kDeviceError, vals, po.cell,
-        po.meta, po.vw, view, geom, grid_size, d_grid, grid_stride,
-        plan->partials.as<Real>(), ib.split_tiles, ib.num_split, num_tiles,
-        num_ctas, stage, s));
-    plan->mark(4, s);
-    plan->mark(5, s);
-    // tile bounds, item counts, 2 scans, item emit, then per plane group
-    // the gridding pass and its partial reduction
-    plan->stats.num_launches += 1 + 1 + 6 + 1 + 2 * num_groups;
-    plan->events_valid = plan->profile;
+  if (want_spans) {
+    const size_t half = (size_t)geom.tiles_v * sizeof(uint32_t);
+    GG_TRY(plan->spans.ensure(2 * half));
+    GG_CUDA(cudaMemsetAsync(plan->spans.p, 0xFF, half, s));
+    GG_CUDA(cudaMemsetAsync(plan->spans.as<char>() + half, 0, half, s));
+    GG_CUDA(launch_touched_spans(plan->tile_start.as<uint32_t>(), b.num_tiles,
+                                 geom.tiles_total, geom.tiles_u,
+                                 plan->spans.as<uint32_t>(),
+                                 plan->spans.as<uint32_t>() + geom.tiles_v,
+                                 s));
+    GG_CUDA(cudaMemcpyAsync(plan->h_spans, plan->spans.p, 2 * half,
+                            cudaMemcpyDeviceToHost, s));
+    GG_CUDA(cudaEventRecord(plan->spans_ready, s));
+    plan->stats.num_launches += 1;
   }
+
+  int sms = 0;
+  GG_TRY(num_sms_of_current(&sms));
+  int per_sm = grid_tiles_ctas_per_sm<Real>(geom.tile_u, b.stage);
+  if (plan->ctas_per_sm > 0) per_sm = std::min(per_sm, plan->ctas_per_sm);
+  const int num_ctas = sms * per_sm;
+  plan->stats.slice_staging = b.stage ? 1 : 0;
+  ItemBuffers ib;
+  GG_TRY(build_work_items<Real>(plan, b, num_ctas, true, s, &ib));
+  plan->kept.rec_vis = b.vals;
+  plan->kept.num_ctas = num_ctas;
+  if (plan->grid_wait) GG_CUDA(cudaStreamWaitEvent(s, plan->grid_wait, 0));
+  plan->mark(3, s);
+  GG_CUDA(launch_grid_tiles<Real>(
+      ib.items, ib.group_items, ib.counter, sc + kDeviceError, b.vals,
+      po.cell, po.meta, po.vw, view, geom, grid_size, d_grid, grid_stride,
+      plan->partials.as<Real>(), ib.split_tiles, ib.num_split, b.num_tiles,
+      num_ctas, b.stage, s));
+  plan->mark(4, s);
+  plan->mark(5, s);
+  // per plane group the gridding pass and its partial reduction
+  plan->stats.num_launches += 2 * b.num_groups;
+  plan->events_valid = plan->profile;
   return GG_OK;
 }
 
@@ -1125,34 +1196,45 @@ int degrid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   if (dev != K->device || dev != plan->device)
     return set_error(GG_ERR_INVALID_ARG,
                      "plan, kernel stack and current device differ");
-  // Gather order: by 32 x 32-cell block, then w-plane (plan's sort buffers;
-  // geometry kept for a batched replay is discarded).
+  // The gridder's placement, records and work items (32 x 64-cell tiles;
+  // geometry kept for a batched replay is discarded), then the tile
+  // kernel and the per-visibility sums.
+  plan->stats = gg_stats{};
+  plan->stats.num_points = num_points;
+  plan->events_valid = false;
   plan->kept.valid = false;
   const size_t n = num_points;
-  GG_TRY(plan->keys0.ensure(n * 4));
-  GG_TRY(plan->vals0.ensure(n * 4));
-  GG_TRY(plan->keys1.ensure(n * 4));
-  GG_TRY(plan->vals1.ensure(n * 4));
-  GG_TRY(plan->sort_tmp.ensure(radix_temp_bytes(n)));
-  const int blocks_u = (grid_size + 31) / 32;
-  const int block_bits =
-      ceil_log2((unsigned long long)blocks_u * blocks_u + 1);
-  int plane_bits = ceil_log2((unsigned long long)K->num_planes);
-  if (block_bits + plane_bits > 32) plane_bits = 0;
   const StackView view = K->view();
-  GG_CUDA(launch_degrid_keys<Real>(pp, view, blocks_u, plane_bits,
-                                   plan->keys0.as<uint32_t>(),
-                                   plan->vals0.as<uint32_t>(), s));
-  bool in_alt = false;
-  GG_CUDA(radix_sort_pairs(plan->keys0.as<uint32_t>(),
-                           plan->vals0.as<uint32_t>(),
-                           plan->keys1.as<uint32_t>(),
-                           plan->vals1.as<uint32_t>(), n, 32,
-                           plan->sort_tmp.p, s, &in_alt));
-  GG_CUDA(launch_degrid<Real>(
-      pp, view,
-      in_alt ? plan->vals1.as<uint32_t>() : plan->vals0.as<uint32_t>(),
-      d_grid, d_out, s));
+  PlaceOut po;
+  GG_TRY(place_and_count<Real>(plan, K, pp, kDegridShape, nullptr, nullptr, s,
+                               &po));
+  Bins b;
+  GG_TRY(bin_records<Real>(plan, K, n, po, grid_size, 1, nullptr, s, &b));
+  if (b.total == 0) {
+    GG_CUDA(cudaMemsetAsync(d_out, 0, 2 * n * sizeof(Real), s));
+    return GG_OK;
+  }
+  if (b.total > 0x7FFFFFFFu)
+    return set_error(GG_ERR_UNSUPPORTED,
+                     "%u records: degridding takes at most 2^31 - 1 per call",
+                     b.total);
+  int sms = 0;
+  GG_TRY(num_sms_of_current(&sms));
+  int per_sm = degrid_tiles_ctas_per_sm<Real>();
+  if (plan->ctas_per_sm > 0) per_sm = std::min(per_sm, plan->ctas_per_sm);
+  const int num_ctas = sms * per_sm;
+  ItemBuffers ib;
+  GG_TRY(build_work_items<Real>(plan, b, num_ctas, false, s, &ib));
+  GG_TRY(plan->rec_out.ensure((size_t)b.total * 2 * sizeof(Real)));
+  uint32_t* sc = plan->scalars.as<uint32_t>();
+  GG_CUDA(launch_degrid_tiles<Real>(
+      ib.items, ib.num_items, ib.counter, sc + kDeviceError, b.vals, po.cell,
+      po.meta, plan->rec_offset.as<uint32_t>(), view, b.geom, grid_size,
+      d_grid, plan->rec_out.p, num_ctas, s));
+  GG_CUDA(launch_degrid_finish<Real>(po.rec_count,
+                                     plan->rec_offset.as<uint32_t>(),
+                                     plan->rec_out.p, n, d_out, s));
+  plan->stats.num_launches += 2;
   return GG_OK;
 }
 

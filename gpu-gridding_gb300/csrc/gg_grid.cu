@@ -39,34 +39,15 @@
 #include <type_traits>
 
 #include "gg_internal.h"
+#include "gg_tiles.cuh"
 
 namespace gg {
 
 namespace {
 
-constexpr int kRows = 8;          // rows per lane (registers)
-constexpr int kWarps = 8;         // consumer warps per CTA
-constexpr int kConsumers = kWarps * 32;
-constexpr int kThreads = kConsumers + 32;  // + one producer warp
-constexpr int kCells = kConsumers * kRows; // 2048 cells per tile
-constexpr int kRing = 4;          // record buffers in flight
-constexpr int kBuf = 128;         // records per buffer
-constexpr int kPerLane = kBuf / 32;
 constexpr int kSlots = 2;         // staged kernel slices
 constexpr int kSliceBytes = 26624;  // per slot: (2s+15)(2s+1) taps, s <= 25 (FP32)
 constexpr int kRunMin = 24;       // records of one group that pay for staging
-static_assert(kRows - 1 <= kSlicePad, "slices need kRows-1 padding rows");
-// Bound on every mbarrier wait (each failed probe sleeps ~100 ns): a wait
-// that runs out (> ~1 s) sets the error flag and the CTA returns.
-constexpr unsigned kWaitLimit = 1u << 24;
-
-template <int TW>
-struct WarpShape {
-  static constexpr int kLanesY = 32 / TW;          // lane rows per warp
-  static constexpr int kBand = kLanesY * kRows;    // rows per warp band
-  static constexpr int kTileU = TW;
-  static constexpr int kTileV = kWarps * kBand;
-};
 
 // Visibility coefficients of one record with the conjugation folded in:
 // re += a*t.re + b*t.im, im += c*t.re + d*t.im.  Stored as (a, d, c, b) so
@@ -133,74 +114,10 @@ struct Smem {
 static_assert((51 + 2 * kSlicePad) * 51 <= kSliceBytes / 8, "FP32 slot size");
 static_assert((33 + 2 * kSlicePad) * 33 <= kSliceBytes / 16, "FP64 slot size");
 
-// ---- mbarrier and bulk-copy helpers (shared::cta) --------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(count)
-               : "memory");
-}
-// Release-arrive: the caller's earlier shared-memory writes are visible to
-// a thread whose wait observes the phase completion.
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile(
-      "{\n\t.reg .b64 st;\n\t"
-      "mbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar))
-      : "memory");
-}
-// Adds `bytes` of expected asynchronous transactions to the current phase.
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile(
-      "mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(
-          smem_u32(bar)),
-      "r"(bytes)
-      : "memory");
-}
-__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Acquire-wait for the completion of the phase with the given parity;
-// false when the bound runs out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (unsigned i = 0; i < kWaitLimit; ++i) {
-    if (mbar_test(bar, parity)) return true;
-    if (i >= 32) __nanosleep(64);
-  }
-  return false;
-}
-// Bulk copy global -> shared (16-byte aligned, size a multiple of 16),
-// completing `bytes` transactions on `bar`.
-__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src,
-                                              uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
-      "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-
 // Record data in shared memory (int4 per record).  A record whose taps are
-// read from the slab stack in global memory (src < 0) holds
-//   x = A + Cp, y = A + Cn, z = B,
-//   w = Lf | c0 << 8 | (c1 - c0) << 16
-// where A is the slab tap index of tile row 0 for a column offset of 0, B
-// the slab taps per tile row (+-row pitch), Cp + col and Cn - col the
-// column offsets on the non-negative and the negative side of the column
-// fold (which begins at lane column Lf), and [c0, c1] the footprint's
-// columns in the tile; so the tap of tile cell (row, col) is
-// slabs[(col >= Lf ? x + col : y - col) + row * B] for c0 <= col <= c1,
-// zero elsewhere.  A record whose slice is staged in a shared-memory slot
-// (src >= 0) holds
+// read from the slab stack in global memory (src < 0) holds slab_record's
+// descriptor (gg_tiles.cuh).  A record whose slice is staged in a
+// shared-memory slot (src >= 0) holds
 //   x = org:   tap index of tile cell (0, 0) on the staged slice
 //   y = rstep: +-(2s+1), slice rows per tile row (mirrored for ov < 0)
 //   z = ulo:   first footprint column (tile-relative)
@@ -366,23 +283,8 @@ __device__ bool produce(const GridArgs<Real>& a, Smem<Real, kStage>& sm) {
             if (src < 0) {
               // Slab of (plane, |ov|); rows mirrored for ov < 0, columns by
               // residue on either side of the fold ou + k*os = 0.
-              const int os = a.view.oversample;
-              const int M = slab_cols_m(s, os, omax);
-              const int pitch = os * M;
-              const int sb = (int)(a.view.sbase[plane] +
-                                   abs(ov) * slab_taps(s, os, omax));
-              const int A = ov >= 0 ? sb + (s + kSlicePad - gv) * pitch
-                                    : sb + (s + kSlicePad + gv) * pitch;
-              const int B = ov >= 0 ? pitch : -pitch;
-              const int ap = ((ou % os) + os) % os, an = ((-ou % os) + os) % os;
-              const int bp = (ou - ap) / os, bn = (-ou - an) / os;
-              const int Cp = ap * M + bp - gu, Cn = an * M + bn + gu;
-              // floor(ou / os); the fold lane is gu - floor(ou / os).
-              const int fl = ou >= 0 ? ou / os : -((-ou + os - 1) / os);
-              const int Lf = min(max(gu - fl, 0), WS::kTileU);
-              const int c0 = max(gu - s, 0), c1 = min(gu + s, WS::kTileU - 1);
               sm.rec[slot][t] =
-                  make_int4(A + Cp, A + Cn, B, Lf | (c0 << 8) | ((c1 - c0) << 16));
+                  slab_record<TW>(a.view, plane, s, ou, ov, gu, gv);
             } else {
               // Tap index of S[0][0] relative to the padded slice start.
               const int org = kSlicePad * F + (s - sv * gv) * F +
@@ -421,29 +323,6 @@ __device__ bool produce(const GridArgs<Real>& a, Smem<Real, kStage>& sm) {
       b0 += kBuf;
     } while (b0 < item.rec_end);
   }
-}
-
-// Read-only tap load that asks L2 to keep the line (evict_last policy):
-// the compact stack is re-read by every tile while the grid streams past.
-__device__ __forceinline__ float2 ld_tap(const float2* p, uint64_t pol) {
-  float2 v;
-  asm("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
-      : "=f"(v.x), "=f"(v.y)
-      : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ double2 ld_tap(const double2* p, uint64_t pol) {
-  double2 v;
-  asm("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
-      : "=d"(v.x), "=d"(v.y)
-      : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ uint64_t evict_last_policy() {
-  uint64_t pol;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;"
-               : "=l"(pol));
-  return pol;
 }
 
 // Loads the kRows taps of one record for this lane: from the record's

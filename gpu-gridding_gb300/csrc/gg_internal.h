@@ -242,16 +242,26 @@ cudaError_t launch_kernel_generate(int num_planes, const int* d_support,
 cudaError_t measure_fp32_fma(int num_sms, double* tflops_best, float* ms_out);
 
 // ---- adjoint (gg_degrid.cu) -----------------------------------------------
-// Sort keys (32 x 32-cell block, then w-plane in plane_bits bits; skipped
-// points last) and identity values of the degridding order.
+// Resident CTAs per SM of the degridding kernel.
 template <typename Real>
-cudaError_t launch_degrid_keys(PlaceParams<Real> p, StackView view,
-                               int blocks_u, int plane_bits, uint32_t* keys,
-                               uint32_t* vals, cudaStream_t s);
-// out_vis[order[w]] for every w (one warp each).
+int degrid_tiles_ctas_per_sm();
+// One persistent launch over the whole work-item queue (32 x 64-cell tiles
+// only): rec_out[rec_offset[v] + rank] = the record's share of
+// conj(tap) * grid for every record, rank = the record's tile among
+// visibility v's tiles in emission order.
 template <typename Real>
-cudaError_t launch_degrid(PlaceParams<Real> p, StackView view,
-                          const uint32_t* order, const Real* grid,
-                          Real* out_vis, cudaStream_t s);
+cudaError_t launch_degrid_tiles(const WorkItem* items,
+                                const uint32_t* num_items, uint32_t* counter,
+                                uint32_t* error, const uint32_t* rec_vis,
+                                const uint32_t* cell, const uint32_t* meta,
+                                const uint32_t* rec_offset, StackView view,
+                                TileGeom geom, int grid_size, const Real* grid,
+                                void* rec_out, int num_ctas, cudaStream_t s);
+// out[v] = the sum of visibility v's count[v] partial results from
+// rec_out[offset[v]] on, in order, in FP64.
+template <typename Real>
+cudaError_t launch_degrid_finish(const uint32_t* count, const uint32_t* offset,
+                                 const void* rec_out, unsigned long long n,
+                                 Real* out, cudaStream_t s);
 
 }  // namespace gg

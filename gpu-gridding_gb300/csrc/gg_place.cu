@@ -32,11 +32,14 @@ k_place(PlaceParams<Real> p, StackView v, TileGeom g, PlaceOut out) {
   unsigned long long skip = 0, macs = 0;
   if (i < p.num_points) {
     const Placement r = place_one(p, v, i);
-    const Real w = p.weight[i];
-    R2 vw;
-    vw.x = rmul(w, p.vis[2 * i]);
-    vw.y = rmul(w, p.vis[2 * i + 1]);
-    ((R2*)out.vw)[i] = vw;
+    // Degridding places coordinates only (no visibilities, weights, norm).
+    const Real w = p.weight ? p.weight[i] : (Real)0;
+    if (p.vis) {
+      R2 vw;
+      vw.x = rmul(w, p.vis[2 * i]);
+      vw.y = rmul(w, p.vis[2 * i + 1]);
+      ((R2*)out.vw)[i] = vw;
+    }
     out.cell[i] = pack_cell(r.gu, r.gv);
     out.meta[i] = pack_meta(r.plane, r.ou, r.ov, r.conj_neg, r.skipped);
     if (r.skipped) {
@@ -49,7 +52,7 @@ k_place(PlaceParams<Real> p, StackView v, TileGeom g, PlaceOut out) {
       const double ts = v.tap_sum[((size_t)r.plane * side + (r.ou + v.omax)) *
                                       side + (r.ov + v.omax)];
       // oskar_grid_wproj.c:210: *norm += sum * weight_i (FP64).
-      norm = __dmul_rn(ts, (double)w);
+      if (p.weight) norm = __dmul_rn(ts, (double)w);
     }
   }
   // Block reductions by warp shuffles, then one partial per block; the
