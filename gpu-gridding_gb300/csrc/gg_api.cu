@@ -564,9 +564,11 @@ TileGeom make_geom(int shape, int grid_size, int num_grids,
   return g;
 }
 
-// Plane groups for a call: consecutive w-planes whose slabs together stay
-// within the byte budget (plan->plane_group_mb, or half the L2 cache), so that each gridding pass reads a stack slice that stays
-// resident in L2.  At most max_groups groups (the sort key's spare bits).
+// Plane groups for a call: consecutive w-planes cut into as many groups as
+// the byte budget (plan->plane_group_mb, or half the L2 cache) needs, with
+// even slab bytes per group, so that each gridding pass reads a stack slice
+// that stays resident in L2.  At most max_groups groups (the sort key's
+// spare bits).
 // Uploads the plane -> group table when it changes; returns the number of
 // groups in *num_groups.
 int plane_groups(gg_plan* plan, const gg_kernels* K, int max_groups,
@@ -594,23 +596,28 @@ int plane_groups(gg_plan* plan, const gg_kernels* K, int max_groups,
   }
   // More groups than allowed: widen the budget until they fit.
   budget = std::max(budget, (total + max_groups - 1) / max_groups);
+  // As many groups as the budget needs, with even byte counts: plane p
+  // joins the group that holds the middle of its bytes (a greedy fill to
+  // the budget would leave the last group with the remainder, and the first
+  // groups' slabs, at the full budget, less likely to stay in L2).
+  const long long want = std::max(1LL, (total + budget - 1) / budget);
+  const double target = (double)total / (double)want;
   std::vector<int>& grp = plan->h_plane_group;
   grp.assign(K->num_planes, 0);
-  int g = 0;
-  long long acc = 0;
+  int g = -1;
+  long long last = -1, before = 0;
   for (int p = 0; p < K->num_planes; ++p) {
-    if (acc > 0 && acc + bytes[p] > budget) {
+    const long long q = std::min(
+        want - 1, (long long)(((double)before + 0.5 * (double)bytes[p]) /
+                              target));
+    if (q != last) {
       ++g;
-      acc = 0;
+      last = q;
     }
     grp[p] = g;
-    acc += bytes[p];
+    before += bytes[p];
   }
-  int groups = g + 1;
-  if (groups > max_groups) {   // rounding left one group too many: merge
-    for (int& x : grp) x = std::min(x, max_groups - 1);
-    groups = max_groups;
-  }
+  const int groups = g + 1;
   GG_TRY(plan->plane_group.ensure((size_t)K->num_planes * sizeof(int)));
   GG_CUDA(cudaMemcpyAsync(plan->plane_group.p, grp.data(),
                           (size_t)K->num_planes * sizeof(int),

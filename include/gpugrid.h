@@ -186,8 +186,9 @@ GG_API int gg_plan_set_slice_staging(gg_plan* plan, int mode);
  *   ctas_per_sm    resident gridding CTAs per SM, 0 (default) = as many as
  *                  fit, else min(that, what fits), 1..32
  *   plane_group_mb kernel bytes per gridding pass: the w-planes are cut
- *                  into groups of consecutive planes whose re-laid kernels
- *                  fit this many MiB and each group is gridded in its own
+ *                  into as few groups of consecutive planes as keep each
+ *                  group's re-laid kernels within this many MiB (about
+ *                  equal in size) and each group is gridded in its own
  *                  pass, so that a pass's kernels stay in L2; 0 (default) =
  *                  half the device's L2 cache, 0..1048576
  * gg_plan_set_tile_shape and gg_plan_set_slice_staging set the first two

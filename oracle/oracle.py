@@ -76,6 +76,11 @@ def lib():
             _sz, _i32p, ctypes.c_int, ctypes.c_int, _f32p, _sz, _f32p, _f32p,
             _f32p, ctypes.c_float, ctypes.c_float, ctypes.c_int, _f64p, _f64p]
         L.oracle_degrid_wproj_f_fp64.restype = None
+        L.oracle_degrid_wproj_d.argtypes = [
+            _sz, _i32p, ctypes.c_int, ctypes.c_int, _f64p, _sz, _f64p, _f64p,
+            _f64p, ctypes.c_double, ctypes.c_double, ctypes.c_int, _f64p,
+            _f64p]
+        L.oracle_degrid_wproj_d.restype = None
         for suffix, p, c in (("f", _f32p, ctypes.c_float),
                              ("d", _f64p, ctypes.c_double)):
             w = getattr(L, f"oracle_grid_weights_write_{suffix}")
@@ -206,6 +211,19 @@ def degrid_fp64(wl, grid):
         wl.num_points, _c(wl.uu, np.float32), _c(wl.vv, np.float32),
         _c(wl.ww, np.float32), np.float32(wl.cell_size_rad),
         np.float32(wl.w_scale), wl.grid_size, g.reshape(-1), out.reshape(-1))
+    return out
+
+
+def degrid_d(wl, grid):
+    """Adjoint of the FP64 gridding map (FP64 placement and cube)."""
+    g = _c(grid, np.float64)
+    out = np.zeros((wl.num_points, 2), np.float64)
+    lib().oracle_degrid_wproj_d(
+        wl.num_w_planes, _c(wl.support, np.int32), wl.oversample,
+        wl.conv_size_half, _c(wl.conv_func, np.float64).reshape(-1),
+        wl.num_points, _c(wl.uu, np.float64), _c(wl.vv, np.float64),
+        _c(wl.ww, np.float64), float(wl.cell_size_rad), float(wl.w_scale),
+        wl.grid_size, g.reshape(-1), out.reshape(-1))
     return out
 
 

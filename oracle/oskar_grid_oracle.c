@@ -351,6 +351,52 @@ ORACLE_API void oracle_degrid_wproj_f_fp64(size_t num_w_planes,
     }
 }
 
+/* The same adjoint for oskar_grid_wproj_d: FP64 placement rules and an FP64
+ * kernel cube (oskar_grid_wproj.c:114-131 declares the _d variant). */
+ORACLE_API void oracle_degrid_wproj_d(size_t num_w_planes,
+        const int* support, int oversample, int conv_size_half,
+        const double* conv_func, size_t num_points, const double* uu,
+        const double* vv, const double* ww, double cell_size_rad,
+        double w_scale, int grid_size, const double* grid, double* out_vis)
+{
+    size_t i;
+    const size_t plane_stride = (size_t)(conv_size_half * conv_size_half);
+    const int centre = grid_size / 2;
+    const double scale = grid_size * cell_size_rad;
+    for (i = 0; i < num_points; ++i)
+    {
+        int j, k;
+        double acc_re = 0.0, acc_im = 0.0;
+        const oracle_place_t p = place_d(uu[i], vv[i], ww[i], scale, centre,
+                grid_size, oversample, num_w_planes, support, w_scale);
+        const double conj = p.conj_neg ? -1.0 : 1.0;
+        const size_t kstart = (size_t)p.plane * plane_stride;
+        const int s = p.support;
+        if (!p.skipped)
+        {
+            for (j = -s; j <= s; ++j)
+            {
+                const size_t row = (size_t)(p.gv + j) * (size_t)grid_size +
+                        (size_t)p.gu;
+                const size_t krow = kstart +
+                        (size_t)abs(p.ov + j * oversample) * conv_size_half;
+                for (k = -s; k <= s; ++k)
+                {
+                    const size_t t = (krow + abs(p.ou + k * oversample)) << 1;
+                    const size_t c = (row + k) << 1;
+                    const double c_re = conv_func[t];
+                    const double c_im = conv_func[t + 1] * conj;
+                    const double g_re = grid[c], g_im = grid[c + 1];
+                    acc_re += c_re * g_re + c_im * g_im;
+                    acc_im += c_re * g_im - c_im * g_re;
+                }
+            }
+        }
+        out_vis[2 * i] = acc_re;
+        out_vis[2 * i + 1] = acc_im;
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Multi-threaded restatement of oskar_grid_wproj_f                         */
 /* ------------------------------------------------------------------------ */

@@ -146,3 +146,46 @@ def test_finite_differences_fp64_cfg1_subset(pkg, synthetic, torch):
     print(f"finite differences: analytic {analytic:.9e} numeric "
           f"{numeric:.9e} rel {rel:.2e}")
     assert rel <= 1e-6
+
+
+def test_degrid_fp64_matches_fp64_oracle(pkg, oracle_mod, synthetic, torch):
+    """FP64 degridding against the FP64 adjoint (FP64 placement and cube)."""
+    wl = synthetic.random_uniform_workload("degrid_d", 3_000, 512, 16, 2, 10,
+                                           seed=21, cell_size_rad=8e-5)
+    s = _setup(pkg, torch, wl, "d")
+    rng = np.random.default_rng(5)
+    y = rng.standard_normal((wl.grid_size, wl.grid_size, 2))
+    out = _adjoint(pkg, torch, s, torch.from_numpy(y).cuda()).cpu().numpy()
+    ref = oracle_mod.degrid_d(wl, y)
+    assert max_rel(out, ref) <= 1e-12
+    p = oracle_mod.place(wl, "d")
+    assert p["num_skipped"] < wl.num_points
+    assert not out[p["skipped"] == 1].any()
+
+
+DEGRID_TUNINGS = [{"plane_group_mb": 1}, {"items_per_cta": 1},
+                  {"items_per_cta": 64}, {"sort_detail": 0},
+                  {"sort_detail": 1, "ctas_per_sm": 1}]
+
+
+def test_degrid_bit_identical_across_tunings(pkg, synthetic, torch):
+    """Each record's partial result is formed the same way whichever CTA
+    takes it, and each visibility adds its records in emission order, so
+    plane groups, work-item splitting, record order and CTA count leave
+    the output bit for bit unchanged."""
+    wl = synthetic.config0().subset(40_000)
+    s = _setup(pkg, torch, wl, "f")
+    g = torch.Generator(device="cuda").manual_seed(7)
+    y = torch.randn((wl.grid_size, wl.grid_size, 2), generator=g,
+                    device="cuda", dtype=torch.float32)
+    base = _adjoint(pkg, torch, s, y).cpu().numpy()
+    again = _adjoint(pkg, torch, s, y).cpu().numpy()
+    assert np.array_equal(base.view(np.uint32), again.view(np.uint32))
+    for t in DEGRID_TUNINGS:
+        plan = pkg.Plan()
+        plan.set_tuning(t)
+        s2 = dict(s, plan=plan)
+        got = _adjoint(pkg, torch, s2, y).cpu().numpy()
+        if t.get("plane_group_mb") == 1:
+            assert plan.stats()["num_plane_groups"] > 1
+        assert np.array_equal(got.view(np.uint32), base.view(np.uint32)), t

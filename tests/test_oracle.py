@@ -100,6 +100,26 @@ def test_adjoint_oracle_dot_product(oracle_mod):
     assert abs(lhs - rhs) <= 1e-10 * abs(lhs)
 
 
+def test_adjoint_oracle_dot_product_fp64(oracle_mod, synthetic):
+    """<G x, y> = <x, G^H y> for the FP64 gridding map and its FP64
+    adjoint (FP64 placement and cube)."""
+    wl = synthetic.random_uniform_workload("adj_d", 1500, 256, 12, 1, 8,
+                                           seed=8, cell_size_rad=1.5e-4)
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal((wl.num_points, 2)).astype(np.float32)
+    y = rng.standard_normal((wl.grid_size, wl.grid_size, 2))
+    wl1 = wl.subset(wl.num_points)
+    wl1.vis = x
+    wl1.weight = np.ones(wl.num_points, np.float32)
+    gx, ns, _ = oracle_mod.grid_d(wl1)
+    assert ns < wl.num_points
+    aty = oracle_mod.degrid_d(wl1, y)
+    xs = x.astype(np.float64)
+    lhs = (gx[..., 0] * y[..., 0] + gx[..., 1] * y[..., 1]).sum()
+    rhs = (xs[:, 0] * aty[:, 0] + xs[:, 1] * aty[:, 1]).sum()
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
 @pytest.mark.skipif("not __import__('oracle').ref_available()",
                     reason="reference source tree not present")
 @pytest.mark.parametrize("seed", [1, 2])
