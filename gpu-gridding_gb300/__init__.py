@@ -38,7 +38,7 @@ EXPORTED_SYMBOLS = (
     "gg_kernels_destroy", "gg_plan_create",
     "gg_plan_destroy", "gg_plan_last_stats", "gg_plan_set_tile_shape",
     "gg_plan_set_slice_staging", "gg_plan_set_tuning", "gg_plan_get_tuning",
-    "gg_host_set_tuning", "gg_host_get_tuning",
+    "gg_host_set_tuning", "gg_host_get_tuning", "gg_host_last_transfer",
     "gg_plan_set_profiling",
     "gg_plan_phase_ms", "gg_measure_fp32_fma_tflops", "gg_grid_wproj_f_device",
     "gg_grid_wproj_f_device_noalloc", "gg_grid_wproj_f_batched_device",
@@ -187,6 +187,8 @@ def _declare(L):
     L.gg_host_set_tuning.restype = ctypes.c_int
     L.gg_host_get_tuning.argtypes = [ctypes.POINTER(Tuning)]
     L.gg_host_get_tuning.restype = ctypes.c_int
+    L.gg_host_last_transfer.argtypes = [ctypes.POINTER(ctypes.c_ulonglong)] * 2
+    L.gg_host_last_transfer.restype = ctypes.c_int
     L.gg_plan_check.argtypes = [_vp, _vp]
     L.gg_plan_check.restype = ctypes.c_int
     L.gg_plan_set_profiling.argtypes = [_vp, ctypes.c_int]
@@ -464,6 +466,14 @@ def set_host_tuning(tuning=None) -> None:
         return
     t = tuning if isinstance(tuning, Tuning) else Tuning.from_dict(tuning)
     _check(lib().gg_host_set_tuning(ctypes.byref(t)))
+
+
+def host_last_transfer() -> tuple:
+    """(host->device, device->host) bytes of the last host-pointer gridding
+    call on the current device."""
+    a, b = ctypes.c_ulonglong(0), ctypes.c_ulonglong(0)
+    _check(lib().gg_host_last_transfer(ctypes.byref(a), ctypes.byref(b)))
+    return int(a.value), int(b.value)
 
 
 def host_tuning() -> dict:

@@ -124,6 +124,8 @@ struct DeviceState {
   cudaEvent_t spans_ready = nullptr;
   uint32_t* h_spans = nullptr;
   static constexpr int kSpanCap = 2 * (kMaxGridSize / 64 + 2);
+  // Bytes the last host-pointer gridding call copied each way.
+  unsigned long long last_h2d = 0, last_d2h = 0;
 };
 
 std::mutex g_devices_mu;
@@ -177,6 +179,7 @@ int num_sms_of_current(int* sms) {
 struct gg_kernels {
   unsigned long long id = 0;   // unique per handle (plans cache by it)
   int device = 0;
+  unsigned long long h2d_bytes = 0;  // host bytes the last fill uploaded
   bool is_double = false;
   int num_planes = 0, oversample = 0, omax = 0, conv_size_half = 0;
   int support_max = 0;
@@ -251,6 +254,7 @@ int kernels_fill(gg_kernels* k, size_t num_w_planes, const int* support,
                         conv_func));
   static std::atomic<unsigned long long> next_id{1};
   k->id = next_id.fetch_add(1);
+  k->h2d_bytes = 0;
   k->support_max = 0;
   auto fail = [&](int code) { return code; };
   if (current_device(&k->device) != GG_OK) return fail(GG_ERR_CUDA);
@@ -320,16 +324,44 @@ int kernels_fill(gg_kernels* k, size_t num_w_planes, const int* support,
                               num_w_planes * sizeof(long long),
                               cudaMemcpyHostToDevice, s), "sbase H2D")))
     return fail(r);
+  k->h2d_bytes += num_w_planes * (sizeof(int) + 2 * sizeof(long long));
   const size_t cube = num_w_planes * (size_t)conv_size_half * conv_size_half *
                       2 * sizeof(Real);
   DevBuf local;
   DevBuf& staged = stage ? *stage : local;
   const Real* d_conv = conv_func;
   if (!on_device) {
+    // Only the square of each plane that the preparation kernels read goes
+    // up (cube_read_extent: about a third of the cube when supports vary
+    // across the stack); a run of planes with the same extent is one 3-D
+    // copy.  The rest of the staging buffer is never read.
     if ((r = staged.ensure(cube))) return fail(r);
-    if ((r = cu(cudaMemcpyAsync(staged.p, conv_func, cube,
-                                cudaMemcpyHostToDevice, s), "conv_func H2D")))
-      return fail(r);
+    const size_t pitch = (size_t)conv_size_half * 2 * sizeof(Real);
+    const size_t plane_elems = (size_t)conv_size_half * conv_size_half * 2;
+    size_t p0 = 0;
+    while (p0 < num_w_planes) {
+      const int e = cube_read_extent(support[p0], oversample, k->omax,
+                                     conv_size_half);
+      size_t p1 = p0 + 1;
+      while (p1 < num_w_planes &&
+             cube_read_extent(support[p1], oversample, k->omax,
+                              conv_size_half) == e)
+        ++p1;
+      cudaMemcpy3DParms prm = {};
+      prm.srcPtr = make_cudaPitchedPtr(
+          (void*)(conv_func + p0 * plane_elems), pitch,
+          (size_t)conv_size_half * 2 * sizeof(Real), conv_size_half);
+      prm.dstPtr = make_cudaPitchedPtr(
+          staged.as<Real>() + p0 * plane_elems, pitch,
+          (size_t)conv_size_half * 2 * sizeof(Real), conv_size_half);
+      prm.extent = make_cudaExtent((size_t)e * 2 * sizeof(Real), (size_t)e,
+                                   p1 - p0);
+      prm.kind = cudaMemcpyHostToDevice;
+      if ((r = cu(cudaMemcpy3DAsync(&prm, s), "conv_func H2D")))
+        return fail(r);
+      k->h2d_bytes += (unsigned long long)e * e * 2 * sizeof(Real) * (p1 - p0);
+      p0 = p1;
+    }
     d_conv = staged.as<Real>();
   }
   StackView v = k->view();
@@ -1380,6 +1412,7 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   // caller's grid already holds them.  One 2-D copy per run of tile rows
   // with the same column span; the whole grid when the spans are unknown;
   // nothing when there were no visibilities.
+  unsigned long long d2h_grid = 0;
   if (n) {
     GG_CUDA(cudaStreamWaitEvent(s, st->grid_ready, 0));
     if (plan->spans_written) {
@@ -1406,11 +1439,13 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
                                   plan->in_grid.as<char>() + off, row_bytes,
                                   (c1 - c0) * cell_bytes, r1 - r0,
                                   cudaMemcpyDeviceToHost, s));
+        d2h_grid += (c1 - c0) * cell_bytes * (r1 - r0);
         tv = te;
       }
     } else {
       GG_CUDA(cudaMemcpyAsync(grid, plan->in_grid.p, grid_bytes,
                               cudaMemcpyDeviceToHost, s));
+      d2h_grid = grid_bytes;
     }
   }
   double norm_out = 0.0;
@@ -1423,6 +1458,18 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   GG_TRY(check_device_error(plan, s));
   *norm = norm_out;
   *num_skipped = (size_t)skip_out;
+  // Bytes moved: the cube and its plane tables, the inputs, the grid and
+  // norm up; the grid spans, norm, skip count, the placement scalars, the
+  // spans and the error flag down.
+  st->last_h2d = K->h2d_bytes + (n ? 6 * n * sizeof(Real) + grid_bytes : 0) +
+                 sizeof(double);
+  st->last_d2h = d2h_grid + sizeof(double) + sizeof(unsigned long long) +
+                 sizeof(uint32_t) +
+                 (n ? 4 * kScalarCount + 8 +
+                          (plan->spans_written && plan->spans_async
+                               ? 2 * (size_t)plan->spans_tiles_v * 4
+                               : 0)
+                    : 0);
   return GG_OK;
 }
 
@@ -1922,6 +1969,21 @@ GG_API int gg_host_set_tuning(const gg_tuning* t) {
   std::lock_guard<std::mutex> lk(st->mu);
   GG_TRY(ensure_device_plan(st));
   return gg_plan_set_tuning(st->plan, t ? t : &defaults);
+}
+
+GG_API int gg_host_last_transfer(unsigned long long* h2d_bytes,
+                                 unsigned long long* d2h_bytes) {
+  t_last_error.clear();
+  if (!h2d_bytes || !d2h_bytes)
+    return set_error(GG_ERR_INVALID_ARG, "NULL argument");
+  int dev;
+  GG_TRY(current_device(&dev));
+  DeviceState* st;
+  GG_TRY(device_state(dev, &st));
+  std::lock_guard<std::mutex> lk(st->mu);
+  *h2d_bytes = st->last_h2d;
+  *d2h_bytes = st->last_d2h;
+  return GG_OK;
 }
 
 GG_API int gg_host_get_tuning(gg_tuning* t) {

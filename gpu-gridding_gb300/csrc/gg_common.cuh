@@ -110,6 +110,17 @@ __host__ __device__ inline long long slab_taps(int s, int os, int omax) {
               slab_cols_m(s, os, omax) + 1) & ~1LL;
 }
 
+// Rows and columns of a plane's quadrant cube that the stack preparation
+// reads (slices and tap sums: |off| + s*os with |off| <= omax; slabs:
+// columns r + m*os with r < os, m < M): the square [0, E)^2 below
+// E = min(csh, 1 + max(s*os + omax, M*os - 1)).
+__host__ __device__ inline int cube_read_extent(int s, int os, int omax,
+                                                int csh) {
+  const int a = s * os + omax, b = slab_cols_m(s, os, omax) * os - 1;
+  const int e = 1 + (a > b ? a : b);
+  return e < csh ? e : csh;
+}
+
 // Taps one slice occupies: padding rows included, rounded up to an even
 // count so that every slice starts 16-byte aligned (bulk copies need it).
 __host__ __device__ inline long long slice_taps(int s) {

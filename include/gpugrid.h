@@ -214,6 +214,13 @@ GG_API int gg_plan_get_tuning(const gg_plan* plan, gg_tuning* tuning);
 GG_API int gg_host_set_tuning(const gg_tuning* tuning);
 GG_API int gg_host_get_tuning(gg_tuning* tuning);
 
+/* Bytes the last host-pointer gridding call on the current device copied
+ * host -> device (kernel cube and plane tables, the call's arrays, the
+ * grid, norm) and device -> host (the grid rows' spans that hold records,
+ * norm, skip count and a few status words); 0, 0 before the first call. */
+GG_API int gg_host_last_transfer(unsigned long long* h2d_bytes,
+                                 unsigned long long* d2h_bytes);
+
 /* Phase timing.  With profiling enabled, every gridding call made with the
  * plan records CUDA events on its stream around five phases:
  *   0 placement (placement, skip/norm reduction, record offsets)

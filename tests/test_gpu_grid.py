@@ -382,6 +382,36 @@ def test_dropin_copies_back_touched_spans(pkg, oracle_mod, synthetic, torch,
     assert max_rel(g0, gr) <= 1e-5
 
 
+def test_dropin_transfer_bytes(pkg, synthetic, torch):
+    """The drop-in reports what it copied: everything up, and only the
+    touched spans of the grid down (a centre patch here)."""
+    G = 1024
+    wl = synthetic.random_uniform_workload(
+        "xfer", 10_000, G, 16, 2, 8, seed=9, cell_size_rad=6e-5,
+        sigma_frac=0.01, clip_frac=0.03)
+    pkg.grid_f(wl)
+    h2d, d2h = pkg.host_last_transfer()
+    n = wl.num_points
+    # Of the cube only each plane's square up to the last row and column
+    # the stack preparation reads goes up.
+    omax = (wl.oversample + 1) // 2
+    ext = np.minimum(wl.conv_size_half,
+                     1 + np.maximum(wl.support * wl.oversample + omax,
+                                    (wl.support + 1 + (omax >= wl.oversample))
+                                    * wl.oversample - 1))
+    cube = int((ext.astype(np.int64) ** 2).sum()) * 8
+    assert cube < wl.conv_func.nbytes
+    assert h2d == cube + wl.num_w_planes * 20 + 24 * n + 8 * G * G + 8
+    assert 0 < d2h < G * G * 8 // 10
+    empty = dataclasses.replace(wl, uu=wl.uu[:0], vv=wl.vv[:0],
+                                ww=wl.ww[:0], vis=wl.vis[:0],
+                                weight=wl.weight[:0])
+    pkg.grid_f(empty)
+    h2d, d2h = pkg.host_last_transfer()
+    assert h2d == cube + wl.num_w_planes * 20 + 8
+    assert d2h == 8 + 8 + 4
+
+
 def test_dropin_nothing_gridded_leaves_grid(pkg, synthetic, torch):
     """Every visibility off the grid (all skipped), and no visibilities at
     all: the grid comes back bit-for-bit unchanged and the norm as given."""
