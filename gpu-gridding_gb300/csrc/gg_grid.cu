@@ -453,7 +453,8 @@ k_grid_tiles(GridArgs<Real> a) {
       const bool touch =
           c0 + lane < nb && (sm.band[slot][c0 + lane] & warp_bits) != 0u;
       uint32_t m = __ballot_sync(0xffffffffu, touch);
-      // Two records at a time: 2 * kRows independent tap loads per lane in
+      // Up to three records at a time (FP32; two for FP64, whose taps take
+      // twice the registers): 3 * kRows independent tap loads per lane in
       // flight.  Each cell takes the records in queue order.
       while (m) {
         const int tA = c0 + __ffs(m) - 1;
@@ -467,8 +468,19 @@ k_grid_tiles(GridArgs<Real> a) {
           R2 tb[kRows];
           load_record<Real, TW, kStage>(sm, slot, tB, slabs, gzeros, my_bit,
                                         lx, rowl, pol, tb);
-          accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
-          accumulate<Real>(sm.cf[slot][tB], tb, acc, acq);
+          if (sizeof(Real) == 4 && m) {
+            const int tC = c0 + __ffs(m) - 1;
+            m &= m - 1;
+            R2 tc[kRows];
+            load_record<Real, TW, kStage>(sm, slot, tC, slabs, gzeros,
+                                          my_bit, lx, rowl, pol, tc);
+            accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
+            accumulate<Real>(sm.cf[slot][tB], tb, acc, acq);
+            accumulate<Real>(sm.cf[slot][tC], tc, acc, acq);
+          } else {
+            accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
+            accumulate<Real>(sm.cf[slot][tB], tb, acc, acq);
+          }
         } else {
           accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
         }
