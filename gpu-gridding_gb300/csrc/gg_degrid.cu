@@ -17,7 +17,7 @@
 // order and stores the record's partial result at its emission slot
 // (rec_offset[visibility] + its tile's rank among the visibility's tiles).
 // k_degrid_finish then adds each visibility's partial results in emission
-// order in FP64.  Nothing is accumulated with atomics, so the result does
+// order.  Nothing is accumulated with atomics, so the result does
 // not depend on scheduling.
 //
 // The reference has no degridder; this one is pinned by the dot-product
@@ -347,25 +347,28 @@ k_degrid_tiles(DegridArgs<Real> a) {
   }
 }
 
-// out[i] = sum of visibility i's partial results in emission order (FP64,
-// rounded once); skipped visibilities have no records and get 0.
+// out[i] = sum of visibility i's partial results in emission order, in the
+// call's precision (a visibility has a handful of records: its footprint's
+// tiles); skipped visibilities have no records and get 0.
 template <typename Real>
 __global__ void k_degrid_finish(const uint32_t* __restrict__ count,
                                 const uint32_t* __restrict__ offset,
                                 const typename Vec2<Real>::type* __restrict__
                                     rec_out,
                                 unsigned long long n, Real* __restrict__ out) {
+  using R2 = typename Vec2<Real>::type;
   const unsigned long long i =
       (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint32_t c = count[i], o = offset[i];
-  double re = 0.0, im = 0.0;
+  R2 acc;
+  acc.x = acc.y = 0;
   for (uint32_t k = 0; k < c; ++k) {
-    re += (double)rec_out[o + k].x;
-    im += (double)rec_out[o + k].y;
+    const R2 v = rec_out[o + k];
+    acc.x += v.x;
+    acc.y += v.y;
   }
-  out[2 * i] = (Real)re;
-  out[2 * i + 1] = (Real)im;
+  ((R2*)out)[i] = acc;
 }
 
 template <typename Real>

@@ -258,7 +258,7 @@ cudaError_t launch_degrid_tiles(const WorkItem* items,
                                 TileGeom geom, int grid_size, const Real* grid,
                                 void* rec_out, int num_ctas, cudaStream_t s);
 // out[v] = the sum of visibility v's count[v] partial results from
-// rec_out[offset[v]] on, in order, in FP64.
+// rec_out[offset[v]] on, in order.
 template <typename Real>
 cudaError_t launch_degrid_finish(const uint32_t* count, const uint32_t* offset,
                                  const void* rec_out, unsigned long long n,

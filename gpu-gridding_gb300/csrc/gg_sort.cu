@@ -140,10 +140,17 @@ k_radix_hist(const uint32_t* __restrict__ keys, size_t n, int shift,
   h[threadIdx.x] = 0;
   __syncthreads();
   const size_t base = (size_t)blockIdx.x * kRadixTile;
-#pragma unroll 4
+  // All loads first (independent, in flight together), then the counts.
+  uint32_t k[kRadixRounds];
+#pragma unroll
   for (int r = 0; r < kRadixRounds; ++r) {
-    size_t idx = base + (size_t)r * kRadixThreads + threadIdx.x;
-    if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 0xFF], 1u);
+    const size_t idx = base + (size_t)r * kRadixThreads + threadIdx.x;
+    k[r] = idx < n ? keys[idx] : 0u;
+  }
+#pragma unroll
+  for (int r = 0; r < kRadixRounds; ++r) {
+    const size_t idx = base + (size_t)r * kRadixThreads + threadIdx.x;
+    if (idx < n) atomicAdd(&h[(k[r] >> shift) & 0xFF], 1u);
   }
   __syncthreads();
   // Digit-major layout: the scan then yields, for each (digit, block), the
@@ -151,53 +158,87 @@ k_radix_hist(const uint32_t* __restrict__ keys, size_t n, int shift,
   hist[(size_t)threadIdx.x * num_blocks + blockIdx.x] = h[threadIdx.x];
 }
 
+// Stable scatter of one 4096-key block: the keys are first ordered by digit
+// in shared memory (in block order within a digit), then written out in
+// that order, so keys with the same digit go to consecutive addresses and a
+// warp's stores form a few contiguous runs instead of 32 scattered words.
+// hist holds the block's digit counts (digit-major, as k_radix_hist wrote
+// them) and offsets their exclusive scan (global start of each (digit,
+// block) run).
 __global__ void __launch_bounds__(kRadixThreads)
 k_radix_scatter(const uint32_t* __restrict__ keys,
                 const uint32_t* __restrict__ vals, size_t n, int shift,
-                int num_blocks, const uint32_t* __restrict__ offsets,
+                int num_blocks, const uint32_t* __restrict__ hist,
+                const uint32_t* __restrict__ offsets,
                 uint32_t* __restrict__ keys_out,
                 uint32_t* __restrict__ vals_out) {
-  __shared__ uint32_t digit_base[kRadixDigits];
+  __shared__ uint32_t s_keys[kRadixTile];
+  __shared__ uint32_t s_vals[kRadixTile];
+  __shared__ uint32_t digit_base[kRadixDigits];   // global run start
+  __shared__ uint32_t local_start[kRadixDigits];  // block-local run start
+  __shared__ uint32_t placed[kRadixDigits];       // keys placed so far
   __shared__ uint32_t warp_count[kRadixWarps][kRadixDigits];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  digit_base[threadIdx.x] =
-      offsets[(size_t)threadIdx.x * num_blocks + blockIdx.x];
+  const size_t cell = (size_t)threadIdx.x * num_blocks + blockIdx.x;
+  digit_base[threadIdx.x] = offsets[cell];
+  uint32_t total;
+  local_start[threadIdx.x] = block_exclusive_scan(hist[cell], &total);
+  placed[threadIdx.x] = 0;
   const uint32_t lt_mask = (1u << lane) - 1u;
   const size_t base = (size_t)blockIdx.x * kRadixTile;
+  const int valid_n = (int)min((size_t)kRadixTile, n - base);
+  // The block's keys and values, all loads in flight together.
+  uint32_t kr[kRadixRounds], vr[kRadixRounds];
+#pragma unroll
   for (int r = 0; r < kRadixRounds; ++r) {
-    if (base + (size_t)r * kRadixThreads >= n) break;  // block-uniform
+    const int t = r * kRadixThreads + threadIdx.x;
+    kr[r] = t < valid_n ? keys[base + t] : 0u;
+    vr[r] = t < valid_n ? vals[base + t] : 0u;
+  }
+  // Phase 1: stable placement in shared memory, 256 keys per round.
+#pragma unroll
+  for (int r = 0; r < kRadixRounds; ++r) {
+    if (r * kRadixThreads >= valid_n) break;   // block-uniform
 #pragma unroll
     for (int w = 0; w < kRadixWarps; ++w) warp_count[w][threadIdx.x] = 0;
     __syncthreads();
-    size_t idx = base + (size_t)r * kRadixThreads + threadIdx.x;
-    bool valid = idx < n;
-    uint32_t key = valid ? keys[idx] : 0u;
-    uint32_t val = valid ? vals[idx] : 0u;
+    const int t = r * kRadixThreads + threadIdx.x;
+    const bool valid = t < valid_n;
+    const uint32_t key = kr[r];
+    const uint32_t val = vr[r];
     // Invalid lanes take digit 256 so they never match a valid one.
-    uint32_t digit = valid ? ((key >> shift) & 0xFF) : 256u;
-    uint32_t peers = __match_any_sync(0xffffffffu, digit);
-    uint32_t rank = __popc(peers & lt_mask);
-    int leader = __ffs(peers) - 1;
-    if (valid && lane == leader) warp_count[warp][digit] = __popc(peers);
+    const uint32_t digit = valid ? ((key >> shift) & 0xFF) : 256u;
+    const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+    const uint32_t rank = __popc(peers & lt_mask);
+    if (valid && lane == __ffs(peers) - 1)
+      warp_count[warp][digit] = __popc(peers);
     __syncthreads();
-    // Per-digit exclusive prefix across warps (thread t owns digit t).
+    // Per-digit prefix across warps (thread t owns digit t).
     {
-      uint32_t running = digit_base[threadIdx.x];
+      uint32_t running = placed[threadIdx.x];
 #pragma unroll
       for (int w = 0; w < kRadixWarps; ++w) {
-        uint32_t c = warp_count[w][threadIdx.x];
+        const uint32_t c = warp_count[w][threadIdx.x];
         warp_count[w][threadIdx.x] = running;
         running += c;
       }
-      digit_base[threadIdx.x] = running;
+      placed[threadIdx.x] = running;
     }
     __syncthreads();
     if (valid) {
-      uint32_t pos = warp_count[warp][digit] + rank;
-      keys_out[pos] = key;
-      vals_out[pos] = val;
+      const uint32_t pos = local_start[digit] + warp_count[warp][digit] + rank;
+      s_keys[pos] = key;
+      s_vals[pos] = val;
     }
     __syncthreads();
+  }
+  // Phase 2: write the block out in digit order.
+  for (int i = threadIdx.x; i < valid_n; i += kRadixThreads) {
+    const uint32_t key = s_keys[i];
+    const uint32_t d = (key >> shift) & 0xFF;
+    const uint32_t pos = digit_base[d] + ((uint32_t)i - local_start[d]);
+    keys_out[pos] = key;
+    vals_out[pos] = s_vals[i];
   }
 }
 
@@ -256,7 +297,7 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals,
                                        scan_tmp, s);
     if (e != cudaSuccess) return e;
     k_radix_scatter<<<(unsigned)nb, kRadixThreads, 0, s>>>(
-        k_in, v_in, n, shift, (int)nb, offs, k_out, v_out);
+        k_in, v_in, n, shift, (int)nb, hist, offs, k_out, v_out);
     uint32_t* t;
     t = k_in; k_in = k_out; k_out = t;
     t = v_in; v_in = v_out; v_out = t;
