@@ -169,6 +169,10 @@ struct TileGeom {
   int num_groups;            // plane groups (passes), >= 1
   int tiles_total;           // num_grids * tiles_u * tiles_v
   const int* plane_group;    // [P] group of each plane (num_groups > 1)
+  // > 0: the last plane group is gridded in two passes, tile rows below
+  // split_tv first; its records in rows >= split_tv form the extra final
+  // group num_groups - 1 (single-grid calls).
+  int split_tv;
 };
 
 // Work item of the gridding kernel: a range of sorted records of one tile.

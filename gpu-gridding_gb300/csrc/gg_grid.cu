@@ -810,7 +810,8 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                               int grid_size, Real* grid, long long grid_stride,
                               Real* partials, const int4* split_tiles,
                               const uint32_t* num_split, int max_split,
-                              int num_ctas, bool stage, cudaStream_t s) {
+                              int num_ctas, bool stage, cudaStream_t s,
+                              int event_group, cudaEvent_t event) {
   GridArgs<Real> a;
   a.items = items;
   a.group_items = group_items;
@@ -845,6 +846,10 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                                   partials, geom, g, grid_size, grid,
                                   grid_stride, s);
     if (e != cudaSuccess) return e;
+    if (event && g == event_group) {
+      e = cudaEventRecord(event, s);
+      if (e != cudaSuccess) return e;
+    }
   }
   return cudaSuccess;
 }
@@ -855,11 +860,11 @@ template cudaError_t launch_grid_tiles<float>(
     const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
     float*, long long, float*, const int4*, const uint32_t*, int, int, bool,
-    cudaStream_t);
+    cudaStream_t, int, cudaEvent_t);
 template cudaError_t launch_grid_tiles<double>(
     const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
     double*, long long, double*, const int4*, const uint32_t*, int, int, bool,
-    cudaStream_t);
+    cudaStream_t, int, cudaEvent_t);
 
 }  // namespace gg

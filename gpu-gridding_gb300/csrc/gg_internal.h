@@ -184,6 +184,7 @@ cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
 // One persistent launch per plane group, in group order, each followed by
 // the reduction of that group's split tiles (grid += their partials in
 // chunk order, FP64): the grid takes the groups' contributions in order.
+// When event is set it is recorded on s after group event_group's pass.
 template <typename Real>
 cudaError_t launch_grid_tiles(const WorkItem* items,
                               const uint32_t* group_items,
@@ -194,7 +195,9 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                               int grid_size, Real* grid, long long grid_stride,
                               Real* partials, const int4* split_tiles,
                               const uint32_t* num_split, int max_split,
-                              int num_ctas, bool stage, cudaStream_t s);
+                              int num_ctas, bool stage, cudaStream_t s,
+                              int event_group = -1,
+                              cudaEvent_t event = nullptr);
 // stage: the kernel variant that stages kernel slices in shared memory.
 template <typename Real>
 int grid_tiles_ctas_per_sm(int tile_u, bool stage);

@@ -185,8 +185,13 @@ __global__ void k_emit(const uint32_t* __restrict__ cell,
     for (int tu = tu0; tu <= tu1; ++tu) {
       uint32_t tile = (uint32_t)grid_index * tiles_per_grid +
                       (uint32_t)tv * g.tiles_u + (uint32_t)tu;
-      if (g.num_groups > 1)
-        tile += (uint32_t)g.plane_group[plane] * (uint32_t)g.tiles_total;
+      if (g.num_groups > 1) {
+        uint32_t group = g.plane_group ? (uint32_t)g.plane_group[plane] : 0u;
+        if (g.split_tv > 0 && group == (uint32_t)g.num_groups - 2 &&
+            tv >= g.split_tv)
+          ++group;
+        tile += group * (uint32_t)g.tiles_total;
+      }
       keys[pos] = low_bits >= 32 ? low : ((tile << low_bits) | low);
       vals[pos] = vid;
       ++pos;

@@ -382,6 +382,37 @@ def test_dropin_copies_back_touched_spans(pkg, oracle_mod, synthetic, torch,
     assert max_rel(g0, gr) <= 1e-5
 
 
+@pytest.mark.parametrize("prec", ["f", "d"])
+def test_dropin_split_last_pass(pkg, oracle_mod, synthetic, torch, prec):
+    """On grids of 128 MiB and more the host-pointer call grids the last
+    plane group in two passes by tile rows and copies the upper rows back
+    while the lower ones are gridded: a random starting grid must still
+    come back as start + contributions, bit for bit where nothing was
+    added, with the reference's placement."""
+    G = 4096
+    wl = synthetic.random_uniform_workload(
+        "split", 60_000, G, 64, 2, 16, seed=23, cell_size_rad=1.2e-5,
+        sigma_frac=0.15, clip_frac=0.45)
+    dt = np.float32 if prec == "f" else np.float64
+    grid_fn = pkg.grid_f if prec == "f" else pkg.grid_d
+    start = np.random.default_rng(8).standard_normal((G, G, 2)).astype(dt)
+    g0, ns0, nm0 = grid_fn(wl)
+    g1, ns1, nm1 = grid_fn(wl, start.copy(), 1.5)
+    assert ns1 == ns0 < wl.num_points
+    assert max_rel(g1, start + g0) <= (1e-6 if prec == "f" else 1e-14)
+    untouched = g0 == 0
+    assert untouched.any() and (~untouched).any()
+    assert np.array_equal(g1[untouched], start[untouched])
+    if prec == "f":
+        gr, nsr, _ = oracle_mod.grid_f(wl)
+        assert ns0 == nsr
+        assert max_rel(g0, gr) <= 1e-5
+    else:
+        gr, nsr, _ = oracle_mod.grid_d(wl)
+        assert ns0 == nsr
+        assert max_rel(g0, gr) <= 1e-12
+
+
 def test_dropin_transfer_bytes(pkg, synthetic, torch):
     """The drop-in reports what it copied: everything up, and only the
     touched spans of the grid down (a centre patch here)."""
