@@ -535,6 +535,23 @@ def run_ours(args):
         plan, uu, vv, weight, cell, G, dens, nskip, stream))
     ms_wread = timed(lambda: pkg.grid_weights_read_device(
         plan, uu, vv, weight, w_out, cell, G, dens, nskip, stream))
+    # One training step of the autograd binding: the forward gridding into
+    # a new grid, then the backward (the degridding kernel and the vis /
+    # weight gradients) for dL/dgrid = a fixed random array.
+    vis_req = vis.clone().requires_grad_(True)
+    w_req = weight.clone().requires_grad_(True)
+    target = torch.randn((G, G, 2), dtype=torch.float32, device=dev,
+                         generator=torch.Generator(device=dev).manual_seed(5))
+
+    def fwd_bwd():
+        vis_req.grad = None
+        w_req.grad = None
+        g = pkg.GridWproj.apply(vis_req, w_req, uu, vv, ww, stack, plan, cell,
+                                wsc, G)
+        g.backward(target)
+
+    with torch.cuda.stream(stream):
+        ms_fb = timed(fwd_bwd)
     neighbours = {
         "degrid": {"ms_per_step": ms_degrid,
                    "mvis_s": num_vis / (ms_degrid * 1e-3) / 1e6,
@@ -543,6 +560,8 @@ def run_ours(args):
                           "mvis_s": num_vis / (ms_wwrite * 1e-3) / 1e6},
         "weights_read": {"ms_per_step": ms_wread,
                          "mvis_s": num_vis / (ms_wread * 1e-3) / 1e6},
+        "forward_backward": {"ms_per_step": ms_fb,
+                             "mvis_s": num_vis / (ms_fb * 1e-3) / 1e6},
     }
     del out_vis, dens, w_out
 
