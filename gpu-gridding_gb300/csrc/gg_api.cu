@@ -503,6 +503,11 @@ struct gg_plan {
   DevBuf nterm, chunk_begin, grid_chunk0, chunk_part, grid_offsets;
   // Degridding: partial result of every record, at its emission slot.
   DevBuf rec_out;
+  // Queue order of the tiles (ItemBuffers::tile_order) and the geometry it
+  // was made for: grid_size, tile_u, tile_v, num_grids.
+  DevBuf tile_order;
+  std::vector<int> h_tile_order;
+  int to_key[4] = {0, 0, 0, 0};
   // Staging of the host-pointer entry points.
   DevBuf in_uu, in_vv, in_ww, in_vis, in_weight, in_grid, in_misc;
   // Geometry kept by the last batched call for replays on new amplitudes:
@@ -821,7 +826,7 @@ struct Bins {
   uint32_t total = 0;
   int shape = 0;
   bool stage = false;
-  int num_groups = 1, num_tiles = 0;
+  int num_groups = 1, num_tiles = 0, grid_size = 0;
   TileGeom geom{};
   const uint32_t* keys = nullptr;
   const uint32_t* vals = nullptr;
@@ -898,6 +903,7 @@ int bin_records(gg_plan* plan, const gg_kernels* K, size_t n,
   b->stage = stage;
   b->num_groups = num_groups;
   b->num_tiles = num_tiles;
+  b->grid_size = grid_size;
   b->geom = geom;
   if (total == 0) return GG_OK;
 
@@ -926,6 +932,44 @@ int bin_records(gg_plan* plan, const gg_kernels* K, size_t n,
   GG_CUDA(launch_tile_bounds(b->keys, total, low_bits, num_tiles,
                              plan->tile_start.as<uint32_t>(), s));
   plan->stats.num_launches += 1;
+  return GG_OK;
+}
+
+// Queue order of the tiles of one group: grid by grid, and within a grid by
+// the distance of the tile's centre from the uv origin (the grid centre),
+// nearest first.  On telescope data the w-plane of a visibility grows with
+// its baseline, so tiles at the same distance use similar planes and the
+// CTAs running at one time share more kernel slabs in L2; the heavy
+// central tiles also start first.  Uploaded when the geometry changes.
+int tile_queue_order(gg_plan* plan, const TileGeom& g, int grid_size,
+                     cudaStream_t s, const int** out) {
+  const int key[4] = {grid_size, g.tile_u, g.tile_v, g.num_grids};
+  if (!std::equal(key, key + 4, plan->to_key) ||
+      (int)plan->h_tile_order.size() != g.tiles_total) {
+    const int tpg = g.tiles_u * g.tiles_v;
+    std::vector<long long> r2(g.tiles_total);
+    for (int l = 0; l < g.tiles_total; ++l) {
+      const int tl = l % tpg;
+      const long long du =
+          (long long)(tl % g.tiles_u) * g.tile_u + g.tile_u / 2 - grid_size / 2;
+      const long long dv =
+          (long long)(tl / g.tiles_u) * g.tile_v + g.tile_v / 2 - grid_size / 2;
+      r2[l] = du * du + dv * dv;
+    }
+    std::vector<int>& ord = plan->h_tile_order;
+    ord.resize(g.tiles_total);
+    for (int l = 0; l < g.tiles_total; ++l) ord[l] = l;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+      const int ga = a / tpg, gb = b / tpg;
+      return ga != gb ? ga < gb : r2[a] < r2[b];
+    });
+    GG_TRY(plan->tile_order.ensure(ord.size() * sizeof(int)));
+    GG_CUDA(cudaMemcpyAsync(plan->tile_order.p, ord.data(),
+                            ord.size() * sizeof(int), cudaMemcpyHostToDevice,
+                            s));
+    std::copy(key, key + 4, plan->to_key);
+  }
+  *out = plan->tile_order.as<int>();
   return GG_OK;
 }
 
@@ -967,6 +1011,7 @@ int build_work_items(gg_plan* plan, const Bins& b, int num_ctas,
   ib->num_split = sc + kNumSplit;
   ib->counter = sc + kCounter;
   ib->scan_tmp = plan->scan_tmp.p;
+  GG_TRY(tile_queue_order(plan, b.geom, b.grid_size, s, &ib->tile_order));
   GG_CUDA(launch_build_items(plan->tile_start.as<uint32_t>(), num_tiles,
                              b.total, chunk, *ib, s));
   // item counts, 2 scans, item emit

@@ -617,27 +617,41 @@ __global__ void k_touched_spans(const uint32_t* __restrict__ tile_start,
 
 // A[t] = chunks of tile t if it is split (more than one chunk), else 0;
 // B[t] = 1 if tile t has exactly one chunk.
+// Virtual tile at queue rank i (see ItemBuffers::tile_order).
+__device__ __forceinline__ int tile_at_rank(int i, int T,
+                                            const int* __restrict__ order) {
+  if (!order) return i;
+  const int g = i / T;
+  return g * T + order[i - g * T];
+}
+
+// Counts per queue rank i (tile t = tile_at_rank(i)):
+// A[i] = chunks of t if it is split (more than one chunk), else 0;
+// B[i] = 1 if t has exactly one chunk.
 __global__ void k_item_counts(const uint32_t* __restrict__ tile_start,
-                              int num_tiles, uint32_t chunk,
+                              int num_tiles, int num_groups,
+                              const int* __restrict__ order, uint32_t chunk,
                               uint32_t* __restrict__ A,
                               uint32_t* __restrict__ B) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= num_tiles) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= num_tiles) return;
+  const int t = tile_at_rank(i, num_tiles / num_groups, order);
   const uint32_t c = tile_start[t + 1] - tile_start[t];
   const uint32_t chunks = (c + chunk - 1) / chunk;
-  A[t] = chunks > 1 ? chunks : 0;
-  B[t] = chunks == 1 ? 1 : 0;
+  A[i] = chunks > 1 ? chunks : 0;
+  B[i] = chunks == 1 ? 1 : 0;
 }
 
 // The queue is group-major (see ItemBuffers); within plane group g the
 // chunks of split tiles come first (they are the largest items), then the
-// single-chunk tiles.  With exclusive scans sA (split chunks) and sB
-// (single-chunk tiles) over the virtual tiles, group g starts at
-// sA[gT] + sB[gT] (T = tiles per group), split chunk j of virtual tile t
-// sits at sA[t] + sB[gT] + j and single tile t at sA[(g+1)T] + sB[t].
-// Partial slot of a split chunk = sA[t] + j.
+// single-chunk tiles, each part in rank order.  With exclusive scans sA
+// (split chunks) and sB (single-chunk tiles) over the ranks, group g
+// starts at sA[gT] + sB[gT] (T = tiles per group), split chunk j of rank i
+// sits at sA[i] + sB[gT] + j and single rank i at sA[(g+1)T] + sB[i].
+// Partial slot of a split chunk = sA[i] + j.
 __global__ void k_item_emit(const uint32_t* __restrict__ tile_start,
-                            int num_tiles, int num_groups, uint32_t chunk,
+                            int num_tiles, int num_groups,
+                            const int* __restrict__ order, uint32_t chunk,
                             const uint32_t* __restrict__ sA,
                             const uint32_t* __restrict__ sB,
                             const uint32_t* __restrict__ totA,
@@ -647,14 +661,15 @@ __global__ void k_item_emit(const uint32_t* __restrict__ tile_start,
                             uint32_t* __restrict__ num_split,
                             uint32_t* __restrict__ num_items,
                             uint32_t* __restrict__ group_items) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int T = num_tiles / num_groups;
-  auto scanA = [&](int i) { return i < num_tiles ? sA[i] : *totA; };
-  auto scanB = [&](int i) { return i < num_tiles ? sB[i] : *totB; };
-  if (t == 0) *num_items = *totA + *totB;
-  if (t <= num_groups) group_items[t] = scanA(t * T) + scanB(t * T);
-  if (t >= num_tiles) return;
-  const int g = t / T;
+  auto scanA = [&](int r) { return r < num_tiles ? sA[r] : *totA; };
+  auto scanB = [&](int r) { return r < num_tiles ? sB[r] : *totB; };
+  if (i == 0) *num_items = *totA + *totB;
+  if (i <= num_groups) group_items[i] = scanA(i * T) + scanB(i * T);
+  if (i >= num_tiles) return;
+  const int g = i / T;
+  const int t = tile_at_rank(i, T, order);
   const uint32_t s0 = tile_start[t], s1 = tile_start[t + 1];
   const uint32_t c = s1 - s0;
   if (c == 0) return;
@@ -662,9 +677,9 @@ __global__ void k_item_emit(const uint32_t* __restrict__ tile_start,
   if (chunks == 1) {
     WorkItem w;
     w.tile = t; w.rec_begin = (int)s0; w.rec_end = (int)s1; w.slot = -1;
-    items[scanA((g + 1) * T) + sB[t]] = w;
+    items[scanA((g + 1) * T) + sB[i]] = w;
   } else {
-    const uint32_t first = sA[t];
+    const uint32_t first = sA[i];
     const uint32_t pos = first + scanB(g * T);
     for (uint32_t j = 0; j < chunks; ++j) {
       WorkItem w;
@@ -744,7 +759,8 @@ cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
   uint32_t* A = b.chunks;
   uint32_t* B = b.split_chunks;
   const int blocks = (num_tiles + 256) / 256;   // one more thread: bounds
-  k_item_counts<<<blocks, 256, 0, s>>>(tile_start, num_tiles, chunk, A, B);
+  k_item_counts<<<blocks, 256, 0, s>>>(tile_start, num_tiles, b.num_groups,
+                                       b.tile_order, chunk, A, B);
   cudaError_t e;
   e = exclusive_scan_u32(A, A, num_tiles, b.num_slots, b.scan_tmp, s);
   if (e != cudaSuccess) return e;
@@ -754,7 +770,8 @@ cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
   e = cudaMemsetAsync(b.num_split, 0, sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
   k_item_emit<<<blocks, 256, 0, s>>>(tile_start, num_tiles, b.num_groups,
-                                     chunk, A, B, b.num_slots, b.counter,
+                                     b.tile_order, chunk, A, B, b.num_slots,
+                                     b.counter,
                                      b.items, b.split_tiles, b.num_split,
                                      b.num_items, b.group_items);
   e = cudaGetLastError();

@@ -177,6 +177,9 @@ struct ItemBuffers {
   uint32_t* num_split;    // [1]
   uint32_t* counter;      // [1] work counter of the persistent kernel
   void* scan_tmp;
+  // Queue order of the tiles within a group: rank r of group g is virtual
+  // tile g * T + tile_order[r] (T = tiles per group); null = tile order.
+  const int* tile_order = nullptr;
 };
 cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
                                uint32_t num_records, uint32_t chunk,
