@@ -123,6 +123,7 @@ struct DeviceState {
   cudaEvent_t grid_ready = nullptr;
   cudaEvent_t spans_ready = nullptr;
   cudaEvent_t top_done = nullptr;   // upper tile rows final (split pass)
+  cudaEvent_t top_up = nullptr;     // upper grid rows uploaded
   uint32_t* h_spans = nullptr;
   static constexpr int kSpanCap = 2 * (kMaxGridSize / 64 + 2);
   // Bytes the last host-pointer gridding call copied each way.
@@ -476,11 +477,16 @@ struct gg_plan {
   // (when spans_async) is recorded once they have reached h_spans.
   uint32_t* h_spans = nullptr;
   int h_spans_cap = 0;
-  // Split pass (single-grid calls, when split_event is set): the last
-  // plane group is gridded in two passes by tile rows and split_event is
-  // recorded once rows below split_tv are final; split_launched says the
-  // last call did so.
+  // Split passes (single-grid calls, when split_event is set and
+  // split_row > 0): the first and the last plane group are gridded in two
+  // passes by tile rows, rows [0, split_row) first (TileGeom::split_tv).
+  // The first group's upper pass waits for split_wait (the upper rows'
+  // upload) and its lower pass for grid_wait; split_event is recorded once
+  // the upper rows are final.  split_launched says the last call recorded
+  // it, split_tv is that call's split in tile rows.
   cudaEvent_t split_event = nullptr;
+  cudaEvent_t split_wait = nullptr;
+  int split_row = 0;
   bool split_launched = false;
   int split_tv = 0;
   cudaEvent_t spans_ready = nullptr;
@@ -860,27 +866,30 @@ int bin_records(gg_plan* plan, const gg_kernels* K, size_t n,
                                    tile_u_of_shape(shape)) *
                                   ((grid_size + tile_v_of_shape(shape) - 1) /
                                    tile_v_of_shape(shape)));
-  // A split last pass needs one more group, so one more key bit.  It pays
-  // only on large grids: on a small one the copy it overlaps is shorter
-  // than the extra pass's tail (2048^2 FP32: 4 % slower end to end; 8192^2:
-  // 6 % faster).
+  // Split passes need up to two more groups, so key bits for them.  The
+  // caller sets split_row (a multiple of every tile height) only on large
+  // grids, where the copies they overlap outweigh the extra passes' tails.
   const int spare = 32 - base_bits;
-  const int tiles_v = (grid_size + tile_v_of_shape(shape) - 1) /
-                      tile_v_of_shape(shape);
-  const bool split = plan->split_event && num_grids == 1 && spare >= 1 &&
-                     tiles_v >= 2 &&
-                     (size_t)grid_size * grid_size * 2 * sizeof(Real) >=
-                         ((size_t)128 << 20);
+  const int tile_v = tile_v_of_shape(shape);
+  const bool split = plan->split_event && num_grids == 1 && spare >= 2 &&
+                     plan->split_row > 0 && plan->split_row < grid_size &&
+                     plan->split_row % tile_v == 0;
   int pgroups = 1;
   GG_TRY(plane_groups(plan, K,
                       spare <= 0 ? 1
-                                 : (1 << std::min(6, spare)) - (split ? 1 : 0),
+                                 : (1 << std::min(6, spare)) - (split ? 2 : 0),
                       s, &pgroups));
-  const int num_groups = pgroups + (split ? 1 : 0);
+  // One plane group: its two passes serve both the upload and the copy
+  // back.  Otherwise the first group's split waits for the upload in two
+  // halves and the last group's split overlaps the copy back.
+  const int split_mask = !split ? 0 : (pgroups == 1 ? 1 : 3);
+  const int num_groups =
+      pgroups + (split_mask & 1) + ((split_mask >> 1) & 1);
   TileGeom geom = make_geom(shape, grid_size, num_grids, K, &key_bits,
                             plan->sort_detail, num_groups,
                             plan->plane_group.as<int>());
-  geom.split_tv = split ? tiles_v / 2 : 0;
+  geom.split_tv = split ? plan->split_row / tile_v : 0;
+  geom.split_mask = split_mask;
   const int num_tiles = num_groups * geom.tiles_total;
   plan->stats.num_plane_groups = pgroups;
   plan->split_tv = geom.split_tv;
@@ -1072,15 +1081,25 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
   GG_TRY(build_work_items<Real>(plan, b, num_ctas, true, s, &ib));
   plan->kept.rec_vis = b.vals;
   plan->kept.num_ctas = num_ctas;
-  if (plan->grid_wait) GG_CUDA(cudaStreamWaitEvent(s, plan->grid_wait, 0));
+  // Per pass: the upload it waits for, and the event of the last upper pass.
+  std::vector<cudaEvent_t> wait_before(geom.num_groups, nullptr);
+  std::vector<cudaEvent_t> record_after(geom.num_groups, nullptr);
+  wait_before[0] = plan->grid_wait;
+  if (geom.split_mask & 1) {
+    if (plan->split_wait) wait_before[0] = plan->split_wait;
+    wait_before[1] = plan->grid_wait;
+  }
+  const int upper_done = (geom.split_mask & 2) ? geom.num_groups - 2
+                         : geom.split_mask == 1 ? 0
+                                                : -1;
+  if (upper_done >= 0) record_after[upper_done] = plan->split_event;
   plan->mark(3, s);
   GG_CUDA(launch_grid_tiles<Real>(
       ib.items, ib.group_items, ib.counter, sc + kDeviceError, b.vals,
       po.cell, po.meta, po.vw, view, geom, grid_size, d_grid, grid_stride,
       plan->partials.as<Real>(), ib.split_tiles, ib.num_split, b.num_tiles,
-      num_ctas, b.stage, s, geom.split_tv > 0 ? geom.num_groups - 2 : -1,
-      geom.split_tv > 0 ? plan->split_event : nullptr));
-  plan->split_launched = geom.split_tv > 0;
+      num_ctas, b.stage, s, wait_before.data(), record_after.data()));
+  plan->split_launched = upper_done >= 0;
   plan->mark(4, s);
   plan->mark(5, s);
   // per plane group the gridding pass and its partial reduction
@@ -1369,7 +1388,7 @@ int ensure_copy_stream(DeviceState* st) {
     GG_CUDA(cudaStreamCreateWithFlags(&st->copy_stream,
                                       cudaStreamNonBlocking));
   for (cudaEvent_t* e : {&st->vis_ready, &st->grid_ready, &st->spans_ready,
-                         &st->top_done})
+                         &st->top_done, &st->top_up})
     if (!*e) GG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   if (!st->h_spans)
     GG_CUDA(cudaMallocHost(&st->h_spans,
@@ -1454,9 +1473,26 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
                             cudaMemcpyHostToDevice, cs));
   }
   GG_CUDA(cudaEventRecord(st->vis_ready, cs));
-  if (n)
+  // On grids of 128 MiB and more the grid goes up in two halves by rows
+  // (the split a multiple of 256 rows, so of every tile height): the
+  // first plane group's upper pass waits for the upper half only, and the
+  // upper rows go back while the last group's lower pass runs.  On smaller
+  // grids the copies those passes would overlap are shorter than the extra
+  // passes' tails (2048^2 FP32: 4 % slower end to end).
+  const int split_row =
+      grid_bytes >= ((size_t)128 << 20) ? grid_size / 2 / 256 * 256 : 0;
+  if (n && split_row > 0) {
+    const size_t upper = (size_t)split_row * row_bytes;
+    GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, upper,
+                            cudaMemcpyHostToDevice, cs));
+    GG_CUDA(cudaEventRecord(st->top_up, cs));
+    GG_CUDA(cudaMemcpyAsync(plan->in_grid.as<char>() + upper,
+                            (const char*)grid + upper, grid_bytes - upper,
+                            cudaMemcpyHostToDevice, cs));
+  } else if (n) {
     GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, grid_bytes,
                             cudaMemcpyHostToDevice, cs));
+  }
   GG_CUDA(cudaEventRecord(st->grid_ready, cs));
   GG_CUDA(cudaStreamWaitEvent(s, st->vis_ready, 0));
   const double norm_in = *norm;
@@ -1468,6 +1504,8 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   plan->spans_ready = st->spans_ready;
   plan->spans_written = false;
   plan->split_event = st->top_done;
+  plan->split_wait = split_row > 0 ? st->top_up : nullptr;
+  plan->split_row = split_row;
   plan->split_launched = false;
   const int rc = grid_pipeline<Real>(plan, K, n, plan->in_uu.as<Real>(),
                                      plan->in_vv.as<Real>(),
@@ -1481,6 +1519,8 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   plan->h_spans = nullptr;
   plan->spans_ready = nullptr;
   plan->split_event = nullptr;
+  plan->split_wait = nullptr;
+  plan->split_row = 0;
   GG_TRY(rc);
   // Copy back only what the call can have changed: cells outside every tile
   // that holds records were neither read nor written on the device, so the

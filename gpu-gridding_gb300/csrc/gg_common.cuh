@@ -169,10 +169,13 @@ struct TileGeom {
   int num_groups;            // plane groups (passes), >= 1
   int tiles_total;           // num_grids * tiles_u * tiles_v
   const int* plane_group;    // [P] group of each plane (num_groups > 1)
-  // > 0: the last plane group is gridded in two passes, tile rows below
-  // split_tv first; its records in rows >= split_tv form the extra final
-  // group num_groups - 1 (single-grid calls).
+  // > 0: plane groups are gridded in two passes by tile rows (rows below
+  // split_tv first) -- the first plane group when bit 0 of split_mask is
+  // set, the last one when bit 1 is (single-grid calls).  Virtual groups:
+  // [first upper, first lower,] middle groups..., [last upper, last lower];
+  // num_groups counts them all.
   int split_tv;
+  int split_mask;
 };
 
 // Work item of the gridding kernel: a range of sorted records of one tile.

@@ -828,7 +828,8 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                               Real* partials, const int4* split_tiles,
                               const uint32_t* num_split, int max_split,
                               int num_ctas, bool stage, cudaStream_t s,
-                              int event_group, cudaEvent_t event) {
+                              const cudaEvent_t* wait_before,
+                              const cudaEvent_t* record_after) {
   GridArgs<Real> a;
   a.items = items;
   a.group_items = group_items;
@@ -855,6 +856,10 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
   void* args[] = {&a};
   for (int g = 0; g < geom.num_groups; ++g) {
     a.group = g;
+    if (wait_before && wait_before[g]) {
+      e = cudaStreamWaitEvent(s, wait_before[g], 0);
+      if (e != cudaSuccess) return e;
+    }
     e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     e = cudaLaunchKernel(fn, dim3(num_ctas), dim3(kThreads), args, smem, s);
@@ -863,8 +868,8 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                                   partials, geom, g, grid_size, grid,
                                   grid_stride, s);
     if (e != cudaSuccess) return e;
-    if (event && g == event_group) {
-      e = cudaEventRecord(event, s);
+    if (record_after && record_after[g]) {
+      e = cudaEventRecord(record_after[g], s);
       if (e != cudaSuccess) return e;
     }
   }
@@ -877,11 +882,11 @@ template cudaError_t launch_grid_tiles<float>(
     const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
     float*, long long, float*, const int4*, const uint32_t*, int, int, bool,
-    cudaStream_t, int, cudaEvent_t);
+    cudaStream_t, const cudaEvent_t*, const cudaEvent_t*);
 template cudaError_t launch_grid_tiles<double>(
     const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
     double*, long long, double*, const int4*, const uint32_t*, int, int, bool,
-    cudaStream_t, int, cudaEvent_t);
+    cudaStream_t, const cudaEvent_t*, const cudaEvent_t*);
 
 }  // namespace gg

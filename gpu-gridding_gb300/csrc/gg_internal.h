@@ -187,7 +187,9 @@ cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
 // One persistent launch per plane group, in group order, each followed by
 // the reduction of that group's split tiles (grid += their partials in
 // chunk order, FP64): the grid takes the groups' contributions in order.
-// When event is set it is recorded on s after group event_group's pass.
+// wait_before[g] / record_after[g] (arrays of num_groups events, entries
+// may be null): s waits for the first before group g's pass and records
+// the second after it (and its reduction).
 template <typename Real>
 cudaError_t launch_grid_tiles(const WorkItem* items,
                               const uint32_t* group_items,
@@ -199,8 +201,8 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                               Real* partials, const int4* split_tiles,
                               const uint32_t* num_split, int max_split,
                               int num_ctas, bool stage, cudaStream_t s,
-                              int event_group = -1,
-                              cudaEvent_t event = nullptr);
+                              const cudaEvent_t* wait_before = nullptr,
+                              const cudaEvent_t* record_after = nullptr);
 // stage: the kernel variant that stages kernel slices in shared memory.
 template <typename Real>
 int grid_tiles_ctas_per_sm(int tile_u, bool stage);

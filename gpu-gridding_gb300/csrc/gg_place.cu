@@ -187,9 +187,15 @@ __global__ void k_emit(const uint32_t* __restrict__ cell,
                       (uint32_t)tv * g.tiles_u + (uint32_t)tu;
       if (g.num_groups > 1) {
         uint32_t group = g.plane_group ? (uint32_t)g.plane_group[plane] : 0u;
-        if (g.split_tv > 0 && group == (uint32_t)g.num_groups - 2 &&
-            tv >= g.split_tv)
-          ++group;
+        if (g.split_tv > 0) {
+          const uint32_t lower = tv >= g.split_tv ? 1u : 0u;
+          const uint32_t last = (uint32_t)(g.num_groups - 1 -
+                                           __popc((unsigned)g.split_mask));
+          uint32_t v = group;
+          if (g.split_mask & 1) v = group == 0 ? lower : group + 1;
+          if ((g.split_mask & 2) && group == last) v += lower;
+          group = v;
+        }
         tile += group * (uint32_t)g.tiles_total;
       }
       keys[pos] = low_bits >= 32 ? low : ((tile << low_bits) | low);

@@ -343,14 +343,22 @@ def test_unusual_parameters_vs_oracle(pkg, oracle_mod, synthetic, torch, os_,
     assert max_rel(gd, gr) <= 1e-12
 
 
-def _start_grid(G, seed):
-    return np.random.default_rng(seed).standard_normal(
-        (G, G, 2)).astype(np.float32)
+def _start_grid(G, seed, pinned=False, dtype=np.float32, torch=None):
+    """Random starting grid; pinned=True puts it in page-locked memory (the
+    drop-in's copies then run asynchronously on the copy engines)."""
+    g = np.random.default_rng(seed).standard_normal((G, G, 2)).astype(dtype)
+    if not pinned:
+        return g
+    t = torch.empty((G, G, 2), dtype=getattr(torch, np.dtype(dtype).name),
+                    pin_memory=True)
+    t.numpy()[...] = g
+    return t.numpy()
 
 
+@pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("where", ["disk", "patch_centre", "patch_corner"])
 def test_dropin_copies_back_touched_spans(pkg, oracle_mod, synthetic, torch,
-                                          where):
+                                          where, pinned):
     """The host-pointer call copies back only the tile rows' spans that
     hold records.  With a random starting grid the result must be start +
     the contributions everywhere, and bit-for-bit the start wherever
@@ -370,7 +378,7 @@ def test_dropin_copies_back_touched_spans(pkg, oracle_mod, synthetic, torch,
                 vv=(wl.vv - np.float32(0.4 * extent)).astype(np.float32))
     start = _start_grid(G, 3)
     g0, ns0, nm0 = pkg.grid_f(wl)
-    g1, ns1, nm1 = pkg.grid_f(wl, start.copy(), 2.0)
+    g1, ns1, nm1 = pkg.grid_f(wl, _start_grid(G, 3, pinned, torch=torch), 2.0)
     assert ns1 == ns0 < wl.num_points
     assert abs(nm1 - (nm0 + 2.0)) <= 1e-12 * abs(nm1)
     assert max_rel(g1, start + g0) <= 1e-6
@@ -382,22 +390,31 @@ def test_dropin_copies_back_touched_spans(pkg, oracle_mod, synthetic, torch,
     assert max_rel(g0, gr) <= 1e-5
 
 
+@pytest.mark.parametrize("groups_mb", [0, 1])
+@pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("prec", ["f", "d"])
-def test_dropin_split_last_pass(pkg, oracle_mod, synthetic, torch, prec):
-    """On grids of 128 MiB and more the host-pointer call grids the last
-    plane group in two passes by tile rows and copies the upper rows back
-    while the lower ones are gridded: a random starting grid must still
-    come back as start + contributions, bit for bit where nothing was
-    added, with the reference's placement."""
+def test_dropin_split_passes(pkg, oracle_mod, synthetic, torch, prec, pinned,
+                             groups_mb):
+    """On grids of 128 MiB and more the host-pointer call uploads the grid
+    in two halves by rows and grids the first and last plane groups (or
+    the only one) in two passes by tile rows, the upper rows first, and
+    copies the upper rows back while the lower ones are gridded.  A random
+    starting grid must still come back as start + contributions, bit for
+    bit where nothing was added, with the reference's placement; with one
+    plane group and with several (1 MiB groups)."""
     G = 4096
     wl = synthetic.random_uniform_workload(
         "split", 60_000, G, 64, 2, 16, seed=23, cell_size_rad=1.2e-5,
         sigma_frac=0.15, clip_frac=0.45)
     dt = np.float32 if prec == "f" else np.float64
     grid_fn = pkg.grid_f if prec == "f" else pkg.grid_d
-    start = np.random.default_rng(8).standard_normal((G, G, 2)).astype(dt)
-    g0, ns0, nm0 = grid_fn(wl)
-    g1, ns1, nm1 = grid_fn(wl, start.copy(), 1.5)
+    start = _start_grid(G, 8, dtype=dt)
+    pkg.set_host_tuning({"plane_group_mb": groups_mb})
+    try:
+        g0, ns0, nm0 = grid_fn(wl)
+        g1, ns1, nm1 = grid_fn(wl, _start_grid(G, 8, pinned, dt, torch), 1.5)
+    finally:
+        pkg.set_host_tuning(None)
     assert ns1 == ns0 < wl.num_points
     assert max_rel(g1, start + g0) <= (1e-6 if prec == "f" else 1e-14)
     untouched = g0 == 0
@@ -432,8 +449,12 @@ def test_dropin_transfer_bytes(pkg, synthetic, torch):
                                     * wl.oversample - 1))
     cube = int((ext.astype(np.int64) ** 2).sum()) * 8
     assert cube < wl.conv_func.nbytes
-    assert h2d == cube + wl.num_w_planes * 20 + 24 * n + 8 * G * G + 8
+    stack_and_inputs = cube + wl.num_w_planes * 20 + 24 * n + 8
+    assert h2d == stack_and_inputs + 8 * G * G
     assert 0 < d2h < G * G * 8 // 10
+    # A pinned grid moves the same bytes.
+    pkg.grid_f(wl, _start_grid(G, 1, True, torch=torch))
+    assert pkg.host_last_transfer() == (h2d, d2h)
     empty = dataclasses.replace(wl, uu=wl.uu[:0], vv=wl.vv[:0],
                                 ww=wl.ww[:0], vis=wl.vis[:0],
                                 weight=wl.weight[:0])
@@ -455,6 +476,9 @@ def test_dropin_nothing_gridded_leaves_grid(pkg, synthetic, torch):
     g, ns, nm = pkg.grid_f(wl, start.copy(), 3.5)
     assert ns == wl.num_points
     assert nm == 3.5
+    assert np.array_equal(g, start)
+    g, ns, nm = pkg.grid_f(wl, _start_grid(G, 4, True, torch=torch), 3.5)
+    assert ns == wl.num_points and nm == 3.5
     assert np.array_equal(g, start)
     empty = dataclasses.replace(wl, uu=wl.uu[:0], vv=wl.vv[:0], ww=wl.ww[:0],
                                 vis=wl.vis[:0], weight=wl.weight[:0])
