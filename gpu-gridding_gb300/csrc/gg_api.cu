@@ -983,18 +983,23 @@ int tile_queue_order(gg_plan* plan, const TileGeom& g, int grid_size,
 }
 
 // The work-item queue of binned records for num_ctas persistent CTAs: heavy
-// tiles are split into items of `chunk` records so that the call has about
-// items_per_cta items per CTA.  Items: at most one more per tile than
+// tiles are split into items of `chunk` records so that each of the call's
+// `passes` launches has about items_per_cta items per CTA (the gridding
+// passes of the groups; one launch for degridding).  Items: at most one
+// more per tile than
 // total / chunk; partial-tile slots (split tiles only): at most
 // 2 * total / chunk, each a tile of partial sums when partial_tiles is set
 // (gridding; the degridder's items write no tile).
 template <typename Real>
-int build_work_items(gg_plan* plan, const Bins& b, int num_ctas,
+int build_work_items(gg_plan* plan, const Bins& b, int num_ctas, int passes,
                      bool partial_tiles, cudaStream_t s, ItemBuffers* ib) {
   using R2 = typename Vec2<Real>::type;
   uint32_t* sc = plan->scalars.as<uint32_t>();
   const int num_tiles = b.num_tiles;
-  const unsigned long long f = (unsigned long long)plan->items_per_cta;
+  // items_per_cta items per CTA in each of the call's passes: every pass
+  // ends with a tail up to one item long.
+  const unsigned long long f =
+      (unsigned long long)plan->items_per_cta * (unsigned long long)passes;
   const uint32_t chunk = (uint32_t)std::max<unsigned long long>(
       64, ((unsigned long long)b.total + f * num_ctas - 1) / (f * num_ctas));
   const size_t item_cap = (size_t)num_tiles + 2 * f * (size_t)num_ctas + 16;
@@ -1078,7 +1083,8 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
   const int num_ctas = sms * per_sm;
   plan->stats.slice_staging = b.stage ? 1 : 0;
   ItemBuffers ib;
-  GG_TRY(build_work_items<Real>(plan, b, num_ctas, true, s, &ib));
+  GG_TRY(build_work_items<Real>(plan, b, num_ctas, geom.num_groups, true, s,
+                                &ib));
   plan->kept.rec_vis = b.vals;
   plan->kept.num_ctas = num_ctas;
   // Per pass: the upload it waits for, and the event of the last upper pass.
@@ -1353,7 +1359,7 @@ int degrid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   if (plan->ctas_per_sm > 0) per_sm = std::min(per_sm, plan->ctas_per_sm);
   const int num_ctas = sms * per_sm;
   ItemBuffers ib;
-  GG_TRY(build_work_items<Real>(plan, b, num_ctas, false, s, &ib));
+  GG_TRY(build_work_items<Real>(plan, b, num_ctas, 1, false, s, &ib));
   GG_TRY(plan->rec_out.ensure((size_t)b.total * 2 * sizeof(Real)));
   uint32_t* sc = plan->scalars.as<uint32_t>();
   GG_CUDA(launch_degrid_tiles<Real>(
