@@ -33,7 +33,7 @@ from typing import Callable, Dict, Iterable, Optional
 import numpy as np
 
 CACHE_ENV = "GPUGRID_TUNE_CACHE"
-CACHE_VERSION = 4
+CACHE_VERSION = 5
 
 #: The plan's settings before any tuning (each call chooses shape/staging).
 DEFAULT_TUNING = {"tile_u": 0, "slice_staging": -1, "items_per_cta": 4,

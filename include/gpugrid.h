@@ -178,9 +178,10 @@ GG_API int gg_plan_set_slice_staging(gg_plan* plan, int mode);
  * or num_skipped).
  *   tile_u         32, 16 or 8 (cells across a tile); 0 = chosen per call
  *   slice_staging  -1 chosen per call, 0 off, 1 on (bit-identical results)
- *   items_per_cta  work items per persistent CTA that the split of heavy
- *                  tiles aims for, 1..64 (default 4): more items balance
- *                  the load better but write more partial tiles
+ *   items_per_cta  work items per persistent CTA in each gridding pass
+ *                  that the split of heavy tiles aims for, 1..64 (default
+ *                  4): more items balance the load better but write more
+ *                  partial tiles
  *   sort_detail    order of a tile's records: 2 (default) by w-plane then
  *                  kernel-offset class, 1 by w-plane, 0 visibility order
  *   ctas_per_sm    resident gridding CTAs per SM, 0 (default) = as many as
