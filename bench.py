@@ -190,6 +190,23 @@ def rank_info():
             int(os.environ.get("WORLD_SIZE", "1")))
 
 
+def max_over_ranks(x, dist=None, device="cpu"):
+    """The largest x over the ranks of the process group (x itself when
+    dist is None): the job's step time is its slowest replica's."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world, units_per_rank, seconds):
+    """Whole-job rate in millions of units per second: every one of the
+    world replicas processed units_per_rank in (at most) seconds."""
+    return world * units_per_rank / seconds / 1e6
+
+
 def load_workload(name):
     synthetic = importlib.import_module("gpu-gridding_gb300.synthetic")
     return synthetic.WORKLOADS[name]()
@@ -441,14 +458,10 @@ def run_ours(args):
         barrier()
         ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
     clk = clocks.stop()
-    ms_max = ms
-    if dist is not None:
-        t = torch.tensor([ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
+    ms_max = max_over_ranks(ms, dist, dev)
     stats = plan.stats()
     num_vis = wl.num_points
-    value = world * num_vis / (ms_max * 1e-3) / 1e6
+    value = replica_throughput(world, num_vis, ms_max * 1e-3)
     macs = stats["num_macs"]
     gflops = world * 8.0 * macs / (ms_max * 1e-3) / 1e9
 
@@ -501,14 +514,11 @@ def run_ours(args):
         for _ in range(args.e2e_steps):
             e2e_step()
         te = (time.perf_counter() - te) / args.e2e_steps
-        if dist is not None:
-            t = torch.tensor([te], dtype=torch.float64, device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            te = float(t.item())
+        te = max_over_ranks(te, dist, dev)
         # Bytes the drop-in copied in its last call (every step copies the
         # same): the grid comes back only where tiles hold records.
         h2d, d2h = pkg.host_last_transfer()
-        e2e = {"value": world * num_vis / te / 1e6, "unit": UNIT,
+        e2e = {"value": replica_throughput(world, num_vis, te), "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
     # The operations either side of the gridder on the same workload: the
