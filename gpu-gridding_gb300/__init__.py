@@ -39,6 +39,7 @@ EXPORTED_SYMBOLS = (
     "gg_plan_destroy", "gg_plan_last_stats", "gg_plan_set_tile_shape",
     "gg_plan_set_slice_staging", "gg_plan_set_tuning", "gg_plan_get_tuning",
     "gg_host_set_tuning", "gg_host_get_tuning", "gg_host_last_transfer",
+    "gg_plan_probe_bounded_wait",
     "gg_plan_set_profiling",
     "gg_plan_phase_ms", "gg_measure_fp32_fma_tflops", "gg_grid_wproj_f_device",
     "gg_grid_wproj_f_device_noalloc", "gg_grid_wproj_f_batched_device",
@@ -189,6 +190,8 @@ def _declare(L):
     L.gg_host_get_tuning.restype = ctypes.c_int
     L.gg_host_last_transfer.argtypes = [ctypes.POINTER(ctypes.c_ulonglong)] * 2
     L.gg_host_last_transfer.restype = ctypes.c_int
+    L.gg_plan_probe_bounded_wait.argtypes = [_vp, ctypes.c_uint, _vp]
+    L.gg_plan_probe_bounded_wait.restype = ctypes.c_int
     L.gg_plan_check.argtypes = [_vp, _vp]
     L.gg_plan_check.restype = ctypes.c_int
     L.gg_plan_set_profiling.argtypes = [_vp, ctypes.c_int]
@@ -422,6 +425,12 @@ class Plan:
         t = Tuning()
         _check(lib().gg_plan_get_tuning(self.handle, ctypes.byref(t)))
         return t.as_dict()
+
+    def probe_bounded_wait(self, iterations: int = 1000, stream=None) -> None:
+        """Run the failure-path probe (gg_plan_probe_bounded_wait): raises
+        GridError, and the plan reports the error from then on."""
+        _check(lib().gg_plan_probe_bounded_wait(
+            self.handle, int(iterations), _stream_ptr(stream)))
 
     def set_profiling(self, enable: bool = True) -> None:
         _check(lib().gg_plan_set_profiling(self.handle, int(enable)))

@@ -2455,6 +2455,23 @@ GG_API void oskar_degrid_wproj_d(const size_t num_w_planes,
             gg_last_error());
 }
 
+GG_API int gg_plan_probe_bounded_wait(gg_plan* plan, unsigned iterations,
+                                      void* stream) {
+  t_last_error.clear();
+  if (!plan) return set_error(GG_ERR_INVALID_ARG, "plan is NULL");
+  if (iterations < 1 || iterations > (1u << 20))
+    return set_error(GG_ERR_INVALID_ARG,
+                     "iterations = %u outside [1, 1048576]", iterations);
+  int dev;
+  GG_TRY(current_device(&dev));
+  if (dev != plan->device)
+    return set_error(GG_ERR_INVALID_ARG, "plan and current device differ");
+  cudaStream_t s = (cudaStream_t)stream;
+  GG_CUDA(launch_wait_probe(iterations,
+                            plan->scalars.as<uint32_t>() + kDeviceError, s));
+  return check_device_error(plan, s);
+}
+
 GG_API int gg_plan_check(gg_plan* plan, void* stream) {
   t_last_error.clear();
   if (!plan) return set_error(GG_ERR_INVALID_ARG, "plan is NULL");

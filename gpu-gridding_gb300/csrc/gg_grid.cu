@@ -617,6 +617,17 @@ __global__ void k_touched_spans(const uint32_t* __restrict__ tile_start,
 
 // A[t] = chunks of tile t if it is split (more than one chunk), else 0;
 // B[t] = 1 if tile t has exactly one chunk.
+// Failure-path probe: every thread waits, bounded by `limit` probes, on an
+// mbarrier that nothing arrives at -- the wait the gridding kernels use --
+// so the wait runs out, the kernel sets the error flag and returns.
+__global__ void k_wait_probe(unsigned limit, uint32_t* __restrict__ error) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  const bool ok = mbar_wait(&bar, 0, limit);
+  if (!ok && threadIdx.x == 0) atomicExch(error, 1u);
+}
+
 // Virtual tile at queue rank i (see ItemBuffers::tile_order).
 __device__ __forceinline__ int tile_at_rank(int i, int T,
                                             const int* __restrict__ order) {
@@ -740,6 +751,12 @@ cudaError_t launch_tile_bounds(const uint32_t* keys, uint32_t n, int shift,
   const long long work = (long long)n + 1;
   const int blocks = (int)std::min<long long>((work + 255) / 256, 65536);
   k_tile_bounds<<<blocks, 256, 0, s>>>(keys, n, shift, num_tiles, tile_start);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wait_probe(unsigned limit, uint32_t* error,
+                              cudaStream_t s) {
+  k_wait_probe<<<1, 64, 0, s>>>(limit, error);
   return cudaGetLastError();
 }
 

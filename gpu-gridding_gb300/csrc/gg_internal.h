@@ -153,6 +153,10 @@ cudaError_t launch_batch_totals(const uint32_t* meta, const double* nterm,
 cudaError_t launch_tile_bounds(const uint32_t* keys, uint32_t n, int shift,
                                int num_tiles, uint32_t* tile_start,
                                cudaStream_t s);
+// One CTA whose threads wait, bounded by `limit` probes, on an mbarrier
+// that nothing arrives at, then set *error (see gg_plan_probe_bounded_wait).
+cudaError_t launch_wait_probe(unsigned limit, uint32_t* error,
+                              cudaStream_t s);
 // Touched spans of a single-grid call: for every virtual tile t holding
 // records (tile_start[t + 1] > tile_start[t]), with real tile r = t mod
 // tiles_total at row r / tiles_u and column r mod tiles_u, lo[row] takes the

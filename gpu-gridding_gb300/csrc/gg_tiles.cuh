@@ -69,9 +69,10 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 // Acquire-wait for the completion of the phase with the given parity;
-// false when the bound runs out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (unsigned i = 0; i < kWaitLimit; ++i) {
+// false when `limit` probes have failed.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          unsigned limit = kWaitLimit) {
+  for (unsigned i = 0; i < limit; ++i) {
     if (mbar_test(bar, parity)) return true;
     if (i >= 32) __nanosleep(64);
   }

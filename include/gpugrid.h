@@ -314,6 +314,15 @@ GG_API int gg_grid_wproj_d_batched_replay(gg_plan* plan,
  * this plan flagged a failure (a bounded wait that ran out). */
 GG_API int gg_plan_check(gg_plan* plan, void* stream);
 
+/* Diagnostic of that failure path, safe to run: a kernel waits, bounded by
+ * `iterations` probes (1..1048576, each failed probe sleeping ~64 ns), on
+ * an mbarrier that nothing arrives at -- the kind of wait the gridding
+ * kernels bound -- so the wait runs out, the kernel sets the plan's error
+ * flag and returns.  Returns GG_ERR_CUDA (with its message) as the plan
+ * then does from every call; the device and other plans stay usable. */
+GG_API int gg_plan_probe_bounded_wait(gg_plan* plan, unsigned iterations,
+                                      void* stream);
+
 /* Allocation-free form of gg_grid_wproj_f_device, for callers that cannot
  * allocate device memory while they grid (a real-time loop that must not
  * stall on cudaMalloc, or code running under another framework's memory
