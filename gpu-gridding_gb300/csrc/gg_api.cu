@@ -985,7 +985,8 @@ int tile_queue_order(gg_plan* plan, const TileGeom& g, int grid_size,
 // The work-item queue of binned records for num_ctas persistent CTAs: heavy
 // tiles are split into items of `chunk` records so that each of the call's
 // `passes` launches has about items_per_cta items per CTA (the gridding
-// passes of the groups; one launch for degridding).  Items: at most one
+// passes of the groups; the degridder's single launch asks for as many
+// items as all of them).  Items: at most one
 // more per tile than
 // total / chunk; partial-tile slots (split tiles only): at most
 // 2 * total / chunk, each a tile of partial sums when partial_tiles is set
@@ -1359,7 +1360,10 @@ int degrid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   if (plan->ctas_per_sm > 0) per_sm = std::min(per_sm, plan->ctas_per_sm);
   const int num_ctas = sms * per_sm;
   ItemBuffers ib;
-  GG_TRY(build_work_items<Real>(plan, b, num_ctas, 1, false, s, &ib));
+  // One launch over the queue of all plane groups, as many items as the
+  // gridding's passes together.
+  GG_TRY(build_work_items<Real>(plan, b, num_ctas, b.num_groups, false, s,
+                                &ib));
   GG_TRY(plan->rec_out.ensure((size_t)b.total * 2 * sizeof(Real)));
   uint32_t* sc = plan->scalars.as<uint32_t>();
   GG_CUDA(launch_degrid_tiles<Real>(
