@@ -1366,6 +1366,7 @@ int degrid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
                                 &ib));
   GG_TRY(plan->rec_out.ensure((size_t)b.total * 2 * sizeof(Real)));
   uint32_t* sc = plan->scalars.as<uint32_t>();
+  if (plan->grid_wait) GG_CUDA(cudaStreamWaitEvent(s, plan->grid_wait, 0));
   GG_CUDA(launch_degrid_tiles<Real>(
       ib.items, ib.num_items, ib.counter, sc + kDeviceError, b.vals, po.cell,
       po.meta, plan->rec_offset.as<uint32_t>(), view, b.geom, grid_size,
@@ -1816,26 +1817,42 @@ int degrid_host(size_t num_w_planes, const int* support, int oversample,
   GG_TRY(plan->in_ww.ensure(n * sizeof(Real) + 16));
   GG_TRY(plan->in_vis.ensure(2 * n * sizeof(Real) + 16));
   GG_TRY(plan->in_grid.ensure(grid_bytes));
+  // As in the gridding call: the coordinates and then the grid go up on the
+  // side stream behind the kernel stack's cube; placement waits for the
+  // coordinates only, and only the degridding kernel for the grid.
+  GG_TRY(ensure_copy_stream(st));
+  struct CopyGuard {   // the side stream reads the caller's arrays
+    cudaStream_t s;
+    ~CopyGuard() { cudaStreamSynchronize(s); }
+  } copy_guard{st->copy_stream};
+  cudaStream_t cs = st->copy_stream;
   if (n) {
     GG_CUDA(cudaMemcpyAsync(plan->in_uu.p, uu, n * sizeof(Real),
-                            cudaMemcpyHostToDevice, s));
+                            cudaMemcpyHostToDevice, cs));
     GG_CUDA(cudaMemcpyAsync(plan->in_vv.p, vv, n * sizeof(Real),
-                            cudaMemcpyHostToDevice, s));
+                            cudaMemcpyHostToDevice, cs));
     GG_CUDA(cudaMemcpyAsync(plan->in_ww.p, ww, n * sizeof(Real),
-                            cudaMemcpyHostToDevice, s));
+                            cudaMemcpyHostToDevice, cs));
   }
-  GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, grid_bytes,
-                          cudaMemcpyHostToDevice, s));
-  GG_TRY(degrid_pipeline<Real>(plan, K, n, plan->in_uu.as<Real>(),
-                               plan->in_vv.as<Real>(), plan->in_ww.as<Real>(),
-                               cell_size_rad, w_scale, grid_size,
-                               plan->in_grid.as<Real>(),
-                               plan->in_vis.as<Real>(), s));
+  GG_CUDA(cudaEventRecord(st->vis_ready, cs));
+  if (n)
+    GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, grid_bytes,
+                            cudaMemcpyHostToDevice, cs));
+  GG_CUDA(cudaEventRecord(st->grid_ready, cs));
+  GG_CUDA(cudaStreamWaitEvent(s, st->vis_ready, 0));
+  plan->grid_wait = st->grid_ready;
+  const int rc = degrid_pipeline<Real>(
+      plan, K, n, plan->in_uu.as<Real>(), plan->in_vv.as<Real>(),
+      plan->in_ww.as<Real>(), cell_size_rad, w_scale, grid_size,
+      plan->in_grid.as<Real>(), plan->in_vis.as<Real>(), s);
+  plan->grid_wait = nullptr;
+  GG_TRY(rc);
   if (n)
     GG_CUDA(cudaMemcpyAsync(vis, plan->in_vis.p, 2 * n * sizeof(Real),
                             cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaStreamSynchronize(s));
-  return GG_OK;
+  GG_CUDA(cudaStreamSynchronize(cs));
+  return check_device_error(plan, s);
 }
 
 template <typename Real>

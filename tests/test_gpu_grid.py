@@ -390,19 +390,20 @@ def test_dropin_copies_back_touched_spans(pkg, oracle_mod, synthetic, torch,
     assert max_rel(g0, gr) <= 1e-5
 
 
+@pytest.mark.parametrize("G", [4096, 4099])
 @pytest.mark.parametrize("groups_mb", [0, 1])
 @pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("prec", ["f", "d"])
 def test_dropin_split_passes(pkg, oracle_mod, synthetic, torch, prec, pinned,
-                             groups_mb):
+                             groups_mb, G):
     """On grids of 128 MiB and more the host-pointer call uploads the grid
     in two halves by rows and grids the first and last plane groups (or
     the only one) in two passes by tile rows, the upper rows first, and
     copies the upper rows back while the lower ones are gridded.  A random
     starting grid must still come back as start + contributions, bit for
     bit where nothing was added, with the reference's placement; with one
-    plane group and with several (1 MiB groups)."""
-    G = 4096
+    plane group and with several (1 MiB groups), on an even grid and on an
+    odd one (ragged last tiles; the split row a multiple of 256)."""
     wl = synthetic.random_uniform_workload(
         "split", 60_000, G, 64, 2, 16, seed=23, cell_size_rad=1.2e-5,
         sigma_frac=0.15, clip_frac=0.45)
