@@ -41,6 +41,7 @@ sys.path.insert(0, HERE)
 METRIC = ("Mvis/s & GFLOP/s on 1 GB300, batched vs plain, grid err "
           "≤1e-5 vs FP64 oracle")
 UNIT = "Mvis/s"
+GRID_TOL = 1e-5     # max |grid - FP64 oracle| / max |FP64 oracle|
 PUBLISHED_P100_MVIS = {"cfg1": 2152800 / 0.074 / 1e6,
                        "cfg2": 31395840 / 0.781 / 1e6,
                        "cfg2b": 31395840 / 0.553 / 1e6}
@@ -165,6 +166,9 @@ def parse_args():
                     choices=sorted(WORKLOAD_TEXT))
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the grid-error check against the FP64 "
+                         "oracle (runs after the timed region)")
     ap.add_argument("--tile-shape", type=int, default=0,
                     help="force the tile width (32, 16, 8); 0 = automatic")
     ap.add_argument("--staging", type=int, default=-1,
@@ -307,13 +311,55 @@ def gpu_uuid(torch, dev):
 # ---------------------------------------------------------------------------
 # CPU runs (reference algorithm on the host cores)
 # ---------------------------------------------------------------------------
-def cpu_run(wl, threads):
+def load_oracle():
     sys.path.insert(0, os.path.join(HERE, "oracle"))
     import oracle
+    return oracle
+
+
+def cpu_run(wl, threads, keep=False):
+    """Seconds for one host-threaded oskar_grid_wproj_f pass over the
+    workload; with keep, also the grid, skip count and norm."""
+    oracle = load_oracle()
     grid = np.zeros((wl.grid_size, wl.grid_size, 2), np.float32)
     t0 = time.perf_counter()
-    oracle.grid_f_mt(wl, grid, 0.0, threads=threads)
-    return time.perf_counter() - t0
+    _, ns, nm = oracle.grid_f_mt(wl, grid, 0.0, threads=threads)
+    t = time.perf_counter() - t0
+    return (t, grid, ns, nm) if keep else t
+
+
+def max_rel_err(a, ref):
+    """max |a - ref| / max |ref|, in FP64."""
+    a = np.asarray(a, np.float64)
+    ref = np.asarray(ref, np.float64)
+    scale = float(np.abs(ref).max())
+    err = float(np.abs(a - ref).max())
+    return err / scale if scale > 0 else err
+
+
+def accuracy_vs_fp64(wl, grid, nskip, norm, threads, cpu_result=None):
+    """The measured workload's grid against the FP64-accumulation oracle
+    (FP32 placement, no rounding in the sums): max-rel grid error, skip
+    count and norm, beside the same error of the reference's own FP32
+    gridder (the host-threaded restatement, when it ran)."""
+    oracle = load_oracle()
+    t0 = time.perf_counter()
+    g64, ns64, nm64 = oracle.grid_f_fp64acc_mt(wl, threads=threads)
+    out = {"tolerance": GRID_TOL,
+           "grid_max_rel_err": max_rel_err(grid, g64),
+           "num_skipped": int(nskip), "num_skipped_fp64": ns64,
+           "norm_rel_err": abs(norm - nm64) / abs(nm64) if nm64 else
+               abs(norm - nm64)}
+    if cpu_result is not None:
+        _, gref, ns_ref, nm_ref = cpu_result
+        out["reference_f_max_rel_err"] = max_rel_err(gref, g64)
+        out["reference_f_num_skipped"] = int(ns_ref)
+        out["reference_f_norm_rel_err"] = abs(nm_ref - nm64) / abs(nm64) \
+            if nm64 else abs(nm_ref - nm64)
+    out["ok"] = bool(out["grid_max_rel_err"] <= GRID_TOL and
+                     out["num_skipped"] == ns64)
+    out["oracle_seconds"] = time.perf_counter() - t0
+    return out
 
 
 def run_reference(args):
@@ -580,16 +626,31 @@ def run_ours(args):
         batched = measure_batched(pkg, torch, args.batched_steps,
                                   tune=tune_cache)
 
-    cpu = None
+    cpu, cpu_result = None, None
+    threads = os.cpu_count() or 1
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        tc = cpu_run(wl, threads)
+        cpu_result = cpu_run(wl, threads, keep=True)
+        tc = cpu_result[0]
         cpu = {"value": num_vis / tc / 1e6, "unit": UNIT, "cores": threads,
                "kind": "port",
                "sample": f"whole workload ({num_vis} vis), one run; the "
                          "oracle's restatement of oskar_grid_wproj_f "
                          "(bit-identical to the reference build), grid rows "
                          f"split over {threads} host threads"}
+
+    accuracy = None
+    if rank == 0 and not args.no_accuracy:
+        # One clean call on the same inputs and plan, outside the timed
+        # region, checked against the FP64 oracle.
+        grid.zero_()
+        norm.zero_()
+        nskip.zero_()
+        step()
+        torch.cuda.synchronize()
+        accuracy = accuracy_vs_fp64(wl, grid.cpu().numpy(),
+                                    int(nskip.item()), float(norm.item()),
+                                    threads, cpu_result)
+    cpu_result = None
 
     if rank == 0:
         line = {
@@ -621,6 +682,7 @@ def run_ours(args):
                 "hbm_peak_gbs": peaks.get("hbm_gbs"),
                 "hbm_peak_source": peak_kind},
             "cpu_baseline": cpu,
+            "accuracy": accuracy,
             "e2e": e2e,
             "gpu_launches": args.steps * stats["num_launches"],
             "clocks": clk,

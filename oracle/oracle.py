@@ -72,6 +72,9 @@ def lib():
         L.oracle_grid_wproj_f_mt.argtypes = [ctypes.c_int] + \
             L.oracle_grid_wproj_f.argtypes
         L.oracle_grid_wproj_f_mt.restype = ctypes.c_int
+        L.oracle_grid_wproj_f_fp64acc_mt.argtypes = [ctypes.c_int] + \
+            L.oracle_grid_wproj_f_fp64acc.argtypes
+        L.oracle_grid_wproj_f_fp64acc_mt.restype = ctypes.c_int
         L.oracle_degrid_wproj_f_fp64.argtypes = [
             _sz, _i32p, ctypes.c_int, ctypes.c_int, _f32p, _sz, _f32p, _f32p,
             _f32p, ctypes.c_float, ctypes.c_float, ctypes.c_int, _f64p, _f64p]
@@ -181,6 +184,26 @@ def grid_f_fp64acc(wl, grid=None, norm=0.0):
         _c(wl.weight, np.float32), np.float32(wl.cell_size_rad),
         np.float32(wl.w_scale), wl.grid_size, ctypes.byref(ns),
         ctypes.byref(nm), grid.reshape(-1))
+    return grid, int(ns.value), float(nm.value)
+
+
+def grid_f_fp64acc_mt(wl, grid=None, norm=0.0, threads=None):
+    """grid_f_fp64acc on host threads; bit-identical to it."""
+    grid = new_grid(wl, np.float64) if grid is None else grid
+    assert grid.dtype == np.float64 and grid.flags.c_contiguous
+    threads = threads or os.cpu_count() or 1
+    ns = ctypes.c_size_t(0)
+    nm = ctypes.c_double(norm)
+    rc = lib().oracle_grid_wproj_f_fp64acc_mt(
+        threads, wl.num_w_planes, _c(wl.support, np.int32), wl.oversample,
+        wl.conv_size_half, _c(wl.conv_func, np.float32).reshape(-1),
+        wl.num_points, _c(wl.uu, np.float32), _c(wl.vv, np.float32),
+        _c(wl.ww, np.float32), _c(wl.vis, np.float32).reshape(-1),
+        _c(wl.weight, np.float32), np.float32(wl.cell_size_rad),
+        np.float32(wl.w_scale), wl.grid_size, ctypes.byref(ns),
+        ctypes.byref(nm), grid.reshape(-1))
+    if rc != 0:
+        raise MemoryError("oracle_grid_wproj_f_fp64acc_mt: no scratch memory")
     return grid, int(ns.value), float(nm.value)
 
 

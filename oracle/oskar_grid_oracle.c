@@ -422,6 +422,7 @@ typedef struct
     const int* support;
     size_t num_w_planes;
     float cell_size_rad, w_scale;
+    double* grid64;     /* non-null: FP64 accumulation into this grid */
     int next;           /* work counter, atomically incremented */
     int phase;          /* 0: placement + tap sums, 1: gridding bands */
     size_t chunk;
@@ -471,6 +472,33 @@ static void mt_grid_band(mt_job_t* job, int band)
         j0 = r0 - p->gv; if (j0 < -p->support) j0 = -p->support;
         j1 = r1 - 1 - p->gv; if (j1 > p->support) j1 = p->support;
         if (j0 > j1) continue;
+        if (job->grid64)
+        {
+            /* Same accumulation as oracle_grid_wproj_f_fp64acc. */
+            const double conj = p->conj_neg ? -1.0 : 1.0;
+            const double w_i = job->weight[i];
+            const double v_re = w_i * (double)job->vis[2 * i];
+            const double v_im = w_i * (double)job->vis[2 * i + 1];
+            const size_t kstart = (size_t)p->plane * job->plane_stride;
+            const int s = p->support;
+            for (j = j0; j <= j1; ++j)
+            {
+                const size_t row = (size_t)(p->gv + j) * (size_t)G +
+                        (size_t)p->gu;
+                const size_t krow = kstart +
+                        (size_t)abs(p->ov + j * os) * job->conv_size_half;
+                for (k = -s; k <= s; ++k)
+                {
+                    const size_t t = (krow + abs(p->ou + k * os)) << 1;
+                    const size_t c = (row + k) << 1;
+                    const double c_re = job->conv_func[t];
+                    const double c_im = (double)job->conv_func[t + 1] * conj;
+                    job->grid64[c]     += (v_re * c_re - v_im * c_im);
+                    job->grid64[c + 1] += (v_im * c_re + v_re * c_im);
+                }
+            }
+        }
+        else
         {
             const float conj = p->conj_neg ? -1.0f : 1.0f;
             const float w_i = job->weight[i];
@@ -535,14 +563,13 @@ static void mt_run(mt_job_t* job, int num_threads)
     free(th);
 }
 
-/* Same arguments and results as oracle_grid_wproj_f, run on num_threads
- * host threads.  Returns 0, or -1 when scratch memory cannot be had. */
-ORACLE_API int oracle_grid_wproj_f_mt(int num_threads, size_t num_w_planes,
+static int mt_grid(int num_threads, size_t num_w_planes,
         const int* support, int oversample, int conv_size_half,
         const float* conv_func, size_t num_points, const float* uu,
         const float* vv, const float* ww, const float* vis,
         const float* weight, float cell_size_rad, float w_scale,
-        int grid_size, size_t* num_skipped, double* norm, float* grid)
+        int grid_size, size_t* num_skipped, double* norm, float* grid,
+        double* grid64)
 {
     size_t i, n_skip = 0;
     mt_job_t job;
@@ -558,7 +585,7 @@ ORACLE_API int oracle_grid_wproj_f_mt(int num_threads, size_t num_w_planes,
         return -1;
     }
     job.conv_func = conv_func; job.vis = vis; job.weight = weight;
-    job.grid = grid; job.num_points = num_points;
+    job.grid = grid; job.grid64 = grid64; job.num_points = num_points;
     job.plane_stride = (size_t)(conv_size_half * conv_size_half);
     job.oversample = oversample; job.conv_size_half = conv_size_half;
     job.grid_size = grid_size;
@@ -585,6 +612,36 @@ ORACLE_API int oracle_grid_wproj_f_mt(int num_threads, size_t num_w_planes,
     free((void*)job.place);
     free(job.tap_sum);
     return 0;
+}
+
+/* Same arguments and results as oracle_grid_wproj_f, run on num_threads
+ * host threads.  Returns 0, or -1 when scratch memory cannot be had. */
+ORACLE_API int oracle_grid_wproj_f_mt(int num_threads, size_t num_w_planes,
+        const int* support, int oversample, int conv_size_half,
+        const float* conv_func, size_t num_points, const float* uu,
+        const float* vv, const float* ww, const float* vis,
+        const float* weight, float cell_size_rad, float w_scale,
+        int grid_size, size_t* num_skipped, double* norm, float* grid)
+{
+    return mt_grid(num_threads, num_w_planes, support, oversample,
+            conv_size_half, conv_func, num_points, uu, vv, ww, vis, weight,
+            cell_size_rad, w_scale, grid_size, num_skipped, norm, grid, NULL);
+}
+
+/* oracle_grid_wproj_f_fp64acc on num_threads host threads: every cell
+ * receives its FP64 contributions in input order, so the grid and the norm
+ * are bit-identical to the serial function's.  Returns 0, or -1 when scratch
+ * memory cannot be had. */
+ORACLE_API int oracle_grid_wproj_f_fp64acc_mt(int num_threads,
+        size_t num_w_planes, const int* support, int oversample,
+        int conv_size_half, const float* conv_func, size_t num_points,
+        const float* uu, const float* vv, const float* ww, const float* vis,
+        const float* weight, float cell_size_rad, float w_scale,
+        int grid_size, size_t* num_skipped, double* norm, double* grid)
+{
+    return mt_grid(num_threads, num_w_planes, support, oversample,
+            conv_size_half, conv_func, num_points, uu, vv, ww, vis, weight,
+            cell_size_rad, w_scale, grid_size, num_skipped, norm, NULL, grid);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -82,6 +82,20 @@ def test_fp64_yardstick_close_to_reference_f(oracle_mod):
     assert max_rel(z["grid_out"], g64) < 1e-5
 
 
+@pytest.mark.parametrize("name", ["small_f", "edges_f", "os3_f"])
+def test_multithreaded_fp64_yardstick_bit_exact(oracle_mod, name):
+    """The host-threaded FP64 yardstick (the benchmark's error check) gives
+    the serial one's grid, norm and skip count bit for bit."""
+    wl, z = load_golden(name)
+    g1, ns1, nm1 = oracle_mod.grid_f_fp64acc(
+        wl, z["grid_in"].astype(np.float64), float(z["norm_in"]))
+    g4, ns4, nm4 = oracle_mod.grid_f_fp64acc_mt(
+        wl, z["grid_in"].astype(np.float64), float(z["norm_in"]), threads=4)
+    assert ns4 == ns1 == int(z["num_skipped"])
+    assert nm4 == nm1
+    assert np.array_equal(g4.view(np.uint8), g1.view(np.uint8))
+
+
 def test_adjoint_oracle_dot_product(oracle_mod):
     """<G x, y> = <x, G^H y> for the FP64 oracle pair."""
     wl, _ = load_golden("small_f")
