@@ -39,6 +39,8 @@ EXPORTED_SYMBOLS = (
     "gg_plan_destroy", "gg_plan_last_stats", "gg_plan_set_tile_shape",
     "gg_plan_set_slice_staging", "gg_plan_set_tuning", "gg_plan_get_tuning",
     "gg_host_set_tuning", "gg_host_get_tuning", "gg_host_last_transfer",
+    "gg_host_set_grid_access", "gg_host_get_grid_access",
+    "gg_host_set_profiling", "gg_host_phase_ms",
     "gg_plan_probe_bounded_wait",
     "gg_plan_set_profiling",
     "gg_plan_phase_ms", "gg_measure_fp32_fma_tflops", "gg_grid_wproj_f_device",
@@ -190,6 +192,15 @@ def _declare(L):
     L.gg_host_get_tuning.restype = ctypes.c_int
     L.gg_host_last_transfer.argtypes = [ctypes.POINTER(ctypes.c_ulonglong)] * 2
     L.gg_host_last_transfer.restype = ctypes.c_int
+    L.gg_host_set_grid_access.argtypes = [ctypes.c_int]
+    L.gg_host_set_grid_access.restype = ctypes.c_int
+    L.gg_host_get_grid_access.argtypes = [ctypes.POINTER(ctypes.c_int)]
+    L.gg_host_get_grid_access.restype = ctypes.c_int
+    L.gg_host_set_profiling.argtypes = [ctypes.c_int]
+    L.gg_host_set_profiling.restype = ctypes.c_int
+    L.gg_host_phase_ms.argtypes = [ctypes.POINTER(ctypes.c_float),
+                                   ctypes.c_int]
+    L.gg_host_phase_ms.restype = ctypes.c_int
     L.gg_plan_probe_bounded_wait.argtypes = [_vp, ctypes.c_uint, _vp]
     L.gg_plan_probe_bounded_wait.restype = ctypes.c_int
     L.gg_plan_check.argtypes = [_vp, _vp]
@@ -483,6 +494,39 @@ def host_last_transfer() -> tuple:
     a, b = ctypes.c_ulonglong(0), ctypes.c_ulonglong(0)
     _check(lib().gg_host_last_transfer(ctypes.byref(a), ctypes.byref(b)))
     return int(a.value), int(b.value)
+
+
+# How the host-pointer gridding calls reach the caller's grid and cube (see
+# gg_host_set_grid_access): copied, used in place when page-locked, or (the
+# default) in place also when pageable, on devices that read pageable memory
+# through the host's page tables.
+GRID_ACCESS_COPY, GRID_ACCESS_PINNED, GRID_ACCESS_PAGEABLE = 0, 1, 2
+
+
+def set_host_grid_access(mode: int) -> None:
+    _check(lib().gg_host_set_grid_access(int(mode)))
+
+
+def host_grid_access() -> int:
+    m = ctypes.c_int(0)
+    _check(lib().gg_host_get_grid_access(ctypes.byref(m)))
+    return int(m.value)
+
+
+HOST_PHASES = ("staging", "placement", "binning", "work_items", "grid_tiles",
+               "finish")
+
+
+def set_host_profiling(enable: bool) -> None:
+    """Phase events in the host-pointer gridding calls on this device."""
+    _check(lib().gg_host_set_profiling(1 if enable else 0))
+
+
+def host_phase_ms() -> dict:
+    """Phase times (ms) of the last profiled host-pointer gridding call."""
+    ms = (ctypes.c_float * len(HOST_PHASES))()
+    _check(lib().gg_host_phase_ms(ms, len(HOST_PHASES)))
+    return dict(zip(HOST_PHASES, (float(x) for x in ms)))
 
 
 def host_tuning() -> dict:

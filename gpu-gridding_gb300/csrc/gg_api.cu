@@ -22,6 +22,9 @@
 #include <string>
 #include <vector>
 
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include "gg_internal.h"
 #include "../../include/gpugrid.h"
 
@@ -109,11 +112,17 @@ struct DeviceState {
   cudaStream_t stream = nullptr;
   int num_sms = 0;
   gg_plan* plan = nullptr;  // workspace of the host-pointer entry points
-  // Kernel stack the host-pointer entry points rebuild on every call (the
-  // caller may change its cube between calls), with its buffers and the
-  // cube's staging copy kept from call to call.
+  // Kernel stack of the host-pointer entry points.  Every call stages the
+  // caller's cube (the caller may change it between calls) into one of two
+  // buffers, the other holding the cube the stack was last made from; when
+  // the geometry is the same, a device comparison of the two decides
+  // whether the re-layout and tap-sum kernels run (cube_changed), so a
+  // caller that passes the same cube call after call pays for its transfer
+  // only.  cube_cur: buffer of the stack's cube, -1 = none.
   gg_kernels* host_kernels = nullptr;
-  DevBuf host_cube;
+  DevBuf host_cube[2];
+  DevBuf cube_changed;
+  int cube_cur = -1;
   // Side stream that uploads a host call's visibilities and grid while the
   // kernel stack is rebuilt (vis_ready, grid_ready mark the two uploads),
   // and the pinned tile-row spans of the grid cells a call touched
@@ -126,8 +135,18 @@ struct DeviceState {
   cudaEvent_t top_up = nullptr;     // upper grid rows uploaded
   uint32_t* h_spans = nullptr;
   static constexpr int kSpanCap = 2 * (kMaxGridSize / 64 + 2);
-  // Bytes the last host-pointer gridding call copied each way.
+  // Bytes the last host-pointer gridding call moved each way.
   unsigned long long last_h2d = 0, last_d2h = 0;
+  // How host-pointer gridding calls reach the caller's grid
+  // (gg_host_set_grid_access), and whether kernels may address pageable
+  // host memory (-1 = not asked yet).
+  int grid_access = GG_GRID_ACCESS_PAGEABLE;
+  int pageable_access = -1;
+  // Phase timing of the host-pointer gridding calls (gg_host_set_profiling):
+  // the call's start and end on its stream around the plan's phase events.
+  bool profile = false;
+  bool profile_valid = false;
+  cudaEvent_t call_start = nullptr, call_end = nullptr, copies_done = nullptr;
 };
 
 std::mutex g_devices_mu;
@@ -251,7 +270,9 @@ int validate_stack(size_t num_w_planes, const int* support, int oversample,
 template <typename Real>
 int kernels_fill(gg_kernels* k, size_t num_w_planes, const int* support,
                  int oversample, int conv_size_half, const Real* conv_func,
-                 int on_device, cudaStream_t s, DevBuf* stage, bool sync) {
+                 int on_device, cudaStream_t s, DevBuf* stage, bool sync,
+                 const Real* mapped = nullptr, const DevBuf* previous = nullptr,
+                 int* changed = nullptr) {
   GG_TRY(validate_stack(num_w_planes, support, oversample, conv_size_half,
                         conv_func));
   static std::atomic<unsigned long long> next_id{1};
@@ -332,7 +353,22 @@ int kernels_fill(gg_kernels* k, size_t num_w_planes, const int* support,
   DevBuf local;
   DevBuf& staged = stage ? *stage : local;
   const Real* d_conv = conv_func;
-  if (!on_device) {
+  if (!on_device && mapped) {
+    // A host cube the device addresses: the same squares, read by a gather
+    // kernel at the link's rate (3-D copies move one row of a plane per
+    // DMA and run far below it).
+    if ((r = staged.ensure(cube))) return fail(r);
+    if ((r = cu(launch_cube_gather<Real>(mapped, k->view(), staged.as<Real>(),
+                                         s),
+                "cube gather")))
+      return fail(r);
+    for (size_t p = 0; p < num_w_planes; ++p) {
+      const unsigned long long e = (unsigned long long)cube_read_extent(
+          support[p], oversample, k->omax, conv_size_half);
+      k->h2d_bytes += e * e * 2 * sizeof(Real);
+    }
+    d_conv = staged.as<Real>();
+  } else if (!on_device) {
     // Only the square of each plane that the preparation kernels read goes
     // up (cube_read_extent: about a third of the cube when supports vary
     // across the stack); a run of planes with the same extent is one 3-D
@@ -367,15 +403,35 @@ int kernels_fill(gg_kernels* k, size_t num_w_planes, const int* support,
     d_conv = staged.as<Real>();
   }
   StackView v = k->view();
-  if ((r = cu(launch_stack_relayout<Real>(d_conv, v, k->taps.p, total, s),
+  if (changed) {
+    // Re-lay only a cube that differs from previous (same geometry), whose
+    // re-layout k still holds; without previous, always.
+    if (previous) {
+      if ((r = cu(cudaMemsetAsync(changed, 0, sizeof(int), s), "flag")) ||
+          (r = cu(launch_cube_compare<Real>(d_conv, previous->as<Real>(), v,
+                                            changed, s),
+                  "cube compare")))
+        return fail(r);
+    } else {
+      const int one = 1;
+      if ((r = cu(cudaMemcpyAsync(changed, &one, sizeof(int),
+                                  cudaMemcpyHostToDevice, s),
+                  "flag")))
+        return fail(r);
+    }
+  }
+  if ((r = cu(launch_stack_relayout<Real>(d_conv, v, k->taps.p, total, s,
+                                          changed),
               "relayout")))
     return fail(r);
-  if ((r = cu(launch_stack_relayout_slabs<Real>(d_conv, v, k->slabs.p, s),
+  if ((r = cu(launch_stack_relayout_slabs<Real>(d_conv, v, k->slabs.p, s,
+                                                changed),
               "slab relayout")))
     return fail(r);
   StackView raw = v;
   raw.taps = d_conv;
-  if ((r = cu(launch_tap_sums<Real>(raw, k->tap_sum.as<double>(), s),
+  if ((r = cu(launch_tap_sums<Real>(raw, k->tap_sum.as<double>(),
+                                    k->support_max, s, changed),
               "tap sums")))
     return fail(r);
   // The staging copy (and the caller's host array) must outlive the
@@ -516,6 +572,12 @@ struct gg_plan {
   int to_key[4] = {0, 0, 0, 0};
   // Staging of the host-pointer entry points.
   DevBuf in_uu, in_vv, in_ww, in_vis, in_weight, in_grid, in_misc;
+  // Direct mode of a single-grid call (see launch_tile_groups): the device
+  // address of the caller's grid in host memory, or null; the per-tile
+  // plane-group table; direct_launched says the last call used it.
+  void* host_grid = nullptr;
+  DevBuf tile_groups;
+  bool direct_launched = false;
   // Geometry kept by the last batched call for replays on new amplitudes:
   // placement (cell, meta), sorted records, work items and launch shape.
   struct Kept {
@@ -556,7 +618,7 @@ enum Scalar {
 constexpr int kDegridShape = 0;
 // 64-bit device scalars live after the 32-bit ones.
 constexpr size_t kScalar64Offset = 64;
-enum Scalar64 { kMacs = 0, kSkipScratch, kScalar64Count };
+enum Scalar64 { kMacs = 0, kSkipScratch, kDirectCells, kScalar64Count };
 
 unsigned long long* scalar64(gg_plan* p, int i) {
   return (unsigned long long*)((char*)p->scalars.p + kScalar64Offset) + i;
@@ -1100,12 +1162,28 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
                          : geom.split_mask == 1 ? 0
                                                 : -1;
   if (upper_done >= 0) record_after[upper_done] = plan->split_event;
+  const uint32_t* tile_groups = nullptr;
+  if (plan->host_grid) {
+    if (num_grids != 1 || geom.split_mask != 0 || geom.num_groups >= 0xFFFF)
+      return set_error(GG_ERR_UNSUPPORTED,
+                       "direct grid access needs one grid, no split passes "
+                       "and fewer than 65535 plane groups");
+    GG_TRY(plan->tile_groups.ensure((size_t)geom.tiles_total * 4));
+    GG_CUDA(launch_tile_groups(plan->tile_start.as<uint32_t>(),
+                               geom.num_groups, geom, grid_size,
+                               plan->tile_groups.as<uint32_t>(),
+                               scalar64(plan, kDirectCells), s));
+    tile_groups = plan->tile_groups.as<uint32_t>();
+    plan->direct_launched = true;
+    plan->stats.num_launches += 1;
+  }
   plan->mark(3, s);
   GG_CUDA(launch_grid_tiles<Real>(
       ib.items, ib.group_items, ib.counter, sc + kDeviceError, b.vals,
       po.cell, po.meta, po.vw, view, geom, grid_size, d_grid, grid_stride,
       plan->partials.as<Real>(), ib.split_tiles, ib.num_split, b.num_tiles,
-      num_ctas, b.stage, s, wait_before.data(), record_after.data()));
+      num_ctas, b.stage, s, wait_before.data(), record_after.data(),
+      (Real*)plan->host_grid, tile_groups));
   plan->split_launched = upper_done >= 0;
   plan->mark(4, s);
   plan->mark(5, s);
@@ -1378,6 +1456,63 @@ int degrid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   return GG_OK;
 }
 
+// True when every page of [p, p + bytes) is resident.  A page the process
+// has never touched would be faulted in through the device's address
+// translation on first access, at some 25 microseconds a page on a Grace
+// host: such arrays (a freshly allocated zero grid, say) are copied
+// instead.
+bool pages_resident(const void* p, size_t bytes) {
+  static const long page = sysconf(_SC_PAGESIZE);
+  if (page <= 0 || bytes == 0) return false;
+  const uintptr_t a = (uintptr_t)p & ~(uintptr_t)(page - 1);
+  const uintptr_t e = (uintptr_t)p + bytes;
+  thread_local std::vector<unsigned char> vec;
+  vec.resize((e - a + page - 1) / page);
+  if (mincore((void*)a, e - a, vec.data()) != 0) return false;
+  for (unsigned char c : vec)
+    if (!(c & 1)) return false;
+  return true;
+}
+
+// The device address of a host array of a host-pointer call when kernels
+// may read (and, for the grid, write) it in place under the device's access
+// mode (page-locked and mapped, or pageable and resident on a device that
+// reads pageable memory through the host's page tables), else null.
+void* direct_host_address(DeviceState* st, int dev, const void* grid,
+                          size_t bytes, size_t align) {
+  if (st->grid_access == GG_GRID_ACCESS_COPY ||
+      (uintptr_t)grid % align != 0)
+    return nullptr;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, grid) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type == cudaMemoryTypeHost) return at.devicePointer;
+  if (at.type != cudaMemoryTypeUnregistered ||
+      st->grid_access != GG_GRID_ACCESS_PAGEABLE)
+    return nullptr;
+  if (st->pageable_access < 0) {
+    // Pageable memory in place only where the device reads it through the
+    // host's page tables (address translation services on a coherent link):
+    // no page moves to the device, so the caller's arrays stay where they
+    // are.
+    int v = 0, ats = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) !=
+            cudaSuccess ||
+        cudaDeviceGetAttribute(
+            &ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) !=
+            cudaSuccess) {
+      cudaGetLastError();
+      v = ats = 0;
+    }
+    st->pageable_access = v && ats;
+  }
+  return st->pageable_access && pages_resident(grid, bytes)
+             ? const_cast<void*>(grid)
+             : nullptr;
+}
+
 // Host-pointer drop-in: stage inputs, grid on the device, copy back.
 // The kernel stack of a host-pointer call, rebuilt from the caller's cube
 // into the device's reused stack object (the caller holds the device lock
@@ -1387,10 +1522,33 @@ int host_kernels(DeviceState* st, size_t num_w_planes, const int* support,
                  int oversample, int conv_size_half, const Real* conv_func,
                  cudaStream_t s, gg_kernels** out) {
   if (!st->host_kernels) st->host_kernels = new gg_kernels();
-  GG_TRY(kernels_fill<Real>(st->host_kernels, num_w_planes, support,
-                            oversample, conv_size_half, conv_func, 0, s,
-                            &st->host_cube, false));
-  *out = st->host_kernels;
+  gg_kernels* k = st->host_kernels;
+  int dev;
+  GG_TRY(current_device(&dev));
+  const Real* mapped = (const Real*)direct_host_address(
+      st, dev, conv_func,
+      num_w_planes * (size_t)conv_size_half * conv_size_half * 2 *
+          sizeof(Real),
+      2 * sizeof(Real));
+  // The stack still holds the re-layout of host_cube[cube_cur] when the
+  // geometry (precision, planes, supports, oversampling, cube size) is the
+  // same as then.
+  const bool same_geometry =
+      st->cube_cur >= 0 && k->is_double == (sizeof(Real) == 8) &&
+      k->device == dev && k->num_planes == (int)num_w_planes &&
+      k->oversample == oversample && k->conv_size_half == conv_size_half &&
+      std::equal(support, support + num_w_planes, k->h_support.begin());
+  const int next = st->cube_cur == 0 ? 1 : 0;
+  const DevBuf* previous = same_geometry ? &st->host_cube[st->cube_cur]
+                                         : nullptr;
+  GG_TRY(st->cube_changed.ensure(sizeof(int)));
+  st->cube_cur = -1;   // until the new stack is in place
+  GG_TRY(kernels_fill<Real>(k, num_w_planes, support, oversample,
+                            conv_size_half, conv_func, 0, s,
+                            &st->host_cube[next], false, mapped, previous,
+                            st->cube_changed.as<int>()));
+  st->cube_cur = next;
+  *out = k;
   return GG_OK;
 }
 
@@ -1467,10 +1625,18 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   // the side stream: placement waits for the visibilities only, and the
   // grid upload runs under the stack rebuild, placement and sort; only the
   // gridding passes wait for it.
+  st->profile_valid = false;
+  if (st->profile) GG_CUDA(cudaEventRecord(st->call_start, s));
   gg_kernels* K = nullptr;
   GG_TRY(host_kernels<Real>(st, num_w_planes, support, oversample,
                             conv_size_half, conv_func, s, &K));
   cudaStream_t cs = st->copy_stream;
+  // In place: the gridding kernels read and write the caller's grid over
+  // the host link (no upload, no copy back, no split passes).
+  void* direct = n && num_w_planes < 0xFFFF
+                     ? direct_host_address(st, dev, grid, grid_bytes,
+                                           2 * sizeof(Real))
+                     : nullptr;
   if (n) {
     GG_CUDA(cudaMemcpyAsync(plan->in_uu.p, uu, n * sizeof(Real),
                             cudaMemcpyHostToDevice, cs));
@@ -1490,9 +1656,12 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   // upper rows go back while the last group's lower pass runs.  On smaller
   // grids the copies those passes would overlap are shorter than the extra
   // passes' tails (2048^2 FP32: 4 % slower end to end).
-  const int split_row =
-      grid_bytes >= ((size_t)128 << 20) ? grid_size / 2 / 256 * 256 : 0;
-  if (n && split_row > 0) {
+  const int split_row = !direct && grid_bytes >= ((size_t)128 << 20)
+                            ? grid_size / 2 / 256 * 256
+                            : 0;
+  if (direct) {
+    // nothing to upload
+  } else if (n && split_row > 0) {
     const size_t upper = (size_t)split_row * row_bytes;
     GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, upper,
                             cudaMemcpyHostToDevice, cs));
@@ -1509,15 +1678,20 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   const double norm_in = *norm;
   GG_CUDA(cudaMemcpyAsync(d_norm, &norm_in, sizeof(double),
                           cudaMemcpyHostToDevice, s));
-  plan->grid_wait = st->grid_ready;
-  plan->h_spans = st->h_spans;
+  plan->grid_wait = direct ? nullptr : st->grid_ready;
+  plan->h_spans = direct ? nullptr : st->h_spans;
   plan->h_spans_cap = DeviceState::kSpanCap;
   plan->spans_ready = st->spans_ready;
   plan->spans_written = false;
-  plan->split_event = st->top_done;
+  plan->split_event = direct ? nullptr : st->top_done;
   plan->split_wait = split_row > 0 ? st->top_up : nullptr;
   plan->split_row = split_row;
   plan->split_launched = false;
+  plan->host_grid = direct;
+  plan->direct_launched = false;
+  if (direct)
+    GG_CUDA(cudaMemsetAsync(scalar64(plan, kDirectCells), 0,
+                            sizeof(unsigned long long), s));
   const int rc = grid_pipeline<Real>(plan, K, n, plan->in_uu.as<Real>(),
                                      plan->in_vv.as<Real>(),
                                      plan->in_ww.as<Real>(),
@@ -1532,6 +1706,7 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   plan->split_event = nullptr;
   plan->split_wait = nullptr;
   plan->split_row = 0;
+  plan->host_grid = nullptr;
   GG_TRY(rc);
   // Copy back only what the call can have changed: cells outside every tile
   // that holds records were neither read nor written on the device, so the
@@ -1540,8 +1715,15 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   // nothing when there were no visibilities.  When the last plane group was
   // gridded in two passes, the upper tile rows go back on the side stream
   // as soon as they are final, while the lower rows are still gridded.
-  unsigned long long d2h_grid = 0;
-  if (n) {
+  unsigned long long d2h_grid = 0, direct_cells = 0;
+  if (direct) {
+    // The kernels wrote the grid in place; only the count of the cells
+    // they moved comes back (none when nothing was gridded).
+    if (plan->direct_launched)
+      GG_CUDA(cudaMemcpyAsync(&direct_cells, scalar64(plan, kDirectCells),
+                              sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost, s));
+  } else if (n) {
     GG_CUDA(cudaStreamWaitEvent(s, st->grid_ready, 0));
     if (plan->spans_written) {
       if (plan->spans_async) GG_CUDA(cudaEventSynchronize(st->spans_ready));
@@ -1587,22 +1769,34 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
                           cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaMemcpyAsync(&skip_out, d_skip, sizeof(unsigned long long),
                           cudaMemcpyDeviceToHost, s));
+  if (st->profile) {
+    GG_CUDA(cudaEventRecord(st->copies_done, cs));
+    GG_CUDA(cudaStreamWaitEvent(s, st->copies_done, 0));
+    GG_CUDA(cudaEventRecord(st->call_end, s));
+  }
   GG_CUDA(cudaStreamSynchronize(s));
   GG_CUDA(cudaStreamSynchronize(cs));
   GG_TRY(check_device_error(plan, s));
+  st->profile_valid = st->profile && plan->events_valid;
   *norm = norm_out;
   *num_skipped = (size_t)skip_out;
   // Bytes moved: the cube and its plane tables, the inputs, the grid and
   // norm up; the grid spans, norm, skip count, the placement scalars, the
   // spans and the error flag down.
-  st->last_h2d = K->h2d_bytes + (n ? 6 * n * sizeof(Real) + grid_bytes : 0) +
+  // In place, the tiles that hold records cross the link once each way.
+  const unsigned long long direct_bytes = direct_cells * 2 * sizeof(Real);
+  st->last_h2d = K->h2d_bytes +
+                 (n ? 6 * n * sizeof(Real) +
+                          (direct ? direct_bytes : grid_bytes)
+                    : 0) +
                  sizeof(double);
-  st->last_d2h = d2h_grid + sizeof(double) + sizeof(unsigned long long) +
-                 sizeof(uint32_t) +
+  st->last_d2h = d2h_grid + direct_bytes + sizeof(double) +
+                 sizeof(unsigned long long) + sizeof(uint32_t) +
                  (n ? 4 * kScalarCount + 8 +
                           (plan->spans_written && plan->spans_async
                                ? 2 * (size_t)plan->spans_tiles_v * 4
-                               : 0)
+                               : 0) +
+                          (direct && plan->direct_launched ? 8 : 0)
                     : 0);
   return GG_OK;
 }
@@ -2119,6 +2313,69 @@ GG_API int gg_host_set_tuning(const gg_tuning* t) {
   std::lock_guard<std::mutex> lk(st->mu);
   GG_TRY(ensure_device_plan(st));
   return gg_plan_set_tuning(st->plan, t ? t : &defaults);
+}
+
+GG_API int gg_host_set_grid_access(int mode) {
+  t_last_error.clear();
+  if (mode < GG_GRID_ACCESS_COPY || mode > GG_GRID_ACCESS_PAGEABLE)
+    return set_error(GG_ERR_INVALID_ARG, "grid access mode %d unknown", mode);
+  int dev;
+  GG_TRY(current_device(&dev));
+  DeviceState* st;
+  GG_TRY(device_state(dev, &st));
+  std::lock_guard<std::mutex> lk(st->mu);
+  st->grid_access = mode;
+  return GG_OK;
+}
+
+GG_API int gg_host_set_profiling(int enable) {
+  t_last_error.clear();
+  int dev;
+  GG_TRY(current_device(&dev));
+  DeviceState* st;
+  GG_TRY(device_state(dev, &st));
+  std::lock_guard<std::mutex> lk(st->mu);
+  GG_TRY(ensure_device_plan(st));
+  if (enable && !st->call_start)
+    for (cudaEvent_t* e : {&st->call_start, &st->call_end, &st->copies_done})
+      GG_CUDA(cudaEventCreate(e));
+  st->profile = enable != 0;
+  st->profile_valid = false;
+  return gg_plan_set_profiling(st->plan, enable);
+}
+
+GG_API int gg_host_phase_ms(float* ms, int n) {
+  t_last_error.clear();
+  if (!ms || n < 0) return set_error(GG_ERR_INVALID_ARG, "NULL argument");
+  int dev;
+  GG_TRY(current_device(&dev));
+  DeviceState* st;
+  GG_TRY(device_state(dev, &st));
+  std::lock_guard<std::mutex> lk(st->mu);
+  if (!st->profile_valid)
+    return set_error(GG_ERR_INVALID_ARG,
+                     "no profiled call: enable profiling and make a "
+                     "host-pointer gridding call that grids at least one "
+                     "visibility");
+  const gg_plan* p = st->plan;
+  // staging, the plan's phases 0..3, then the rest of the call.
+  cudaEvent_t marks[7] = {st->call_start, p->ev[0], p->ev[1], p->ev[2],
+                          p->ev[3], p->ev[4], st->call_end};
+  for (int i = 0; i < n && i < 6; ++i)
+    GG_CUDA(cudaEventElapsedTime(&ms[i], marks[i], marks[i + 1]));
+  return GG_OK;
+}
+
+GG_API int gg_host_get_grid_access(int* mode) {
+  t_last_error.clear();
+  if (!mode) return set_error(GG_ERR_INVALID_ARG, "mode is NULL");
+  int dev;
+  GG_TRY(current_device(&dev));
+  DeviceState* st;
+  GG_TRY(device_state(dev, &st));
+  std::lock_guard<std::mutex> lk(st->mu);
+  *mode = st->grid_access;
+  return GG_OK;
 }
 
 GG_API int gg_host_last_transfer(unsigned long long* h2d_bytes,

@@ -83,7 +83,29 @@ struct GridArgs {
   Real* grid;
   long long grid_stride;
   typename Vec2<Real>::type* partials;
+  // Direct mode (single grid, tile_groups non-null): the caller's grid at
+  // host, addressed in place.  tile_groups[tile] = first | last << 16, the
+  // first and last plane group with records in the tile: the first reads
+  // the tile's cells from host, the last writes them to host, the others
+  // go through grid (scratch).
+  Real* host;
+  const uint32_t* tile_groups;
 };
+
+// Source and destination of a tile's read-modify-write in plane group
+// `group`: the scratch grid g, or the caller's grid h in direct mode.
+template <typename R2>
+__device__ __forceinline__ void tile_ends(const uint32_t* tile_groups, int rt,
+                                          int group, R2* g, R2* h, R2*& src,
+                                          R2*& dst) {
+  src = g;
+  dst = g;
+  if (tile_groups) {
+    const uint32_t fl = tile_groups[rt];
+    if ((int)(fl & 0xFFFFu) == group) src = h;
+    if ((int)(fl >> 16) == group) dst = h;
+  }
+}
 
 // Shared-memory layout of one CTA (dynamic shared memory).  Without slice
 // staging the CTA needs about 50 KB, leaving the rest of the SM's unified
@@ -520,16 +542,19 @@ k_grid_tiles(GridArgs<Real> a) {
       }
       const int col = u0 + lx;
       if (item.slot < 0) {
-        R2* g = (R2*)(a.grid + (long long)gi * a.grid_stride);
+        R2 *src, *dst;
+        tile_ends<R2>(a.tile_groups, rt, a.group,
+                      (R2*)(a.grid + (long long)gi * a.grid_stride),
+                      (R2*)a.host, src, dst);
 #pragma unroll
         for (int r = 0; r < kRows; ++r) {
           const int row = v0 + rowl + r;
           if (row < G_size && col < G_size) {
-            R2* p = g + (size_t)row * G_size + col;
-            R2 old = __ldcs(p);
+            const size_t off = (size_t)row * G_size + col;
+            R2 old = __ldcs(src + off);
             old.x += out[r].x;
             old.y += out[r].y;
-            __stcs(p, old);
+            __stcs(dst + off, old);
           }
         }
       } else {
@@ -555,7 +580,8 @@ __global__ void k_reduce_partials(const int4* __restrict__ split_tiles,
                                   const uint32_t* __restrict__ num_split,
                                   const typename Vec2<Real>::type* __restrict__ partials,
                                   TileGeom g, int group, int G, Real* grid,
-                                  long long grid_stride) {
+                                  long long grid_stride, Real* host,
+                                  const uint32_t* __restrict__ tile_groups) {
   using R2 = typename Vec2<Real>::type;
   using WS = WarpShape<TW>;
   const int tiles_per_grid = g.tiles_u * g.tiles_v;
@@ -568,15 +594,18 @@ __global__ void k_reduce_partials(const int4* __restrict__ split_tiles,
     const int tl = rt - gi * tiles_per_grid;
     const int u0 = (tl % g.tiles_u) * WS::kTileU;
     const int v0 = (tl / g.tiles_u) * WS::kTileV;
-    R2* gp = (R2*)(grid + (long long)gi * grid_stride);
+    R2 *src, *dst;
+    tile_ends<R2>(tile_groups, rt, group,
+                  (R2*)(grid + (long long)gi * grid_stride), (R2*)host, src,
+                  dst);
     for (int e = threadIdx.x; e < kCells; e += blockDim.x) {
       const int r = e / kConsumers, t = e % kConsumers;
       const int w = t >> 5, ln = t & 31;
       const int row = v0 + w * WS::kBand + (ln / TW) * kRows + r;
       const int col = u0 + ln % TW;
       if (row >= G || col >= G) continue;
-      R2* p = gp + (size_t)row * G + col;
-      const R2 old = *p;
+      const size_t off = (size_t)row * G + col;
+      const R2 old = src[off];
       double sx = old.x, sy = old.y;
       for (int c = 0; c < d.z; ++c) {
         const R2 q = partials[(size_t)(d.y + c) * kCells + e];
@@ -586,7 +615,7 @@ __global__ void k_reduce_partials(const int4* __restrict__ split_tiles,
       R2 nw;
       nw.x = (Real)sx;
       nw.y = (Real)sy;
-      *p = nw;
+      dst[off] = nw;
     }
   }
 }
@@ -613,6 +642,36 @@ __global__ void k_touched_spans(const uint32_t* __restrict__ tile_start,
     atomicMin(&lo[r / tiles_u], (uint32_t)(r % tiles_u));
     atomicMax(&hi[r / tiles_u], (uint32_t)(r % tiles_u) + 1u);
   }
+}
+
+// out[t] = first | last << 16: the first and last plane group with records
+// in real tile t (0xFFFF | 0xFFFF << 16 when none), for a single grid.
+// *cells += the grid cells of the tiles that have records (clipped to the
+// grid), the cells a direct-mode call reads and writes at host.
+__global__ void k_tile_groups(const uint32_t* __restrict__ tile_start,
+                              int num_groups, int tiles_total, int tiles_u,
+                              int tile_u, int tile_v, int G,
+                              uint32_t* __restrict__ out,
+                              unsigned long long* cells) {
+  unsigned long long mine = 0;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < tiles_total;
+       t += gridDim.x * blockDim.x) {
+    uint32_t first = 0xFFFFu, last = 0xFFFFu;
+    for (int g = 0; g < num_groups; ++g) {
+      const size_t v = (size_t)g * tiles_total + t;
+      if (tile_start[v + 1] > tile_start[v]) {
+        if (first == 0xFFFFu) first = (uint32_t)g;
+        last = (uint32_t)g;
+      }
+    }
+    out[t] = first | (last << 16);
+    if (first != 0xFFFFu) {
+      const int u0 = (t % tiles_u) * tile_u, v0 = (t / tiles_u) * tile_v;
+      mine += (unsigned long long)min(tile_u, G - u0) * min(tile_v, G - v0);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) mine += __shfl_down_sync(0xffffffffu, mine, o);
+  if ((threadIdx.x & 31) == 0 && mine) atomicAdd(cells, mine);
 }
 
 // A[t] = chunks of tile t if it is split (more than one chunk), else 0;
@@ -760,6 +819,17 @@ cudaError_t launch_wait_probe(unsigned limit, uint32_t* error,
   return cudaGetLastError();
 }
 
+cudaError_t launch_tile_groups(const uint32_t* tile_start, int num_groups,
+                               const TileGeom& geom, int grid_size,
+                               uint32_t* out, unsigned long long* cells,
+                               cudaStream_t s) {
+  const int blocks = std::min(1024, (geom.tiles_total + 255) / 256);
+  k_tile_groups<<<blocks < 1 ? 1 : blocks, 256, 0, s>>>(
+      tile_start, num_groups, geom.tiles_total, geom.tiles_u, geom.tile_u,
+      geom.tile_v, grid_size, out, cells);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_touched_spans(const uint32_t* tile_start, int num_tiles,
                                  int tiles_total, int tiles_u, uint32_t* lo,
                                  uint32_t* hi, cudaStream_t s) {
@@ -815,20 +885,21 @@ cudaError_t launch_reduce_group(const int4* split_tiles,
                                 const uint32_t* num_split, int max_split,
                                 const Real* partials, TileGeom geom, int group,
                                 int grid_size, Real* grid,
-                                long long grid_stride, cudaStream_t s) {
+                                long long grid_stride, Real* host,
+                                const uint32_t* tile_groups, cudaStream_t s) {
   if (max_split <= 0) return cudaSuccess;
   const int blocks = std::min(max_split, 4096);
   using P2 = const typename Vec2<Real>::type*;
   switch (geom.tile_u) {
     case 32: k_reduce_partials<Real, 32><<<blocks, 256, 0, s>>>(
         split_tiles, num_split, (P2)partials, geom, group, grid_size, grid,
-        grid_stride); break;
+        grid_stride, host, tile_groups); break;
     case 16: k_reduce_partials<Real, 16><<<blocks, 256, 0, s>>>(
         split_tiles, num_split, (P2)partials, geom, group, grid_size, grid,
-        grid_stride); break;
+        grid_stride, host, tile_groups); break;
     case 8: k_reduce_partials<Real, 8><<<blocks, 256, 0, s>>>(
         split_tiles, num_split, (P2)partials, geom, group, grid_size, grid,
-        grid_stride); break;
+        grid_stride, host, tile_groups); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -846,7 +917,8 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                               const uint32_t* num_split, int max_split,
                               int num_ctas, bool stage, cudaStream_t s,
                               const cudaEvent_t* wait_before,
-                              const cudaEvent_t* record_after) {
+                              const cudaEvent_t* record_after,
+                              Real* host_grid, const uint32_t* tile_groups) {
   GridArgs<Real> a;
   a.items = items;
   a.group_items = group_items;
@@ -863,6 +935,8 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
   a.grid = grid;
   a.grid_stride = grid_stride;
   a.partials = (typename Vec2<Real>::type*)partials;
+  a.host = tile_groups ? host_grid : grid;
+  a.tile_groups = tile_groups;
   if (geom.tile_u != 32 && geom.tile_u != 16 && geom.tile_u != 8)
     return cudaErrorInvalidValue;
   void* fn = nullptr;
@@ -883,7 +957,7 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
     if (e != cudaSuccess) return e;
     e = launch_reduce_group<Real>(split_tiles, num_split, max_split,
                                   partials, geom, g, grid_size, grid,
-                                  grid_stride, s);
+                                  grid_stride, a.host, tile_groups, s);
     if (e != cudaSuccess) return e;
     if (record_after && record_after[g]) {
       e = cudaEventRecord(record_after[g], s);
@@ -899,11 +973,13 @@ template cudaError_t launch_grid_tiles<float>(
     const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
     float*, long long, float*, const int4*, const uint32_t*, int, int, bool,
-    cudaStream_t, const cudaEvent_t*, const cudaEvent_t*);
+    cudaStream_t, const cudaEvent_t*, const cudaEvent_t*, float*,
+    const uint32_t*);
 template cudaError_t launch_grid_tiles<double>(
     const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
     double*, long long, double*, const int4*, const uint32_t*, int, int, bool,
-    cudaStream_t, const cudaEvent_t*, const cudaEvent_t*);
+    cudaStream_t, const cudaEvent_t*, const cudaEvent_t*, double*,
+    const uint32_t*);
 
 }  // namespace gg

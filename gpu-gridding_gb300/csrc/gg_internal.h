@@ -32,18 +32,35 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals,
 // ---- kernel stack preparation (gg_stack.cu) -------------------------------
 // Re-lays conv_func (device, [P][csh][csh] complex) into the residue-split
 // layout and forms the FP64 tap sums in the reference's summation order.
+// With `changed` given, each of these kernels returns at once while
+// *changed == 0 (a cube equal to the one the outputs were made from).
 template <typename Real>
 cudaError_t launch_stack_relayout(const Real* d_conv_func, StackView view,
                                   void* d_taps_out, long long total_taps,
-                                  cudaStream_t s);
+                                  cudaStream_t s,
+                                  const int* changed = nullptr);
 // Fills the slab stack (view.slabs layout, planes at view.sbase).
 template <typename Real>
 cudaError_t launch_stack_relayout_slabs(const Real* d_conv_func,
                                         StackView view, void* d_out,
-                                        cudaStream_t s);
+                                        cudaStream_t s,
+                                        const int* changed = nullptr);
+// support_max: the largest support of the stack (sizes the row window).
 template <typename Real>
 cudaError_t launch_tap_sums(StackView view, double* d_tap_sum,
-                            cudaStream_t s);
+                            int support_max, cudaStream_t s,
+                            const int* changed = nullptr);
+// *changed = 1 when the read squares of cubes a and b (device) differ in
+// any bit; *changed is left as it is otherwise.
+template <typename Real>
+cudaError_t launch_cube_compare(const Real* a, const Real* b, StackView view,
+                                int* changed, cudaStream_t s);
+// dst[p] = src[p] over each plane's read square [0, cube_read_extent)^2;
+// src is a cube in host memory that the device addresses (view.support must
+// already be on the device).
+template <typename Real>
+cudaError_t launch_cube_gather(const Real* src, StackView view, Real* dst,
+                               cudaStream_t s);
 
 // ---- placement and binning (gg_place.cu) ----------------------------------
 // Tile shapes of the gridding kernel: every tile holds 2048 cells, tile_u
@@ -206,7 +223,20 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                               const uint32_t* num_split, int max_split,
                               int num_ctas, bool stage, cudaStream_t s,
                               const cudaEvent_t* wait_before = nullptr,
-                              const cudaEvent_t* record_after = nullptr);
+                              const cudaEvent_t* record_after = nullptr,
+                              Real* host_grid = nullptr,
+                              const uint32_t* tile_groups = nullptr);
+// Direct mode of a single-grid call: per real tile, the first and last
+// plane group with records (first | last << 16, 0xFFFF when none), and
+// *cells += the grid cells of the tiles with records.  With tile_groups
+// given, launch_grid_tiles reads each such tile's cells from host_grid in
+// its first group's pass, writes them back there in its last group's, and
+// keeps the sums in between in grid: every cell takes the same additions in
+// the same order as when grid holds a copy of host_grid.
+cudaError_t launch_tile_groups(const uint32_t* tile_start, int num_groups,
+                               const TileGeom& geom, int grid_size,
+                               uint32_t* out, unsigned long long* cells,
+                               cudaStream_t s);
 // stage: the kernel variant that stages kernel slices in shared memory.
 template <typename Real>
 int grid_tiles_ctas_per_sm(int tile_u, bool stage);

@@ -6,6 +6,9 @@
 // (compact_wkernels, oskar_grid_wproj_gpu.cu:1461-1643).  Here the re-layout
 // runs once per kernel stack on the device and the result is kept in a
 // handle.
+#include <algorithm>
+#include <type_traits>
+
 #include "gg_internal.h"
 
 namespace gg {
@@ -18,8 +21,10 @@ namespace {
 // K[|cv + (jj-s)*os|][|cu + (kk-s)*os|] (see StackView).
 template <typename Real>
 __global__ void k_relayout(const Real* __restrict__ conv, StackView v,
-                           typename Vec2<Real>::type* __restrict__ out) {
+                           typename Vec2<Real>::type* __restrict__ out,
+                           const int* changed) {
   using R2 = typename Vec2<Real>::type;
+  if (changed && *changed == 0) return;
   const int p = blockIdx.y;
   const int os = v.oversample, csh = v.conv_size_half;
   const int s = v.support[p];
@@ -57,8 +62,10 @@ __global__ void k_relayout(const Real* __restrict__ conv, StackView v,
 // rows, and taps beyond the cube, are zero.
 template <typename Real>
 __global__ void k_relayout_slabs(const Real* __restrict__ conv, StackView v,
-                                 typename Vec2<Real>::type* __restrict__ out) {
+                                 typename Vec2<Real>::type* __restrict__ out,
+                                 const int* changed) {
   using R2 = typename Vec2<Real>::type;
+  if (changed && *changed == 0) return;
   const int p = blockIdx.y;
   const int os = v.oversample, csh = v.conv_size_half;
   const int s = v.support[p];
@@ -95,7 +102,8 @@ __global__ void k_relayout_slabs(const Real* __restrict__ conv, StackView v,
 // the reference's per-visibility sum.
 template <typename Real>
 __global__ void k_tap_sums(const Real* __restrict__ conv, StackView v,
-                           double* __restrict__ tap_sum) {
+                           double* __restrict__ tap_sum, const int* changed) {
+  if (changed && *changed == 0) return;
   const int side = 2 * v.omax + 1;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= v.num_planes * side * side) return;
@@ -131,55 +139,232 @@ __global__ void k_tap_sums(const Real* __restrict__ conv, StackView v,
   tap_sum[idx] = sum;
 }
 
+// The same sums, one block per plane: loader warps stream the rows of
+// nrows consecutive footprint rows j (for every offset class ov the row
+// |ov + j*os|, real parts only) into one half of a double-buffered shared
+// window while the first threads (one per offset class (ou, ov)) add the
+// other half's rows in the reference's (j, k) order.  Bit-identical to
+// k_tap_sums; the window is 2 * nrows * side * W values, W = omax + s*os + 1.
+template <typename Real>
+__global__ void k_tap_sums_rows(const Real* __restrict__ conv, StackView v,
+                                double* __restrict__ tap_sum, int sum_threads,
+                                int nrows, int W, const int* changed) {
+  if (changed && *changed == 0) return;
+  extern __shared__ __align__(16) unsigned char tap_rows_raw[];
+  Real* win = (Real*)tap_rows_raw;
+  // Widest planes (longest addition chains) first: supports grow with
+  // the plane index in a w-projection stack.
+  const int p = v.num_planes - 1 - (int)blockIdx.x;
+  const int omax = v.omax, side = 2 * omax + 1;
+  const int os = v.oversample, csh = v.conv_size_half;
+  const int s = v.support[p];
+  const int nsum = side * side;
+  const size_t kstart = (size_t)p * csh * csh;
+  const int tid = threadIdx.x;
+  const bool summer = tid < sum_threads;
+  const int lt = tid - sum_threads, nl = (int)blockDim.x - sum_threads;
+  const int half = nrows * side * W;   // values per buffer half
+  // Rows of footprint rows j0 .. j0 + nrows - 1 (clipped at s) into half b.
+  auto load = [&](int j0, int b) {
+    Real* dst = win + (size_t)b * half;
+    const int n = min(nrows, s - j0 + 1) * side * W;
+    for (int e0 = lt; e0 < n; e0 += 4 * nl) {
+      Real x[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int e = e0 + q * nl;
+        x[q] = Real(0);
+        if (e < n) {
+          const int rr = e / W, c = e - rr * W;
+          const int jj = rr / side, r = rr - jj * side;
+          const int t = abs(r - omax + (j0 + jj) * os);
+          if (t < csh && c < csh)
+            x[q] = conv[(kstart + (size_t)t * csh + c) * 2];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (e0 + q * nl < n) dst[e0 + q * nl] = x[q];
+    }
+  };
+  if (!summer) load(-s, 0);
+  __syncthreads();
+  double sum = 0.0;
+  const int ou = tid / side - omax, r = tid % side;
+  int b = 0;
+  for (int j0 = -s; j0 <= s; j0 += nrows) {
+    if (!summer) {
+      if (j0 + nrows <= s) load(j0 + nrows, b ^ 1);
+    } else if (tid < nsum) {
+      const int m = min(nrows, s - j0 + 1);
+      for (int jj = 0; jj < m; ++jj) {
+        const Real* row = win + (size_t)b * half + ((size_t)jj * side + r) * W;
+        for (int k = -s; k <= s; ++k)
+          sum = __dadd_rn(sum, (double)row[abs(ou + k * os)]);
+      }
+    }
+    __syncthreads();
+    b ^= 1;
+  }
+  if (tid < nsum) tap_sum[(size_t)p * nsum + tid] = sum;
+}
+
+// Copies the square [0, E_p)^2 that the preparation kernels read of each
+// plane p (E_p = cube_read_extent) from a cube in host memory that the
+// device addresses (page-locked and mapped, or pageable on a device that
+// reads pageable memory) to the same place in a device cube.  One warp per
+// row: the row's E_p complex taps are contiguous, so a warp's loads are
+// coalesced whatever the row pitch; 4 loads per lane are in flight before
+// the stores to cover the host link's latency.  blockIdx.x = plane,
+// blockIdx.y * 8 + warp = row.
+template <typename Real>
+__global__ void k_cube_gather(const typename Vec2<Real>::type* __restrict__ src,
+                              StackView v,
+                              typename Vec2<Real>::type* __restrict__ dst) {
+  using R2 = typename Vec2<Real>::type;
+  const int p = blockIdx.x;
+  const int row = blockIdx.y * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  const int csh = v.conv_size_half;
+  const int e = cube_read_extent(v.support[p], v.oversample, v.omax, csh);
+  if (row >= e) return;
+  const size_t off = ((size_t)p * csh + row) * csh;
+  const R2* a = src + off;
+  R2* b = dst + off;
+  for (int c = lane; c < e; c += 128) {
+    R2 t[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (c + 32 * q < e) t[q] = a[c + 32 * q];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (c + 32 * q < e) b[c + 32 * q] = t[q];
+  }
+}
+
+// *changed = 1 if the read squares of two cubes differ in any bit (the
+// squares k_cube_gather copies; same launch shape).
+template <typename Real>
+__global__ void k_cube_compare(const typename Vec2<Real>::type* __restrict__ a,
+                               const typename Vec2<Real>::type* __restrict__ b,
+                               StackView v, int* changed) {
+  using W = typename std::conditional<sizeof(Real) == 4, unsigned long long,
+                                      ulonglong2>::type;
+  const int p = blockIdx.x;
+  const int row = blockIdx.y * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  const int csh = v.conv_size_half;
+  const int e = cube_read_extent(v.support[p], v.oversample, v.omax, csh);
+  if (row >= e) return;
+  const size_t off = ((size_t)p * csh + row) * csh;
+  const W* x = (const W*)(a + off);
+  const W* y = (const W*)(b + off);
+  bool diff = false;
+  for (int c = lane; c < e; c += 32) {
+    const W u = x[c], w = y[c];
+    if constexpr (sizeof(Real) == 4) diff |= u != w;
+    else diff |= (u.x != w.x) | (u.y != w.y);
+  }
+  if (__any_sync(0xffffffffu, diff) && lane == 0) *changed = 1;
+}
+
 }  // namespace
+
+template <typename Real>
+cudaError_t launch_cube_compare(const Real* a, const Real* b, StackView view,
+                                int* changed, cudaStream_t s) {
+  if (view.num_planes <= 0) return cudaSuccess;
+  dim3 grid(view.num_planes, (view.conv_size_half + 7) / 8);
+  using R2 = typename Vec2<Real>::type;
+  k_cube_compare<Real><<<grid, 256, 0, s>>>((const R2*)a, (const R2*)b, view,
+                                            changed);
+  return cudaGetLastError();
+}
+
+template <typename Real>
+cudaError_t launch_cube_gather(const Real* src, StackView view, Real* dst,
+                               cudaStream_t s) {
+  if (view.num_planes <= 0) return cudaSuccess;
+  dim3 grid(view.num_planes, (view.conv_size_half + 7) / 8);
+  using R2 = typename Vec2<Real>::type;
+  k_cube_gather<Real><<<grid, 256, 0, s>>>((const R2*)src, view, (R2*)dst);
+  return cudaGetLastError();
+}
 
 template <typename Real>
 cudaError_t launch_stack_relayout(const Real* d_conv_func, StackView view,
                                   void* d_taps_out, long long total_taps,
-                                  cudaStream_t s) {
+                                  cudaStream_t s, const int* changed) {
   (void)total_taps;
   dim3 grid(64, view.num_planes);
   k_relayout<Real><<<grid, 256, 0, s>>>(
-      d_conv_func, view, (typename Vec2<Real>::type*)d_taps_out);
+      d_conv_func, view, (typename Vec2<Real>::type*)d_taps_out, changed);
   return cudaGetLastError();
 }
 
 template <typename Real>
 cudaError_t launch_stack_relayout_slabs(const Real* d_conv_func,
                                         StackView view, void* d_out,
-                                        cudaStream_t s) {
+                                        cudaStream_t s, const int* changed) {
   dim3 grid(64, view.num_planes);
   k_relayout_slabs<Real><<<grid, 256, 0, s>>>(
-      d_conv_func, view, (typename Vec2<Real>::type*)d_out);
+      d_conv_func, view, (typename Vec2<Real>::type*)d_out, changed);
   return cudaGetLastError();
 }
 
 template <typename Real>
 cudaError_t launch_tap_sums(StackView view, double* d_tap_sum,
-                            cudaStream_t s) {
+                            int support_max, cudaStream_t s,
+                            const int* changed) {
   // The raw cube is needed for the reference-order sums; it is passed in
   // view.taps by the caller for this launch only.
   const int side = 2 * view.omax + 1;
-  const int n = view.num_planes * side * side;
+  const int nsum = side * side;
+  // Row window of the block-per-plane kernel: up to 8 footprint rows per
+  // half, within the default 48 KB of shared memory.
+  const long long W = view.omax + (long long)support_max * view.oversample + 1;
+  const long long per_row = (long long)side * W * (long long)sizeof(Real);
+  const int nrows = (int)std::min<long long>(8, (48 << 10) / (2 * per_row));
+  const int sum_threads = (nsum + 31) / 32 * 32;
+  if (nrows >= 1 && sum_threads + 256 <= 1024) {
+    const size_t smem = (size_t)2 * nrows * per_row;
+    k_tap_sums_rows<Real><<<view.num_planes, sum_threads + 256, smem, s>>>(
+        (const Real*)view.taps, view, d_tap_sum, sum_threads, nrows, (int)W,
+        changed);
+    return cudaGetLastError();
+  }
+  const int n = view.num_planes * nsum;
   k_tap_sums<Real><<<(n + 127) / 128, 128, 0, s>>>(
-      (const Real*)view.taps, view, d_tap_sum);
+      (const Real*)view.taps, view, d_tap_sum, changed);
   return cudaGetLastError();
 }
 
 template cudaError_t launch_stack_relayout<float>(const float*, StackView,
                                                   void*, long long,
-                                                  cudaStream_t);
+                                                  cudaStream_t, const int*);
 template cudaError_t launch_stack_relayout<double>(const double*, StackView,
                                                    void*, long long,
-                                                   cudaStream_t);
+                                                   cudaStream_t, const int*);
 template cudaError_t launch_stack_relayout_slabs<float>(const float*,
                                                         StackView, void*,
-                                                        cudaStream_t);
+                                                        cudaStream_t,
+                                                        const int*);
 template cudaError_t launch_stack_relayout_slabs<double>(const double*,
                                                          StackView, void*,
-                                                         cudaStream_t);
-template cudaError_t launch_tap_sums<float>(StackView, double*, cudaStream_t);
-template cudaError_t launch_tap_sums<double>(StackView, double*,
-                                             cudaStream_t);
+                                                         cudaStream_t,
+                                                         const int*);
+template cudaError_t launch_cube_compare<float>(const float*, const float*,
+                                                StackView, int*, cudaStream_t);
+template cudaError_t launch_cube_compare<double>(const double*, const double*,
+                                                 StackView, int*,
+                                                 cudaStream_t);
+template cudaError_t launch_cube_gather<float>(const float*, StackView,
+                                               float*, cudaStream_t);
+template cudaError_t launch_cube_gather<double>(const double*, StackView,
+                                                double*, cudaStream_t);
+template cudaError_t launch_tap_sums<float>(StackView, double*, int,
+                                            cudaStream_t, const int*);
+template cudaError_t launch_tap_sums<double>(StackView, double*, int,
+                                             cudaStream_t, const int*);
 
 }  // namespace gg

@@ -215,10 +215,60 @@ GG_API int gg_plan_get_tuning(const gg_plan* plan, gg_tuning* tuning);
 GG_API int gg_host_set_tuning(const gg_tuning* tuning);
 GG_API int gg_host_get_tuning(gg_tuning* tuning);
 
-/* Bytes the last host-pointer gridding call on the current device copied
+/* How the host-pointer gridding calls on the current device reach the
+ * caller's grid and kernel cube.
+ *   GG_GRID_ACCESS_COPY:     both are copied to the device (the cube's read
+ *                            squares by 3-D copies); the grid is gridded
+ *                            there and the rows' spans that hold records
+ *                            are copied back.
+ *   GG_GRID_ACCESS_PINNED:   page-locked arrays that the device can address
+ *                            (cudaHostAlloc / cudaMallocHost,
+ *                            cudaHostRegister with mapping) are used in
+ *                            place: the gridding kernels read each tile that
+ *                            holds records once and write it once over the
+ *                            host link during the gridding passes, and a
+ *                            kernel gathers the cube's read squares.  Other
+ *                            arrays are copied.
+ *   GG_GRID_ACCESS_PAGEABLE: (default) as PINNED, and pageable (malloc)
+ *                            arrays too where the device reads pageable
+ *                            memory through the host's page tables
+ *                            (cudaDevAttrPageableMemoryAccess and
+ *                            ...UsesHostPageTables, e.g. Grace hosts) and
+ *                            every page of the array is resident (mincore):
+ *                            a page first touched by the device is faulted
+ *                            in at some 25 us, so a freshly allocated zero
+ *                            grid is copied.
+ * An array must be aligned to its complex element (8 bytes for _f, 16 for
+ * _d) to be used in place.  The grid in place is bit-identical to the
+ * device-pointer call's; copied, it is too on grids under 128 MiB (above,
+ * the copy's split passes change the rounding only). */
+enum {
+    GG_GRID_ACCESS_COPY = 0,
+    GG_GRID_ACCESS_PINNED = 1,
+    GG_GRID_ACCESS_PAGEABLE = 2
+};
+GG_API int gg_host_set_grid_access(int mode);
+GG_API int gg_host_get_grid_access(int* mode);
+
+/* Phase timing of the host-pointer gridding calls on the current device.
+ * With profiling enabled, gg_host_phase_ms fills ms[0..n-1] (n <= 6) for
+ * the last such call that gridded at least one visibility:
+ *   0 staging: the call's start to placement (kernel stack re-layout, the
+ *     inputs' upload)
+ *   1-4 the phases 0-3 of gg_plan_phase_ms (placement, binning, work
+ *     decomposition, tile-gridding passes)
+ *   5 the rest: the end of the passes to the end of the call (grid copy
+ *     back, scalars).
+ * Off by default (no events recorded). */
+GG_API int gg_host_set_profiling(int enable);
+GG_API int gg_host_phase_ms(float* ms, int n);
+
+/* Bytes the last host-pointer gridding call on the current device moved
  * host -> device (kernel cube and plane tables, the call's arrays, the
- * grid, norm) and device -> host (the grid rows' spans that hold records,
- * norm, skip count and a few status words); 0, 0 before the first call. */
+ * grid or, in place, the cells of the tiles that hold records, norm) and
+ * device -> host (the grid rows' spans that hold records or, in place, the
+ * same tiles' cells, norm, skip count and a few status words); 0, 0 before
+ * the first call. */
 GG_API int gg_host_last_transfer(unsigned long long* h2d_bytes,
                                  unsigned long long* d2h_bytes);
 

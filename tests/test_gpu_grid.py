@@ -11,6 +11,7 @@ Bars (the tolerances are written in each assertion):
 """
 from __future__ import annotations
 
+import contextlib
 import dataclasses
 
 import numpy as np
@@ -301,6 +302,34 @@ def test_empty_and_all_skipped_device(pkg, synthetic, torch):
     assert ns == 100 and nm == 1.0 and not g.any()
 
 
+@pytest.mark.parametrize("oversample,s_max,prec", [
+    (4, 72, "f"), (2, 30, "f"), (8, 40, "f"), (4, 60, "d"), (14, 72, "f")])
+def test_tap_sums_bit_exact_per_visibility(pkg, oracle_mod, synthetic,
+                                           oversample, s_max, prec):
+    """The per-(plane, offset class) tap sums of the norm: with one
+    visibility per call the norm is that visibility's sum times its weight,
+    so it must equal the reference's serial sum bit for bit, on every plane
+    up to the largest support, for oversampling 2 to 14 (the last case's row
+    window exceeds the block-per-plane kernel's and takes the per-sum
+    kernel)."""
+    wl = synthetic.random_uniform_workload(
+        "taps", 40, 1024, 6, max(1, s_max // 3), s_max,
+        oversample=oversample, seed=41 + oversample, cell_size_rad=1e-4)
+    grid_fn = pkg.grid_f if prec == "f" else pkg.grid_d
+    oracle_fn = oracle_mod.grid_f if prec == "f" else oracle_mod.grid_d
+    planes = set()
+    for i in range(wl.num_points):
+        one = dataclasses.replace(
+            wl, uu=wl.uu[i:i + 1], vv=wl.vv[i:i + 1], ww=wl.ww[i:i + 1],
+            vis=wl.vis[i:i + 1], weight=wl.weight[i:i + 1])
+        g, ns, nm = grid_fn(one)
+        gr, nsr, nmr = oracle_fn(one)
+        assert ns == nsr and nm == nmr, i
+        if not ns:
+            planes.add(int(oracle_mod.place(one, prec)["plane"][0]))
+    assert wl.num_w_planes - 1 in planes      # the largest support
+
+
 def test_nonfinite_kernel_tap_stays_in_its_footprints(pkg, oracle_mod,
                                                       synthetic, torch):
     """A NaN kernel tap reaches exactly the grid cells whose footprints use
@@ -343,6 +372,24 @@ def test_unusual_parameters_vs_oracle(pkg, oracle_mod, synthetic, torch, os_,
     assert max_rel(gd, gr) <= 1e-12
 
 
+@contextlib.contextmanager
+def _access(pkg, mode):
+    """Grid access mode of the host calls for the duration of a block."""
+    old = pkg.host_grid_access()
+    pkg.set_host_grid_access(mode)
+    try:
+        yield
+    finally:
+        pkg.set_host_grid_access(old)
+
+
+def _pinned_like(a, torch):
+    t = torch.empty(a.shape, dtype=getattr(torch, a.dtype.name),
+                    pin_memory=True)
+    t.numpy()[...] = a
+    return t.numpy()
+
+
 def _start_grid(G, seed, pinned=False, dtype=np.float32, torch=None):
     """Random starting grid; pinned=True puts it in page-locked memory (the
     drop-in's copies then run asynchronously on the copy engines)."""
@@ -355,14 +402,16 @@ def _start_grid(G, seed, pinned=False, dtype=np.float32, torch=None):
     return t.numpy()
 
 
+@pytest.mark.parametrize("mode", ["copy", "in_place"])
 @pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("where", ["disk", "patch_centre", "patch_corner"])
 def test_dropin_copies_back_touched_spans(pkg, oracle_mod, synthetic, torch,
-                                          where, pinned):
+                                          where, pinned, mode):
     """The host-pointer call copies back only the tile rows' spans that
-    hold records.  With a random starting grid the result must be start +
-    the contributions everywhere, and bit-for-bit the start wherever
-    nothing was added (cells outside every footprint)."""
+    hold records (or, in place, reads and writes only the tiles that hold
+    records).  With a random starting grid the result must be start + the
+    contributions everywhere, and bit-for-bit the start wherever nothing
+    was added (cells outside every footprint)."""
     G = 1800
     if where == "disk":
         wl = synthetic.random_uniform_workload(
@@ -377,8 +426,11 @@ def test_dropin_copies_back_touched_spans(pkg, oracle_mod, synthetic, torch,
                 wl, uu=(wl.uu + np.float32(0.4 * extent)).astype(np.float32),
                 vv=(wl.vv - np.float32(0.4 * extent)).astype(np.float32))
     start = _start_grid(G, 3)
-    g0, ns0, nm0 = pkg.grid_f(wl)
-    g1, ns1, nm1 = pkg.grid_f(wl, _start_grid(G, 3, pinned, torch=torch), 2.0)
+    with _access(pkg, pkg.GRID_ACCESS_COPY if mode == "copy"
+                 else pkg.GRID_ACCESS_PAGEABLE):
+        g0, ns0, nm0 = pkg.grid_f(wl)
+        g1, ns1, nm1 = pkg.grid_f(wl, _start_grid(G, 3, pinned, torch=torch),
+                                  2.0)
     assert ns1 == ns0 < wl.num_points
     assert abs(nm1 - (nm0 + 2.0)) <= 1e-12 * abs(nm1)
     assert max_rel(g1, start + g0) <= 1e-6
@@ -412,8 +464,10 @@ def test_dropin_split_passes(pkg, oracle_mod, synthetic, torch, prec, pinned,
     start = _start_grid(G, 8, dtype=dt)
     pkg.set_host_tuning({"plane_group_mb": groups_mb})
     try:
-        g0, ns0, nm0 = grid_fn(wl)
-        g1, ns1, nm1 = grid_fn(wl, _start_grid(G, 8, pinned, dt, torch), 1.5)
+        with _access(pkg, pkg.GRID_ACCESS_COPY):
+            g0, ns0, nm0 = grid_fn(wl)
+            g1, ns1, nm1 = grid_fn(wl, _start_grid(G, 8, pinned, dt, torch),
+                                   1.5)
     finally:
         pkg.set_host_tuning(None)
     assert ns1 == ns0 < wl.num_points
@@ -431,6 +485,155 @@ def test_dropin_split_passes(pkg, oracle_mod, synthetic, torch, prec, pinned,
         assert max_rel(g0, gr) <= 1e-12
 
 
+@pytest.mark.parametrize("G", [1800, 4099])
+@pytest.mark.parametrize("tuning", [{}, {"plane_group_mb": 1},
+                                    {"plane_group_mb": 1, "items_per_cta": 16}])
+@pytest.mark.parametrize("prec", ["f", "d"])
+def test_dropin_grid_access_modes(pkg, synthetic, torch, prec, tuning, G):
+    """The caller's grid read and written in place by the gridding kernels
+    (page-locked, and pageable where the device addresses it) gives the
+    device-pointer call's grid, skip count and norm bit for bit, with one
+    plane group and with several (a tile's first group reads the host grid,
+    its last writes it back), with split heavy tiles (their partial sums
+    reduced into the host grid) and with ragged edge tiles.  The copied
+    grid agrees bit for bit below 128 MiB; above, its split passes size
+    their work items per pass, which changes only the rounding."""
+    wl = synthetic.random_uniform_workload(
+        "access", 40_000, G, 48, 2, 14, seed=31, cell_size_rad=2.4e-5,
+        sigma_frac=0.12, clip_frac=0.45)
+    dt = np.float32 if prec == "f" else np.float64
+    grid_fn = pkg.grid_f if prec == "f" else pkg.grid_d
+    mode = pkg.host_grid_access()
+    results = {}
+    pkg.set_host_tuning(tuning)
+    try:
+        for name, m, pinned in (("copy", pkg.GRID_ACCESS_COPY, True),
+                                ("pinned", pkg.GRID_ACCESS_PINNED, True),
+                                ("pageable", pkg.GRID_ACCESS_PAGEABLE, False)):
+            pkg.set_host_grid_access(m)
+            g = _start_grid(G, 3, pinned, dt, torch)
+            # A page-locked cube is gathered by a kernel in place too.
+            w = dataclasses.replace(wl, conv_func=_pinned_like(
+                wl.conv_func.astype(dt), torch)) if pinned else wl
+            results[name] = grid_fn(w, g, 0.25) + pkg.host_last_transfer()
+    finally:
+        pkg.set_host_tuning(None)
+        pkg.set_host_grid_access(mode)
+    # The device-pointer call with the same settings.
+    dev = torch.device("cuda", 0)
+    tt = torch.float32 if prec == "f" else torch.float64
+    plan = pkg.Plan()
+    plan.set_tuning(tuning)
+    stack = pkg.KernelStack.from_workload(wl, prec)
+    d = {k: torch.from_numpy(np.ascontiguousarray(getattr(wl, k), dt)).to(dev)
+         for k in ("uu", "vv", "ww", "vis", "weight")}
+    grid = torch.from_numpy(_start_grid(G, 3, dtype=dt)).to(dev)
+    norm = torch.full((1,), 0.25, dtype=torch.float64, device=dev)
+    nskip = torch.zeros(1, dtype=torch.int64, device=dev)
+    pkg.grid_wproj_device(plan, stack, d["uu"], d["vv"], d["ww"], d["vis"],
+                          d["weight"], dt(wl.cell_size_rad), dt(wl.w_scale), G,
+                          grid, norm, nskip)
+    torch.cuda.synchronize()
+    gd = grid.cpu().numpy()
+    assert grid.dtype == tt
+    full = G * G * 2 * np.dtype(dt).itemsize
+    assert results["copy"][3] > full         # the copy uploads the grid
+    assert results["pinned"][3] < results["copy"][3]  # in place: tiles only
+    for name in ("pinned", "pageable"):
+        g, ns, nm = results[name][:3]
+        assert ns == int(nskip.item()) and nm == float(norm.item()), name
+        assert np.array_equal(g.view(np.uint8), gd.view(np.uint8)), name
+    g, ns, nm = results["copy"][:3]
+    assert ns == int(nskip.item())
+    if full < (128 << 20):
+        assert nm == float(norm.item())
+        assert np.array_equal(g.view(np.uint8), gd.view(np.uint8))
+    else:
+        start = _start_grid(G, 3, dtype=dt)
+        assert max_rel(g - start, gd - start) <= (
+            1e-6 if prec == "f" else 1e-14)
+        assert abs(nm - float(norm.item())) <= 1e-12 * abs(nm)
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_dropin_stack_reuse_follows_the_cube(pkg, synthetic, torch, pinned):
+    """The host calls re-lay the kernel stack only when the cube differs
+    from the one it was made from.  Gridding with cube A, A again, then B
+    (A with one row of taps scaled, in place in the same array), then B
+    again must give exactly what fresh stacks give, in every grid access
+    mode; a call with another geometry in between forces a fresh stack."""
+    wl = synthetic.random_uniform_workload(
+        "reuse", 20_000, 1024, 16, 4, 16, seed=43, cell_size_rad=4e-5)
+    other = synthetic.random_uniform_workload("other", 200, 512, 8, 2, 8,
+                                              seed=44)
+    cube_a = wl.conv_func.copy()
+    cube_b = cube_a.copy()
+    cube_b[:, 1, :, 0] *= np.float32(1.25)
+    arr = _pinned_like(cube_a, torch) if pinned else cube_a.copy()
+    w = dataclasses.replace(wl, conv_func=arr)
+    mode = pkg.host_grid_access()
+    try:
+        for m in (pkg.GRID_ACCESS_COPY, pkg.GRID_ACCESS_PINNED,
+                  pkg.GRID_ACCESS_PAGEABLE):
+            pkg.set_host_grid_access(m)
+            fresh = {}
+            for name, cube in (("a", cube_a), ("b", cube_b)):
+                pkg.grid_f(other)                 # another geometry
+                arr[...] = cube
+                fresh[name] = pkg.grid_f(w)
+            arr[...] = cube_a
+            pkg.grid_f(other)
+            seq = [pkg.grid_f(w), pkg.grid_f(w)]
+            arr[...] = cube_b
+            seq += [pkg.grid_f(w), pkg.grid_f(w)]
+            for got, name in zip(seq, "aabb"):
+                g, ns, nm = got
+                assert (ns, nm) == fresh[name][1:], (m, name)
+                assert np.array_equal(g.view(np.uint8),
+                                      fresh[name][0].view(np.uint8)), (m, name)
+            assert fresh["a"][2] != fresh["b"][2]
+    finally:
+        pkg.set_host_grid_access(mode)
+
+
+def test_dropin_fresh_pageable_grid_is_copied(pkg, synthetic):
+    """A freshly allocated pageable grid (np.zeros: its pages not yet
+    touched) is copied rather than used in place, where the device would
+    fault every page in; once its pages exist it is used in place.  Both
+    give the copy's result."""
+    G = 2048
+    wl = synthetic.random_uniform_workload(
+        "fresh", 30_000, G, 32, 2, 12, seed=37, cell_size_rad=3e-5)
+    with _access(pkg, pkg.GRID_ACCESS_COPY):
+        g0, ns0, nm0 = pkg.grid_f(wl)
+        h2d_copy = pkg.host_last_transfer()[0]
+    with _access(pkg, pkg.GRID_ACCESS_PAGEABLE):
+        g1, ns1, nm1 = pkg.grid_f(wl)       # np.zeros inside grid_f
+        h2d_fresh = pkg.host_last_transfer()[0]
+        g2 = np.zeros((G, G, 2), np.float32)
+        g2[...] = 0.0                        # pages touched
+        g2, ns2, nm2 = pkg.grid_f(wl, g2)
+        h2d_touched = pkg.host_last_transfer()[0]
+    assert h2d_fresh == h2d_copy             # the whole grid went up
+    assert h2d_touched < h2d_copy            # in place: touched tiles only
+    for g, ns, nm in ((g1, ns1, nm1), (g2, ns2, nm2)):
+        assert (ns, nm) == (ns0, nm0)
+        assert np.array_equal(g.view(np.uint8), g0.view(np.uint8))
+
+
+def test_grid_access_mode_setting(pkg):
+    mode = pkg.host_grid_access()
+    assert mode == pkg.GRID_ACCESS_PAGEABLE   # the default
+    try:
+        for m in (pkg.GRID_ACCESS_COPY, pkg.GRID_ACCESS_PINNED):
+            pkg.set_host_grid_access(m)
+            assert pkg.host_grid_access() == m
+        with pytest.raises(pkg.GridError):
+            pkg.set_host_grid_access(3)
+    finally:
+        pkg.set_host_grid_access(mode)
+
+
 def test_dropin_transfer_bytes(pkg, synthetic, torch):
     """The drop-in reports what it copied: everything up, and only the
     touched spans of the grid down (a centre patch here)."""
@@ -438,8 +641,9 @@ def test_dropin_transfer_bytes(pkg, synthetic, torch):
     wl = synthetic.random_uniform_workload(
         "xfer", 10_000, G, 16, 2, 8, seed=9, cell_size_rad=6e-5,
         sigma_frac=0.01, clip_frac=0.03)
-    pkg.grid_f(wl)
-    h2d, d2h = pkg.host_last_transfer()
+    with _access(pkg, pkg.GRID_ACCESS_COPY):
+        pkg.grid_f(wl)
+        h2d, d2h = pkg.host_last_transfer()
     n = wl.num_points
     # Of the cube only each plane's square up to the last row and column
     # the stack preparation reads goes up.
@@ -453,21 +657,41 @@ def test_dropin_transfer_bytes(pkg, synthetic, torch):
     stack_and_inputs = cube + wl.num_w_planes * 20 + 24 * n + 8
     assert h2d == stack_and_inputs + 8 * G * G
     assert 0 < d2h < G * G * 8 // 10
-    # A pinned grid moves the same bytes.
-    pkg.grid_f(wl, _start_grid(G, 1, True, torch=torch))
-    assert pkg.host_last_transfer() == (h2d, d2h)
+    # A pinned grid copied moves the same bytes; addressed in place, only
+    # the tiles that hold records cross the link, once each way (no more
+    # than the spans the copy brings back, which cover those tiles).
+    pinned = _start_grid(G, 1, True, torch=torch)
+    with _access(pkg, pkg.GRID_ACCESS_COPY):
+        pkg.grid_f(wl, pinned)
+        assert pkg.host_last_transfer() == (h2d, d2h)
+    with _access(pkg, pkg.GRID_ACCESS_PINNED):
+        pkg.grid_f(wl, pinned)
+        h2d_p, d2h_p = pkg.host_last_transfer()
+    tiles = h2d_p - stack_and_inputs
+    assert 0 < tiles <= d2h - 8 - 8 - 4 - 4 * 7 - 8 - 8
+    assert tiles % 8 == 0 and tiles % (32 * 8) == 0
+    assert d2h_p == tiles + 8 + 8 + 4 + 4 * 7 + 8 + 8
     empty = dataclasses.replace(wl, uu=wl.uu[:0], vv=wl.vv[:0],
                                 ww=wl.ww[:0], vis=wl.vis[:0],
                                 weight=wl.weight[:0])
-    pkg.grid_f(empty)
-    h2d, d2h = pkg.host_last_transfer()
-    assert h2d == cube + wl.num_w_planes * 20 + 8
-    assert d2h == 8 + 8 + 4
+    for m in (pkg.GRID_ACCESS_COPY, pkg.GRID_ACCESS_PAGEABLE):
+        with _access(pkg, m):
+            pkg.grid_f(empty)
+            h2d, d2h = pkg.host_last_transfer()
+        assert h2d == cube + wl.num_w_planes * 20 + 8
+        assert d2h == 8 + 8 + 4
 
 
-def test_dropin_nothing_gridded_leaves_grid(pkg, synthetic, torch):
+@pytest.mark.parametrize("mode", ["copy", "in_place"])
+def test_dropin_nothing_gridded_leaves_grid(pkg, synthetic, torch, mode):
     """Every visibility off the grid (all skipped), and no visibilities at
     all: the grid comes back bit-for-bit unchanged and the norm as given."""
+    with _access(pkg, pkg.GRID_ACCESS_COPY if mode == "copy"
+                 else pkg.GRID_ACCESS_PAGEABLE):
+        _nothing_gridded(pkg, synthetic, torch)
+
+
+def _nothing_gridded(pkg, synthetic, torch):
     G = 512
     wl = synthetic.random_uniform_workload("off_grid", 5_000, G, 8, 2, 6,
                                            seed=5)
