@@ -553,7 +553,14 @@ def run_ours(args):
                                h["weight"], cell, wsc, G, h_grid, 0.0)
 
     e2e = None
+    host_tuning = None
     if args.e2e_steps > 0:
+        # The host calls start from the plan's settings; the tile order and
+        # plane groups are re-timed on the host buffers themselves, where
+        # the grid is used in place (outside the timed region).
+        if not args.tuning:
+            at = importlib.import_module(pkg.__name__ + ".autotune")
+            host_tuning = at.autotune_host(pkg, e2e_step, plan.tuning())
         e2e_step()
         barrier()
         te = time.perf_counter()
@@ -568,7 +575,8 @@ def run_ours(args):
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "host_buffers": "page-locked",
                "grid_access": ["copy", "pinned", "pageable"][
-                   pkg.host_grid_access()]}
+                   pkg.host_grid_access()],
+               "host_tuning": host_tuning or pkg.host_tuning()}
         # The same call on pageable (malloc) buffers, as a numpy caller
         # passes them (the grid's pages already touched).
         hp = {k: np.ascontiguousarray(v).copy() for k, v in h.items()}

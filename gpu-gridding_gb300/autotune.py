@@ -9,7 +9,8 @@ no placement, norm or skip count (gg_tuning in the C header):
 * ``sort_detail``   -- record order within a tile (plane + offset class,
   plane only, or visibility order),
 * ``ctas_per_sm``   -- resident gridding CTAs per SM (0 = as many as fit),
-* ``plane_group_mb`` -- kernel bytes per gridding pass (0 = half of L2).
+* ``plane_group_mb`` -- kernel bytes per gridding pass (0 = half of L2),
+* ``tile_order``    -- tiles taken by distance from the centre or row by row.
 
 :func:`search` runs a coordinate search over them with a caller-supplied
 timing function; :func:`autotune` times real gridding calls of a workload
@@ -33,11 +34,12 @@ from typing import Callable, Dict, Iterable, Optional
 import numpy as np
 
 CACHE_ENV = "GPUGRID_TUNE_CACHE"
-CACHE_VERSION = 5
+CACHE_VERSION = 6
 
 #: The plan's settings before any tuning (each call chooses shape/staging).
 DEFAULT_TUNING = {"tile_u": 0, "slice_staging": -1, "items_per_cta": 4,
-                  "sort_detail": 2, "ctas_per_sm": 0, "plane_group_mb": 0}
+                  "sort_detail": 2, "ctas_per_sm": 0, "plane_group_mb": 0,
+                  "tile_order": 0}
 
 #: Values tried per setting, in search order.
 SEARCH_SPACE = (
@@ -48,6 +50,7 @@ SEARCH_SPACE = (
     (("ctas_per_sm",), [(0,), (1,)]),
     (("plane_group_mb",), [(0,), (16,), (32,), (48,), (64,), (96,),
                            (1 << 20,)]),
+    (("tile_order",), [(0,), (1,)]),
 )
 
 
@@ -155,6 +158,46 @@ def search(measure: Callable[[dict], float],
 
 def _device_name(torch) -> str:
     return torch.cuda.get_device_name(torch.cuda.current_device())
+
+
+#: Settings the host-pointer calls are re-timed over, starting from the
+#: plan's tuning: where the grid is the caller's host memory used in place,
+#: the tile order and the plane groups change how its pages are touched.
+HOST_SEARCH = (("tile_order", (0, 1)), ("plane_group_mb", (None, 1 << 20)))
+
+
+def autotune_host(pkg, call: Callable[[], object], base: dict,
+                  steps: int = 3) -> dict:
+    """Tune the host-pointer entry points of the current device by timing
+    ``call`` (one host-pointer gridding call on the caller's production
+    buffers) with ``base`` and its variants over :data:`HOST_SEARCH`
+    (``None`` = the base value); applies the fastest with
+    ``pkg.set_host_tuning`` and returns it with its time ("ms").  Calls
+    accumulate into the caller's grid, so pass scratch buffers."""
+    import time
+
+    def measure(t):
+        pkg.set_host_tuning(t)
+        call()
+        best = math.inf
+        for _ in range(max(1, steps)):
+            t0 = time.perf_counter()
+            call()
+            best = min(best, time.perf_counter() - t0)
+        return best * 1e3
+
+    best = dict(base)
+    best_ms = measure(best)
+    for name, values in HOST_SEARCH:
+        for v in values:
+            cand = dict(best, **{name: base[name] if v is None else v})
+            if cand == best:
+                continue
+            ms = measure(cand)
+            if ms < best_ms:
+                best, best_ms = cand, ms
+    pkg.set_host_tuning(best)
+    return dict(best, ms=best_ms)
 
 
 def autotune(pkg, plan, stack, uu, vv, ww, vis, weight, cell_size_rad,

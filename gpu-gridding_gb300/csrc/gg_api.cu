@@ -523,6 +523,7 @@ struct gg_plan {
   int sort_detail = 2;    // low sort-key fields: 2 plane+class, 1 plane, 0
   int ctas_per_sm = 0;    // cap on resident gridding CTAs, 0 = none
   int plane_group_mb = 0; // slab bytes per plane group, 0 = L2 size / 2
+  int queue_order = 0;    // tuning tile_order: 0 radius, 1 row by row
   // Event the gridding passes wait for (a grid upload on another stream),
   // or null.
   cudaEvent_t grid_wait = nullptr;
@@ -569,7 +570,7 @@ struct gg_plan {
   // was made for: grid_size, tile_u, tile_v, num_grids.
   DevBuf tile_order;
   std::vector<int> h_tile_order;
-  int to_key[4] = {0, 0, 0, 0};
+  int to_key[5] = {0, 0, 0, 0, -1};
   // Staging of the host-pointer entry points.
   DevBuf in_uu, in_vv, in_ww, in_vis, in_weight, in_grid, in_misc;
   // Direct mode of a single-grid call (see launch_tile_groups): the device
@@ -1014,8 +1015,9 @@ int bin_records(gg_plan* plan, const gg_kernels* K, size_t n,
 // central tiles also start first.  Uploaded when the geometry changes.
 int tile_queue_order(gg_plan* plan, const TileGeom& g, int grid_size,
                      cudaStream_t s, const int** out) {
-  const int key[4] = {grid_size, g.tile_u, g.tile_v, g.num_grids};
-  if (!std::equal(key, key + 4, plan->to_key) ||
+  const int key[5] = {grid_size, g.tile_u, g.tile_v, g.num_grids,
+                      plan->queue_order};
+  if (!std::equal(key, key + 5, plan->to_key) ||
       (int)plan->h_tile_order.size() != g.tiles_total) {
     const int tpg = g.tiles_u * g.tiles_v;
     std::vector<long long> r2(g.tiles_total);
@@ -1025,7 +1027,7 @@ int tile_queue_order(gg_plan* plan, const TileGeom& g, int grid_size,
           (long long)(tl % g.tiles_u) * g.tile_u + g.tile_u / 2 - grid_size / 2;
       const long long dv =
           (long long)(tl / g.tiles_u) * g.tile_v + g.tile_v / 2 - grid_size / 2;
-      r2[l] = du * du + dv * dv;
+      r2[l] = plan->queue_order == 1 ? l : du * du + dv * dv;
     }
     std::vector<int>& ord = plan->h_tile_order;
     ord.resize(g.tiles_total);
@@ -1038,7 +1040,7 @@ int tile_queue_order(gg_plan* plan, const TileGeom& g, int grid_size,
     GG_CUDA(cudaMemcpyAsync(plan->tile_order.p, ord.data(),
                             ord.size() * sizeof(int), cudaMemcpyHostToDevice,
                             s));
-    std::copy(key, key + 4, plan->to_key);
+    std::copy(key, key + 5, plan->to_key);
   }
   *out = plan->tile_order.as<int>();
   return GG_OK;
@@ -2277,6 +2279,9 @@ GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* t) {
     return set_error(GG_ERR_INVALID_ARG,
                      "plane_group_mb = %d outside [0, 1048576]",
                      t->plane_group_mb);
+  if (t->tile_order < 0 || t->tile_order > 1)
+    return set_error(GG_ERR_INVALID_ARG, "tile_order = %d: 0 or 1",
+                     t->tile_order);
   const int old_shape = plan->forced_shape;
   GG_TRY(gg_plan_set_tile_shape(plan, t->tile_u));
   const int r = gg_plan_set_slice_staging(plan, t->slice_staging);
@@ -2288,6 +2293,7 @@ GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* t) {
   plan->sort_detail = t->sort_detail;
   plan->ctas_per_sm = t->ctas_per_sm;
   plan->plane_group_mb = t->plane_group_mb;
+  plan->queue_order = t->tile_order;
   return GG_OK;
 }
 
@@ -2300,12 +2306,13 @@ GG_API int gg_plan_get_tuning(const gg_plan* plan, gg_tuning* t) {
   t->sort_detail = plan->sort_detail;
   t->ctas_per_sm = plan->ctas_per_sm;
   t->plane_group_mb = plan->plane_group_mb;
+  t->tile_order = plan->queue_order;
   return GG_OK;
 }
 
 GG_API int gg_host_set_tuning(const gg_tuning* t) {
   t_last_error.clear();
-  const gg_tuning defaults{0, -1, 4, 2, 0, 0};
+  const gg_tuning defaults{0, -1, 4, 2, 0, 0, 0};
   int dev;
   GG_TRY(current_device(&dev));
   DeviceState* st;

@@ -192,6 +192,12 @@ GG_API int gg_plan_set_slice_staging(gg_plan* plan, int mode);
  *                  equal in size) and each group is gridded in its own
  *                  pass, so that a pass's kernels stay in L2; 0 (default) =
  *                  half the device's L2 cache, 0..1048576
+ *   tile_order     order in which the persistent CTAs take the tiles: 0
+ *                  (default) by distance from the grid centre (baseline
+ *                  length, so w and the kernels read stay alike among the
+ *                  tiles gridded at one time), 1 row by row (the tiles in
+ *                  flight share grid rows: fewer pages touched at once when
+ *                  the grid is the caller's host memory, used in place)
  * gg_plan_set_tile_shape and gg_plan_set_slice_staging set the first two
  * fields alone. */
 typedef struct
@@ -202,6 +208,7 @@ typedef struct
     int sort_detail;
     int ctas_per_sm;
     int plane_group_mb;
+    int tile_order;
 } gg_tuning;
 
 GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* tuning);

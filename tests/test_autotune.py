@@ -83,7 +83,8 @@ def test_search_finds_separable_optimum(at):
 
     best, ms, trials = at.search(cost)
     assert best == {"tile_u": 16, "slice_staging": 1, "items_per_cta": 8,
-                    "sort_detail": 1, "ctas_per_sm": 0, "plane_group_mb": 0}
+                    "sort_detail": 1, "ctas_per_sm": 0, "plane_group_mb": 0,
+                    "tile_order": 0}
     assert math.isclose(ms, 10.0)
     keys = [json.dumps(t, sort_keys=True) for t in calls]
     assert len(keys) == len(set(keys)) == len(trials)
@@ -101,4 +102,24 @@ def test_tuning_struct_round_trip(pkg):
     t = pkg.Tuning.from_dict({"tile_u": 8, "sort_detail": 0})
     assert t.as_dict() == {"tile_u": 8, "slice_staging": -1,
                            "items_per_cta": 4, "sort_detail": 0,
-                           "ctas_per_sm": 0, "plane_group_mb": 0}
+                           "ctas_per_sm": 0, "plane_group_mb": 0,
+                           "tile_order": 0}
+
+
+def test_host_search_keeps_the_fastest(at):
+    """autotune_host re-times the host calls over the tile order and the
+    plane groups from the plan's settings and applies the fastest."""
+    applied = []
+
+    class FakePkg:
+        @staticmethod
+        def set_host_tuning(t):
+            applied.append(dict(t))
+
+    base = dict(at.DEFAULT_TUNING, plane_group_mb=64)
+    got = at.autotune_host(FakePkg, lambda: None, base, steps=1)
+    assert {k: got[k] for k in base} in applied
+    assert applied[-1] == {k: got[k] for k in base}
+    tried = {(t["tile_order"], t["plane_group_mb"]) for t in applied}
+    assert (0, 64) in tried and (1, 64) in tried
+    assert got["ms"] >= 0
