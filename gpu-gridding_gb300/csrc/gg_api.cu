@@ -18,6 +18,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -128,6 +129,12 @@ struct DeviceState {
   // and the pinned tile-row spans of the grid cells a call touched
   // (spans_ready marks their arrival).
   cudaStream_t copy_stream = nullptr;
+  // Stream of the stack build (cube staging, comparison, re-layout, tap
+  // sums), which runs beside placement and binning: tables_ready marks the
+  // plane tables on the call's stream, stack_ready the finished stack.
+  cudaStream_t stack_stream = nullptr;
+  cudaEvent_t tables_ready = nullptr, stack_ready = nullptr;
+  cudaEvent_t cube_staged = nullptr;   // the call's cube on the device
   cudaEvent_t vis_ready = nullptr;
   cudaEvent_t grid_ready = nullptr;
   cudaEvent_t spans_ready = nullptr;
@@ -171,7 +178,12 @@ int device_state(int dev, DeviceState** out) {
                        cudaGetErrorString(e));
     }
     st->num_sms = sms;
-    e = cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking);
+    // The call stream at the highest priority: the stack stream's kernels
+    // (lowest) then take only the SMs the call's own kernels leave free.
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    e = cudaStreamCreateWithPriority(&st->stream, cudaStreamNonBlocking,
+                                     greatest);
     if (e != cudaSuccess) {
       delete st;
       return set_error(GG_ERR_CUDA, "cudaStreamCreate: %s",
@@ -267,12 +279,25 @@ int validate_stack(size_t num_w_planes, const int* support, int oversample,
 // host cube is copied through *stage (a local buffer when stage is NULL).
 // With sync = false the caller must synchronise s before the host cube or
 // *stage may change.
+// Where kernels_fill runs its parts: the zero buffer and the plane tables
+// on `light` (their copies ahead of anything the caller queues there
+// next), then `between` (the caller's own work, e.g. its next uploads on
+// `light`), then the heavy part (the cube's staging and the stack kernels)
+// on `heavy`, after the tables (`tables`, recorded on `light`) and after
+// `after` when set; `done` is recorded on `heavy` at the end.
+struct StackStreams {
+  cudaStream_t light, heavy;
+  cudaEvent_t tables, after, done;
+  std::function<int()> between;
+  cudaEvent_t staged;   // recorded on `heavy` once the cube is on the device
+};
+
 template <typename Real>
 int kernels_fill(gg_kernels* k, size_t num_w_planes, const int* support,
                  int oversample, int conv_size_half, const Real* conv_func,
                  int on_device, cudaStream_t s, DevBuf* stage, bool sync,
                  const Real* mapped = nullptr, const DevBuf* previous = nullptr,
-                 int* changed = nullptr) {
+                 int* changed = nullptr, const StackStreams* ss = nullptr) {
   GG_TRY(validate_stack(num_w_planes, support, oversample, conv_size_half,
                         conv_func));
   static std::atomic<unsigned long long> next_id{1};
@@ -331,6 +356,8 @@ int kernels_fill(gg_kernels* k, size_t num_w_planes, const int* support,
       (r = k->tap_sum.ensure(num_w_planes * (2 * k->omax + 1) *
                              (2 * k->omax + 1) * sizeof(double))))
     return fail(r);
+  const cudaStream_t s_call = s;
+  if (ss) s = ss->light;
   if (cudaMemsetAsync(k->zeros.p, 0, k->zeros.bytes, s) != cudaSuccess)
     return fail(set_error(GG_ERR_CUDA, "zero buffer memset failed"));
   auto cu = [&](cudaError_t e, const char* what) -> int {
@@ -348,6 +375,17 @@ int kernels_fill(gg_kernels* k, size_t num_w_planes, const int* support,
                               cudaMemcpyHostToDevice, s), "sbase H2D")))
     return fail(r);
   k->h2d_bytes += num_w_planes * (sizeof(int) + 2 * sizeof(long long));
+  const cudaStream_t s_tables = s;
+  if (ss) {
+    if ((r = cu(cudaEventRecord(ss->tables, s_tables), "tables event")))
+      return fail(r);
+    if (ss->between && (r = ss->between()) != GG_OK) return fail(r);
+    if ((r = cu(cudaStreamWaitEvent(ss->heavy, ss->tables, 0), "wait")) ||
+        (ss->after &&
+         (r = cu(cudaStreamWaitEvent(ss->heavy, ss->after, 0), "wait"))))
+      return fail(r);
+    s = ss->heavy;
+  }
   const size_t cube = num_w_planes * (size_t)conv_size_half * conv_size_half *
                       2 * sizeof(Real);
   DevBuf local;
@@ -402,6 +440,9 @@ int kernels_fill(gg_kernels* k, size_t num_w_planes, const int* support,
     }
     d_conv = staged.as<Real>();
   }
+  if (ss && ss->staged &&
+      (r = cu(cudaEventRecord(ss->staged, s), "staged event")))
+    return fail(r);
   StackView v = k->view();
   if (changed) {
     // Re-lay only a cube that differs from previous (same geometry), whose
@@ -434,10 +475,14 @@ int kernels_fill(gg_kernels* k, size_t num_w_planes, const int* support,
                                     k->support_max, s, changed),
               "tap sums")))
     return fail(r);
+  if (ss && (r = cu(cudaEventRecord(ss->done, s), "stack event")))
+    return fail(r);
   // The staging copy (and the caller's host array) must outlive the
   // kernels that read it.
   if (sync || !stage)
-    if ((r = cu(cudaStreamSynchronize(s), "kernel stack sync")))
+    if ((r = cu(cudaStreamSynchronize(s), "kernel stack sync")) ||
+        (r = cu(cudaStreamSynchronize(s_tables), "kernel stack sync")) ||
+        (r = cu(cudaStreamSynchronize(s_call), "kernel stack sync")))
       return fail(r);
   return GG_OK;
 }
@@ -527,6 +572,13 @@ struct gg_plan {
   // Event the gridding passes wait for (a grid upload on another stream),
   // or null.
   cudaEvent_t grid_wait = nullptr;
+  // Kernel stack built on another stream (host calls): placement leaves
+  // the norm terms out, and once stack_wait is done they are formed from
+  // the placed points' weights (norm_weight, device, the call's Real) and
+  // added to norm_out; the gridding and degridding kernels wait for it too.
+  cudaEvent_t stack_wait = nullptr;
+  const void* norm_weight = nullptr;
+  double* norm_out = nullptr;
   // Touched spans (single-grid calls, when h_spans is set): per tile row
   // tv, the tile columns [lo[tv], hi[tv]) that hold records, lo at
   // h_spans[0..tiles_v) and hi after it (hi = 0: no records in the row).
@@ -822,6 +874,7 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   pp.grid_size = grid_size;
   pp.grid_centre = grid_size / 2;
   pp.num_points = n;
+  pp.defer_norm = plan->stack_wait != nullptr;
 
   if (n == 0) {
     GG_CUDA(cudaMemsetAsync(d_num_skipped, 0, sizeof(unsigned long long), s));
@@ -871,8 +924,10 @@ int place_and_count(gg_plan* plan, const gg_kernels* K,
   po.blk_macs = plan->blk_macs.as<unsigned long long>();
   GG_CUDA(launch_place<Real>(pp, view, TileGeom{}, 0, 0, po, s));
   GG_CUDA(launch_place_finalize(po.blk_norm, po.blk_skip, po.blk_macs, nblk,
-                                n, forced_shape, d_norm, d_num_skipped,
-                                scalar64(plan, kMacs), sc + kShape, s));
+                                n, forced_shape,
+                                pp.defer_norm ? nullptr : d_norm,
+                                d_num_skipped, scalar64(plan, kMacs),
+                                sc + kShape, s));
   GG_CUDA(launch_count_records(po.cell, po.meta, n, view, sc + kShape,
                                po.rec_count, s));
   GG_CUDA(exclusive_scan_u32(po.rec_count, plan->rec_offset.as<uint32_t>(), n,
@@ -1111,6 +1166,16 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
   Bins b;
   GG_TRY(bin_records<Real>(plan, K, n, po, grid_size, num_grids,
                            d_grid_offsets, s, &b));
+  if (plan->stack_wait) {
+    // The stack was built beside placement and binning.
+    GG_CUDA(cudaStreamWaitEvent(s, plan->stack_wait, 0));
+    if (plan->norm_out) {
+      GG_CUDA(launch_norm_terms<Real>(po.meta, (const Real*)plan->norm_weight,
+                                      n, view, plan->blk_norm.as<double>(),
+                                      plan->norm_out, s));
+      plan->stats.num_launches += 2;
+    }
+  }
   const TileGeom& geom = b.geom;
   const bool want_spans = plan->h_spans && num_grids == 1 &&
                           2 * geom.tiles_v <= plan->h_spans_cap;
@@ -1447,6 +1512,7 @@ int degrid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   GG_TRY(plan->rec_out.ensure((size_t)b.total * 2 * sizeof(Real)));
   uint32_t* sc = plan->scalars.as<uint32_t>();
   if (plan->grid_wait) GG_CUDA(cudaStreamWaitEvent(s, plan->grid_wait, 0));
+  if (plan->stack_wait) GG_CUDA(cudaStreamWaitEvent(s, plan->stack_wait, 0));
   GG_CUDA(launch_degrid_tiles<Real>(
       ib.items, ib.num_items, ib.counter, sc + kDeviceError, b.vals, po.cell,
       po.meta, plan->rec_offset.as<uint32_t>(), view, b.geom, grid_size,
@@ -1522,7 +1588,8 @@ void* direct_host_address(DeviceState* st, int dev, const void* grid,
 template <typename Real>
 int host_kernels(DeviceState* st, size_t num_w_planes, const int* support,
                  int oversample, int conv_size_half, const Real* conv_func,
-                 cudaStream_t s, gg_kernels** out) {
+                 cudaStream_t s, std::function<int()> uploads,
+                 gg_kernels** out) {
   if (!st->host_kernels) st->host_kernels = new gg_kernels();
   gg_kernels* k = st->host_kernels;
   int dev;
@@ -1545,10 +1612,17 @@ int host_kernels(DeviceState* st, size_t num_w_planes, const int* support,
                                          : nullptr;
   GG_TRY(st->cube_changed.ensure(sizeof(int)));
   st->cube_cur = -1;   // until the new stack is in place
+  // The plane tables go first on the side stream, then the caller's
+  // uploads (`uploads`, which records vis_ready there); the heavy part runs
+  // on the stack stream after them, beside placement and binning on s, and
+  // stack_ready marks its end.
+  const StackStreams ss{st->copy_stream, st->stack_stream, st->tables_ready,
+                        st->vis_ready, st->stack_ready, std::move(uploads),
+                        st->cube_staged};
   GG_TRY(kernels_fill<Real>(k, num_w_planes, support, oversample,
                             conv_size_half, conv_func, 0, s,
                             &st->host_cube[next], false, mapped, previous,
-                            st->cube_changed.as<int>()));
+                            st->cube_changed.as<int>(), &ss));
   st->cube_cur = next;
   *out = k;
   return GG_OK;
@@ -1558,8 +1632,15 @@ int ensure_copy_stream(DeviceState* st) {
   if (!st->copy_stream)
     GG_CUDA(cudaStreamCreateWithFlags(&st->copy_stream,
                                       cudaStreamNonBlocking));
+  if (!st->stack_stream) {
+    int least = 0, greatest = 0;
+    GG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    GG_CUDA(cudaStreamCreateWithPriority(&st->stack_stream,
+                                         cudaStreamNonBlocking, least));
+  }
   for (cudaEvent_t* e : {&st->vis_ready, &st->grid_ready, &st->spans_ready,
-                         &st->top_done, &st->top_up})
+                         &st->top_done, &st->top_up, &st->tables_ready,
+                         &st->stack_ready, &st->cube_staged})
     if (!*e) GG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   if (!st->h_spans)
     GG_CUDA(cudaMallocHost(&st->h_spans,
@@ -1617,21 +1698,22 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   double* d_norm = plan->in_misc.as<double>();
   unsigned long long* d_skip = (unsigned long long*)(plan->in_misc.as<char>() + 8);
   GG_TRY(ensure_copy_stream(st));
-  struct CopyGuard {   // the side stream reads the caller's arrays
-    cudaStream_t s;
-    ~CopyGuard() { cudaStreamSynchronize(s); }
-  } copy_guard{st->copy_stream};
-  // Host-to-device copies run one after another in the order they are
-  // issued, so the kernel stack's cube goes first (the stack is rebuilt
-  // from it on the call's stream), then the visibilities and the grid on
-  // the side stream: placement waits for the visibilities only, and the
-  // grid upload runs under the stack rebuild, placement and sort; only the
-  // gridding passes wait for it.
+  struct CopyGuard {   // the side streams read the caller's arrays
+    cudaStream_t s, t;
+    ~CopyGuard() {
+      cudaStreamSynchronize(s);
+      cudaStreamSynchronize(t);
+    }
+  } copy_guard{st->copy_stream, st->stack_stream};
+  // The visibilities go over the link first, on the side stream, and
+  // placement and binning start as soon as they are in.  The kernel stack
+  // is built beside them on the stack stream, its cube behind the
+  // visibilities on the link; placement leaves out the norm terms, which
+  // are formed once the stack is ready, before the gridding passes.  In
+  // copy mode the grid goes up on the side stream behind the visibilities,
+  // and only the gridding passes wait for it.
   st->profile_valid = false;
   if (st->profile) GG_CUDA(cudaEventRecord(st->call_start, s));
-  gg_kernels* K = nullptr;
-  GG_TRY(host_kernels<Real>(st, num_w_planes, support, oversample,
-                            conv_size_half, conv_func, s, &K));
   cudaStream_t cs = st->copy_stream;
   // In place: the gridding kernels read and write the caller's grid over
   // the host link (no upload, no copy back, no split passes).
@@ -1639,19 +1721,26 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
                      ? direct_host_address(st, dev, grid, grid_bytes,
                                            2 * sizeof(Real))
                      : nullptr;
-  if (n) {
-    GG_CUDA(cudaMemcpyAsync(plan->in_uu.p, uu, n * sizeof(Real),
-                            cudaMemcpyHostToDevice, cs));
-    GG_CUDA(cudaMemcpyAsync(plan->in_vv.p, vv, n * sizeof(Real),
-                            cudaMemcpyHostToDevice, cs));
-    GG_CUDA(cudaMemcpyAsync(plan->in_ww.p, ww, n * sizeof(Real),
-                            cudaMemcpyHostToDevice, cs));
-    GG_CUDA(cudaMemcpyAsync(plan->in_vis.p, vis, 2 * n * sizeof(Real),
-                            cudaMemcpyHostToDevice, cs));
-    GG_CUDA(cudaMemcpyAsync(plan->in_weight.p, weight, n * sizeof(Real),
-                            cudaMemcpyHostToDevice, cs));
-  }
-  GG_CUDA(cudaEventRecord(st->vis_ready, cs));
+  if (st->profile) GG_CUDA(cudaStreamWaitEvent(cs, st->call_start, 0));
+  auto uploads = [&]() -> int {
+    if (n) {
+      GG_CUDA(cudaMemcpyAsync(plan->in_uu.p, uu, n * sizeof(Real),
+                              cudaMemcpyHostToDevice, cs));
+      GG_CUDA(cudaMemcpyAsync(plan->in_vv.p, vv, n * sizeof(Real),
+                              cudaMemcpyHostToDevice, cs));
+      GG_CUDA(cudaMemcpyAsync(plan->in_ww.p, ww, n * sizeof(Real),
+                              cudaMemcpyHostToDevice, cs));
+      GG_CUDA(cudaMemcpyAsync(plan->in_vis.p, vis, 2 * n * sizeof(Real),
+                              cudaMemcpyHostToDevice, cs));
+      GG_CUDA(cudaMemcpyAsync(plan->in_weight.p, weight, n * sizeof(Real),
+                              cudaMemcpyHostToDevice, cs));
+    }
+    GG_CUDA(cudaEventRecord(st->vis_ready, cs));
+    return GG_OK;
+  };
+  gg_kernels* K = nullptr;
+  GG_TRY(host_kernels<Real>(st, num_w_planes, support, oversample,
+                            conv_size_half, conv_func, s, uploads, &K));
   // On grids of 128 MiB and more the grid goes up in two halves by rows
   // (the split a multiple of 256 rows, so of every tile height): the
   // first plane group's upper pass waits for the upper half only, and the
@@ -1661,6 +1750,9 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   const int split_row = !direct && grid_bytes >= ((size_t)128 << 20)
                             ? grid_size / 2 / 256 * 256
                             : 0;
+  // Copied grids go over the link after the cube, so that the stack is
+  // ready when the first pass can start.
+  if (!direct && n) GG_CUDA(cudaStreamWaitEvent(cs, st->cube_staged, 0));
   if (direct) {
     // nothing to upload
   } else if (n && split_row > 0) {
@@ -1677,9 +1769,9 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   }
   GG_CUDA(cudaEventRecord(st->grid_ready, cs));
   GG_CUDA(cudaStreamWaitEvent(s, st->vis_ready, 0));
-  const double norm_in = *norm;
-  GG_CUDA(cudaMemcpyAsync(d_norm, &norm_in, sizeof(double),
-                          cudaMemcpyHostToDevice, s));
+  // The starting norm is set by a one-thread kernel rather than a copy, so
+  // that it does not queue behind the uploads on the copy engines.
+  GG_CUDA(launch_store_f64(d_norm, *norm, s));
   plan->grid_wait = direct ? nullptr : st->grid_ready;
   plan->h_spans = direct ? nullptr : st->h_spans;
   plan->h_spans_cap = DeviceState::kSpanCap;
@@ -1691,6 +1783,9 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   plan->split_launched = false;
   plan->host_grid = direct;
   plan->direct_launched = false;
+  plan->stack_wait = st->stack_ready;
+  plan->norm_weight = plan->in_weight.p;
+  plan->norm_out = d_norm;
   if (direct)
     GG_CUDA(cudaMemsetAsync(scalar64(plan, kDirectCells), 0,
                             sizeof(unsigned long long), s));
@@ -1709,6 +1804,9 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   plan->split_wait = nullptr;
   plan->split_row = 0;
   plan->host_grid = nullptr;
+  plan->stack_wait = nullptr;
+  plan->norm_weight = nullptr;
+  plan->norm_out = nullptr;
   GG_TRY(rc);
   // Copy back only what the call can have changed: cells outside every tile
   // that holds records were neither read nor written on the device, so the
@@ -1778,6 +1876,7 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   }
   GG_CUDA(cudaStreamSynchronize(s));
   GG_CUDA(cudaStreamSynchronize(cs));
+  GG_CUDA(cudaStreamSynchronize(st->stack_stream));
   GG_TRY(check_device_error(plan, s));
   st->profile_valid = st->profile && plan->events_valid;
   *norm = norm_out;
@@ -2003,9 +2102,6 @@ int degrid_host(size_t num_w_planes, const int* support, int oversample,
   cudaStream_t s = st->stream;
   GG_TRY(ensure_device_plan(st));
   gg_plan* plan = st->plan;
-  gg_kernels* K = nullptr;
-  GG_TRY(host_kernels<Real>(st, num_w_planes, support, oversample,
-                            conv_size_half, conv_func, s, &K));
   const size_t n = num_points;
   const size_t grid_bytes = (size_t)grid_size * grid_size * 2 * sizeof(Real);
   GG_TRY(plan->in_uu.ensure(n * sizeof(Real) + 16));
@@ -2013,41 +2109,56 @@ int degrid_host(size_t num_w_planes, const int* support, int oversample,
   GG_TRY(plan->in_ww.ensure(n * sizeof(Real) + 16));
   GG_TRY(plan->in_vis.ensure(2 * n * sizeof(Real) + 16));
   GG_TRY(plan->in_grid.ensure(grid_bytes));
-  // As in the gridding call: the coordinates and then the grid go up on the
-  // side stream behind the kernel stack's cube; placement waits for the
-  // coordinates only, and only the degridding kernel for the grid.
+  // As in the gridding call: the coordinates go up first on the side
+  // stream, the kernel stack is built beside placement on the stack stream
+  // behind them, and the grid follows the coordinates on the side stream;
+  // only the degridding kernel waits for the stack and the grid.
   GG_TRY(ensure_copy_stream(st));
-  struct CopyGuard {   // the side stream reads the caller's arrays
-    cudaStream_t s;
-    ~CopyGuard() { cudaStreamSynchronize(s); }
-  } copy_guard{st->copy_stream};
+  struct CopyGuard {   // the side streams read the caller's arrays
+    cudaStream_t s, t;
+    ~CopyGuard() {
+      cudaStreamSynchronize(s);
+      cudaStreamSynchronize(t);
+    }
+  } copy_guard{st->copy_stream, st->stack_stream};
   cudaStream_t cs = st->copy_stream;
+  auto uploads = [&]() -> int {
+    if (n) {
+      GG_CUDA(cudaMemcpyAsync(plan->in_uu.p, uu, n * sizeof(Real),
+                              cudaMemcpyHostToDevice, cs));
+      GG_CUDA(cudaMemcpyAsync(plan->in_vv.p, vv, n * sizeof(Real),
+                              cudaMemcpyHostToDevice, cs));
+      GG_CUDA(cudaMemcpyAsync(plan->in_ww.p, ww, n * sizeof(Real),
+                              cudaMemcpyHostToDevice, cs));
+    }
+    GG_CUDA(cudaEventRecord(st->vis_ready, cs));
+    return GG_OK;
+  };
+  gg_kernels* K = nullptr;
+  GG_TRY(host_kernels<Real>(st, num_w_planes, support, oversample,
+                            conv_size_half, conv_func, s, uploads, &K));
   if (n) {
-    GG_CUDA(cudaMemcpyAsync(plan->in_uu.p, uu, n * sizeof(Real),
-                            cudaMemcpyHostToDevice, cs));
-    GG_CUDA(cudaMemcpyAsync(plan->in_vv.p, vv, n * sizeof(Real),
-                            cudaMemcpyHostToDevice, cs));
-    GG_CUDA(cudaMemcpyAsync(plan->in_ww.p, ww, n * sizeof(Real),
-                            cudaMemcpyHostToDevice, cs));
-  }
-  GG_CUDA(cudaEventRecord(st->vis_ready, cs));
-  if (n)
+    GG_CUDA(cudaStreamWaitEvent(cs, st->cube_staged, 0));
     GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, grid_bytes,
                             cudaMemcpyHostToDevice, cs));
+  }
   GG_CUDA(cudaEventRecord(st->grid_ready, cs));
   GG_CUDA(cudaStreamWaitEvent(s, st->vis_ready, 0));
   plan->grid_wait = st->grid_ready;
+  plan->stack_wait = st->stack_ready;
   const int rc = degrid_pipeline<Real>(
       plan, K, n, plan->in_uu.as<Real>(), plan->in_vv.as<Real>(),
       plan->in_ww.as<Real>(), cell_size_rad, w_scale, grid_size,
       plan->in_grid.as<Real>(), plan->in_vis.as<Real>(), s);
   plan->grid_wait = nullptr;
+  plan->stack_wait = nullptr;
   GG_TRY(rc);
   if (n)
     GG_CUDA(cudaMemcpyAsync(vis, plan->in_vis.p, 2 * n * sizeof(Real),
                             cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaStreamSynchronize(s));
   GG_CUDA(cudaStreamSynchronize(cs));
+  GG_CUDA(cudaStreamSynchronize(st->stack_stream));
   return check_device_error(plan, s);
 }
 

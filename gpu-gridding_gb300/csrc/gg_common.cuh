@@ -153,6 +153,9 @@ struct PlaceParams {
   int grid_size;
   int grid_centre;
   unsigned long long num_points;
+  // Norm terms left to launch_norm_terms (the kernel stack's tap sums are
+  // not ready yet when placement runs).
+  bool defer_norm = false;
 };
 
 // Tile geometry shared by the binning and gridding kernels.

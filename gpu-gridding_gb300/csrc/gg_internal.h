@@ -103,6 +103,16 @@ template <typename Real>
 cudaError_t launch_place(PlaceParams<Real> p, StackView view, TileGeom geom,
                          int grid_index, unsigned long long vis_offset,
                          PlaceOut out, cudaStream_t s);
+// *p = v on stream s (device p), without a copy-engine transfer.
+cudaError_t launch_store_f64(double* p, double v, cudaStream_t s);
+// For a placement made with PlaceParams::defer_norm: the norm terms from
+// the placed meta and the stack's tap sums, reduced in k_place's block
+// order, then *d_norm += their sum exactly as launch_place_finalize would.
+template <typename Real>
+cudaError_t launch_norm_terms(const uint32_t* meta, const Real* weight,
+                              unsigned long long n, StackView view,
+                              double* blk_norm, double* d_norm,
+                              cudaStream_t s);
 // Sums the per-block partials: *d_norm += norm, *d_num_skipped = skips,
 // *d_macs = macs (all device pointers), and picks the tile shape for the
 // call into *d_shape: forced_shape if >= 0, else from the mean footprint

@@ -49,10 +49,12 @@ k_place(PlaceParams<Real> p, StackView v, TileGeom g, PlaceOut out) {
       const unsigned long long f = 2ull * s + 1;
       macs = f * f;
       const int side = 2 * v.omax + 1;
-      const double ts = v.tap_sum[((size_t)r.plane * side + (r.ou + v.omax)) *
-                                      side + (r.ov + v.omax)];
+      const double ts =
+          p.defer_norm ? 0.0
+                       : v.tap_sum[((size_t)r.plane * side + (r.ou + v.omax)) *
+                                       side + (r.ov + v.omax)];
       // oskar_grid_wproj.c:210: *norm += sum * weight_i (FP64).
-      if (p.weight) norm = __dmul_rn(ts, (double)w);
+      if (p.weight && !p.defer_norm) norm = __dmul_rn(ts, (double)w);
     }
   }
   // Block reductions by warp shuffles, then one partial per block; the
@@ -79,6 +81,38 @@ k_place(PlaceParams<Real> p, StackView v, TileGeom g, PlaceOut out) {
   }
 }
 
+// The norm terms of a placement made with defer_norm: the same per-point
+// products and the same block reduction as k_place, so blk_norm is
+// bit-identical to what k_place would have written.
+template <typename Real>
+__global__ void __launch_bounds__(kPlaceThreads)
+k_norm_terms(const uint32_t* __restrict__ meta, const Real* __restrict__ weight,
+             unsigned long long n, StackView v, double* __restrict__ blk_norm) {
+  const unsigned long long i =
+      (unsigned long long)blockIdx.x * kPlaceThreads + threadIdx.x;
+  double norm = 0.0;
+  if (i < n) {
+    const uint32_t m = meta[i];
+    if (!meta_skipped(m)) {
+      const int side = 2 * v.omax + 1;
+      const double ts = v.tap_sum[((size_t)meta_plane(m) * side +
+                                   (meta_ou(m) + v.omax)) * side +
+                                  (meta_ov(m) + v.omax)];
+      norm = __dmul_rn(ts, (double)weight[i]);
+    }
+  }
+  __shared__ double s_norm[kPlaceThreads / 32];
+  norm = warp_sum(norm);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) s_norm[warp] = norm;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double bn = 0.0;
+    for (int w = 0; w < kPlaceThreads / 32; ++w) bn += s_norm[w];
+    blk_norm[blockIdx.x] = bn;
+  }
+}
+
 __global__ void k_place_finalize(const double* __restrict__ blk_norm,
                                  const unsigned long long* __restrict__ blk_skip,
                                  const unsigned long long* __restrict__ blk_macs,
@@ -96,7 +130,9 @@ __global__ void k_place_finalize(const double* __restrict__ blk_norm,
   double n = 0.0;
   unsigned long long s = 0, m = 0;
   for (int b = threadIdx.x; b < num_blocks; b += blockDim.x) {
-    n += blk_norm[b]; s += blk_skip[b]; m += blk_macs[b];
+    n += blk_norm[b];
+    if (blk_skip) s += blk_skip[b];
+    if (blk_macs) m += blk_macs[b];
   }
   n = warp_sum(n); s = warp_sum(s); m = warp_sum(m);
   if (lane == 0) { s_n[warp] = n; s_s[warp] = s; s_m[warp] = m; }
@@ -111,7 +147,7 @@ __global__ void k_place_finalize(const double* __restrict__ blk_norm,
       if (d_norm) *d_norm += n;
       if (d_num_skipped) *d_num_skipped = s;
       if (d_macs) *d_macs = m;
-      *d_shape = choose_shape(m, n_points - s, forced_shape);
+      if (d_shape) *d_shape = choose_shape(m, n_points - s, forced_shape);
     }
   }
 }
@@ -264,6 +300,29 @@ cudaError_t launch_place_finalize(const double* blk_norm,
   return cudaGetLastError();
 }
 
+__global__ void k_store_f64(double* p, double v) { *p = v; }
+
+cudaError_t launch_store_f64(double* p, double v, cudaStream_t s) {
+  k_store_f64<<<1, 1, 0, s>>>(p, v);
+  return cudaGetLastError();
+}
+
+template <typename Real>
+cudaError_t launch_norm_terms(const uint32_t* meta, const Real* weight,
+                              unsigned long long n, StackView view,
+                              double* blk_norm, double* d_norm,
+                              cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const int nb = place_num_blocks(n);
+  k_norm_terms<Real><<<nb, kPlaceThreads, 0, s>>>(meta, weight, n, view,
+                                                 blk_norm);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_place_finalize<<<1, 1024, 0, s>>>(blk_norm, nullptr, nullptr, nb, n, 0,
+                                      d_norm, nullptr, nullptr, nullptr);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_count_records(const uint32_t* cell, const uint32_t* meta,
                                  unsigned long long n, StackView view,
                                  const uint32_t* d_shape, uint32_t* count,
@@ -290,6 +349,12 @@ cudaError_t launch_emit_records(const uint32_t* cell, const uint32_t* meta,
   return cudaGetLastError();
 }
 
+template cudaError_t launch_norm_terms<float>(const uint32_t*, const float*,
+                                              unsigned long long, StackView,
+                                              double*, double*, cudaStream_t);
+template cudaError_t launch_norm_terms<double>(const uint32_t*, const double*,
+                                               unsigned long long, StackView,
+                                               double*, double*, cudaStream_t);
 template cudaError_t launch_place<float>(PlaceParams<float>, StackView,
                                          TileGeom, int, unsigned long long,
                                          PlaceOut, cudaStream_t);

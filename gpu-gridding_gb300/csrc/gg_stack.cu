@@ -213,32 +213,39 @@ __global__ void k_tap_sums_rows(const Real* __restrict__ conv, StackView v,
 // plane p (E_p = cube_read_extent) from a cube in host memory that the
 // device addresses (page-locked and mapped, or pageable on a device that
 // reads pageable memory) to the same place in a device cube.  One warp per
-// row: the row's E_p complex taps are contiguous, so a warp's loads are
-// coalesced whatever the row pitch; 4 loads per lane are in flight before
-// the stores to cover the host link's latency.  blockIdx.x = plane,
-// blockIdx.y * 8 + warp = row.
+// row at a time, rows taken grid-stride over planes x csh (rows at or past
+// E_p skipped): a row's E_p complex taps are contiguous, so a warp's loads
+// are coalesced whatever the row pitch, and 4 loads per lane are in flight
+// before the stores.  The host link, not the SMs, bounds the copy, so a
+// few blocks (about 64k loads in flight) reach its rate and leave the other
+// SMs to the kernels that run beside it.
 template <typename Real>
 __global__ void k_cube_gather(const typename Vec2<Real>::type* __restrict__ src,
                               StackView v,
                               typename Vec2<Real>::type* __restrict__ dst) {
   using R2 = typename Vec2<Real>::type;
-  const int p = blockIdx.x;
-  const int row = blockIdx.y * 8 + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   const int csh = v.conv_size_half;
-  const int e = cube_read_extent(v.support[p], v.oversample, v.omax, csh);
-  if (row >= e) return;
-  const size_t off = ((size_t)p * csh + row) * csh;
-  const R2* a = src + off;
-  R2* b = dst + off;
-  for (int c = lane; c < e; c += 128) {
-    R2 t[4];
+  const long long rows = (long long)v.num_planes * csh;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long f = (long long)blockIdx.x * (blockDim.x >> 5) +
+                     (threadIdx.x >> 5);
+       f < rows; f += warps) {
+    const int p = (int)(f / csh), row = (int)(f - (long long)p * csh);
+    const int e = cube_read_extent(v.support[p], v.oversample, v.omax, csh);
+    if (row >= e) continue;
+    const size_t off = (size_t)f * csh;
+    const R2* a = src + off;
+    R2* b = dst + off;
+    for (int c = lane; c < e; c += 128) {
+      R2 t[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-      if (c + 32 * q < e) t[q] = a[c + 32 * q];
+      for (int q = 0; q < 4; ++q)
+        if (c + 32 * q < e) t[q] = a[c + 32 * q];
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-      if (c + 32 * q < e) b[c + 32 * q] = t[q];
+      for (int q = 0; q < 4; ++q)
+        if (c + 32 * q < e) b[c + 32 * q] = t[q];
+    }
   }
 }
 
@@ -285,9 +292,8 @@ template <typename Real>
 cudaError_t launch_cube_gather(const Real* src, StackView view, Real* dst,
                                cudaStream_t s) {
   if (view.num_planes <= 0) return cudaSuccess;
-  dim3 grid(view.num_planes, (view.conv_size_half + 7) / 8);
   using R2 = typename Vec2<Real>::type;
-  k_cube_gather<Real><<<grid, 256, 0, s>>>((const R2*)src, view, (R2*)dst);
+  k_cube_gather<Real><<<16, 1024, 0, s>>>((const R2*)src, view, (R2*)dst);
   return cudaGetLastError();
 }
 
