@@ -571,12 +571,18 @@ def run_ours(args):
         # Bytes the drop-in copied in its last call (every step copies the
         # same): the grid comes back only where tiles hold records.
         h2d, d2h = pkg.host_last_transfer()
+        # One more call with phase events (not timed above).
+        pkg.set_host_profiling(True)
+        e2e_step()
+        host_phases = pkg.host_phase_ms()
+        pkg.set_host_profiling(False)
         e2e = {"value": replica_throughput(world, num_vis, te), "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "host_buffers": "page-locked",
                "grid_access": ["copy", "pinned", "pageable"][
                    pkg.host_grid_access()],
-               "host_tuning": host_tuning or pkg.host_tuning()}
+               "host_tuning": host_tuning or pkg.host_tuning(),
+               "phase_ms": host_phases}
         # The same call on pageable (malloc) buffers, as a numpy caller
         # passes them (the grid's pages already touched).
         hp = {k: np.ascontiguousarray(v).copy() for k, v in h.items()}
