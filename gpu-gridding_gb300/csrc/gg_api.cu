@@ -2137,19 +2137,25 @@ int degrid_host(size_t num_w_planes, const int* support, int oversample,
   gg_kernels* K = nullptr;
   GG_TRY(host_kernels<Real>(st, num_w_planes, support, oversample,
                             conv_size_half, conv_func, s, uploads, &K));
-  if (n) {
+  // A grid the device addresses is read in place by the degridding kernel
+  // (each work item loads its tile once); others go up behind the cube.
+  const void* direct =
+      n ? direct_host_address(st, dev, grid, grid_bytes, 2 * sizeof(Real))
+        : nullptr;
+  if (n && !direct) {
     GG_CUDA(cudaStreamWaitEvent(cs, st->cube_staged, 0));
     GG_CUDA(cudaMemcpyAsync(plan->in_grid.p, grid, grid_bytes,
                             cudaMemcpyHostToDevice, cs));
   }
   GG_CUDA(cudaEventRecord(st->grid_ready, cs));
   GG_CUDA(cudaStreamWaitEvent(s, st->vis_ready, 0));
-  plan->grid_wait = st->grid_ready;
+  plan->grid_wait = direct ? nullptr : st->grid_ready;
   plan->stack_wait = st->stack_ready;
   const int rc = degrid_pipeline<Real>(
       plan, K, n, plan->in_uu.as<Real>(), plan->in_vv.as<Real>(),
       plan->in_ww.as<Real>(), cell_size_rad, w_scale, grid_size,
-      plan->in_grid.as<Real>(), plan->in_vis.as<Real>(), s);
+      direct ? (const Real*)direct : plan->in_grid.as<Real>(),
+      plan->in_vis.as<Real>(), s);
   plan->grid_wait = nullptr;
   plan->stack_wait = nullptr;
   GG_TRY(rc);
