@@ -222,8 +222,9 @@ GG_API int gg_plan_get_tuning(const gg_plan* plan, gg_tuning* tuning);
 GG_API int gg_host_set_tuning(const gg_tuning* tuning);
 GG_API int gg_host_get_tuning(gg_tuning* tuning);
 
-/* How the host-pointer gridding calls on the current device reach the
- * caller's grid and kernel cube.
+/* How the host-pointer gridding and degridding calls on the current device
+ * reach the caller's grid and kernel cube (degridding only reads the
+ * grid: in place, each work item loads its tile once).
  *   GG_GRID_ACCESS_COPY:     both are copied to the device (the cube's read
  *                            squares by 3-D copies); the grid is gridded
  *                            there and the rows' spans that hold records
