@@ -124,10 +124,10 @@ struct DeviceState {
   DevBuf host_cube[2];
   DevBuf cube_changed;
   int cube_cur = -1;
-  // Side stream that uploads a host call's visibilities and grid while the
-  // kernel stack is rebuilt (vis_ready, grid_ready mark the two uploads),
-  // and the pinned tile-row spans of the grid cells a call touched
-  // (spans_ready marks their arrival).
+  // Side stream that uploads a host call's plane tables, visibilities and
+  // (copied) grid (vis_ready, grid_ready mark the uploads), and the pinned
+  // tile-row spans of the grid cells a copied call touched (spans_ready
+  // marks their arrival).
   cudaStream_t copy_stream = nullptr;
   // Stream of the stack build (cube staging, comparison, re-layout, tap
   // sums), which runs beside placement and binning: tables_ready marks the
@@ -1581,7 +1581,7 @@ void* direct_host_address(DeviceState* st, int dev, const void* grid,
              : nullptr;
 }
 
-// Host-pointer drop-in: stage inputs, grid on the device, copy back.
+// Host-pointer drop-in: inputs staged, the grid used in place or copied.
 // The kernel stack of a host-pointer call, rebuilt from the caller's cube
 // into the device's reused stack object (the caller holds the device lock
 // and synchronises s before returning).
