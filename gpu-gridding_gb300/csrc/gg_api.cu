@@ -1582,9 +1582,10 @@ void* direct_host_address(DeviceState* st, int dev, const void* grid,
 }
 
 // Host-pointer drop-in: inputs staged, the grid used in place or copied.
-// The kernel stack of a host-pointer call, rebuilt from the caller's cube
-// into the device's reused stack object (the caller holds the device lock
-// and synchronises s before returning).
+// The kernel stack of a host-pointer call in the device's reused stack
+// object: the caller's cube is staged every call and re-laid only when it
+// differs from the one the stack was made from (the caller holds the
+// device lock and synchronises the streams before returning).
 template <typename Real>
 int host_kernels(DeviceState* st, size_t num_w_planes, const int* support,
                  int oversample, int conv_size_half, const Real* conv_func,
