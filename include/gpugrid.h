@@ -247,7 +247,10 @@ GG_API int gg_host_get_tuning(gg_tuning* tuning);
  *                            in at some 25 us, so a freshly allocated zero
  *                            grid is copied.
  * An array must be aligned to its complex element (8 bytes for _f, 16 for
- * _d) to be used in place.  The grid in place is bit-identical to the
+ * _d) to be used in place.  The grid is written in place, so it must be
+ * writable memory (as it must for any mode: it is accumulated): never a
+ * read-only mapping or a cudaHostRegisterReadOnly registration, which the
+ * device could not write; use GG_GRID_ACCESS_COPY for such arrays.  The grid in place is bit-identical to the
  * device-pointer call's; copied, it is too on grids under 128 MiB (above,
  * the copy's split passes change the rounding only). */
 enum {
