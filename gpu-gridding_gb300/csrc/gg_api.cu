@@ -1773,6 +1773,9 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   // The starting norm is set by a one-thread kernel rather than a copy, so
   // that it does not queue behind the uploads on the copy engines.
   GG_CUDA(launch_store_f64(d_norm, *norm, s));
+  if (direct)
+    GG_CUDA(cudaMemsetAsync(scalar64(plan, kDirectCells), 0,
+                            sizeof(unsigned long long), s));
   plan->grid_wait = direct ? nullptr : st->grid_ready;
   plan->h_spans = direct ? nullptr : st->h_spans;
   plan->h_spans_cap = DeviceState::kSpanCap;
@@ -1787,9 +1790,6 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   plan->stack_wait = st->stack_ready;
   plan->norm_weight = plan->in_weight.p;
   plan->norm_out = d_norm;
-  if (direct)
-    GG_CUDA(cudaMemsetAsync(scalar64(plan, kDirectCells), 0,
-                            sizeof(unsigned long long), s));
   const int rc = grid_pipeline<Real>(plan, K, n, plan->in_uu.as<Real>(),
                                      plan->in_vv.as<Real>(),
                                      plan->in_ww.as<Real>(),
