@@ -1,7 +1,7 @@
 // FP32 fused-multiply-add throughput probe: the denominator of the
 // gridding kernel's roofline.  The gridder's arithmetic is FP32 FMA on the
-// CUDA cores (4 FMA per complex multiply-add), a peak the driver's measured
-// peaks (HBM copy, bf16 tensor GEMM) do not cover, so it is measured here:
+// CUDA cores (4 FMA per complex multiply-add), a peak that an HBM copy or
+// a bf16 tensor GEMM does not measure, so it is measured here:
 // every SM runs independent FMA chains long enough to reach steady clocks.
 #include "gg_internal.h"
 
