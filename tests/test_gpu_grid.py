@@ -621,6 +621,37 @@ def test_dropin_fresh_pageable_grid_is_copied(pkg, synthetic):
         assert np.array_equal(g.view(np.uint8), g0.view(np.uint8))
 
 
+def test_host_phase_times(pkg, synthetic):
+    """With profiling on, a host call's phase times are there and add up
+    to about its duration; off, none are recorded; a call without
+    visibilities leaves nothing to report."""
+    import time
+    wl = synthetic.random_uniform_workload("phases", 50_000, 1024, 16, 2, 8,
+                                           seed=47, cell_size_rad=6e-5)
+    pkg.grid_f(wl)
+    pkg.set_host_profiling(True)
+    try:
+        t0 = time.perf_counter()
+        pkg.grid_f(wl)
+        wall = (time.perf_counter() - t0) * 1e3
+        ph = pkg.host_phase_ms()
+        assert set(ph) == set(pkg.HOST_PHASES)
+        assert all(v >= 0.0 for v in ph.values())
+        assert ph["grid_tiles"] > 0.0
+        assert 0.0 < sum(ph.values()) <= wall * 1.05 + 0.1
+        empty = dataclasses.replace(wl, uu=wl.uu[:0], vv=wl.vv[:0],
+                                    ww=wl.ww[:0], vis=wl.vis[:0],
+                                    weight=wl.weight[:0])
+        pkg.grid_f(empty)
+        with pytest.raises(pkg.GridError):
+            pkg.host_phase_ms()
+    finally:
+        pkg.set_host_profiling(False)
+    pkg.grid_f(wl)
+    with pytest.raises(pkg.GridError):
+        pkg.host_phase_ms()
+
+
 def test_grid_access_mode_setting(pkg):
     mode = pkg.host_grid_access()
     assert mode == pkg.GRID_ACCESS_PAGEABLE   # the default
