@@ -2,10 +2,12 @@
 """Benchmark of the GB300 W-projection gridder.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload cfg1|cfg0|cfg2|cfg2b]
+                    [--workload cfg2|cfg2b|cfg2s|cfg1|cfg0]
 
-Prints one JSON line (rank 0).  A step is one gridding call over the whole
-workload (placement, binning, sort, tile gridding, partial reduction) onto a
+Prints one JSON line (rank 0).  The default workload is the SKA-LOW
+EL56-82-shaped snapshot (cfg2: 31,395,840 visibilities, 8192^2 grid, 601
+w-planes, support 4..72), the configuration the metric is stated on.  A step
+is one gridding call over the whole workload (placement, binning, sort, tile gridding, partial reduction) onto a
 complex64 grid that stays in HBM; inputs are resident on the device when the
 timed region starts (``value``).  ``e2e`` is the same metric through the
 reference-facing drop-in (oskar_grid_wproj_f, host buffers) with every host
@@ -162,7 +164,7 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="cfg1",
+    ap.add_argument("--workload", default="cfg2",
                     choices=sorted(WORKLOAD_TEXT))
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -328,38 +330,132 @@ def cpu_run(wl, threads, keep=False):
     return (t, grid, ns, nm) if keep else t
 
 
+def _err_sums(a, ref, rows=512):
+    """(max |a - ref|, sum |a - ref|^2, max |ref|, sum |ref|^2) in FP64 over
+    complex grids [G, G, 2], by bands of rows (no whole-grid temporaries)."""
+    a = np.asarray(a)
+    ref = np.asarray(ref)
+    a2 = a.reshape(-1, *a.shape[-2:]) if a.ndim >= 2 else a.reshape(1, -1)
+    r2 = ref.reshape(a2.shape)
+    emax = esq = rmax = rsq = 0.0
+    for i in range(0, a2.shape[0], rows):
+        x = np.asarray(a2[i:i + rows], np.float64)
+        y = np.asarray(r2[i:i + rows], np.float64)
+        d = x - y
+        if d.size:
+            emax = max(emax, float(np.abs(d).max()))
+            rmax = max(rmax, float(np.abs(y).max()))
+        esq += float((d * d).sum())
+        rsq += float((y * y).sum())
+    return emax, esq, rmax, rsq
+
+
 def max_rel_err(a, ref):
     """max |a - ref| / max |ref|, in FP64."""
-    a = np.asarray(a, np.float64)
-    ref = np.asarray(ref, np.float64)
-    scale = float(np.abs(ref).max())
-    err = float(np.abs(a - ref).max())
-    return err / scale if scale > 0 else err
+    emax, _, rmax, _ = _err_sums(a, ref)
+    return emax / rmax if rmax > 0 else emax
 
 
-def accuracy_vs_fp64(wl, grid, nskip, norm, threads, cpu_result=None):
-    """The measured workload's grid against the FP64-accumulation oracle
-    (FP32 placement, no rounding in the sums): max-rel grid error, skip
-    count and norm, beside the same error of the reference's own FP32
-    gridder (the host-threaded restatement, when it ran)."""
+def error_vs(a, ref):
+    """Max and RMS relative error of grid a against grid ref:
+    max |a - ref| / max |ref| and sqrt(sum |a - ref|^2 / sum |ref|^2)."""
+    emax, esq, rmax, rsq = _err_sums(a, ref)
+    return {"max_rel": emax / rmax if rmax > 0 else emax,
+            "rms_rel": float(np.sqrt(esq / rsq)) if rsq > 0 else
+                float(np.sqrt(esq))}
+
+
+def rel(x, ref):
+    return abs(x - ref) / abs(ref) if ref else abs(x - ref)
+
+
+def accuracy_vs_fp64(wl, grid, nskip, norm, threads, cpu_result=None,
+                     with_d=True):
+    """The measured workload's grid, skip count and norm against the
+    oracles, after the timed region:
+
+    * `vs_fp64`: the FP64-accumulation oracle with the FP32 placement of
+      oskar_grid_wproj_f (the yardstick of the 1e-5 bound);
+    * `vs_reference_d`: the reference's own FP64 gridder oskar_grid_wproj_d
+      on the inputs promoted to FP64 (FP64 placement), with the count of
+      visibilities whose FP32 and FP64 placements differ
+      (`placement_disagreements`), which that comparison includes;
+    * `vs_reference_f` (when the reference's FP32 gridder ran on the host,
+      cpu_result): the GPU grid against it, with the stated tolerance
+      max(1e-5, the reference _f's own max-rel error against the FP64
+      oracle + 1e-6), and the reference _f's own errors beside ours.
+
+    All errors are max |a - ref| / max |ref| and
+    sqrt(sum |a - ref|^2 / sum |ref|^2)."""
     oracle = load_oracle()
     t0 = time.perf_counter()
     g64, ns64, nm64 = oracle.grid_f_fp64acc_mt(wl, threads=threads)
+    e64 = error_vs(grid, g64)
     out = {"tolerance": GRID_TOL,
-           "grid_max_rel_err": max_rel_err(grid, g64),
+           "grid_max_rel_err": e64["max_rel"],
+           "grid_rms_rel_err": e64["rms_rel"],
            "num_skipped": int(nskip), "num_skipped_fp64": ns64,
-           "norm_rel_err": abs(norm - nm64) / abs(nm64) if nm64 else
-               abs(norm - nm64)}
+           "norm_rel_err": rel(norm, nm64),
+           "vs_fp64": dict(e64, norm_rel=rel(norm, nm64),
+                           oracle="FP64 sums, FP32 placement")}
+    ok = e64["max_rel"] <= GRID_TOL and int(nskip) == ns64
+    gref = None
     if cpu_result is not None:
         _, gref, ns_ref, nm_ref = cpu_result
-        out["reference_f_max_rel_err"] = max_rel_err(gref, g64)
+        ef = error_vs(gref, g64)
+        out["reference_f_max_rel_err"] = ef["max_rel"]
         out["reference_f_num_skipped"] = int(ns_ref)
-        out["reference_f_norm_rel_err"] = abs(nm_ref - nm64) / abs(nm64) \
-            if nm64 else abs(nm_ref - nm64)
-    out["ok"] = bool(out["grid_max_rel_err"] <= GRID_TOL and
-                     out["num_skipped"] == ns64)
+        out["reference_f_norm_rel_err"] = rel(nm_ref, nm64)
+        tol_f = max(GRID_TOL, ef["max_rel"] + 1e-6)
+        eg = error_vs(grid, gref)
+        out["vs_reference_f"] = dict(
+            eg, tolerance=tol_f, norm_rel=rel(norm, nm_ref),
+            num_skipped_equal=int(nskip) == int(ns_ref),
+            reference_f_vs_fp64=ef)
+        ok = ok and eg["max_rel"] <= tol_f and int(nskip) == int(ns_ref)
+    del g64
+    if with_d:
+        gd, nsd, nmd = oracle.grid_d_promoted_mt(wl, threads=threads)
+        dis, dis_gridded = oracle.placement_disagreements(wl)
+        out["vs_reference_d"] = dict(
+            error_vs(grid, gd), norm_rel=rel(norm, nmd),
+            num_skipped_d=nsd, placement_disagreements=dis,
+            placement_disagreements_gridded=dis_gridded,
+            oracle="oskar_grid_wproj_d on the inputs promoted to FP64")
+        if gref is not None:
+            out["vs_reference_d"]["reference_f_vs_d"] = error_vs(gref, gd)
+        del gd
+    out["ok"] = bool(ok)
     out["oracle_seconds"] = time.perf_counter() - t0
     return out
+
+
+# Visibilities per CPU step of the reference arm: a strided sample keeps a
+# step to a few seconds on the host cores while holding the workload's own
+# uv, w and support distribution.
+CPU_SAMPLE_VIS = 8_000_000
+# Visibilities of the single-thread figure (a strided sample again).
+CPU_SAMPLE_VIS_1T = 1_000_000
+
+
+def cpu_sample(wl, target):
+    k = max(1, -(-wl.num_points // target))
+    return wl.strided(k), k
+
+
+def single_thread_rate(wl):
+    """Mvis/s of the serial restatement of oskar_grid_wproj_f on one host
+    thread, on a strided sample of about CPU_SAMPLE_VIS_1T visibilities."""
+    sample, k = cpu_sample(wl, CPU_SAMPLE_VIS_1T)
+    oracle = load_oracle()
+    grid = np.zeros((wl.grid_size, wl.grid_size, 2), np.float32)
+    t0 = time.perf_counter()
+    oracle.grid_f(sample, grid)
+    t = time.perf_counter() - t0
+    return {"value": sample.num_points / t / 1e6, "unit": UNIT, "cores": 1,
+            "kind": "port",
+            "sample": f"every {k}th visibility ({sample.num_points} vis), "
+                      "serial restatement of oskar_grid_wproj_f, one run"}
 
 
 def run_reference(args):
@@ -367,12 +463,15 @@ def run_reference(args):
     if rank != 0:
         return 0
     wl = load_workload(args.workload)
+    sample, k = cpu_sample(wl, CPU_SAMPLE_VIS)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_run(wl, threads)
-    times = [cpu_run(wl, threads) for _ in range(args.steps)]
+        cpu_run(sample, threads)
+    times = [cpu_run(sample, threads) for _ in range(args.steps)]
     t = statistics.mean(times)
-    value = wl.num_points / t / 1e6
+    value = sample.num_points / t / 1e6
+    what = ("whole workload" if k == 1 else
+            f"every {k}th visibility of the workload")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
@@ -382,7 +481,7 @@ def run_reference(args):
         "config": workload_config(args.workload, wl),
         "cpu_baseline": {
             "value": value, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"whole workload ({wl.num_points} vis) per step; the "
+            "sample": f"{what} ({sample.num_points} vis) per step; the "
                       "oracle's restatement of oskar_grid_wproj_f "
                       "(bit-identical to the reference build), grid rows "
                       f"split over {threads} host threads"},
@@ -678,7 +777,8 @@ def run_ours(args):
                "sample": f"whole workload ({num_vis} vis), one run; the "
                          "oracle's restatement of oskar_grid_wproj_f "
                          "(bit-identical to the reference build), grid rows "
-                         f"split over {threads} host threads"}
+                         f"split over {threads} host threads",
+               "single_thread": single_thread_rate(wl)}
 
     accuracy = None
     if rank == 0 and not args.no_accuracy:

@@ -44,7 +44,8 @@ EXPORTED_SYMBOLS = (
     "gg_plan_probe_bounded_wait",
     "gg_plan_set_profiling",
     "gg_plan_phase_ms", "gg_measure_fp32_fma_tflops", "gg_grid_wproj_f_device",
-    "gg_grid_wproj_f_device_noalloc", "gg_grid_wproj_f_batched_device",
+    "gg_grid_wproj_f_device_noalloc", "gg_noalloc_probe_bounded_wait",
+    "gg_grid_wproj_f_batched_device",
     "gg_grid_wproj_d_batched_device", "gg_grid_wproj_f_batched_replay",
     "gg_grid_wproj_d_batched_replay", "gg_plan_check",
     "gg_grid_wproj_d_device", "gg_place_wproj_f_device",

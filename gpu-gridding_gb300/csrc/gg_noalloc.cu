@@ -20,8 +20,16 @@
 //   serialised by the caller;
 // * a call takes at most kNoAllocMaxPoints visibilities, at most
 //   kNoAllocMaxRecords (visibility, tile) records and a grid side of at most
-//   kNoAllocMaxGrid; larger inputs are rejected with GG_ERR_CAPACITY before
-//   any work is queued;
+//   kNoAllocMaxGrid; larger inputs are rejected with GG_ERR_CAPACITY and
+//   leave the caller's grid, norm and num_skipped untouched (the record
+//   count is known only after placement, whose norm and skip totals go to
+//   the scratch array and reach the caller's outputs once the call is
+//   accepted);
+// * if a call's gridding kernel runs out of its bounded wait, that call has
+//   already returned GG_OK; the failure is reported by the next no-alloc
+//   call on the device (whoever makes it), which returns GG_ERR_CUDA
+//   without touching its outputs -- the incomplete grid is the previous
+//   call's;
 // * the device address of the array is looked up (cudaGetSymbolAddress) by
 //   the first call on each device, which must therefore be made with that
 //   device current and before any stream capture begins.
@@ -40,7 +48,7 @@ using namespace gg;
 constexpr size_t kNoAllocMaxPoints = size_t(1) << 17;   // 131,072
 constexpr size_t kNoAllocMaxRecords = size_t(1) << 20;  // 1,048,576
 constexpr int kNoAllocMaxGrid = 8192;
-constexpr int kNoAllocMaxSlots = 128;    // partial tiles of split tiles
+constexpr int kNoAllocMaxSlots = 384;    // partial tiles of split tiles
 constexpr int kNoAllocCells = 2048;      // cells per tile
 constexpr size_t kNoAllocBytes = size_t(32) << 20;
 constexpr int kMaxDevices = 64;
@@ -86,6 +94,16 @@ int ceil_log2_u(unsigned long long x) {
   int b = 0;
   while ((1ull << b) < x) ++b;
   return b;
+}
+
+// Commits an accepted call's placement totals to the caller's outputs:
+// *d_norm += the call's norm, *d_num_skipped = its skip count.
+__global__ void k_noalloc_commit(const double* __restrict__ norm,
+                                 const unsigned long long* __restrict__ skip,
+                                 double* d_norm,
+                                 unsigned long long* d_num_skipped) {
+  *d_norm += *norm;
+  *d_num_skipped = *skip;
 }
 
 #define NA_CUDA(call)                                                   \
@@ -149,6 +167,10 @@ extern "C" GG_API int gg_grid_wproj_f_device_noalloc(
                                         // 3 split, 4 counter, 5 shape,
                                         // 6 error
   unsigned long long* macs = c.take<unsigned long long>(1);
+  // This call's norm and skip totals, committed to the caller's outputs
+  // only once the call is accepted.
+  double* call_norm = c.take<double>(1);
+  unsigned long long* call_skip = c.take<unsigned long long>(1);
   uint32_t* cell = c.take<uint32_t>(maxp);
   uint32_t* meta = c.take<uint32_t>(maxp);
   float2* vw = c.take<float2>(maxp);
@@ -178,6 +200,7 @@ extern "C" GG_API int gg_grid_wproj_f_device_noalloc(
   // call accumulates into.  Word 6, the bounded-wait error flag of the
   // tile kernel, is left for the check below.
   NA_CUDA(cudaMemsetAsync(sc, 0, 6 * sizeof(uint32_t), s));
+  NA_CUDA(cudaMemsetAsync(call_norm, 0, sizeof(double), s));
 
   PlaceParams<float> pp;
   pp.uu = d_uu; pp.vv = d_vv; pp.ww = d_ww; pp.vis = d_vis;
@@ -198,7 +221,7 @@ extern "C" GG_API int gg_grid_wproj_f_device_noalloc(
   const int nblk = place_num_blocks(num_points);
   NA_CUDA(launch_place<float>(pp, view, TileGeom{}, 0, 0, po, s));
   NA_CUDA(launch_place_finalize(blk_norm, blk_skip, blk_macs, nblk,
-                                num_points, -1, d_norm, d_num_skipped, macs,
+                                num_points, -1, call_norm, call_skip, macs,
                                 sc + 5, s));
   NA_CUDA(launch_count_records(cell, meta, num_points, view, sc + 5, count,
                                s));
@@ -215,11 +238,16 @@ extern "C" GG_API int gg_grid_wproj_f_device_noalloc(
   }
   const uint32_t total = host_sc[0];
   const int shape = (int)(host_sc[5] & 0xFFu);
+  const bool stage = ((host_sc[5] >> 8) & 1u) != 0;
   if (total > kNoAllocMaxRecords)
     return record_error(GG_ERR_CAPACITY,
                         "the call needs more (visibility, tile) records than "
-                        "the no-alloc limit of 1048576 (norm and num_skipped "
-                        "were written, the grid was not)");
+                        "the no-alloc limit of 1048576 (grid, norm and "
+                        "num_skipped untouched)");
+  // Accepted: the placement totals reach the caller's outputs.
+  k_noalloc_commit<<<1, 1, 0, s>>>(call_norm, call_skip, d_norm,
+                                   d_num_skipped);
+  NA_CUDA(cudaGetLastError());
   if (total == 0) return GG_OK;
 
   // ---- binning, work items, gridding, reduction ---------------------------
@@ -255,12 +283,18 @@ extern "C" GG_API int gg_grid_wproj_f_device_noalloc(
                              s));
   int sms = 0;
   NA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int num_ctas = sms * grid_tiles_ctas_per_sm<float>(geom.tile_u, false);
-  // At most kNoAllocMaxSlots / 2 chunks' worth of split tiles: split
-  // chunks <= 2 * total / chunk <= kNoAllocMaxSlots.
+  const int num_ctas = sms * grid_tiles_ctas_per_sm<float>(geom.tile_u, stage);
+  // Work items of about total / (2 * num_ctas) records, as the allocating
+  // path sizes them, but never so small that the split tiles need more
+  // partial-tile slots than the array holds: a tile of c > chunk records
+  // splits into at most 2c / chunk chunks, so split chunks
+  // <= 2 * total / chunk <= kNoAllocMaxSlots.
+  const unsigned long long per_item =
+      ((unsigned long long)total + 2ull * num_ctas - 1) / (2ull * num_ctas);
+  const unsigned long long min_chunk =
+      (2ull * total + kNoAllocMaxSlots - 1) / kNoAllocMaxSlots;
   const uint32_t chunk = (uint32_t)std::max<unsigned long long>(
-      64, ((unsigned long long)total + kNoAllocMaxSlots / 2 - 1) /
-              (kNoAllocMaxSlots / 2));
+      64, std::max(per_item, min_chunk));
   ItemBuffers ib;
   ib.chunks = item_a;
   ib.split_chunks = item_b;
@@ -277,6 +311,23 @@ extern "C" GG_API int gg_grid_wproj_f_device_noalloc(
   NA_CUDA(launch_grid_tiles<float>(items, sc + 8, sc + 4, sc + 6, vals, cell,
                                    meta, vw, view, geom, grid_size, d_grid, 0,
                                    (float*)partials, split_tiles, sc + 3,
-                                   num_tiles, num_ctas, false, s));
+                                   num_tiles, num_ctas, stage, s));
+  return GG_OK;
+}
+
+extern "C" GG_API int gg_noalloc_probe_bounded_wait(unsigned iterations,
+                                                    void* stream) {
+  if (iterations < 1 || iterations > (1u << 20))
+    return record_error(GG_ERR_INVALID_ARG, "iterations outside 1..1048576");
+  int dev = 0;
+  NA_CUDA(cudaGetDevice(&dev));
+  unsigned char* scratch = nullptr;
+  const int r = scratch_address(dev, &scratch);
+  if (r != GG_OK) return r;
+  // Word 6 of the first carve (the control words at offset 0).
+  uint32_t* flag = (uint32_t*)scratch + 6;
+  cudaStream_t s = (cudaStream_t)stream;
+  NA_CUDA(launch_wait_probe(iterations, flag, s));
+  NA_CUDA(cudaStreamSynchronize(s));
   return GG_OK;
 }

@@ -73,6 +73,17 @@ class Workload:
             ww=self.ww[a:b], vis=self.vis[a:b], weight=self.weight[a:b],
             channel_offsets=None)
 
+    def strided(self, k: int) -> "Workload":
+        """Every k-th visibility (same kernels and grid): a sample with the
+        workload's own uv, w and support distribution."""
+        if k <= 1:
+            return self
+        return dataclasses.replace(
+            self, name=f"{self.name}[::{k}]", uu=self.uu[::k].copy(),
+            vv=self.vv[::k].copy(), ww=self.ww[::k].copy(),
+            vis=self.vis[::k].copy(), weight=self.weight[::k].copy(),
+            channel_offsets=None)
+
     def subset(self, n: int) -> "Workload":
         """The first n visibilities (same kernels and grid)."""
         return dataclasses.replace(

@@ -393,11 +393,17 @@ GG_API int gg_plan_probe_bounded_wait(gg_plan* plan, unsigned iterations,
  * the call.  The kernel-stack handle is made beforehand (that step
  * allocates).  Limits: num_points <= 131072, grid_size <= 8192, and at most
  * 1048576 (visibility, tile) records; beyond them the call returns
- * GG_ERR_CAPACITY.  All calls on a device share the array, so calls that
- * overlap on the GPU race and must be serialised by the caller.  The first
- * call on each device looks up the array's device address; make it with
- * that device current and before any stream capture.  Same semantics and
- * results as gg_grid_wproj_f_device otherwise (grid and *d_norm accumulated,
+ * GG_ERR_CAPACITY and leaves the grid, *d_norm and *d_num_skipped untouched
+ * (so a caller may split the call and retry).  All calls on a device share
+ * the array, so calls that overlap on the GPU race and must be serialised by
+ * the caller.  The first call on each device looks up the array's device
+ * address; make it with that device current and before any stream capture.
+ * If a call's gridding kernel runs out of its bounded wait (see
+ * gg_plan_check), that call has already returned GG_OK: the failure is
+ * reported by the next no-alloc call on the same device, which returns
+ * GG_ERR_CUDA with its outputs untouched and clears the flag -- the
+ * incomplete grid is the earlier call's.  Same semantics and results as
+ * gg_grid_wproj_f_device otherwise (grid and *d_norm accumulated,
  * *d_num_skipped set; one stream synchronisation per call). */
 GG_API int gg_grid_wproj_f_device_noalloc(const gg_kernels* kernels,
         size_t num_points, const float* d_uu, const float* d_vv,
@@ -405,6 +411,13 @@ GG_API int gg_grid_wproj_f_device_noalloc(const gg_kernels* kernels,
         float cell_size_rad, float w_scale, int grid_size,
         unsigned long long* d_num_skipped, double* d_norm, float* d_grid,
         void* stream);
+
+/* Diagnostic of the no-alloc failure report, safe to run: the bounded wait
+ * of gg_plan_probe_bounded_wait, run out on purpose against the no-alloc
+ * array's error flag on the current device, so that the next
+ * gg_grid_wproj_f_device_noalloc call on it reports GG_ERR_CUDA.  No
+ * counterpart in the reference.  iterations in 1..1048576. */
+GG_API int gg_noalloc_probe_bounded_wait(unsigned iterations, void* stream);
 
 /* Placement only (diagnostic): writes, per visibility, six int32 --
  * cell u, cell v, off_u, off_v, w-plane (after the clamp to the last plane)

@@ -27,13 +27,16 @@ _dp = ctypes.POINTER(ctypes.c_double)
 
 
 def build(reference_dir: str | None = None) -> None:
-    """Compile liboracle.so, and libref.so when the reference tree exists."""
+    """Compile liboracle.so, and libref.so when the reference tree exists.
+
+    The reference tree's location is the Makefile's REFERENCE variable,
+    overridden by reference_dir or $GG_REFERENCE_DIR; the `ref-if-present`
+    target skips the build where the tree is absent."""
     subprocess.check_call(["make", "-s", "-C", HERE, "all"])
-    ref = reference_dir or os.environ.get("GG_REFERENCE_DIR",
-                                          "/root/reference")
-    if os.path.isfile(os.path.join(ref, "oskar_grid_wproj.c")):
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref",
-                               f"REFERENCE={ref}"])
+    ref = reference_dir or os.environ.get("GG_REFERENCE_DIR")
+    extra = [f"REFERENCE={ref}"] if ref else []
+    subprocess.check_call(["make", "-s", "-C", HERE, "ref-if-present"] +
+                          extra)
 
 
 def _grid_sig(fn, real):
@@ -75,6 +78,9 @@ def lib():
         L.oracle_grid_wproj_f_fp64acc_mt.argtypes = [ctypes.c_int] + \
             L.oracle_grid_wproj_f_fp64acc.argtypes
         L.oracle_grid_wproj_f_fp64acc_mt.restype = ctypes.c_int
+        L.oracle_grid_wproj_d_promoted_mt.argtypes = \
+            L.oracle_grid_wproj_f_fp64acc_mt.argtypes
+        L.oracle_grid_wproj_d_promoted_mt.restype = ctypes.c_int
         L.oracle_degrid_wproj_f_fp64.argtypes = [
             _sz, _i32p, ctypes.c_int, ctypes.c_int, _f32p, _sz, _f32p, _f32p,
             _f32p, ctypes.c_float, ctypes.c_float, ctypes.c_int, _f64p, _f64p]
@@ -205,6 +211,42 @@ def grid_f_fp64acc_mt(wl, grid=None, norm=0.0, threads=None):
     if rc != 0:
         raise MemoryError("oracle_grid_wproj_f_fp64acc_mt: no scratch memory")
     return grid, int(ns.value), float(nm.value)
+
+
+def grid_d_promoted_mt(wl, grid=None, norm=0.0, threads=None):
+    """The reference's FP64 gridder (oskar_grid_wproj_d semantics: FP64
+    placement and sums) on the FP32 workload promoted to FP64, on host
+    threads; bit-identical to grid_d on the promoted arrays."""
+    grid = new_grid(wl, np.float64) if grid is None else grid
+    assert grid.dtype == np.float64 and grid.flags.c_contiguous
+    threads = threads or os.cpu_count() or 1
+    ns = ctypes.c_size_t(0)
+    nm = ctypes.c_double(norm)
+    rc = lib().oracle_grid_wproj_d_promoted_mt(
+        threads, wl.num_w_planes, _c(wl.support, np.int32), wl.oversample,
+        wl.conv_size_half, _c(wl.conv_func, np.float32).reshape(-1),
+        wl.num_points, _c(wl.uu, np.float32), _c(wl.vv, np.float32),
+        _c(wl.ww, np.float32), _c(wl.vis, np.float32).reshape(-1),
+        _c(wl.weight, np.float32), np.float32(wl.cell_size_rad),
+        np.float32(wl.w_scale), wl.grid_size, ctypes.byref(ns),
+        ctypes.byref(nm), grid.reshape(-1))
+    if rc != 0:
+        raise MemoryError("oracle_grid_wproj_d_promoted_mt: no scratch "
+                          "memory")
+    return grid, int(ns.value), float(nm.value)
+
+
+def placement_disagreements(wl):
+    """Visibilities whose cell, offsets, plane or skip differ between the
+    FP32 rules (oskar_grid_wproj_f) and the FP64 rules on the promoted
+    coordinates (oskar_grid_wproj_d): (count, count among visibilities
+    gridded by either)."""
+    pf, pd = place(wl, "f"), place(wl, "d")
+    diff = np.zeros(wl.num_points, bool)
+    for k in ("gu", "gv", "ou", "ov", "plane", "skipped"):
+        diff |= pf[k] != pd[k]
+    either = (pf["skipped"] == 0) | (pd["skipped"] == 0)
+    return int(diff.sum()), int((diff & either).sum())
 
 
 def place(wl, precision="f"):

@@ -423,6 +423,7 @@ typedef struct
     size_t num_w_planes;
     float cell_size_rad, w_scale;
     double* grid64;     /* non-null: FP64 accumulation into this grid */
+    int place64;        /* 1: FP64 placement of the promoted coordinates */
     int next;           /* work counter, atomically incremented */
     int phase;          /* 0: placement + tap sums, 1: gridding bands */
     size_t chunk;
@@ -433,13 +434,20 @@ static void mt_place_chunk(mt_job_t* job, size_t i0, size_t i1)
     size_t i;
     const int centre = job->grid_size / 2;
     const float scale = job->grid_size * job->cell_size_rad;
+    /* oskar_grid_wproj.c:59: the FP64 grid scale of the promoted cell. */
+    const double scale64 = job->grid_size * (double)job->cell_size_rad;
     for (i = i0; i < i1; ++i)
     {
         int j, k;
         double tap_sum = 0.0;
-        const oracle_place_t p = place_f(job->uu[i], job->vv[i], job->ww[i],
-                scale, centre, job->grid_size, job->oversample,
-                job->num_w_planes, job->support, job->w_scale);
+        const oracle_place_t p = job->place64 ?
+                place_d((double)job->uu[i], (double)job->vv[i],
+                        (double)job->ww[i], scale64, centre, job->grid_size,
+                        job->oversample, job->num_w_planes, job->support,
+                        (double)job->w_scale) :
+                place_f(job->uu[i], job->vv[i], job->ww[i],
+                        scale, centre, job->grid_size, job->oversample,
+                        job->num_w_planes, job->support, job->w_scale);
         ((oracle_place_t*)job->place)[i] = p;
         if (!p.skipped)
         {
@@ -569,7 +577,7 @@ static int mt_grid(int num_threads, size_t num_w_planes,
         const float* vv, const float* ww, const float* vis,
         const float* weight, float cell_size_rad, float w_scale,
         int grid_size, size_t* num_skipped, double* norm, float* grid,
-        double* grid64)
+        double* grid64, int place64)
 {
     size_t i, n_skip = 0;
     mt_job_t job;
@@ -586,6 +594,7 @@ static int mt_grid(int num_threads, size_t num_w_planes,
     }
     job.conv_func = conv_func; job.vis = vis; job.weight = weight;
     job.grid = grid; job.grid64 = grid64; job.num_points = num_points;
+    job.place64 = place64;
     job.plane_stride = (size_t)(conv_size_half * conv_size_half);
     job.oversample = oversample; job.conv_size_half = conv_size_half;
     job.grid_size = grid_size;
@@ -625,7 +634,8 @@ ORACLE_API int oracle_grid_wproj_f_mt(int num_threads, size_t num_w_planes,
 {
     return mt_grid(num_threads, num_w_planes, support, oversample,
             conv_size_half, conv_func, num_points, uu, vv, ww, vis, weight,
-            cell_size_rad, w_scale, grid_size, num_skipped, norm, grid, NULL);
+            cell_size_rad, w_scale, grid_size, num_skipped, norm, grid, NULL,
+            0);
 }
 
 /* oracle_grid_wproj_f_fp64acc on num_threads host threads: every cell
@@ -641,7 +651,31 @@ ORACLE_API int oracle_grid_wproj_f_fp64acc_mt(int num_threads,
 {
     return mt_grid(num_threads, num_w_planes, support, oversample,
             conv_size_half, conv_func, num_points, uu, vv, ww, vis, weight,
-            cell_size_rad, w_scale, grid_size, num_skipped, norm, NULL, grid);
+            cell_size_rad, w_scale, grid_size, num_skipped, norm, NULL, grid,
+            0);
+}
+
+/* oskar_grid_wproj_d (oskar_grid_wproj.c:37-123) on FP32 inputs promoted
+ * to FP64 -- coordinates, visibilities, weights, kernel cube, cell size and
+ * w scale -- run on num_threads host threads: FP64 placement, FP64 sums in
+ * input order per cell, so grid and norm are bit-identical to the serial
+ * oracle_grid_wproj_d (and the reference's _d) on the promoted arrays.  This
+ * is the reference's own FP64 answer for an FP32 workload; where its FP64
+ * placement puts a visibility in another cell, offset or plane than the
+ * FP32 rules do, it differs from oracle_grid_wproj_f_fp64acc_mt by that
+ * visibility's contribution.  Returns 0, or -1 when scratch memory cannot
+ * be had. */
+ORACLE_API int oracle_grid_wproj_d_promoted_mt(int num_threads,
+        size_t num_w_planes, const int* support, int oversample,
+        int conv_size_half, const float* conv_func, size_t num_points,
+        const float* uu, const float* vv, const float* ww, const float* vis,
+        const float* weight, float cell_size_rad, float w_scale,
+        int grid_size, size_t* num_skipped, double* norm, double* grid)
+{
+    return mt_grid(num_threads, num_w_planes, support, oversample,
+            conv_size_half, conv_func, num_points, uu, vv, ww, vis, weight,
+            cell_size_rad, w_scale, grid_size, num_skipped, norm, NULL, grid,
+            1);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -82,6 +82,28 @@ def test_dot_product_identity(pkg, synthetic, torch, prec, tol):
     assert rel <= tol
 
 
+def test_dot_product_identity_cfg1_shape(pkg, synthetic, torch):
+    """The FP32 dot-product identity on the whole synthetic-challenge shape
+    the gridding/degridding pair is stated on (2,152,800 visibilities,
+    8192^2 grid, 714 w-planes, support 4..36): relative 1e-6."""
+    wl = synthetic.config1()
+    s = _setup(pkg, torch, wl, "f")
+    g = torch.Generator(device="cuda").manual_seed(7)
+    x = torch.randn((wl.num_points, 2), generator=g, device="cuda",
+                    dtype=torch.float32)
+    y = torch.randn((wl.grid_size, wl.grid_size, 2), generator=g,
+                    device="cuda", dtype=torch.float32)
+    ones = torch.ones(wl.num_points, dtype=torch.float32, device="cuda")
+    gx = _forward(pkg, torch, s, x, ones)
+    ghy = _adjoint(pkg, torch, s, y)
+    lhs = _cdot(gx.double(), y.double())
+    rhs = _cdot(x.double(), ghy.double())
+    rel = abs(lhs - rhs) / abs(lhs)
+    print(f"dot-product test (cfg1 shape, FP32): relative mismatch "
+          f"{rel:.2e}")
+    assert rel <= 1e-6
+
+
 def test_degrid_matches_fp64_oracle(pkg, oracle_mod, torch):
     wl, _ = load_golden("small_f")
     s = _setup(pkg, torch, wl, "f")

@@ -5,8 +5,11 @@ Bars (the tolerances are written in each assertion):
   reference's FP32 (and FP64) rules;
 * norm: relative 1e-12 (it is the same FP64 per-visibility sums, added in a
   different order);
-* FP32 grid: max |err| / max |grid| <= 1e-5 against the reference's _f
-  output and against the FP64 oracle with the same placement;
+* FP32 grid: max |err| / max |grid| <= 1e-5 against the FP64 oracle with
+  the same placement; against the reference's _f output, max-rel within
+  max(1e-5, err_f + 1e-6), err_f being _f's own max-rel error against the
+  FP64 oracle (on the small golden cases err_f is far below 1e-5, so the
+  bound is 1e-5);
 * FP64 grid: relative 1e-12 against the reference's _d output.
 """
 from __future__ import annotations
@@ -276,11 +279,16 @@ def test_cfg1_vs_reference_rules(pkg, oracle_mod, synthetic, torch):
     wl = synthetic.config1()
     g, ns, nm = pkg.grid_f(wl)
     gref, nsr, nmr = oracle_mod.grid_f_mt(wl)
+    g64, _, _ = oracle_mod.grid_f_fp64acc_mt(wl)
     assert ns == nsr
     assert abs(nm - nmr) <= 1e-12 * abs(nmr)
     err = max_rel(g, gref)
-    print(f"cfg1 max-rel vs reference _f: {err:.3e}")
-    assert err <= 1e-5
+    err_f = max_rel(gref, g64)
+    tol_f = max(1e-5, err_f + 1e-6)
+    print(f"cfg1 max-rel vs reference _f: {err:.3e} (bound {tol_f:.3e}); "
+          f"vs FP64 {max_rel(g, g64):.3e}, _f vs FP64 {err_f:.3e}")
+    assert err <= tol_f
+    assert max_rel(g, g64) <= 1e-5
 
 
 def test_fp64_path_vs_reference_d(pkg, oracle_mod, synthetic, torch):

@@ -149,3 +149,45 @@ def test_oracle_matches_compiled_reference(oracle_mod, synthetic, seed):
     b, nsb, nmb = oracle_mod.grid_d(wl)
     assert (nsa, nma) == (nsb, nmb)
     assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+@pytest.mark.parametrize("name", ["small_f", "edges_f", "os3_f"])
+def test_promoted_fp64_oracle_is_the_serial_d(oracle_mod, name):
+    """The host-threaded FP64 oracle on promoted FP32 inputs (the error
+    report's `_d` column) equals the serial oskar_grid_wproj_d restatement
+    on the promoted arrays bit for bit -- and the compiled reference's _d
+    where it is built."""
+    wl, _ = load_golden(name)
+    g, ns, nm = oracle_mod.grid_d_promoted_mt(wl, threads=3)
+    g2, ns2, nm2 = oracle_mod.grid_d(wl)
+    assert ns == ns2 and nm == nm2
+    assert np.array_equal(g.view(np.uint8), g2.view(np.uint8))
+    if oracle_mod.ref_available():
+        g3, ns3, nm3 = oracle_mod.grid_d(wl, use_reference=True)
+        assert ns == ns3 and nm == nm3
+        assert np.array_equal(g.view(np.uint8), g3.view(np.uint8))
+
+
+def test_placement_disagreement_count(oracle_mod, synthetic):
+    """The count of visibilities placed differently by the FP32 and the
+    FP64 rules matches an element-wise comparison of the two placements,
+    and is zero where FP32 placement is exact (integer cell positions)."""
+    wl = synthetic.config0().subset(30_000)
+    n, n_gridded = oracle_mod.placement_disagreements(wl)
+    pf, pd = oracle_mod.place(wl, "f"), oracle_mod.place(wl, "d")
+    ref = sum(int(np.any([pf[k][i] != pd[k][i] for k in
+                          ("gu", "gv", "ou", "ov", "plane", "skipped")]))
+              for i in range(wl.num_points))
+    assert n == ref and 0 <= n_gridded <= n
+    # Coordinates that place on exact cell centres with w on exact plane
+    # squares: both rule sets agree everywhere.
+    G, cell = wl.grid_size, wl.cell_size_rad
+    rng = np.random.default_rng(3)
+    k = rng.integers(-200, 200, (2, 1000))
+    scale = np.float32(G * np.float32(cell))
+    exact = synthetic.Workload(**{**wl.__dict__,
+        "uu": (k[0] / scale).astype(np.float32),
+        "vv": (k[1] / scale).astype(np.float32),
+        "ww": np.zeros(1000, np.float32), "vis": wl.vis[:1000],
+        "weight": wl.weight[:1000]})
+    assert oracle_mod.placement_disagreements(exact) == (0, 0)
