@@ -30,7 +30,7 @@ GG_OK = 0
 _ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory",
            4: "unsupported", 5: "capacity"}
 
-# Every entry point declared in include/gpugrid.h.
+# Every entry point declared in include/gpugrid.h and include/gpugrid_io.h.
 EXPORTED_SYMBOLS = (
     "oskar_grid_wproj_d", "oskar_grid_wproj_f", "gg_grid_wproj_d",
     "gg_grid_wproj_f", "gg_last_error", "gg_version", "gg_kernels_create_f",
@@ -58,6 +58,11 @@ EXPORTED_SYMBOLS = (
     "gg_grid_weights_read_f", "gg_grid_weights_read_d",
     "gg_grid_weights_write_f_device", "gg_grid_weights_write_d_device",
     "gg_grid_weights_read_f_device", "gg_grid_weights_read_d_device",
+    # include/gpugrid_io.h: the dataset loaders.
+    "oskar_binary_create", "oskar_binary_free", "oskar_binary_num_tags",
+    "oskar_binary_query", "oskar_binary_read_block", "oskar_binary_read",
+    "oskar_binary_read_int", "oskar_binary_read_double",
+    "gg_vis_read_coords", "gg_vis_scale_coords", "gg_read_kernel",
 )
 
 

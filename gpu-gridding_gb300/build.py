@@ -21,7 +21,7 @@ LIB = os.path.join(BUILD, "libgpugrid.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["gg_api.cu", "gg_sort.cu", "gg_stack.cu", "gg_place.cu",
            "gg_grid.cu", "gg_degrid.cu", "gg_calib.cu", "gg_noalloc.cu",
-           "gg_batch.cu", "gg_weights.cu", "gg_kgen.cu"]
+           "gg_batch.cu", "gg_weights.cu", "gg_kgen.cu", "gg_loaders.cu"]
 
 
 def nvcc() -> str:
@@ -55,7 +55,8 @@ def build(force: bool = False, verbose_ptxas: bool = False,
     cc = nvcc()
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC)
                if h.endswith((".cuh", ".h"))]
-    headers.append(os.path.join(HERE, "..", "include", "gpugrid.h"))
+    headers += [os.path.join(HERE, "..", "include", h)
+                for h in ("gpugrid.h", "gpugrid_io.h")]
     objs = []
     cmds = []
     for src in SOURCES:

@@ -14,10 +14,13 @@ import pytest
 from conftest import ROOT, load_golden
 
 HEADER = os.path.join(ROOT, "include", "gpugrid.h")
+HEADERS = [os.path.join(ROOT, "include", h) for h in
+           sorted(os.listdir(os.path.join(ROOT, "include")))
+           if h.endswith(".h")]
 
 
 def declared_symbols():
-    text = open(HEADER).read()
+    text = "".join(open(h).read() for h in HEADERS)
     return sorted(set(re.findall(r"GG_API\s+[\w\s\*]+?\b(\w+)\s*\(", text)))
 
 
