@@ -10,7 +10,9 @@ no placement, norm or skip count (gg_tuning in the C header):
   plane only, or visibility order),
 * ``ctas_per_sm``   -- resident gridding CTAs per SM (0 = as many as fit),
 * ``plane_group_mb`` -- kernel bytes per gridding pass (0 = half of L2),
-* ``tile_order``    -- tiles taken by distance from the centre or row by row.
+* ``tile_order``    -- tiles taken by distance from the centre or row by row,
+* ``lane_groups``   -- on 32-wide tiles, each consumer warp takes records
+  whole (1) or as two half-warp streams (2).
 
 :func:`search` runs a coordinate search over them with a caller-supplied
 timing function; :func:`autotune` times real gridding calls of a workload
@@ -34,12 +36,12 @@ from typing import Callable, Dict, Iterable, Optional
 import numpy as np
 
 CACHE_ENV = "GPUGRID_TUNE_CACHE"
-CACHE_VERSION = 6
+CACHE_VERSION = 7
 
 #: The plan's settings before any tuning (each call chooses shape/staging).
 DEFAULT_TUNING = {"tile_u": 0, "slice_staging": -1, "items_per_cta": 4,
                   "sort_detail": 2, "ctas_per_sm": 0, "plane_group_mb": 0,
-                  "tile_order": 0}
+                  "tile_order": 0, "lane_groups": 0}
 
 #: Values tried per setting, in search order.
 SEARCH_SPACE = (
@@ -51,6 +53,7 @@ SEARCH_SPACE = (
     (("plane_group_mb",), [(0,), (16,), (32,), (48,), (64,), (96,),
                            (1 << 20,)]),
     (("tile_order",), [(0,), (1,)]),
+    (("lane_groups",), [(0,), (1,)]),
 )
 
 

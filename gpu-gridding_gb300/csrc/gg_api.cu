@@ -569,6 +569,7 @@ struct gg_plan {
   int ctas_per_sm = 0;    // cap on resident gridding CTAs, 0 = none
   int plane_group_mb = 0; // slab bytes per plane group, 0 = L2 size / 2
   int queue_order = 0;    // tuning tile_order: 0 radius, 1 row by row
+  int lane_groups = 0;    // tuning lane_groups: 0 automatic, 1, 2
   // Event the gridding passes wait for (a grid upload on another stream),
   // or null.
   cudaEvent_t grid_wait = nullptr;
@@ -728,6 +729,14 @@ TileGeom make_geom(int shape, int grid_size, int num_grids,
   g.phase_side = K->omax + 1;
   *key_bits = tile_bits + plane_bits + phase_bits;
   return g;
+}
+
+// Record streams per consumer warp (TileGeom::lane_groups): half-warp
+// streams exist for the 32-wide tiles that read taps from the slab stack;
+// 0 (automatic) takes them there.
+int lane_groups_for(const gg_plan* plan, int tile_u, bool stage) {
+  if (tile_u != 32 || stage) return 1;
+  return plan->lane_groups == 1 ? 1 : 2;
 }
 
 // Plane groups for a call: consecutive w-planes cut into as many groups as
@@ -1008,6 +1017,7 @@ int bin_records(gg_plan* plan, const gg_kernels* K, size_t n,
                             plan->plane_group.as<int>());
   geom.split_tv = split ? plan->split_row / tile_v : 0;
   geom.split_mask = split_mask;
+  geom.lane_groups = lane_groups_for(plan, geom.tile_u, stage);
   const int num_tiles = num_groups * geom.tiles_total;
   plan->stats.num_plane_groups = pgroups;
   plan->split_tv = geom.split_tv;
@@ -1208,7 +1218,8 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
 
   int sms = 0;
   GG_TRY(num_sms_of_current(&sms));
-  int per_sm = grid_tiles_ctas_per_sm<Real>(geom.tile_u, b.stage);
+  int per_sm = grid_tiles_ctas_per_sm<Real>(geom.tile_u, b.stage,
+                                            geom.lane_groups);
   if (plan->ctas_per_sm > 0) per_sm = std::min(per_sm, plan->ctas_per_sm);
   const int num_ctas = sms * per_sm;
   plan->stats.slice_staging = b.stage ? 1 : 0;
@@ -2400,6 +2411,9 @@ GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* t) {
   if (t->tile_order < 0 || t->tile_order > 1)
     return set_error(GG_ERR_INVALID_ARG, "tile_order = %d: 0 or 1",
                      t->tile_order);
+  if (t->lane_groups < 0 || t->lane_groups > 2)
+    return set_error(GG_ERR_INVALID_ARG, "lane_groups = %d: 0, 1 or 2",
+                     t->lane_groups);
   const int old_shape = plan->forced_shape;
   GG_TRY(gg_plan_set_tile_shape(plan, t->tile_u));
   const int r = gg_plan_set_slice_staging(plan, t->slice_staging);
@@ -2412,6 +2426,7 @@ GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* t) {
   plan->ctas_per_sm = t->ctas_per_sm;
   plan->plane_group_mb = t->plane_group_mb;
   plan->queue_order = t->tile_order;
+  plan->lane_groups = t->lane_groups;
   return GG_OK;
 }
 
@@ -2425,12 +2440,13 @@ GG_API int gg_plan_get_tuning(const gg_plan* plan, gg_tuning* t) {
   t->ctas_per_sm = plan->ctas_per_sm;
   t->plane_group_mb = plan->plane_group_mb;
   t->tile_order = plan->queue_order;
+  t->lane_groups = plan->lane_groups;
   return GG_OK;
 }
 
 GG_API int gg_host_set_tuning(const gg_tuning* t) {
   t_last_error.clear();
-  const gg_tuning defaults{0, -1, 4, 2, 0, 0, 0};
+  const gg_tuning defaults{0, -1, 4, 2, 0, 0, 0, 0};
   int dev;
   GG_TRY(current_device(&dev));
   DeviceState* st;

@@ -179,6 +179,10 @@ struct TileGeom {
   // num_groups counts them all.
   int split_tv;
   int split_mask;
+  // Record streams per consumer warp of the 32-wide gridding kernel: 1 (or
+  // 0) -- the whole warp takes each record that meets its rows; 2 -- each
+  // half-warp (16 columns) takes the records that meet its own columns.
+  int lane_groups;
 };
 
 // Work item of the gridding kernel: a range of sorted records of one tile.

@@ -125,10 +125,13 @@ struct Smem {
   R2 zero[kZeroTaps];
   R2 hi[kComp ? kRows : 1][kConsumers];
   R2 lo[kComp ? kRows : 1][kConsumers];
-  int4 rec[kRing][kBuf];
-  Coef<Real> cf[kRing][kBuf];
-  uint32_t band[kRing][kBuf];
-  signed char src[kRing][kBuf];   // slice slot of the record, -1 = global
+  // Entry kBuf of every ring buffer is a permanent dummy record (no lane
+  // inside its columns, zero coefficients) that a half-warp whose own
+  // record stream has run out processes in step with the other half.
+  int4 rec[kRing][kBuf + 1];
+  Coef<Real> cf[kRing][kBuf + 1];
+  uint32_t band[kRing][kBuf + 1];
+  signed char src[kRing][kBuf + 1];   // slice slot of the record, -1 = global
   int4 head[kRing];
   uint64_t full[kRing];
   uint64_t empty[kRing];
@@ -160,7 +163,7 @@ __device__ __forceinline__ int group_of(uint32_t meta) {
 
 // The producer warp: takes work items from the queue and streams their
 // records, staged, through the ring.  Returns false if a wait ran out.
-template <typename Real, int TW, bool kStage>
+template <typename Real, int TW, bool kStage, bool kHalves>
 __device__ bool produce(const GridArgs<Real>& a, Smem<Real, kStage>& sm) {
   using R2 = typename Vec2<Real>::type;
   using WS = WarpShape<TW>;
@@ -322,6 +325,12 @@ __device__ bool produce(const GridArgs<Real>& a, Smem<Real, kStage>& sm) {
               const int r0 = gg * kRows;
               if (gv - s <= r0 + kRows - 1 && gv + s >= r0) band |= 1u << gg;
             }
+            if constexpr (kHalves) {
+              // Bits 8 and 9: the footprint meets tile columns 0..15,
+              // 16..31 (the two half-warps' columns).
+              if (gu - s <= 15) band |= 1u << 8;
+              if (gu + s >= 16) band |= 1u << 9;
+            }
             sm.band[slot][t] = band;
             Coef<Real> cf;
             cf.a = v[q].x;
@@ -405,9 +414,12 @@ __device__ __forceinline__ void accumulate(const Coef<Real>& c,
   }
 }
 
-template <typename Real, bool kCompensate, int TW, bool kStage>
+template <typename Real, bool kCompensate, int TW, bool kStage, bool kHalves>
 __global__ void __launch_bounds__(kThreads, sizeof(Real) == 4 ? 2 : 1)
 k_grid_tiles(GridArgs<Real> a) {
+  static_assert(!kHalves || (TW == 32 && !kStage),
+                "half-warp record streams: 32-wide tiles, taps from the "
+                "slab stack");
   using R2 = typename Vec2<Real>::type;
   using WS = WarpShape<TW>;
   using SM = Smem<Real, kStage>;
@@ -419,6 +431,16 @@ k_grid_tiles(GridArgs<Real> a) {
   for (int i = threadIdx.x; i < SM::kZeroTaps; i += blockDim.x) {
     sm.zero[i].x = 0;
     sm.zero[i].y = 0;
+  }
+  if (threadIdx.x < kRing) {
+    // The dummy record: column range starting at 255 (no lane inside it),
+    // so its lanes read the zero buffer, and zero coefficients.
+    sm.rec[threadIdx.x][kBuf] = make_int4(0, 0, 0, 0xFF << 8);
+    Coef<Real> z;
+    z.a = z.b = z.c = z.d = 0;
+    sm.cf[threadIdx.x][kBuf] = z;
+    sm.band[threadIdx.x][kBuf] = 0;
+    sm.src[threadIdx.x][kBuf] = -1;
   }
   if (threadIdx.x == 0) {
     for (int i = 0; i < kRing; ++i) {
@@ -432,7 +454,7 @@ k_grid_tiles(GridArgs<Real> a) {
   __syncthreads();
 
   if (warp == kWarps) {
-    if (!produce<Real, TW, kStage>(a, sm)) atomicExch(a.error, 1u);
+    if (!produce<Real, TW, kStage, kHalves>(a, sm)) atomicExch(a.error, 1u);
     return;
   }
 
@@ -470,6 +492,59 @@ k_grid_tiles(GridArgs<Real> a) {
         }
       }
     }
+    // ---- half-warp record streams (32-wide tiles) ------------------------
+    // Each half-warp takes, in queue order, the records that meet this
+    // warp's rows and its own 16 columns: a footprint narrower than the
+    // warp then keeps both halves busy with different records.  Up to three
+    // records per half at a time; a half whose stream has run out takes the
+    // dummy record.  Each cell still takes its records in queue order.
+    if constexpr (kHalves) {
+      const bool upper = lane >= 16;
+      for (int c0 = 0; c0 < nb; c0 += 32) {
+        const uint32_t bd = c0 + lane < nb ? sm.band[slot][c0 + lane] : 0u;
+        const bool mine = (bd & warp_bits) != 0u;
+        uint32_t m0 = __ballot_sync(0xffffffffu, mine && (bd & 0x100u));
+        uint32_t m1 = __ballot_sync(0xffffffffu, mine && (bd & 0x200u));
+        while (m0 | m1) {
+          const int n = max(__popc(m0), __popc(m1));
+          uint32_t my = upper ? m1 : m0;
+          auto take = [&]() {
+            int t = kBuf;
+            if (my) {
+              t = c0 + __ffs(my) - 1;
+              my &= my - 1;
+            }
+            m0 &= m0 - 1;
+            m1 &= m1 - 1;
+            return t;
+          };
+          const int tA = take();
+          R2 ta[kRows];
+          load_record<Real, TW, kStage>(sm, slot, tA, slabs, gzeros, my_bit,
+                                        lx, rowl, pol, ta);
+          if (n >= 2) {
+            const int tB = take();
+            R2 tb[kRows];
+            load_record<Real, TW, kStage>(sm, slot, tB, slabs, gzeros,
+                                          my_bit, lx, rowl, pol, tb);
+            if (n >= 3) {
+              const int tC = take();
+              R2 tc[kRows];
+              load_record<Real, TW, kStage>(sm, slot, tC, slabs, gzeros,
+                                            my_bit, lx, rowl, pol, tc);
+              accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
+              accumulate<Real>(sm.cf[slot][tB], tb, acc, acq);
+              accumulate<Real>(sm.cf[slot][tC], tc, acc, acq);
+            } else {
+              accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
+              accumulate<Real>(sm.cf[slot][tB], tb, acc, acq);
+            }
+          } else {
+            accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
+          }
+        }
+      }
+    } else
     // ---- this warp's records: those whose footprint meets its band ------
     for (int c0 = 0; c0 < nb; c0 += 32) {
       const bool touch =
@@ -764,20 +839,20 @@ __global__ void k_item_emit(const uint32_t* __restrict__ tile_start,
   }
 }
 
-template <typename Real, int TW, bool kStage>
+template <typename Real, int TW, bool kStage, bool kHalves = false>
 void* grid_kernel_ptr() {
   return (void*)k_grid_tiles<Real, std::is_same<Real, float>::value, TW,
-                             kStage>;
+                             kStage, kHalves>;
 }
 
 // The kernels take more than 48 KB of dynamic shared memory: opt in before
 // querying occupancy or launching.  The opt-in is made once per device, so
 // later launches (replays captured in a CUDA graph among them) make no
 // attribute call.
-template <typename Real, int TW, bool kStage>
+template <typename Real, int TW, bool kStage, bool kHalves = false>
 cudaError_t prepare_grid_kernel(void** fn, size_t* smem) {
   static std::atomic<unsigned long long> opted_in{0};
-  *fn = grid_kernel_ptr<Real, TW, kStage>();
+  *fn = grid_kernel_ptr<Real, TW, kStage, kHalves>();
   *smem = sizeof(Smem<Real, kStage>);
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -792,7 +867,9 @@ cudaError_t prepare_grid_kernel(void** fn, size_t* smem) {
 
 template <typename Real>
 cudaError_t prepare_grid_kernel_for(int tile_u, bool stage, void** fn,
-                                    size_t* smem) {
+                                    size_t* smem, int lane_groups = 1) {
+  if (lane_groups == 2 && tile_u == 32 && !stage)
+    return prepare_grid_kernel<Real, 32, false, true>(fn, smem);
   if (stage)
     return tile_u == 32   ? prepare_grid_kernel<Real, 32, true>(fn, smem)
            : tile_u == 16 ? prepare_grid_kernel<Real, 16, true>(fn, smem)
@@ -868,11 +945,12 @@ cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
 }
 
 template <typename Real>
-int grid_tiles_ctas_per_sm(int tile_u, bool stage) {
+int grid_tiles_ctas_per_sm(int tile_u, bool stage, int lane_groups) {
   void* fn = nullptr;
   size_t smem = 0;
   int n = 0;
-  if (prepare_grid_kernel_for<Real>(tile_u, stage, &fn, &smem) !=
+  if (prepare_grid_kernel_for<Real>(tile_u, stage, &fn, &smem,
+                                    lane_groups) !=
           cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kThreads,
                                                     smem) != cudaSuccess)
@@ -942,7 +1020,7 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
   void* fn = nullptr;
   size_t smem = 0;
   cudaError_t e = prepare_grid_kernel_for<Real>(geom.tile_u, stage, &fn,
-                                                &smem);
+                                                &smem, geom.lane_groups);
   if (e != cudaSuccess) return e;
   void* args[] = {&a};
   for (int g = 0; g < geom.num_groups; ++g) {
@@ -967,8 +1045,8 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
   return cudaSuccess;
 }
 
-template int grid_tiles_ctas_per_sm<float>(int, bool);
-template int grid_tiles_ctas_per_sm<double>(int, bool);
+template int grid_tiles_ctas_per_sm<float>(int, bool, int);
+template int grid_tiles_ctas_per_sm<double>(int, bool, int);
 template cudaError_t launch_grid_tiles<float>(
     const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,

@@ -247,9 +247,10 @@ cudaError_t launch_tile_groups(const uint32_t* tile_start, int num_groups,
                                const TileGeom& geom, int grid_size,
                                uint32_t* out, unsigned long long* cells,
                                cudaStream_t s);
-// stage: the kernel variant that stages kernel slices in shared memory.
+// stage: the kernel variant that stages kernel slices in shared memory;
+// lane_groups: TileGeom::lane_groups.
 template <typename Real>
-int grid_tiles_ctas_per_sm(int tile_u, bool stage);
+int grid_tiles_ctas_per_sm(int tile_u, bool stage, int lane_groups = 1);
 
 // ---- accessors defined in gg_api.cu ---------------------------------------
 // Records a failure for gg_last_error() on this thread; returns code.

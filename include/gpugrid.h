@@ -198,6 +198,12 @@ GG_API int gg_plan_set_slice_staging(gg_plan* plan, int mode);
  *                  tiles gridded at one time), 1 row by row (the tiles in
  *                  flight share grid rows: fewer pages touched at once when
  *                  the grid is the caller's host memory, used in place)
+ *   lane_groups    record streams per consumer warp of the 32-wide tiles
+ *                  (taps read from the slab stack): 1 -- the whole warp
+ *                  takes every record that meets its 8 rows; 2 -- each
+ *                  half-warp takes the records that meet its own 16
+ *                  columns, so two narrow footprints are gridded side by
+ *                  side; 0 (default) = 2 where it applies
  * gg_plan_set_tile_shape and gg_plan_set_slice_staging set the first two
  * fields alone. */
 typedef struct
@@ -209,6 +215,7 @@ typedef struct
     int ctas_per_sm;
     int plane_group_mb;
     int tile_order;
+    int lane_groups;
 } gg_tuning;
 
 GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* tuning);
