@@ -41,7 +41,7 @@ EXPORTED_SYMBOLS = (
     "gg_host_set_tuning", "gg_host_get_tuning", "gg_host_last_transfer",
     "gg_host_set_grid_access", "gg_host_get_grid_access",
     "gg_host_set_profiling", "gg_host_phase_ms",
-    "gg_plan_probe_bounded_wait",
+    "gg_plan_probe_bounded_wait", "gg_plan_set_batch_limit",
     "gg_plan_set_profiling",
     "gg_plan_phase_ms", "gg_measure_fp32_fma_tflops", "gg_grid_wproj_f_device",
     "gg_grid_wproj_f_device_noalloc", "gg_noalloc_probe_bounded_wait",
@@ -210,6 +210,8 @@ def _declare(L):
     L.gg_host_phase_ms.restype = ctypes.c_int
     L.gg_plan_probe_bounded_wait.argtypes = [_vp, ctypes.c_uint, _vp]
     L.gg_plan_probe_bounded_wait.restype = ctypes.c_int
+    L.gg_plan_set_batch_limit.argtypes = [_vp, ctypes.c_ulonglong]
+    L.gg_plan_set_batch_limit.restype = ctypes.c_int
     L.gg_plan_check.argtypes = [_vp, _vp]
     L.gg_plan_check.restype = ctypes.c_int
     L.gg_plan_set_profiling.argtypes = [_vp, ctypes.c_int]
@@ -432,6 +434,11 @@ class Plan:
     def set_slice_staging(self, mode: int = -1) -> None:
         """Kernel-slice staging in shared memory: -1 auto, 0 off, 1 on."""
         _check(lib().gg_plan_set_slice_staging(self.handle, int(mode)))
+
+    def set_batch_limit(self, max_points: int = 0) -> None:
+        """Most visibilities per sub-batch of a batched call (0 = only as
+        the 32-bit record indices require); see gg_plan_set_batch_limit."""
+        _check(lib().gg_plan_set_batch_limit(self.handle, int(max_points)))
 
     def set_tuning(self, tuning) -> None:
         """Apply a Tuning (or a dict of its fields; missing fields take the

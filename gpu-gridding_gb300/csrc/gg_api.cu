@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstring>
 #include <functional>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -570,6 +571,17 @@ struct gg_plan {
   int plane_group_mb = 0; // slab bytes per plane group, 0 = L2 size / 2
   int queue_order = 0;    // tuning tile_order: 0 radius, 1 row by row
   int lane_groups = 0;    // tuning lane_groups: 0 automatic, 1, 2
+  // Batched calls larger than one sort can index (see batched_split): the
+  // grids are cut into sub-batches, each gridded by its own sub-plan, which
+  // keeps its geometry for replays.  A sub-plan takes the sort's transient
+  // buffers (keys, the unsorted side of the values, sort and count scratch)
+  // from `scratch`, its parent, so they exist once.
+  gg_plan* scratch = nullptr;
+  std::vector<std::unique_ptr<gg_plan>> subs;
+  std::vector<int> sub_grid0;     // first grid of each sub-batch, + end
+  std::vector<unsigned long long> sub_vis0;  // first visibility of each
+  bool subs_valid = false;
+  unsigned long long batch_limit = 0;  // visibilities per sub-batch, 0 auto
   // Event the gridding passes wait for (a grid upload on another stream),
   // or null.
   cudaEvent_t grid_wait = nullptr;
@@ -693,6 +705,9 @@ int check_device_error(gg_plan* p, cudaStream_t s) {
   GG_CUDA(cudaMemcpyAsync(&flag, p->scalars.as<uint32_t>() + kDeviceError,
                           4, cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaStreamSynchronize(s));
+  if (!flag && p->subs_valid)
+    for (size_t k = 0; k + 1 < p->sub_grid0.size(); ++k)
+      GG_TRY(check_device_error(p->subs[k].get(), s));
   if (flag)
     return set_error(GG_ERR_CUDA,
                      "a gridding kernel's bounded wait ran out; the results "
@@ -736,7 +751,7 @@ TileGeom make_geom(int shape, int grid_size, int num_grids,
 // 0 (automatic) takes them there.
 int lane_groups_for(const gg_plan* plan, int tile_u, bool stage) {
   if (tile_u != 32 || stage) return 1;
-  return plan->lane_groups == 1 ? 1 : 2;
+  return plan->lane_groups == 0 ? 2 : plan->lane_groups;
 }
 
 // Plane groups for a call: consecutive w-planes cut into as many groups as
@@ -872,6 +887,7 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   plan->stats.num_points = num_points;
   plan->events_valid = false;
   plan->kept.valid = false;
+  plan->subs_valid = false;
 
   const size_t n = num_points;
   PlaceParams<Real> pp;
@@ -1044,24 +1060,32 @@ int bin_records(gg_plan* plan, const gg_kernels* K, size_t n,
   b->geom = geom;
   if (total == 0) return GG_OK;
 
-  GG_TRY(plan->keys0.ensure((size_t)total * 4));
-  GG_TRY(plan->vals0.ensure((size_t)total * 4));
-  GG_TRY(plan->keys1.ensure((size_t)total * 4));
-  GG_TRY(plan->vals1.ensure((size_t)total * 4));
-  GG_TRY(plan->sort_tmp.ensure(radix_temp_bytes(total)));
+  // The sorted values stay with the plan (replays read them); the keys,
+  // the values' other side and the sort scratch are transient and, for a
+  // sub-plan, its parent's.
+  gg_plan* T = plan->scratch ? plan->scratch : plan;
+  const bool alt_final =
+      total > 1 && key_bits > 0 && ((key_bits + 7) / 8) % 2 == 1;
+  DevBuf& v0 = alt_final ? T->vals0 : plan->vals0;
+  DevBuf& v1 = alt_final ? plan->vals1 : T->vals1;
+  GG_TRY(T->keys0.ensure((size_t)total * 4));
+  GG_TRY(v0.ensure((size_t)total * 4));
+  GG_TRY(T->keys1.ensure((size_t)total * 4));
+  GG_TRY(v1.ensure((size_t)total * 4));
+  GG_TRY(T->sort_tmp.ensure(radix_temp_bytes(total)));
   GG_CUDA(launch_emit_records(po.cell, po.meta,
-                              plan->rec_offset.as<uint32_t>(), n, view, geom,
-                              0, 0, plan->keys0.as<uint32_t>(),
-                              plan->vals0.as<uint32_t>(), s, d_grid_offsets,
+                              T->rec_offset.as<uint32_t>(), n, view, geom,
+                              0, 0, T->keys0.as<uint32_t>(),
+                              v0.as<uint32_t>(), s, d_grid_offsets,
                               num_grids));
   bool in_alt = false;
-  GG_CUDA(radix_sort_pairs(plan->keys0.as<uint32_t>(),
-                           plan->vals0.as<uint32_t>(),
-                           plan->keys1.as<uint32_t>(),
-                           plan->vals1.as<uint32_t>(), total, key_bits,
-                           plan->sort_tmp.p, s, &in_alt));
-  b->keys = in_alt ? plan->keys1.as<uint32_t>() : plan->keys0.as<uint32_t>();
-  b->vals = in_alt ? plan->vals1.as<uint32_t>() : plan->vals0.as<uint32_t>();
+  GG_CUDA(radix_sort_pairs(T->keys0.as<uint32_t>(), v0.as<uint32_t>(),
+                           T->keys1.as<uint32_t>(), v1.as<uint32_t>(), total,
+                           key_bits, T->sort_tmp.p, s, &in_alt));
+  if (in_alt != alt_final)
+    return set_error(GG_ERR_CUDA, "internal: sort pass count mismatch");
+  b->keys = in_alt ? T->keys1.as<uint32_t>() : T->keys0.as<uint32_t>();
+  b->vals = in_alt ? v1.as<uint32_t>() : v0.as<uint32_t>();
   plan->stats.num_launches += 1 + 5 * (unsigned)((key_bits + 7) / 8);
   plan->mark(2, s);
 
@@ -1321,6 +1345,7 @@ int batched_pipeline(gg_plan* plan, const gg_kernels* K, int num_grids,
   plan->stats.num_points = n;
   plan->events_valid = false;
   plan->kept.valid = false;
+  plan->subs_valid = false;
   const StackView view = K->view();
   const int tiles_cap = max_tiles(grid_size, num_grids);
 
@@ -1341,8 +1366,11 @@ int batched_pipeline(gg_plan* plan, const gg_kernels* K, int num_grids,
   GG_TRY(plan->cell.ensure(n * 4 + 4));
   GG_TRY(plan->meta.ensure(n * 4 + 4));
   GG_TRY(plan->vw.ensure(n * sizeof(R2) + sizeof(R2)));
-  GG_TRY(plan->rec_count.ensure(n * 4 + 4));
-  GG_TRY(plan->rec_offset.ensure(n * 4 + 4));
+  // Counts and offsets of records per visibility: transient (a sub-plan
+  // takes its parent's).
+  gg_plan* T = plan->scratch ? plan->scratch : plan;
+  GG_TRY(T->rec_count.ensure(n * 4 + 4));
+  GG_TRY(T->rec_offset.ensure(n * 4 + 4));
   GG_TRY(plan->nterm.ensure(n * 8 + 8));
   GG_TRY(plan->chunk_begin.ensure(chunk_begin.size() * 8));
   GG_TRY(plan->grid_chunk0.ensure(grid_chunk0.size() * 4));
@@ -1370,7 +1398,7 @@ int batched_pipeline(gg_plan* plan, const gg_kernels* K, int num_grids,
   po.cell = plan->cell.as<uint32_t>();
   po.meta = plan->meta.as<uint32_t>();
   po.vw = plan->vw.p;
-  po.rec_count = plan->rec_count.as<uint32_t>();
+  po.rec_count = T->rec_count.as<uint32_t>();
   po.blk_norm = nullptr;
   po.blk_skip = nullptr;
   po.blk_macs = nullptr;
@@ -1387,7 +1415,7 @@ int batched_pipeline(gg_plan* plan, const gg_kernels* K, int num_grids,
       sc + kShape, s));
   GG_CUDA(launch_count_records(po.cell, po.meta, n, view, sc + kShape,
                                po.rec_count, s));
-  GG_CUDA(exclusive_scan_u32(po.rec_count, plan->rec_offset.as<uint32_t>(), n,
+  GG_CUDA(exclusive_scan_u32(po.rec_count, T->rec_offset.as<uint32_t>(), n,
                              sc + kTotalRecords, plan->scan_tmp.p, s));
   // place, chunk totals, finalize, count, 3-kernel scan
   plan->stats.num_launches = (num_chunks > 0 ? 7 : 6);
@@ -1411,6 +1439,118 @@ int batched_pipeline(gg_plan* plan, const gg_kernels* K, int num_grids,
   return GG_OK;
 }
 
+// Most (visibility, tile) records one visibility of support s_max can
+// make with the tile shape `shape` (-1: the largest over all shapes): an
+// interval of 2 s + 1 cells meets at most 2 s / w + 2 tiles of width w.
+unsigned long long max_records_per_vis(int s_max, int shape) {
+  unsigned long long r = 1;
+  for (int sh = 0; sh < kNumTileShapes; ++sh) {
+    if (shape >= 0 && sh != shape) continue;
+    const unsigned long long c =
+        (unsigned long long)(2 * s_max / tile_u_of_shape(sh) + 2) *
+        (unsigned long long)(2 * s_max / tile_v_of_shape(sh) + 2);
+    r = std::max(r, c);
+  }
+  return r;
+}
+
+// A batched call whose records might not fit the 32-bit record indices of
+// one sort (or exceed the plan's batch_limit) is cut, between grids, into
+// sub-batches of consecutive grids, each of at most
+// (2^32 - 16) / max_records_per_vis visibilities; each sub-batch is gridded
+// by a sub-plan of its own (placement, sort and persistent gridding
+// launches as in one batched call), in grid order, and keeps its geometry,
+// so that a replay covers every grid.  Calls that fit go straight to
+// batched_pipeline.
+template <typename Real>
+int batched_split(gg_plan* plan, const gg_kernels* K, int num_grids,
+                  const unsigned long long* h_offsets, const Real* uu,
+                  const Real* vv, const Real* ww, const Real* vis,
+                  const Real* weight, Real cell_size_rad, Real w_scale,
+                  int grid_size, unsigned long long* d_num_skipped,
+                  double* d_norm, Real* d_grids, cudaStream_t s) {
+  if (!plan || !K) return set_error(GG_ERR_INVALID_ARG, "plan or kernels is NULL");
+  if (num_grids < 1 || !h_offsets)
+    return set_error(GG_ERR_INVALID_ARG, "need num_grids >= 1 and offsets");
+  plan->subs_valid = false;
+  int s_max = 0;
+  for (int p = 0; p < K->num_planes; ++p)
+    s_max = std::max(s_max, K->h_support[p]);
+  unsigned long long limit =
+      0xFFFFFFF0ull / max_records_per_vis(s_max, plan->forced_shape);
+  if (plan->batch_limit > 0) limit = std::min(limit, plan->batch_limit);
+  const unsigned long long n = h_offsets[num_grids];
+  if (n <= limit || num_grids == 1)
+    return batched_pipeline<Real>(plan, K, num_grids, h_offsets, uu, vv, ww,
+                                  vis, weight, cell_size_rad, w_scale,
+                                  grid_size, d_num_skipped, d_norm, d_grids,
+                                  s);
+  // Sub-batches: consecutive grids while the sum stays within the limit.
+  std::vector<int> g0{0};
+  for (int g = 0; g < num_grids; ++g) {
+    if (h_offsets[g + 1] < h_offsets[g])
+      return set_error(GG_ERR_INVALID_ARG,
+                       "offsets must not decrease (grid %d)", g);
+    const unsigned long long cnt = h_offsets[g + 1] - h_offsets[g];
+    if (cnt > limit)
+      return set_error(GG_ERR_UNSUPPORTED,
+                       "grid %d has %llu visibilities, more than one sort "
+                       "can index with support %d (%llu); split it", g, cnt,
+                       s_max, limit);
+    if (h_offsets[g + 1] - h_offsets[g0.back()] > limit) g0.push_back(g);
+  }
+  g0.push_back(num_grids);
+  const int nsub = (int)g0.size() - 1;
+  while ((int)plan->subs.size() < nsub) {
+    std::unique_ptr<gg_plan> c(new gg_plan());
+    GG_TRY(plan_init(c.get()));
+    c->scratch = plan;
+    plan->subs.push_back(std::move(c));
+  }
+  const long long grid_stride = 2LL * grid_size * grid_size;
+  gg_stats total{};
+  std::vector<unsigned long long> offs;
+  for (int k = 0; k < nsub; ++k) {
+    gg_plan* c = plan->subs[k].get();
+    c->forced_shape = plan->forced_shape;
+    c->forced_stage = plan->forced_stage;
+    c->items_per_cta = plan->items_per_cta;
+    c->sort_detail = plan->sort_detail;
+    c->ctas_per_sm = plan->ctas_per_sm;
+    c->plane_group_mb = plan->plane_group_mb;
+    c->queue_order = plan->queue_order;
+    c->lane_groups = plan->lane_groups;
+    const int a = g0[k], b = g0[k + 1];
+    const unsigned long long v0 = h_offsets[a];
+    offs.assign(h_offsets + a, h_offsets + b + 1);
+    for (auto& o : offs) o -= v0;
+    GG_TRY(batched_pipeline<Real>(
+        c, K, b - a, offs.data(), uu + v0, vv + v0, ww + v0, vis + 2 * v0,
+        weight + v0, cell_size_rad, w_scale, grid_size, d_num_skipped + a,
+        d_norm + a, d_grids + a * grid_stride, s));
+    const gg_stats& st = c->stats;
+    if (k == 0) total = st;
+    else {
+      total.num_points += st.num_points;
+      total.num_records += st.num_records;
+      total.num_macs += st.num_macs;
+      total.num_launches += st.num_launches;
+      total.num_ctas = std::max(total.num_ctas, st.num_ctas);
+      total.num_plane_groups =
+          std::max(total.num_plane_groups, st.num_plane_groups);
+    }
+  }
+  plan->stats = total;
+  plan->events_valid = false;
+  plan->kept.valid = false;
+  plan->subs_valid = false;
+  plan->sub_grid0 = g0;
+  plan->sub_vis0.resize(nsub);
+  for (int k = 0; k < nsub; ++k) plan->sub_vis0[k] = h_offsets[g0[k]];
+  plan->subs_valid = true;
+  return GG_OK;
+}
+
 // Grids new amplitudes and weights on the geometry kept by the plan's last
 // batched call: weighted visibilities and norm terms, per-grid totals, the
 // persistent tile-gridding launch and the partial reduction.  Kernel
@@ -1421,6 +1561,23 @@ int replay_pipeline(gg_plan* plan, const gg_kernels* K, const Real* vis,
                     const Real* weight, unsigned long long* d_num_skipped,
                     double* d_norm, Real* d_grids, cudaStream_t s) {
   if (!plan || !K) return set_error(GG_ERR_INVALID_ARG, "plan or kernels is NULL");
+  if (plan->subs_valid) {
+    // A call cut into sub-batches: each sub-plan replays its grids.
+    const int nsub = (int)plan->sub_grid0.size() - 1;
+    for (int k = 0; k < nsub; ++k) {
+      gg_plan* c = plan->subs[k].get();
+      const int a = plan->sub_grid0[k];
+      const unsigned long long v0 = plan->sub_vis0[k];
+      GG_TRY(replay_pipeline<Real>(
+          c, K, vis ? vis + 2 * v0 : vis, weight ? weight + v0 : weight,
+          d_num_skipped ? d_num_skipped + a : d_num_skipped,
+          d_norm ? d_norm + a : d_norm,
+          d_grids ? d_grids + a * 2LL * c->kept.grid_size * c->kept.grid_size
+                  : d_grids,
+          s));
+    }
+    return GG_OK;
+  }
   const gg_plan::Kept& kp = plan->kept;
   if (!kp.valid)
     return set_error(GG_ERR_INVALID_ARG,
@@ -1495,6 +1652,7 @@ int degrid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   plan->stats.num_points = num_points;
   plan->events_valid = false;
   plan->kept.valid = false;
+  plan->subs_valid = false;
   const size_t n = num_points;
   const StackView view = K->view();
   PlaceOut po;
@@ -1944,6 +2102,7 @@ int weights_write_pipeline(gg_plan* plan, size_t n, const Real* uu,
   if (!d_grid || !d_num_skipped)
     return set_error(GG_ERR_INVALID_ARG, "an output pointer is NULL");
   plan->kept.valid = false;   // the sort buffers are reused below
+  plan->subs_valid = false;
   GG_CUDA(cudaMemsetAsync(d_num_skipped, 0, sizeof(unsigned long long), s));
   if (n == 0) return GG_OK;
   GG_TRY(plan->keys0.ensure(n * 4));
@@ -2359,6 +2518,14 @@ GG_API int gg_plan_destroy(gg_plan* plan) {
   return GG_OK;
 }
 
+GG_API int gg_plan_set_batch_limit(gg_plan* plan,
+                                   unsigned long long max_points) {
+  t_last_error.clear();
+  if (!plan) return set_error(GG_ERR_INVALID_ARG, "plan is NULL");
+  plan->batch_limit = max_points;
+  return GG_OK;
+}
+
 GG_API int gg_plan_last_stats(const gg_plan* plan, gg_stats* stats) {
   if (!plan || !stats) return set_error(GG_ERR_INVALID_ARG, "NULL argument");
   *stats = plan->stats;
@@ -2411,8 +2578,8 @@ GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* t) {
   if (t->tile_order < 0 || t->tile_order > 1)
     return set_error(GG_ERR_INVALID_ARG, "tile_order = %d: 0 or 1",
                      t->tile_order);
-  if (t->lane_groups < 0 || t->lane_groups > 2)
-    return set_error(GG_ERR_INVALID_ARG, "lane_groups = %d: 0, 1 or 2",
+  if (t->lane_groups < 0 || t->lane_groups > 3)
+    return set_error(GG_ERR_INVALID_ARG, "lane_groups = %d: 0..3",
                      t->lane_groups);
   const int old_shape = plan->forced_shape;
   GG_TRY(gg_plan_set_tile_shape(plan, t->tile_u));
@@ -2619,10 +2786,10 @@ GG_API int gg_grid_wproj_f_batched_device(
     unsigned long long* d_num_skipped, double* d_norm, float* d_grids,
     void* stream) {
   t_last_error.clear();
-  return batched_pipeline<float>(plan, kernels, num_grids, offsets, d_uu,
-                                 d_vv, d_ww, d_vis, d_weight, cell_size_rad,
-                                 w_scale, grid_size, d_num_skipped, d_norm,
-                                 d_grids, (cudaStream_t)stream);
+  return batched_split<float>(plan, kernels, num_grids, offsets, d_uu, d_vv,
+                              d_ww, d_vis, d_weight, cell_size_rad, w_scale,
+                              grid_size, d_num_skipped, d_norm, d_grids,
+                              (cudaStream_t)stream);
 }
 
 GG_API int gg_grid_wproj_d_batched_device(
@@ -2633,10 +2800,10 @@ GG_API int gg_grid_wproj_d_batched_device(
     int grid_size, unsigned long long* d_num_skipped, double* d_norm,
     double* d_grids, void* stream) {
   t_last_error.clear();
-  return batched_pipeline<double>(plan, kernels, num_grids, offsets, d_uu,
-                                  d_vv, d_ww, d_vis, d_weight, cell_size_rad,
-                                  w_scale, grid_size, d_num_skipped, d_norm,
-                                  d_grids, (cudaStream_t)stream);
+  return batched_split<double>(plan, kernels, num_grids, offsets, d_uu,
+                               d_vv, d_ww, d_vis, d_weight, cell_size_rad,
+                               w_scale, grid_size, d_num_skipped, d_norm,
+                               d_grids, (cudaStream_t)stream);
 }
 
 GG_API int gg_grid_wproj_f_batched_replay(gg_plan* plan,

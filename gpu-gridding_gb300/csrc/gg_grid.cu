@@ -132,6 +132,9 @@ struct Smem {
   Coef<Real> cf[kRing][kBuf + 1];
   uint32_t band[kRing][kBuf + 1];
   signed char src[kRing][kBuf + 1];   // slice slot of the record, -1 = global
+  // Half-warp record lists of the buffer being gridded (per consumer warp:
+  // the records meeting its rows and columns 0..15, then 16..31).
+  unsigned char half_list[kWarps][2][kBuf];
   int4 head[kRing];
   uint64_t full[kRing];
   uint64_t empty[kRing];
@@ -391,6 +394,24 @@ __device__ __forceinline__ void load_record(const Smem<Real, kStage>& sm,
   for (int r = 0; r < kRows; ++r) out[r] = ld_tap(p + r * step, pol);
 }
 
+// Asks L1 for the lines of one record's taps for this lane (the addresses
+// load_record would read from the slab stack), so that a later
+// load_record of it finds them there.
+template <typename Real, int TW, bool kStage, typename R2>
+__device__ __forceinline__ void prefetch_record(const Smem<Real, kStage>& sm,
+                                                int slot, int t,
+                                                const R2* __restrict__ slabs,
+                                                int lx, int rowl) {
+  const int4 ra = sm.rec[slot][t];
+  const int c0 = (ra.w >> 8) & 0xFF, cw = (int)((unsigned)ra.w >> 16);
+  if ((unsigned)(lx - c0) > (unsigned)cw) return;
+  const int off = (lx >= (ra.w & 0xFF) ? ra.x + lx : ra.y - lx) + rowl * ra.z;
+  const R2* p = slabs + off;
+#pragma unroll
+  for (int r = 0; r < kRows; ++r)
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p + r * ra.z));
+}
+
 // Adds one record's contribution to the lane's cells.  FP32: packed FP32x2
 // FMAs into the (P, Q) pairs (see Coef); FP64: plain FMAs into (re, im).
 template <typename Real, typename R2>
@@ -414,7 +435,8 @@ __device__ __forceinline__ void accumulate(const Coef<Real>& c,
   }
 }
 
-template <typename Real, bool kCompensate, int TW, bool kStage, bool kHalves>
+template <typename Real, bool kCompensate, int TW, bool kStage, bool kHalves,
+          bool kPrefetch>
 __global__ void __launch_bounds__(kThreads, sizeof(Real) == 4 ? 2 : 1)
 k_grid_tiles(GridArgs<Real> a) {
   static_assert(!kHalves || (TW == 32 && !kStage),
@@ -493,57 +515,61 @@ k_grid_tiles(GridArgs<Real> a) {
       }
     }
     // ---- half-warp record streams (32-wide tiles) ------------------------
-    // Each half-warp takes, in queue order, the records that meet this
-    // warp's rows and its own 16 columns: a footprint narrower than the
-    // warp then keeps both halves busy with different records.  Up to three
-    // records per half at a time; a half whose stream has run out takes the
-    // dummy record.  Each cell still takes its records in queue order.
+    // Each half-warp takes, in queue order, the records of the buffer that
+    // meet this warp's rows and its own 16 columns (lists built from the
+    // buffer's band bits), so a record that meets one half only runs beside
+    // another record on the other half.  Up to three records per half at a
+    // time; a half whose list has run out takes the dummy record.  Each
+    // cell still takes its records in queue order.
     if constexpr (kHalves) {
-      const bool upper = lane >= 16;
+      const int hh = lane >> 4;
+      unsigned char* l0 = sm.half_list[warp][0];
+      unsigned char* l1 = sm.half_list[warp][1];
+      const uint32_t lt = (1u << lane) - 1u;
+      int n0 = 0, n1 = 0;
       for (int c0 = 0; c0 < nb; c0 += 32) {
         const uint32_t bd = c0 + lane < nb ? sm.band[slot][c0 + lane] : 0u;
         const bool mine = (bd & warp_bits) != 0u;
-        uint32_t m0 = __ballot_sync(0xffffffffu, mine && (bd & 0x100u));
-        uint32_t m1 = __ballot_sync(0xffffffffu, mine && (bd & 0x200u));
-        while (m0 | m1) {
-          const int n = max(__popc(m0), __popc(m1));
-          uint32_t my = upper ? m1 : m0;
-          auto take = [&]() {
-            int t = kBuf;
-            if (my) {
-              t = c0 + __ffs(my) - 1;
-              my &= my - 1;
-            }
-            m0 &= m0 - 1;
-            m1 &= m1 - 1;
-            return t;
-          };
-          const int tA = take();
-          R2 ta[kRows];
-          load_record<Real, TW, kStage>(sm, slot, tA, slabs, gzeros, my_bit,
-                                        lx, rowl, pol, ta);
-          if (n >= 2) {
-            const int tB = take();
-            R2 tb[kRows];
-            load_record<Real, TW, kStage>(sm, slot, tB, slabs, gzeros,
-                                          my_bit, lx, rowl, pol, tb);
-            if (n >= 3) {
-              const int tC = take();
-              R2 tc[kRows];
-              load_record<Real, TW, kStage>(sm, slot, tC, slabs, gzeros,
-                                            my_bit, lx, rowl, pol, tc);
-              accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
-              accumulate<Real>(sm.cf[slot][tB], tb, acc, acq);
-              accumulate<Real>(sm.cf[slot][tC], tc, acc, acq);
-            } else {
-              accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
-              accumulate<Real>(sm.cf[slot][tB], tb, acc, acq);
-            }
+        const bool in0 = mine && (bd & 0x100u), in1 = mine && (bd & 0x200u);
+        const uint32_t b0 = __ballot_sync(0xffffffffu, in0);
+        const uint32_t b1 = __ballot_sync(0xffffffffu, in1);
+        if (in0) l0[n0 + __popc(b0 & lt)] = (unsigned char)(c0 + lane);
+        if (in1) l1[n1 + __popc(b1 & lt)] = (unsigned char)(c0 + lane);
+        n0 += __popc(b0);
+        n1 += __popc(b1);
+      }
+      __syncwarp();
+      const unsigned char* my = hh ? l1 : l0;
+      const int nmine = hh ? n1 : n0;
+      const int n = max(n0, n1);
+      auto pick = [&](int i) { return i < nmine ? (int)my[i] : kBuf; };
+      for (int i = 0; i < n; i += 3) {
+        const int tA = pick(i);
+        R2 ta[kRows];
+        load_record<Real, TW, kStage>(sm, slot, tA, slabs, gzeros, my_bit,
+                                      lx, rowl, pol, ta);
+        if (n - i >= 2) {
+          const int tB = pick(i + 1);
+          R2 tb[kRows];
+          load_record<Real, TW, kStage>(sm, slot, tB, slabs, gzeros, my_bit,
+                                        lx, rowl, pol, tb);
+          if (n - i >= 3) {
+            const int tC = pick(i + 2);
+            R2 tc[kRows];
+            load_record<Real, TW, kStage>(sm, slot, tC, slabs, gzeros,
+                                          my_bit, lx, rowl, pol, tc);
+            accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
+            accumulate<Real>(sm.cf[slot][tB], tb, acc, acq);
+            accumulate<Real>(sm.cf[slot][tC], tc, acc, acq);
           } else {
             accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
+            accumulate<Real>(sm.cf[slot][tB], tb, acc, acq);
           }
+        } else {
+          accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
         }
       }
+      __syncwarp();
     } else
     // ---- this warp's records: those whose footprint meets its band ------
     for (int c0 = 0; c0 < nb; c0 += 32) {
@@ -571,6 +597,18 @@ k_grid_tiles(GridArgs<Real> a) {
             R2 tc[kRows];
             load_record<Real, TW, kStage>(sm, slot, tC, slabs, gzeros,
                                           my_bit, lx, rowl, pol, tc);
+            if constexpr (kPrefetch) {
+              // The next three records' taps into L1 while these three
+              // are accumulated.
+              uint32_t mp = m;
+#pragma unroll
+              for (int q = 0; q < 3; ++q)
+                if (mp) {
+                  prefetch_record<Real, TW, kStage>(
+                      sm, slot, c0 + __ffs(mp) - 1, slabs, lx, rowl);
+                  mp &= mp - 1;
+                }
+            }
             accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
             accumulate<Real>(sm.cf[slot][tB], tb, acc, acq);
             accumulate<Real>(sm.cf[slot][tC], tc, acc, acq);
@@ -839,20 +877,22 @@ __global__ void k_item_emit(const uint32_t* __restrict__ tile_start,
   }
 }
 
-template <typename Real, int TW, bool kStage, bool kHalves = false>
+template <typename Real, int TW, bool kStage, bool kHalves = false,
+          bool kPrefetch = false>
 void* grid_kernel_ptr() {
   return (void*)k_grid_tiles<Real, std::is_same<Real, float>::value, TW,
-                             kStage, kHalves>;
+                             kStage, kHalves, kPrefetch>;
 }
 
 // The kernels take more than 48 KB of dynamic shared memory: opt in before
 // querying occupancy or launching.  The opt-in is made once per device, so
 // later launches (replays captured in a CUDA graph among them) make no
 // attribute call.
-template <typename Real, int TW, bool kStage, bool kHalves = false>
+template <typename Real, int TW, bool kStage, bool kHalves = false,
+          bool kPrefetch = false>
 cudaError_t prepare_grid_kernel(void** fn, size_t* smem) {
   static std::atomic<unsigned long long> opted_in{0};
-  *fn = grid_kernel_ptr<Real, TW, kStage, kHalves>();
+  *fn = grid_kernel_ptr<Real, TW, kStage, kHalves, kPrefetch>();
   *smem = sizeof(Smem<Real, kStage>);
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -870,6 +910,8 @@ cudaError_t prepare_grid_kernel_for(int tile_u, bool stage, void** fn,
                                     size_t* smem, int lane_groups = 1) {
   if (lane_groups == 2 && tile_u == 32 && !stage)
     return prepare_grid_kernel<Real, 32, false, true>(fn, smem);
+  if (lane_groups == 3 && tile_u == 32 && !stage)
+    return prepare_grid_kernel<Real, 32, false, false, true>(fn, smem);
   if (stage)
     return tile_u == 32   ? prepare_grid_kernel<Real, 32, true>(fn, smem)
            : tile_u == 16 ? prepare_grid_kernel<Real, 16, true>(fn, smem)

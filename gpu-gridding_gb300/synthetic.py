@@ -286,13 +286,22 @@ def config2(variant: str = "EL56-82", seed: int = 20242,
 
 def config4(num_channels: int = 64, seed: int = 20244,
             grid_size: int = 4096, times: int = 240,
-            stations: int = 512) -> Workload:
+            stations: int = 512, threads: int | None = None) -> Workload:
     """Batched multi-channel: the config-2 array at num_channels frequencies
     in 100-200 MHz, each channel with 0-60% of visibilities flagged
     (removed), onto num_channels separate grid_size^2 grids; 339 planes,
-    support 8..44.  Channels are concatenated; channel_offsets[c] is the first
-    visibility of channel c."""
-    rng = np.random.Generator(np.random.PCG64(seed))
+    support 8..44, unit weights, complex N(0, 1) amplitudes.  Channels are
+    concatenated; channel_offsets[c] is the first visibility of channel c.
+
+    Each channel draws from its own PCG64 stream (spawned from the seed), so
+    the channels are generated on `threads` host threads (default: all) and
+    the arrays do not depend on the thread count.  At the default size this
+    is 64 x 31,395,840 x (0.4..1) ~ 1.4e9 visibilities (about 34 GB)."""
+    import concurrent.futures
+    import os
+    ss = np.random.SeedSequence(seed)
+    base_ss, *chan_ss = ss.spawn(1 + num_channels)
+    rng = np.random.Generator(np.random.PCG64(base_ss))
     planes, s_min, s_max = 339, 8, 44
     u_m, v_m, w_m = ska_low_uvw_metres(rng, num_stations=stations,
                                        num_times=times)
@@ -301,21 +310,46 @@ def config4(num_channels: int = 64, seed: int = 20244,
         freqs[-1] / SPEED_OF_LIGHT
     w_max = float(np.abs(w_m).max()) * freqs[-1] / SPEED_OF_LIGHT
     cell = _fit_cell_size(u_max, grid_size, s_max)
-    uu, vv, ww, offs = [], [], [], [0]
-    for f in freqs:
-        keep_frac = 1.0 - rng.uniform(0.0, 0.6)
-        keep = rng.random(u_m.shape[0]) < keep_frac
-        sc = f / SPEED_OF_LIGHT
-        uu.append((u_m[keep] * sc).astype(np.float32))
-        vv.append((v_m[keep] * sc).astype(np.float32))
-        ww.append((w_m[keep] * sc).astype(np.float32))
-        offs.append(offs[-1] + int(keep.sum()))
-    uu = np.concatenate(uu); vv = np.concatenate(vv); ww = np.concatenate(ww)
-    weight = np.ones(uu.shape[0], dtype=np.float32)
+    n_base = u_m.shape[0]
+
+    def keep_mask(c):
+        r = np.random.Generator(np.random.PCG64(chan_ss[c]))
+        keep_frac = 1.0 - r.uniform(0.0, 0.6)
+        return r, r.random(n_base, dtype=np.float32) < np.float32(keep_frac)
+
+    workers = threads or min(16, os.cpu_count() or 1)
+    with concurrent.futures.ThreadPoolExecutor(workers) as ex:
+        counts = list(ex.map(lambda c: int(keep_mask(c)[1].sum()),
+                             range(num_channels)))
+    offs = np.zeros(num_channels + 1, dtype=np.int64)
+    offs[1:] = np.cumsum(counts)
+    n = int(offs[-1])
+    uu = np.empty(n, np.float32)
+    vv = np.empty(n, np.float32)
+    ww = np.empty(n, np.float32)
+    vis = np.empty((n, 2), np.float32)
+
+    def fill(c):
+        r, keep = keep_mask(c)
+        a, b = int(offs[c]), int(offs[c + 1])
+        sc = freqs[c] / SPEED_OF_LIGHT
+        uu[a:b] = u_m[keep] * sc
+        vv[a:b] = v_m[keep] * sc
+        ww[a:b] = w_m[keep] * sc
+        r.standard_normal((b - a, 2), dtype=np.float32, out=vis[a:b])
+
+    with concurrent.futures.ThreadPoolExecutor(workers) as ex:
+        list(ex.map(fill, range(num_channels)))
     support = linear_supports(planes, s_min, s_max)
-    return _finish(f"cfg4_batched_{num_channels}x{grid_size}", rng, support,
-                   4, grid_size, cell, uu, vv, ww, w_max, weight=weight,
-                   channel_offsets=np.asarray(offs, dtype=np.int64))
+    conv_size_half = (int(support.max()) + 1) * 4
+    return Workload(
+        name=f"cfg4_batched_{num_channels}x{grid_size}", num_w_planes=planes,
+        support=support, oversample=4, conv_size_half=conv_size_half,
+        conv_func=make_kernel_stack(support, 4, conv_size_half), uu=uu, vv=vv,
+        ww=ww, vis=vis, weight=np.ones(n, dtype=np.float32),
+        cell_size_rad=float(np.float32(cell)),
+        w_scale=float(np.float32((planes - 1) ** 2 / w_max)),
+        grid_size=grid_size, channel_offsets=offs)
 
 
 WORKLOADS = {
@@ -325,8 +359,8 @@ WORKLOADS = {
     "cfg2b": lambda: config2("EL82-70"),
     "cfg2s": lambda: config2("EL56-82", num_times=60),
     "cfg4": config4,
-    # Config-4 structure at a size a benchmark step can hold: 64 channels
-    # (100-200 MHz, 0-60% flagged) of a 128-station array, 120 times.
+    # Config-4 structure at a reduced size: 64 channels (100-200 MHz, 0-60%
+    # flagged) of a 128-station array, 120 times.
     "cfg4s": lambda: config4(num_channels=64, grid_size=4096, times=120,
                              stations=128),
 }

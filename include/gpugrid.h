@@ -378,6 +378,19 @@ GG_API int gg_grid_wproj_d_batched_replay(gg_plan* plan,
         const double* d_weight, unsigned long long* d_num_skipped,
         double* d_norm, double* d_grids, void* stream);
 
+/* Largest number of visibilities one sub-batch of a batched call takes.
+ * A batched call is cut, between grids, into sub-batches of consecutive
+ * grids whenever its (visibility, tile) records might not fit the 32-bit
+ * record indices of one sort -- more than (2^32 - 16) / r visibilities,
+ * r = (2 s_max / tile_u + 2) * (2 s_max / tile_v + 2), taken over the tile
+ * shapes the plan may choose -- or exceed this limit (0, the default: no
+ * further limit).  Each sub-batch is gridded by a sub-plan that keeps its
+ * geometry, so replays cover every grid; the sort's transient buffers are
+ * shared, so smaller sub-batches need less workspace.  A single grid above
+ * the limit is refused with GG_ERR_UNSUPPORTED. */
+GG_API int gg_plan_set_batch_limit(gg_plan* plan,
+                                   unsigned long long max_points);
+
 /* Synchronises the stream and returns GG_ERR_CUDA if a gridding kernel of
  * this plan flagged a failure (a bounded wait that ran out). */
 GG_API int gg_plan_check(gg_plan* plan, void* stream);

@@ -201,3 +201,89 @@ def test_replay_needs_kept_geometry(pkg, torch, batch):
                           torch.zeros(1, dtype=torch.int64, device="cuda"))
     with pytest.raises(pkg.GridError):   # a single call discarded it
         _replay(pkg, torch, plan, stack, vis, weight, C, G)
+
+
+def _split_limit(wl, per_sub):
+    """A batch limit that holds at most per_sub of the largest channels."""
+    sizes = np.diff(wl.channel_offsets)
+    return int(sizes.max()) * per_sub
+
+
+@pytest.mark.parametrize("per_sub", [1, 2])
+def test_sub_batches_match_one_batch(pkg, oracle_mod, torch, batch, per_sub):
+    """A batched call cut into sub-batches (gg_plan_set_batch_limit; the cut
+    a call larger than one sort's 32-bit record indices takes): every grid
+    as the uncut call gives it -- skips exact, norm 1e-12, grid 1e-6 of the
+    uncut grid and 1e-5 of the FP64 oracle -- with the same MAC and
+    visibility totals."""
+    wl = batch
+    stack = pkg.KernelStack.from_workload(wl, "f")
+    whole = pkg.Plan()
+    ref = _run_batched(pkg, torch, wl, whole, stack)
+    plan = pkg.Plan()
+    plan.set_batch_limit(_split_limit(wl, per_sub))
+    got = _run_batched(pkg, torch, wl, plan, stack)
+    assert np.array_equal(got[2], ref[2])
+    assert np.all(np.abs(got[1] - ref[1]) <=
+                  1e-12 * np.maximum(np.abs(ref[1]), 1.0))
+    st, st_ref = plan.stats(), whole.stats()
+    assert st["num_points"] == st_ref["num_points"] == wl.num_points
+    assert st["num_macs"] == st_ref["num_macs"]
+    for c in range(wl.num_grids):
+        if not ref[0][c].any():
+            assert not got[0][c].any()
+            continue
+        assert max_rel(got[0][c], ref[0][c]) <= 1e-6, c
+        g64, _, _ = oracle_mod.grid_f_fp64acc(wl.channel(c))
+        assert max_rel(got[0][c], g64) <= 1e-5, c
+
+
+def test_sub_batch_replays_and_graph(pkg, torch, batch):
+    """Replays of a call cut into sub-batches cover every grid: with the
+    original amplitudes bit-identical to the call, with new ones to a
+    fresh cut call on them, and captured in a CUDA graph."""
+    import copy
+    wl = batch
+    C, G = wl.num_grids, wl.grid_size
+    stack = pkg.KernelStack.from_workload(wl, "f")
+    plan = pkg.Plan()
+    plan.set_batch_limit(_split_limit(wl, 2))
+    ref = _run_batched(pkg, torch, wl, plan, stack)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    _same(_replay(pkg, torch, plan, stack, dev(wl.vis), dev(wl.weight), C, G),
+          ref)
+    vis2, w2 = _new_values(wl, 9)
+    got = _replay(pkg, torch, plan, stack, dev(vis2), dev(w2), C, G)
+    wl2 = copy.copy(wl)
+    wl2.vis, wl2.weight = vis2, w2
+    plan2 = pkg.Plan()
+    plan2.set_batch_limit(_split_limit(wl, 2))
+    _same(got, _run_batched(pkg, torch, wl2, plan2, stack))
+    vis, weight = dev(wl.vis), dev(wl.weight)
+    grids = torch.zeros((C, G, G, 2), dtype=torch.float32, device="cuda")
+    norms = torch.zeros(C, dtype=torch.float64, device="cuda")
+    skips = torch.full((C,), -1, dtype=torch.int64, device="cuda")
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        grids.zero_()
+        norms.zero_()
+        pkg.grid_wproj_batched_replay(plan, stack, vis, weight, grids, norms,
+                                      skips)
+    vis.copy_(dev(vis2))
+    weight.copy_(dev(w2))
+    graph.replay()
+    pkg.check_plan(plan)
+    _same((grids.cpu().numpy(), norms.cpu().numpy(), skips.cpu().numpy()),
+          got)
+    del graph
+
+
+def test_sub_batch_limit_refuses_a_larger_grid(pkg, torch, batch):
+    wl = batch
+    stack = pkg.KernelStack.from_workload(wl, "f")
+    plan = pkg.Plan()
+    plan.set_batch_limit(int(np.diff(wl.channel_offsets).max()) - 1)
+    with pytest.raises(pkg.GridError) as e:
+        _run_batched(pkg, torch, wl, plan, stack)
+    assert e.value.code == 4
