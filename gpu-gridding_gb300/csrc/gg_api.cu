@@ -2578,8 +2578,8 @@ GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* t) {
   if (t->tile_order < 0 || t->tile_order > 1)
     return set_error(GG_ERR_INVALID_ARG, "tile_order = %d: 0 or 1",
                      t->tile_order);
-  if (t->lane_groups < 0 || t->lane_groups > 3)
-    return set_error(GG_ERR_INVALID_ARG, "lane_groups = %d: 0..3",
+  if (t->lane_groups < 0 || t->lane_groups > 2)
+    return set_error(GG_ERR_INVALID_ARG, "lane_groups = %d: 0, 1 or 2",
                      t->lane_groups);
   const int old_shape = plan->forced_shape;
   GG_TRY(gg_plan_set_tile_shape(plan, t->tile_u));

@@ -125,13 +125,10 @@ struct Smem {
   R2 zero[kZeroTaps];
   R2 hi[kComp ? kRows : 1][kConsumers];
   R2 lo[kComp ? kRows : 1][kConsumers];
-  // Entry kBuf of every ring buffer is a permanent dummy record (no lane
-  // inside its columns, zero coefficients) that a half-warp whose own
-  // record stream has run out processes in step with the other half.
-  int4 rec[kRing][kBuf + 1];
-  Coef<Real> cf[kRing][kBuf + 1];
-  uint32_t band[kRing][kBuf + 1];
-  signed char src[kRing][kBuf + 1];   // slice slot of the record, -1 = global
+  int4 rec[kRing][kBuf];
+  Coef<Real> cf[kRing][kBuf];
+  uint32_t band[kRing][kBuf];
+  signed char src[kRing][kBuf];   // slice slot of the record, -1 = global
   // Half-warp record lists of the buffer being gridded (per consumer warp:
   // the records meeting its rows and columns 0..15, then 16..31).
   unsigned char half_list[kWarps][2][kBuf];
@@ -359,6 +356,23 @@ __device__ bool produce(const GridArgs<Real>& a, Smem<Real, kStage>& sm) {
   }
 }
 
+// The kRows taps of a record with slab descriptor ra for this lane (zeros
+// outside the footprint's columns or when !inband).
+template <typename R2>
+__device__ __forceinline__ void load_slab_taps(const int4 ra, bool inband,
+                                               const R2* __restrict__ slabs,
+                                               const R2* __restrict__ gzeros,
+                                               int lx, int rowl, uint64_t pol,
+                                               R2 (&out)[kRows]) {
+  const int c0 = (ra.w >> 8) & 0xFF, cw = (int)((unsigned)ra.w >> 16);
+  const bool ok = inband && (unsigned)(lx - c0) <= (unsigned)cw;
+  const int off = (lx >= (ra.w & 0xFF) ? ra.x + lx : ra.y - lx) + rowl * ra.z;
+  const R2* p = ok ? slabs + off : gzeros;
+  const int step = ok ? ra.z : 0;
+#pragma unroll
+  for (int r = 0; r < kRows; ++r) out[r] = ld_tap(p + r * step, pol);
+}
+
 // Loads the kRows taps of one record for this lane: from the record's
 // slice slot in shared memory, or from the slab stack (see the record
 // layout above).  Lanes outside the footprint's columns, or outside the
@@ -394,24 +408,6 @@ __device__ __forceinline__ void load_record(const Smem<Real, kStage>& sm,
   for (int r = 0; r < kRows; ++r) out[r] = ld_tap(p + r * step, pol);
 }
 
-// Asks L1 for the lines of one record's taps for this lane (the addresses
-// load_record would read from the slab stack), so that a later
-// load_record of it finds them there.
-template <typename Real, int TW, bool kStage, typename R2>
-__device__ __forceinline__ void prefetch_record(const Smem<Real, kStage>& sm,
-                                                int slot, int t,
-                                                const R2* __restrict__ slabs,
-                                                int lx, int rowl) {
-  const int4 ra = sm.rec[slot][t];
-  const int c0 = (ra.w >> 8) & 0xFF, cw = (int)((unsigned)ra.w >> 16);
-  if ((unsigned)(lx - c0) > (unsigned)cw) return;
-  const int off = (lx >= (ra.w & 0xFF) ? ra.x + lx : ra.y - lx) + rowl * ra.z;
-  const R2* p = slabs + off;
-#pragma unroll
-  for (int r = 0; r < kRows; ++r)
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(p + r * ra.z));
-}
-
 // Adds one record's contribution to the lane's cells.  FP32: packed FP32x2
 // FMAs into the (P, Q) pairs (see Coef); FP64: plain FMAs into (re, im).
 template <typename Real, typename R2>
@@ -435,8 +431,7 @@ __device__ __forceinline__ void accumulate(const Coef<Real>& c,
   }
 }
 
-template <typename Real, bool kCompensate, int TW, bool kStage, bool kHalves,
-          bool kPrefetch>
+template <typename Real, bool kCompensate, int TW, bool kStage, bool kHalves>
 __global__ void __launch_bounds__(kThreads, sizeof(Real) == 4 ? 2 : 1)
 k_grid_tiles(GridArgs<Real> a) {
   static_assert(!kHalves || (TW == 32 && !kStage),
@@ -453,16 +448,6 @@ k_grid_tiles(GridArgs<Real> a) {
   for (int i = threadIdx.x; i < SM::kZeroTaps; i += blockDim.x) {
     sm.zero[i].x = 0;
     sm.zero[i].y = 0;
-  }
-  if (threadIdx.x < kRing) {
-    // The dummy record: column range starting at 255 (no lane inside it),
-    // so its lanes read the zero buffer, and zero coefficients.
-    sm.rec[threadIdx.x][kBuf] = make_int4(0, 0, 0, 0xFF << 8);
-    Coef<Real> z;
-    z.a = z.b = z.c = z.d = 0;
-    sm.cf[threadIdx.x][kBuf] = z;
-    sm.band[threadIdx.x][kBuf] = 0;
-    sm.src[threadIdx.x][kBuf] = -1;
   }
   if (threadIdx.x == 0) {
     for (int i = 0; i < kRing; ++i) {
@@ -519,8 +504,7 @@ k_grid_tiles(GridArgs<Real> a) {
     // meet this warp's rows and its own 16 columns (lists built from the
     // buffer's band bits), so a record that meets one half only runs beside
     // another record on the other half.  Up to three records per half at a
-    // time; a half whose list has run out takes the dummy record.  Each
-    // cell still takes its records in queue order.
+    // time.  Each cell still takes its records in queue order.
     if constexpr (kHalves) {
       const int hh = lane >> 4;
       unsigned char* l0 = sm.half_list[warp][0];
@@ -542,31 +526,36 @@ k_grid_tiles(GridArgs<Real> a) {
       const unsigned char* my = hh ? l1 : l0;
       const int nmine = hh ? n1 : n0;
       const int n = max(n0, n1);
-      auto pick = [&](int i) { return i < nmine ? (int)my[i] : kBuf; };
+      // Entry i of this half's list; past its end the half runs the other
+      // half's entry i with its taps read as zeros (so it adds nothing).
+      const unsigned char* other = hh ? l0 : l1;
+      auto pick = [&](int i) { return (int)(i < nmine ? my[i] : other[i]); };
+      auto taps = [&](int i, int t, R2 (&out)[kRows]) {
+        load_slab_taps(sm.rec[slot][t], i < nmine, slabs, gzeros, lx, rowl,
+                       pol, out);
+      };
+      auto coef = [&](int t) -> const Coef<Real>& { return sm.cf[slot][t]; };
       for (int i = 0; i < n; i += 3) {
         const int tA = pick(i);
         R2 ta[kRows];
-        load_record<Real, TW, kStage>(sm, slot, tA, slabs, gzeros, my_bit,
-                                      lx, rowl, pol, ta);
+        taps(i, tA, ta);
         if (n - i >= 2) {
           const int tB = pick(i + 1);
           R2 tb[kRows];
-          load_record<Real, TW, kStage>(sm, slot, tB, slabs, gzeros, my_bit,
-                                        lx, rowl, pol, tb);
+          taps(i + 1, tB, tb);
           if (n - i >= 3) {
             const int tC = pick(i + 2);
             R2 tc[kRows];
-            load_record<Real, TW, kStage>(sm, slot, tC, slabs, gzeros,
-                                          my_bit, lx, rowl, pol, tc);
-            accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
-            accumulate<Real>(sm.cf[slot][tB], tb, acc, acq);
-            accumulate<Real>(sm.cf[slot][tC], tc, acc, acq);
+            taps(i + 2, tC, tc);
+            accumulate<Real>(coef(tA), ta, acc, acq);
+            accumulate<Real>(coef(tB), tb, acc, acq);
+            accumulate<Real>(coef(tC), tc, acc, acq);
           } else {
-            accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
-            accumulate<Real>(sm.cf[slot][tB], tb, acc, acq);
+            accumulate<Real>(coef(tA), ta, acc, acq);
+            accumulate<Real>(coef(tB), tb, acc, acq);
           }
         } else {
-          accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
+          accumulate<Real>(coef(tA), ta, acc, acq);
         }
       }
       __syncwarp();
@@ -597,18 +586,6 @@ k_grid_tiles(GridArgs<Real> a) {
             R2 tc[kRows];
             load_record<Real, TW, kStage>(sm, slot, tC, slabs, gzeros,
                                           my_bit, lx, rowl, pol, tc);
-            if constexpr (kPrefetch) {
-              // The next three records' taps into L1 while these three
-              // are accumulated.
-              uint32_t mp = m;
-#pragma unroll
-              for (int q = 0; q < 3; ++q)
-                if (mp) {
-                  prefetch_record<Real, TW, kStage>(
-                      sm, slot, c0 + __ffs(mp) - 1, slabs, lx, rowl);
-                  mp &= mp - 1;
-                }
-            }
             accumulate<Real>(sm.cf[slot][tA], ta, acc, acq);
             accumulate<Real>(sm.cf[slot][tB], tb, acc, acq);
             accumulate<Real>(sm.cf[slot][tC], tc, acc, acq);
@@ -877,22 +854,20 @@ __global__ void k_item_emit(const uint32_t* __restrict__ tile_start,
   }
 }
 
-template <typename Real, int TW, bool kStage, bool kHalves = false,
-          bool kPrefetch = false>
+template <typename Real, int TW, bool kStage, bool kHalves = false>
 void* grid_kernel_ptr() {
   return (void*)k_grid_tiles<Real, std::is_same<Real, float>::value, TW,
-                             kStage, kHalves, kPrefetch>;
+                             kStage, kHalves>;
 }
 
 // The kernels take more than 48 KB of dynamic shared memory: opt in before
 // querying occupancy or launching.  The opt-in is made once per device, so
 // later launches (replays captured in a CUDA graph among them) make no
 // attribute call.
-template <typename Real, int TW, bool kStage, bool kHalves = false,
-          bool kPrefetch = false>
+template <typename Real, int TW, bool kStage, bool kHalves = false>
 cudaError_t prepare_grid_kernel(void** fn, size_t* smem) {
   static std::atomic<unsigned long long> opted_in{0};
-  *fn = grid_kernel_ptr<Real, TW, kStage, kHalves, kPrefetch>();
+  *fn = grid_kernel_ptr<Real, TW, kStage, kHalves>();
   *smem = sizeof(Smem<Real, kStage>);
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -910,8 +885,6 @@ cudaError_t prepare_grid_kernel_for(int tile_u, bool stage, void** fn,
                                     size_t* smem, int lane_groups = 1) {
   if (lane_groups == 2 && tile_u == 32 && !stage)
     return prepare_grid_kernel<Real, 32, false, true>(fn, smem);
-  if (lane_groups == 3 && tile_u == 32 && !stage)
-    return prepare_grid_kernel<Real, 32, false, false, true>(fn, smem);
   if (stage)
     return tile_u == 32   ? prepare_grid_kernel<Real, 32, true>(fn, smem)
            : tile_u == 16 ? prepare_grid_kernel<Real, 16, true>(fn, smem)

@@ -63,7 +63,6 @@ TUNINGS = [
     {"tile_u": 32, "slice_staging": 0, "items_per_cta": 4, "lane_groups": 1},
     {"tile_u": 32, "slice_staging": 0, "items_per_cta": 2, "lane_groups": 2,
      "plane_group_mb": 1},
-    {"tile_u": 32, "slice_staging": 0, "items_per_cta": 4, "lane_groups": 3},
 ]
 
 
@@ -94,7 +93,7 @@ def test_tuning_rejects_bad_values(pkg, torch):
     before = plan.tuning()
     for bad in ({"tile_u": 12}, {"slice_staging": 2}, {"items_per_cta": 0},
                 {"items_per_cta": 65}, {"sort_detail": 3},
-                {"ctas_per_sm": -1}, {"tile_order": 2}, {"lane_groups": 4}):
+                {"ctas_per_sm": -1}, {"tile_order": 2}, {"lane_groups": 3}):
         with pytest.raises(pkg.GridError):
             plan.set_tuning(bad)
         assert plan.tuning() == before
