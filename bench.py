@@ -61,15 +61,23 @@ WORKLOAD_TEXT = {
     "cfg4s": "64 channels (100-200 MHz, 0-60% flagged) of a 128-station "
              "SKA-LOW-like array, 120 times, 64 grids of 4096^2, 339 "
              "w-planes, support 8..44",
+    "cfg4": "64 channels (100-200 MHz, 0-60% flagged) of the 512-station "
+            "SKA-LOW array, 240 times, 64 grids of 4096^2, 339 w-planes, "
+            "support 8..44",
 }
 
 
-def measure_batched(pkg, torch, steps, warmup=2, tune=None):
+def measure_batched(pkg, torch, steps, warmup=2, tune=None, name="cfg4",
+                    threads=None):
     """Batched (one call for all channels) vs plain (one call per channel)
-    on the 64-channel workload; both device-resident, CUDA-event timed.
-    tune: a TuningCache -- both plans are autotuned first (the plain plan on
-    channel 0's single calls) -- or None for the per-call heuristics."""
-    wl = load_workload("cfg4s")
+    on the 64-channel workload; both device-resident, CUDA-event timed,
+    plus the batched call's replay on the kept geometry captured in a CUDA
+    graph.  tune: a TuningCache -- the batched plan is tuned on the first
+    six channels, the plain plan on channel 0's single calls -- or None for
+    the per-call heuristics.  After the timing every channel's batched grid
+    is compared with its plain grid on the device, and two channels (the
+    first and the last) with the FP64 oracle on the host."""
+    wl = load_workload(name)
     dev = torch.device("cuda", torch.cuda.current_device())
     to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
     uu, vv, ww, vis, weight = (to(wl.uu), to(wl.vv), to(wl.ww), to(wl.vis),
@@ -77,8 +85,11 @@ def measure_batched(pkg, torch, steps, warmup=2, tune=None):
     C, G = wl.num_grids, wl.grid_size
     offs = [int(x) for x in wl.channel_offsets]
     grids = torch.zeros((C, G, G, 2), dtype=torch.float32, device=dev)
+    plain_grids = torch.zeros((C, G, G, 2), dtype=torch.float32, device=dev)
     norms = torch.zeros(C, dtype=torch.float64, device=dev)
     skips = torch.zeros(C, dtype=torch.int64, device=dev)
+    pnorms = torch.zeros(C, dtype=torch.float64, device=dev)
+    pskips = torch.zeros(C, dtype=torch.int64, device=dev)
     stack = pkg.KernelStack.from_workload(wl, "f")
     plan = pkg.Plan()
     plain_plan = pkg.Plan()
@@ -88,13 +99,18 @@ def measure_batched(pkg, torch, steps, warmup=2, tune=None):
     if tune is not None:
         from importlib import import_module
         at = import_module(pkg.__name__ + ".autotune")
-        a, b = offs[0], offs[1]
+        k = min(6, C)
+        e, a, b = offs[k], offs[0], offs[1]
+        sub_plan = pkg.Plan()
         tuning = {
-            "batched": at.autotune(pkg, plan, stack, uu, vv, ww, vis, weight,
-                                   cell, wsc, G, offsets=offs, cache=tune),
+            "batched": at.autotune(pkg, sub_plan, stack, uu[:e], vv[:e],
+                                   ww[:e], vis[:e], weight[:e], cell, wsc, G,
+                                   offsets=offs[:k + 1], cache=tune),
             "plain": at.autotune(pkg, plain_plan, stack, uu[a:b], vv[a:b],
                                  ww[a:b], vis[a:b], weight[a:b], cell, wsc,
                                  G, cache=tune)}
+        plan.set_tuning(sub_plan.tuning())
+        del sub_plan
 
     def batched():
         pkg.grid_wproj_batched_device(plan, stack, offs, uu, vv, ww, vis,
@@ -106,11 +122,11 @@ def measure_batched(pkg, torch, steps, warmup=2, tune=None):
             a, b = offs[c], offs[c + 1]
             pkg.grid_wproj_device(plain_plan, stack, uu[a:b], vv[a:b], ww[a:b],
                                   vis[a:b], weight[a:b], cell, wsc, G,
-                                  grids[c], norms[c:c + 1], skips[c:c + 1],
-                                  stream)
+                                  plain_grids[c], pnorms[c:c + 1],
+                                  pskips[c:c + 1], stream)
 
     out = {}
-    for name, fn in (("plain", plain), ("batched", batched)):
+    for key, fn in (("plain", plain), ("batched", batched)):
         for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
@@ -122,12 +138,14 @@ def measure_batched(pkg, torch, steps, warmup=2, tune=None):
         t1.record(stream)
         torch.cuda.synchronize()
         ms = t0.elapsed_time(t1) / steps
-        out[name] = {"ms_per_step": ms,
-                     "mvis_s": wl.num_points / (ms * 1e-3) / 1e6}
+        out[key] = {"ms_per_step": ms,
+                    "mvis_s": wl.num_points / (ms * 1e-3) / 1e6}
     out["speedup"] = out["plain"]["ms_per_step"] / out["batched"]["ms_per_step"]
-    out["workload"] = f"cfg4s: {WORKLOAD_TEXT['cfg4s']}"
+    out["workload"] = f"{name}: {WORKLOAD_TEXT[name]}"
     out["num_vis"] = wl.num_points
-    out["macs_per_step"] = plan.stats()["num_macs"]
+    st = plan.stats()
+    out["macs_per_step"] = st["num_macs"]
+    out["records_per_step"] = st["num_records"]
     out["gflops_batched"] = 8.0 * out["macs_per_step"] / (
         out["batched"]["ms_per_step"] * 1e-3) / 1e9
 
@@ -152,9 +170,38 @@ def measure_batched(pkg, torch, steps, warmup=2, tune=None):
     out["replay_graph"] = {"ms_per_step": ms,
                            "mvis_s": wl.num_points / (ms * 1e-3) / 1e6}
     out["replay_speedup_vs_plain"] = out["plain"]["ms_per_step"] / ms
-    out["tuning"] = tuning
+    out["tuning"] = tuning or plan.tuning()
     del graph
-    del grids
+
+    # Accuracy: one clean batched call and one clean plain pass.
+    grids.zero_(); norms.zero_(); plain_grids.zero_(); pnorms.zero_()
+    batched()
+    plain()
+    torch.cuda.synchronize()
+    worst = 0.0
+    for c in range(C):
+        ref = plain_grids[c].double()
+        scale = ref.abs().max().item()
+        if scale > 0:
+            worst = max(worst, (grids[c].double() - ref).abs().max().item()
+                        / scale)
+    acc = {"batched_vs_plain_max_rel": worst,
+           "skips_equal": bool(torch.equal(skips, pskips)),
+           "norm_max_rel": float(((norms - pnorms).abs() /
+                                  pnorms.abs().clamp_min(1e-300)).max())}
+    oracle = load_oracle()
+    for c in sorted({0, C - 1}):
+        ch = wl.channel(c)
+        g64, ns64, nm64 = oracle.grid_f_fp64acc_mt(ch, threads=threads)
+        e = error_vs(grids[c].cpu().numpy(), g64)
+        acc[f"channel{c}_vs_fp64"] = dict(e, skips_equal=int(skips[c]) == ns64)
+        del g64
+    acc["ok"] = bool(acc["skips_equal"] and
+                     all(acc[k]["max_rel"] <= GRID_TOL and
+                         acc[k]["skips_equal"] for k in acc
+                         if k.startswith("channel")))
+    out["accuracy"] = acc
+    del grids, plain_grids
     return out
 
 
@@ -187,6 +234,9 @@ def parse_args():
     ap.add_argument("--batched-steps", type=int, default=3,
                     help="steps of the batched-vs-plain comparison on the "
                          "64-channel workload (0 = skip)")
+    ap.add_argument("--batched-workload", default="cfg4",
+                    choices=["cfg4", "cfg4s"],
+                    help="the 64-channel workload of that comparison")
     return ap.parse_args()
 
 
@@ -765,7 +815,9 @@ def run_ours(args):
     batched = None
     if args.batched_steps > 0 and world == 1:
         batched = measure_batched(pkg, torch, args.batched_steps,
-                                  tune=tune_cache)
+                                  tune=tune_cache,
+                                  name=args.batched_workload,
+                                  threads=os.cpu_count() or 1)
 
     cpu, cpu_result = None, None
     threads = os.cpu_count() or 1

@@ -53,7 +53,7 @@ SEARCH_SPACE = (
     (("plane_group_mb",), [(0,), (16,), (32,), (48,), (64,), (96,),
                            (1 << 20,)]),
     (("tile_order",), [(0,), (1,)]),
-    (("lane_groups",), [(0,), (1,)]),
+    (("lane_groups",), [(0,), (2,)]),
 )
 
 

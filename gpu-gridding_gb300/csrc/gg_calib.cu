@@ -27,6 +27,27 @@ __global__ void __launch_bounds__(256) k_ffma(float* out, int iters,
   if (s == 1234.5f) out[blockIdx.x] = s;
 }
 
+// The same chains as packed FP32x2 FMAs (two FMAs per instruction), the
+// form the gridding kernel issues: the FP32 FMA rate is the larger of the
+// two probes.
+__global__ void __launch_bounds__(256) k_ffma2(float* out, int iters,
+                                               float b, float c) {
+  float2 acc[kChains / 2];
+#pragma unroll
+  for (int k = 0; k < kChains / 2; ++k)
+    acc[k] = make_float2(threadIdx.x * 1e-7f + 2 * k,
+                         threadIdx.x * 1e-7f + 2 * k + 1);
+  const float2 bb = make_float2(b, b), cc = make_float2(c, c);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < kChains / 2; ++k) acc[k] = __ffma2_rn(acc[k], bb, cc);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < kChains / 2; ++k) s += acc[k].x + acc[k].y;
+  if (s == 1234.5f) out[blockIdx.x] = s;
+}
+
 }  // namespace
 
 cudaError_t measure_fp32_fma(int num_sms, double* tflops_best,
@@ -40,9 +61,12 @@ cudaError_t measure_fp32_fma(int num_sms, double* tflops_best,
   const int blocks = num_sms * 8, threads = 256, iters = 1 << 15;
   double best = 0.0;
   float best_ms = 0.f;
-  for (int rep = 0; rep < 6; ++rep) {
+  for (int rep = 0; rep < 12; ++rep) {
     cudaEventRecord(a);
-    k_ffma<<<blocks, threads>>>(dummy, iters, 0.9999f, 1e-4f);
+    if (rep % 2 == 0)
+      k_ffma<<<blocks, threads>>>(dummy, iters, 0.9999f, 1e-4f);
+    else
+      k_ffma2<<<blocks, threads>>>(dummy, iters, 0.9999f, 1e-4f);
     cudaEventRecord(b);
     e = cudaEventSynchronize(b);
     if (e != cudaSuccess) break;
@@ -50,7 +74,7 @@ cudaError_t measure_fp32_fma(int num_sms, double* tflops_best,
     cudaEventElapsedTime(&ms, a, b);
     const double flops = 2.0 * kChains * (double)iters * blocks * threads;
     const double tf = flops / (ms * 1e-3) / 1e12;
-    if (rep > 0 && tf > best) { best = tf; best_ms = ms; }
+    if (rep > 1 && tf > best) { best = tf; best_ms = ms; }
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);

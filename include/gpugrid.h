@@ -203,7 +203,7 @@ GG_API int gg_plan_set_slice_staging(gg_plan* plan, int mode);
  *                  takes every record that meets its 8 rows; 2 -- each
  *                  half-warp takes the records that meet its own 16
  *                  columns, so two narrow footprints are gridded side by
- *                  side; 0 (default) = 2 where it applies
+ *                  side; 0 (default) = 1
  * gg_plan_set_tile_shape and gg_plan_set_slice_staging set the first two
  * fields alone. */
 typedef struct
