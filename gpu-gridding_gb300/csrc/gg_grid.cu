@@ -309,7 +309,9 @@ __device__ bool produce(const GridArgs<Real>& a, Smem<Real, kStage>& sm) {
               // Slab of (plane, |ov|); rows mirrored for ov < 0, columns by
               // residue on either side of the fold ou + k*os = 0.
               sm.rec[slot][t] =
-                  slab_record<TW>(a.view, plane, s, ou, ov, gu, gv);
+                  a.view.oversample == 4
+                      ? slab_record<TW, 4>(a.view, plane, s, ou, ov, gu, gv)
+                      : slab_record<TW>(a.view, plane, s, ou, ov, gu, gv);
             } else {
               // Tap index of S[0][0] relative to the padded slice start.
               const int org = kSlicePad * F + (s - sv * gv) * F +

@@ -122,11 +122,13 @@ __device__ __forceinline__ uint64_t evict_last_policy() {
 // side of the column fold (which begins at lane column Lf), and [c0, c1]
 // the footprint's columns in the tile; so the tap of tile cell (row, col)
 // is slabs[(col >= Lf ? x + col : y - col) + row * B] for c0 <= col <= c1.
-template <int TW>
+template <int TW, int OS = 0>
 __device__ __forceinline__ int4 slab_record(const StackView& v, int plane,
                                             int s, int ou, int ov, int gu,
                                             int gv) {
-  const int os = v.oversample, omax = v.omax;
+  // OS > 0: the oversampling known at compile time (integer divisions and
+  // remainders by it become shifts and masks when it is a power of two).
+  const int os = OS > 0 ? OS : v.oversample, omax = v.omax;
   const int M = slab_cols_m(s, os, omax);
   const int pitch = os * M;
   const int sb = (int)(v.sbase[plane] + abs(ov) * slab_taps(s, os, omax));
