@@ -153,8 +153,13 @@ __device__ bool degrid_produce(const DegridArgs<Real>& a,
             const int plane = meta_plane(m);
             const int s = a.view.support[plane];
             const int gu = cell_u(ce[q]), gv = cell_v(ce[q]);
-            sm.rec[slot][t] = slab_record<kDegridTileU>(
-                a.view, plane, s, meta_ou(m), meta_ov(m), gu - u0, gv - v0);
+            sm.rec[slot][t] =
+                a.view.oversample == 4
+                    ? slab_record<kDegridTileU, 4>(a.view, plane, s,
+                                                   meta_ou(m), meta_ov(m),
+                                                   gu - u0, gv - v0)
+                    : slab_record<kDegridTileU>(a.view, plane, s, meta_ou(m),
+                                                meta_ov(m), gu - u0, gv - v0);
             uint32_t band = 0;
 #pragma unroll
             for (int w = 0; w < kWarps; ++w) {

@@ -260,3 +260,20 @@ def test_load_challenge_assembles_a_workload(ld, expected):
     assert np.array_equal(wl.support, expected["kernel_support"])
     assert wl.grid_size == 2048 and wl.oversample == 4
     assert np.all(wl.weight == 1)
+
+
+@pytest.mark.gpu
+def test_loaded_dataset_grids_on_the_gpu(ld, pkg, oracle_mod):
+    """A workload read by the loaders grids through the drop-in as the FP64
+    oracle says (skips exact, grid max-rel 1e-5, norm 1e-12)."""
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    wl = ld.load_challenge(_path("vis_small_f.vis"),
+                           _path("kernel_small_re.fits"),
+                           _path("kernel_small_im.fits"))
+    g, ns, nm = pkg.grid_f(wl)
+    g64, ns64, nm64 = oracle_mod.grid_f_fp64acc(wl)
+    assert ns == ns64
+    assert abs(nm - nm64) <= 1e-12 * abs(nm64)
+    err = np.abs(g.astype(np.float64) - g64).max() / np.abs(g64).max()
+    assert err <= 1e-5
