@@ -690,9 +690,14 @@ extern "C" GG_API void* gg_read_kernel(const char* file_name, int precision,
   }
 done:
   std::fclose(f);
-  if (*status && data) {
+  if (*status) {
+    // On failure nothing is handed to the caller.
     std::free(data);
     data = nullptr;
+    if (support && *support) {
+      std::free(*support);
+      *support = nullptr;
+    }
   }
   return data;
 }

@@ -211,8 +211,6 @@ def read_kernel(path: str, precision: int = OSKAR_SINGLE) -> tuple:
     libc = ctypes.CDLL(None)
     libc.free.argtypes = [_vp]
     if st.value or not p:
-        if sup:
-            libc.free(ctypes.cast(sup, _vp))
         raise LoaderError(st.value, f"{path}: {_pkg().last_error()}")
     t = ctypes.c_double if precision == OSKAR_DOUBLE else ctypes.c_float
     n = csh.value * csh.value * planes.value

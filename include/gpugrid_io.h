@@ -22,7 +22,8 @@
  *       [num_w_planes][conv_size_half][conv_size_half] in the requested
  *       precision and, when support is non-NULL, a calloc'd support table;
  *       the caller frees both with free().  On failure *status is non-zero,
- *       gg_last_error() says why, and NULL is returned.
+ *       gg_last_error() says why, NULL is returned and *support is left
+ *       NULL (nothing to free).
  */
 #ifndef GPUGRID_IO_H_
 #define GPUGRID_IO_H_
