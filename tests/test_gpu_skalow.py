@@ -145,3 +145,74 @@ def test_skalow_dropin_host_call(pkg, skalow, torch):
         _norm_tol(wl.num_points) * abs(skalow["nm64"])
     expect = skalow["g64"] + grid0
     assert max_rel(grid, expect) <= 1e-5
+
+
+@pytest.fixture(scope="module")
+def skalow_full(synthetic):
+    """The benchmark's default workload itself: 31,395,840 visibilities."""
+    return synthetic.WORKLOADS["cfg2"]()
+
+
+def test_full_skalow_linearity_skips_and_macs(pkg, oracle_mod, skalow_full,
+                                              torch):
+    """Properties that hold at any size, on the full SKA-LOW workload:
+    doubling the amplitudes doubles the grid exactly (every operation on
+    the path is exact under a power-of-two scale), the skip count equals
+    the oracle's FP32 placement count and the complex-MAC count its
+    sum of (2 s + 1)^2 over the gridded visibilities."""
+    wl = skalow_full
+    stack = pkg.KernelStack.from_workload(wl, "f")
+    plan = pkg.Plan()
+    G = wl.grid_size
+    uu, vv, ww = _dev(torch, wl.uu), _dev(torch, wl.vv), _dev(torch, wl.ww)
+    weight = _dev(torch, wl.weight)
+    outs = []
+    for scale in (1.0, 2.0):
+        grid = torch.zeros((G, G, 2), dtype=torch.float32, device="cuda")
+        norm = torch.zeros(1, dtype=torch.float64, device="cuda")
+        ns = torch.zeros(1, dtype=torch.int64, device="cuda")
+        pkg.grid_wproj_device(plan, stack, uu, vv, ww,
+                              _dev(torch, wl.vis * np.float32(scale)), weight,
+                              np.float32(wl.cell_size_rad),
+                              np.float32(wl.w_scale), G, grid, norm, ns)
+        torch.cuda.synchronize()
+        outs.append((grid, int(ns.item())))
+    assert torch.equal(outs[1][0], 2 * outs[0][0])
+    assert outs[0][1] == outs[1][1] == oracle_mod.place(wl)["num_skipped"]
+    assert plan.stats()["num_macs"] == oracle_mod.mac_count(wl)
+
+
+def test_full_skalow_adjoint_dot_product(pkg, skalow_full, torch):
+    """<G x, y> = <x, G^H y> on the full SKA-LOW workload with random
+    complex x and y, FP32 forward and adjoint: relative 1e-6."""
+    wl = skalow_full
+    stack = pkg.KernelStack.from_workload(wl, "f")
+    plan = pkg.Plan()
+    G = wl.grid_size
+    uu, vv, ww = _dev(torch, wl.uu), _dev(torch, wl.vv), _dev(torch, wl.ww)
+    gen = torch.Generator(device="cuda").manual_seed(17)
+    x = torch.randn((wl.num_points, 2), generator=gen, device="cuda")
+    y = torch.randn((G, G, 2), generator=gen, device="cuda")
+    gx = torch.zeros((G, G, 2), dtype=torch.float32, device="cuda")
+    pkg.grid_wproj_device(plan, stack, uu, vv, ww, x,
+                          torch.ones(wl.num_points, device="cuda"),
+                          np.float32(wl.cell_size_rad),
+                          np.float32(wl.w_scale), G, gx,
+                          torch.zeros(1, dtype=torch.float64, device="cuda"),
+                          torch.zeros(1, dtype=torch.int64, device="cuda"))
+    ghy = torch.empty((wl.num_points, 2), dtype=torch.float32, device="cuda")
+    pkg.degrid_wproj_device(plan, stack, uu, vv, ww,
+                            np.float32(wl.cell_size_rad),
+                            np.float32(wl.w_scale), G, y, ghy)
+    torch.cuda.synchronize()
+
+    def cdot(a, b):
+        a, b = a.double(), b.double()
+        re = (a[..., 0] * b[..., 0] + a[..., 1] * b[..., 1]).sum()
+        im = (a[..., 0] * b[..., 1] - a[..., 1] * b[..., 0]).sum()
+        return complex(re.item(), im.item())
+
+    lhs, rhs = cdot(gx, y), cdot(x, ghy)
+    rel = abs(lhs - rhs) / abs(lhs)
+    print(f"full SKA-LOW dot-product test: relative mismatch {rel:.2e}")
+    assert rel <= 1e-6
