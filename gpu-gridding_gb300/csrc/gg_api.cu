@@ -684,7 +684,9 @@ enum Scalar {
 constexpr int kDegridShape = 0;
 // 64-bit device scalars live after the 32-bit ones.
 constexpr size_t kScalar64Offset = 64;
-enum Scalar64 { kMacs = 0, kSkipScratch, kDirectCells, kScalar64Count };
+enum Scalar64 {
+  kMacs = 0, kSkipScratch, kDirectCells, kRecords64, kScalar64Count
+};
 
 unsigned long long* scalar64(gg_plan* p, int i) {
   return (unsigned long long*)((char*)p->scalars.p + kScalar64Offset) + i;
@@ -744,6 +746,21 @@ TileGeom make_geom(int shape, int grid_size, int num_grids,
   g.phase_side = K->omax + 1;
   *key_bits = tile_bits + plane_bits + phase_bits;
   return g;
+}
+
+// Most (visibility, tile) records one visibility of support s_max can
+// make with the tile shape `shape` (-1: the largest over all shapes): an
+// interval of 2 s + 1 cells meets at most 2 s / w + 2 tiles of width w.
+unsigned long long max_records_per_vis(int s_max, int shape) {
+  unsigned long long r = 1;
+  for (int sh = 0; sh < kNumTileShapes; ++sh) {
+    if (shape >= 0 && sh != shape) continue;
+    const unsigned long long c =
+        (unsigned long long)(2 * s_max / tile_u_of_shape(sh) + 2) *
+        (unsigned long long)(2 * s_max / tile_v_of_shape(sh) + 2);
+    r = std::max(r, c);
+  }
+  return r;
 }
 
 // Record streams per consumer warp (TileGeom::lane_groups): half-warp
@@ -997,6 +1014,22 @@ int bin_records(gg_plan* plan, const gg_kernels* K, size_t n,
                      "whose bounded wait ran out");
   const uint32_t total = plan->h_scalars[kTotalRecords];
   const int shape = (int)(plan->h_scalars[kShape] & 0xFFu);
+  // The scan's 32-bit record total wraps past 2^32: where the call could
+  // make that many records, count them in 64 bits and refuse the call
+  // rather than size the sort from a wrapped total.
+  if ((unsigned long long)n * max_records_per_vis(K->support_max, shape) >
+      0xFFFFFFF0ull) {
+    unsigned long long records = 0;
+    GG_CUDA(sum_u32(po.rec_count, n, scalar64(plan, kRecords64), s));
+    GG_CUDA(cudaMemcpyAsync(&records, scalar64(plan, kRecords64),
+                            sizeof(records), cudaMemcpyDeviceToHost, s));
+    GG_CUDA(cudaStreamSynchronize(s));
+    if (records > 0xFFFFFFF0ull)
+      return set_error(GG_ERR_UNSUPPORTED,
+                       "the call makes %llu (visibility, tile) records, more "
+                       "than 2^32-16; split it (batched calls do so by "
+                       "grids)", records);
+  }
   const bool stage = plan->forced_stage >= 0
                          ? plan->forced_stage != 0
                          : ((plan->h_scalars[kShape] >> 8) & 1u) != 0;
@@ -1043,8 +1076,6 @@ int bin_records(gg_plan* plan, const gg_kernels* K, size_t n,
   const int low_bits = geom.plane_bits + geom.phase_bits;
   plan->stats.tile_u = geom.tile_u;
   plan->stats.tile_v = geom.tile_v;
-  // Record counts per visibility are at most a few dozen, so a 32-bit total
-  // can only wrap for inputs far beyond the per-call limit; guard anyway.
   if ((unsigned long long)total > 0xFFFFFFF0ull)
     return set_error(GG_ERR_UNSUPPORTED, "record count overflow");
   plan->kept.num_records = total;
@@ -1438,21 +1469,6 @@ int batched_pipeline(gg_plan* plan, const gg_kernels* K, int num_grids,
   kp.num_chunks = num_chunks;
   kp.valid = true;
   return GG_OK;
-}
-
-// Most (visibility, tile) records one visibility of support s_max can
-// make with the tile shape `shape` (-1: the largest over all shapes): an
-// interval of 2 s + 1 cells meets at most 2 s / w + 2 tiles of width w.
-unsigned long long max_records_per_vis(int s_max, int shape) {
-  unsigned long long r = 1;
-  for (int sh = 0; sh < kNumTileShapes; ++sh) {
-    if (shape >= 0 && sh != shape) continue;
-    const unsigned long long c =
-        (unsigned long long)(2 * s_max / tile_u_of_shape(sh) + 2) *
-        (unsigned long long)(2 * s_max / tile_v_of_shape(sh) + 2);
-    r = std::max(r, c);
-  }
-  return r;
 }
 
 // A batched call whose records might not fit the 32-bit record indices of

@@ -18,6 +18,9 @@ namespace gg {
 size_t scan_temp_bytes(size_t n);
 cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n,
                                uint32_t* d_total, void* tmp, cudaStream_t s);
+// *total (device) = sum of in[0..n) in 64 bits.
+cudaError_t sum_u32(const uint32_t* in, size_t n, unsigned long long* total,
+                    cudaStream_t s);
 
 // ---- stable LSD radix sort of (key, value) pairs (gg_sort.cu) -------------
 // Sorts the first n pairs by key bits [0, end_bit).  Ping-pongs between

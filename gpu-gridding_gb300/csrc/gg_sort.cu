@@ -266,6 +266,34 @@ static cudaError_t scan_impl(Load in, uint32_t* out, size_t n,
   return cudaGetLastError();
 }
 
+// *total = sum of in[0..n) in 64 bits (the scan's 32-bit total wraps).
+__global__ void k_sum_u32(const uint32_t* __restrict__ in, size_t n,
+                          unsigned long long* __restrict__ total) {
+  unsigned long long v = 0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    v += in[i];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __shared__ unsigned long long w[32];
+  if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < (blockDim.x >> 5) ? w[threadIdx.x] : 0ull;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0 && v) atomicAdd(total, v);
+  }
+}
+
+cudaError_t sum_u32(const uint32_t* in, size_t n, unsigned long long* total,
+                    cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(total, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  if (n == 0) return cudaSuccess;
+  const size_t blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+  k_sum_u32<<<(unsigned)blocks, 256, 0, s>>>(in, n, total);
+  return cudaGetLastError();
+}
+
 cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n,
                                uint32_t* d_total, void* tmp, cudaStream_t s) {
   return scan_impl(LoadU32{in}, out, n, d_total, tmp, s);

@@ -768,3 +768,22 @@ def test_dropin_concurrent_threads(pkg, synthetic, torch):
         g0, ns0, nm0 = serial[i % 4]
         assert ns == ns0 and nm == nm0
         assert np.array_equal(g.view(np.uint32), g0.view(np.uint32))
+
+
+def test_wide_support_table_takes_the_64_bit_record_count(pkg, oracle_mod,
+                                                          synthetic, torch):
+    """A call whose support table could make more records than 32-bit
+    indices hold (2 M visibilities x up to 2268 records each with a plane
+    of support 1000) counts its records in 64 bits before sizing the sort;
+    here every visibility lies in the support-4 plane, so the call proceeds
+    and grids as the FP64 oracle says."""
+    wl = synthetic.random_uniform_workload("wide", 2_000_000, 4096, 2, 4,
+                                           1000, seed=21,
+                                           cell_size_rad=2.0e-5)
+    wl.ww = np.zeros_like(wl.ww)
+    assert int(wl.support.max()) == 1000
+    g, ns, nm = pkg.grid_f(wl)
+    g64, ns64, nm64 = oracle_mod.grid_f_fp64acc_mt(wl)
+    assert ns == ns64
+    assert abs(nm - nm64) <= 1e-12 * abs(nm64)
+    assert max_rel(g, g64) <= 1e-5
