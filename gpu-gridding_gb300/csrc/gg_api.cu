@@ -137,6 +137,9 @@ struct DeviceState {
   cudaEvent_t tables_ready = nullptr, stack_ready = nullptr;
   cudaEvent_t cube_staged = nullptr;   // the call's cube on the device
   cudaEvent_t vis_ready = nullptr;
+  // The visibilities go up in kInputChunks pieces, each ready at its event.
+  static constexpr int kInputChunks = 4;
+  cudaEvent_t chunk_ready[kInputChunks] = {};
   cudaEvent_t grid_ready = nullptr;
   cudaEvent_t spans_ready = nullptr;
   cudaEvent_t top_done = nullptr;   // upper tile rows final (split pass)
@@ -577,6 +580,12 @@ struct gg_plan {
   // buffers (keys, the unsorted side of the values, sort and count scratch)
   // from `scratch`, its parent, so they exist once.
   gg_plan* scratch = nullptr;
+  // Inputs of a host call arriving in pieces (set by the drop-in around
+  // its gridding pipeline): placement of points [in_chunk_end[k-1],
+  // in_chunk_end[k]) waits for in_chunk_ready[k].
+  int in_chunks = 0;
+  const cudaEvent_t* in_chunk_ready = nullptr;
+  size_t in_chunk_end[8] = {};
   std::vector<std::unique_ptr<gg_plan>> subs;
   std::vector<int> sub_grid0;     // first grid of each sub-batch, + end
   std::vector<unsigned long long> sub_vis0;  // first visibility of each
@@ -965,7 +974,34 @@ int place_and_count(gg_plan* plan, const gg_kernels* K,
   po.blk_norm = plan->blk_norm.as<double>();
   po.blk_skip = plan->blk_skip.as<unsigned long long>();
   po.blk_macs = plan->blk_macs.as<unsigned long long>();
-  GG_CUDA(launch_place<Real>(pp, view, TileGeom{}, 0, 0, po, s));
+  if (plan->in_chunks > 0) {
+    // Each piece is placed as soon as it is on the device; the pieces
+    // start on block boundaries, so the per-block partials are the ones a
+    // single launch writes.
+    size_t a = 0;
+    for (int k = 0; k < plan->in_chunks; ++k) {
+      const size_t b = plan->in_chunk_end[k];
+      GG_CUDA(cudaStreamWaitEvent(s, plan->in_chunk_ready[k], 0));
+      if (b <= a) continue;
+      PlaceParams<Real> pk = pp;
+      pk.uu = pp.uu + a; pk.vv = pp.vv + a; pk.ww = pp.ww + a;
+      pk.vis = pp.vis ? pp.vis + 2 * a : nullptr;
+      pk.weight = pp.weight ? pp.weight + a : nullptr;
+      pk.num_points = b - a;
+      PlaceOut ok = po;
+      ok.cell = po.cell + a;
+      ok.meta = po.meta + a;
+      ok.vw = po.vw ? (void*)((R2*)po.vw + a) : nullptr;
+      const size_t blk = a / kPlaceBlock;
+      ok.blk_norm = po.blk_norm + blk;
+      ok.blk_skip = po.blk_skip + blk;
+      ok.blk_macs = po.blk_macs + blk;
+      GG_CUDA(launch_place<Real>(pk, view, TileGeom{}, 0, 0, ok, s));
+      a = b;
+    }
+  } else {
+    GG_CUDA(launch_place<Real>(pp, view, TileGeom{}, 0, 0, po, s));
+  }
   GG_CUDA(launch_place_finalize(po.blk_norm, po.blk_skip, po.blk_macs, nblk,
                                 n, forced_shape,
                                 pp.defer_norm ? nullptr : d_norm,
@@ -1829,6 +1865,8 @@ int ensure_copy_stream(DeviceState* st) {
                          &st->top_done, &st->top_up, &st->tables_ready,
                          &st->stack_ready, &st->cube_staged})
     if (!*e) GG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  for (cudaEvent_t& e : st->chunk_ready)
+    if (!e) GG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   if (!st->h_spans)
     GG_CUDA(cudaMallocHost(&st->h_spans,
                            DeviceState::kSpanCap * sizeof(uint32_t)));
@@ -1909,18 +1947,34 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
                                            2 * sizeof(Real))
                      : nullptr;
   if (st->profile) GG_CUDA(cudaStreamWaitEvent(cs, st->call_start, 0));
+  // The visibilities go up in pieces of whole placement blocks, and each
+  // piece is placed while the next one crosses the link.
+  const int nchunks = DeviceState::kInputChunks;
+  size_t chunk_end[DeviceState::kInputChunks];
+  for (int k = 0; k < nchunks; ++k) {
+    const size_t e = (n * (k + 1) / nchunks + kPlaceBlock - 1) /
+                     kPlaceBlock * kPlaceBlock;
+    chunk_end[k] = k + 1 == nchunks ? n : std::min(e, n);
+  }
   auto uploads = [&]() -> int {
-    if (n) {
-      GG_CUDA(cudaMemcpyAsync(plan->in_uu.p, uu, n * sizeof(Real),
-                              cudaMemcpyHostToDevice, cs));
-      GG_CUDA(cudaMemcpyAsync(plan->in_vv.p, vv, n * sizeof(Real),
-                              cudaMemcpyHostToDevice, cs));
-      GG_CUDA(cudaMemcpyAsync(plan->in_ww.p, ww, n * sizeof(Real),
-                              cudaMemcpyHostToDevice, cs));
-      GG_CUDA(cudaMemcpyAsync(plan->in_vis.p, vis, 2 * n * sizeof(Real),
-                              cudaMemcpyHostToDevice, cs));
-      GG_CUDA(cudaMemcpyAsync(plan->in_weight.p, weight, n * sizeof(Real),
-                              cudaMemcpyHostToDevice, cs));
+    size_t a = 0;
+    for (int k = 0; k < nchunks; ++k) {
+      const size_t b = chunk_end[k], m = b - a;
+      if (m) {
+        GG_CUDA(cudaMemcpyAsync(plan->in_uu.as<Real>() + a, uu + a,
+                                m * sizeof(Real), cudaMemcpyHostToDevice, cs));
+        GG_CUDA(cudaMemcpyAsync(plan->in_vv.as<Real>() + a, vv + a,
+                                m * sizeof(Real), cudaMemcpyHostToDevice, cs));
+        GG_CUDA(cudaMemcpyAsync(plan->in_ww.as<Real>() + a, ww + a,
+                                m * sizeof(Real), cudaMemcpyHostToDevice, cs));
+        GG_CUDA(cudaMemcpyAsync(plan->in_vis.as<Real>() + 2 * a, vis + 2 * a,
+                                2 * m * sizeof(Real), cudaMemcpyHostToDevice,
+                                cs));
+        GG_CUDA(cudaMemcpyAsync(plan->in_weight.as<Real>() + a, weight + a,
+                                m * sizeof(Real), cudaMemcpyHostToDevice, cs));
+      }
+      GG_CUDA(cudaEventRecord(st->chunk_ready[k], cs));
+      a = b;
     }
     GG_CUDA(cudaEventRecord(st->vis_ready, cs));
     return GG_OK;
@@ -1955,7 +2009,8 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
                             cudaMemcpyHostToDevice, cs));
   }
   GG_CUDA(cudaEventRecord(st->grid_ready, cs));
-  GG_CUDA(cudaStreamWaitEvent(s, st->vis_ready, 0));
+  // Placement waits for each piece of the visibilities (in_chunk_ready);
+  // whatever runs before it on s needs none of them.
   // The starting norm is set by a one-thread kernel rather than a copy, so
   // that it does not queue behind the uploads on the copy engines.
   GG_CUDA(launch_store_f64(d_norm, *norm, s));
@@ -1976,6 +2031,9 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   plan->stack_wait = st->stack_ready;
   plan->norm_weight = plan->in_weight.p;
   plan->norm_out = d_norm;
+  plan->in_chunks = nchunks;
+  plan->in_chunk_ready = st->chunk_ready;
+  std::copy(chunk_end, chunk_end + nchunks, plan->in_chunk_end);
   const int rc = grid_pipeline<Real>(plan, K, n, plan->in_uu.as<Real>(),
                                      plan->in_vv.as<Real>(),
                                      plan->in_ww.as<Real>(),
@@ -1994,6 +2052,8 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   plan->stack_wait = nullptr;
   plan->norm_weight = nullptr;
   plan->norm_out = nullptr;
+  plan->in_chunks = 0;
+  plan->in_chunk_ready = nullptr;
   GG_TRY(rc);
   // Copy back only what the call can have changed: cells outside every tile
   // that holds records were neither read nor written on the device, so the

@@ -101,6 +101,8 @@ struct PlaceOut {
   unsigned long long* blk_skip;   // [num_blocks]
   unsigned long long* blk_macs;   // [num_blocks]
 };
+// Points per block of the placement kernel (its per-block partials).
+constexpr int kPlaceBlock = 256;
 int place_num_blocks(unsigned long long n);
 template <typename Real>
 cudaError_t launch_place(PlaceParams<Real> p, StackView view, TileGeom geom,

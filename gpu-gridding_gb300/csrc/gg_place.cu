@@ -13,7 +13,7 @@ namespace gg {
 
 namespace {
 
-constexpr int kPlaceThreads = 256;
+constexpr int kPlaceThreads = kPlaceBlock;
 
 template <typename T>
 __device__ __forceinline__ T warp_sum(T x) {
