@@ -91,14 +91,15 @@ class Tuning(ctypes.Structure):
     _fields_ = [("tile_u", ctypes.c_int), ("slice_staging", ctypes.c_int),
                 ("items_per_cta", ctypes.c_int), ("sort_detail", ctypes.c_int),
                 ("ctas_per_sm", ctypes.c_int), ("plane_group_mb", ctypes.c_int),
-                ("tile_order", ctypes.c_int), ("lane_groups", ctypes.c_int)]
+                ("tile_order", ctypes.c_int), ("lane_groups", ctypes.c_int),
+                ("tile_phases", ctypes.c_int)]
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
     @classmethod
     def from_dict(cls, d: dict) -> "Tuning":
-        t = cls(0, -1, 4, 2, 0, 0, 0, 0)
+        t = cls(0, -1, 4, 2, 0, 0, 0, 0, 0)
         for k, _ in cls._fields_:
             if k in d:
                 setattr(t, k, int(d[k]))

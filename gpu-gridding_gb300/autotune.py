@@ -13,6 +13,9 @@ no placement, norm or skip count (gg_tuning in the C header):
 * ``tile_order``    -- tiles taken by distance from the centre or row by row,
 * ``lane_groups``   -- on 32-wide tiles, each consumer warp takes records
   whole (1) or as two half-warp streams (2).
+* ``tile_phases``   -- 1, 2 or 4 tile grids offset by a fraction of a tile
+  width; each visibility is gridded on the one that cuts its footprint
+  into the fewest tile columns, one pass per grid.
 
 :func:`search` runs a coordinate search over them with a caller-supplied
 timing function; :func:`autotune` times real gridding calls of a workload
@@ -36,12 +39,12 @@ from typing import Callable, Dict, Iterable, Optional
 import numpy as np
 
 CACHE_ENV = "GPUGRID_TUNE_CACHE"
-CACHE_VERSION = 7
+CACHE_VERSION = 8
 
 #: The plan's settings before any tuning (each call chooses shape/staging).
 DEFAULT_TUNING = {"tile_u": 0, "slice_staging": -1, "items_per_cta": 4,
                   "sort_detail": 2, "ctas_per_sm": 0, "plane_group_mb": 0,
-                  "tile_order": 0, "lane_groups": 0}
+                  "tile_order": 0, "lane_groups": 0, "tile_phases": 0}
 
 #: Values tried per setting, in search order.
 SEARCH_SPACE = (
@@ -54,6 +57,7 @@ SEARCH_SPACE = (
                            (1 << 20,)]),
     (("tile_order",), [(0,), (1,)]),
     (("lane_groups",), [(0,), (2,)]),
+    (("tile_phases",), [(0,), (2,), (4,)]),
 )
 
 

@@ -574,6 +574,10 @@ struct gg_plan {
   int plane_group_mb = 0; // slab bytes per plane group, 0 = L2 size / 2
   int queue_order = 0;    // tuning tile_order: 0 radius, 1 row by row
   int lane_groups = 0;    // tuning lane_groups: 0 automatic, 1, 2
+  int tile_phases = 0;    // tuning tile_phases: 0 automatic, 1, 2, 4
+  // Tile phases requested for the call being placed (0 automatic, chosen
+  // with the shape; see gridding_phases).
+  int call_phases = 1;
   // Batched calls larger than one sort can index (see batched_split): the
   // grids are cut into sub-batches, each gridded by its own sub-plan, which
   // keeps its geometry for replays.  A sub-plan takes the sort's transient
@@ -731,14 +735,17 @@ int check_device_error(gg_plan* p, cudaStream_t s) {
 // (ordering within a tile gets coarser) if the grids have many tiles.
 TileGeom make_geom(int shape, int grid_size, int num_grids,
                    const gg_kernels* K, int* key_bits, int sort_detail = 2,
-                   int num_groups = 1, const int* plane_group = nullptr) {
+                   int num_groups = 1, const int* plane_group = nullptr,
+                   int phases = 1) {
   TileGeom g{};
   g.tile_u = tile_u_of_shape(shape);
   g.tile_v = tile_v_of_shape(shape);
-  g.tiles_u = (grid_size + g.tile_u - 1) / g.tile_u;
+  g.tile_phases = phases > 1 ? phases : 1;
+  g.tiles_u = (grid_size + g.tile_u - 1) / g.tile_u + (phases > 1 ? 1 : 0);
   g.tiles_v = (grid_size + g.tile_v - 1) / g.tile_v;
   g.num_grids = num_grids;
   g.tiles_total = num_grids * g.tiles_u * g.tiles_v;
+  set_strips(g, grid_size);
   g.num_groups = num_groups;
   g.plane_group = num_groups > 1 ? plane_group : nullptr;
   const int tile_bits = ceil_log2((unsigned long long)num_groups *
@@ -847,13 +854,27 @@ int plane_groups(gg_plan* plan, const gg_kernels* K, int max_groups,
   return GG_OK;
 }
 
+// Most tiles of a call over all shapes, with the extra tile column of
+// tile phases.
 int max_tiles(int grid_size, int num_grids) {
   int m = 0;
   for (int sh = 0; sh < kNumTileShapes; ++sh) {
     const int tu = tile_u_of_shape(sh), tv = tile_v_of_shape(sh);
-    m = std::max(m, ((grid_size + tu - 1) / tu) * ((grid_size + tv - 1) / tv));
+    m = std::max(m, ((grid_size + tu - 1) / tu + 1) *
+                        ((grid_size + tv - 1) / tv));
   }
   return m * num_grids;
+}
+
+// Tile phases requested for a gridding call (TileGeom::tile_phases): the
+// plan's setting (0: chosen with the tile shape, see choose_shape), or 1
+// where four phases' extra sort-key bits and the split passes' would not
+// fit 32-bit keys.
+int gridding_phases(const gg_plan* plan, int grid_size, int num_grids) {
+  if (ceil_log2((unsigned long long)max_tiles(grid_size, num_grids)) + 2 + 2 >
+      32)
+    return 1;
+  return plan->tile_phases;
 }
 
 template <typename Real>
@@ -933,6 +954,7 @@ int grid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
     return GG_OK;
   }
   PlaceOut po;
+  plan->call_phases = gridding_phases(plan, grid_size, 1);
   GG_TRY(place_and_count<Real>(plan, K, pp, plan->forced_shape, d_norm,
                                d_num_skipped, s, &po));
   return bin_and_grid<Real>(plan, K, n, po, grid_size, 1, nullptr, d_grid, 0,
@@ -1006,7 +1028,7 @@ int place_and_count(gg_plan* plan, const gg_kernels* K,
                                 n, forced_shape,
                                 pp.defer_norm ? nullptr : d_norm,
                                 d_num_skipped, scalar64(plan, kMacs),
-                                sc + kShape, s));
+                                sc + kShape, s, plan->call_phases));
   GG_CUDA(launch_count_records(po.cell, po.meta, n, view, sc + kShape,
                                po.rec_count, s));
   GG_CUDA(exclusive_scan_u32(po.rec_count, plan->rec_offset.as<uint32_t>(), n,
@@ -1072,17 +1094,22 @@ int bin_records(gg_plan* plan, const gg_kernels* K, size_t n,
   plan->stats.num_records = total;
   memcpy(&plan->stats.num_macs, (char*)plan->h_scalars + 32, 8);
   int key_bits = 0;
+  // Tile phases (chosen with the shape; placement counted the records with
+  // them): one more tile column and a phase field in the virtual group.
+  const int phases = phases_of_shape(plan->h_scalars[kShape]);
+  const int phase_bits = ceil_log2((unsigned long long)phases);
   // Plane groups: as many as the key's spare bits above the tile index
   // allow (at most 64).
   const int base_bits = ceil_log2((unsigned long long)num_grids *
                                   ((grid_size + tile_u_of_shape(shape) - 1) /
-                                   tile_u_of_shape(shape)) *
+                                       tile_u_of_shape(shape) +
+                                   (phases > 1 ? 1 : 0)) *
                                   ((grid_size + tile_v_of_shape(shape) - 1) /
                                    tile_v_of_shape(shape)));
   // Split passes need up to two more groups, so key bits for them.  The
   // caller sets split_row (a multiple of every tile height) only on large
   // grids, where the copies they overlap outweigh the extra passes' tails.
-  const int spare = 32 - base_bits;
+  const int spare = 32 - base_bits - phase_bits;
   const int tile_v = tile_v_of_shape(shape);
   const bool split = plan->split_event && num_grids == 1 && spare >= 2 &&
                      plan->split_row > 0 && plan->split_row < grid_size &&
@@ -1097,10 +1124,10 @@ int bin_records(gg_plan* plan, const gg_kernels* K, size_t n,
   // halves and the last group's split overlaps the copy back.
   const int split_mask = !split ? 0 : (pgroups == 1 ? 1 : 3);
   const int num_groups =
-      pgroups + (split_mask & 1) + ((split_mask >> 1) & 1);
+      (pgroups + (split_mask & 1) + ((split_mask >> 1) & 1)) * phases;
   TileGeom geom = make_geom(shape, grid_size, num_grids, K, &key_bits,
                             plan->sort_detail, num_groups,
-                            plan->plane_group.as<int>());
+                            plan->plane_group.as<int>(), phases);
   geom.split_tv = split ? plan->split_row / tile_v : 0;
   geom.split_mask = split_mask;
   geom.lane_groups = lane_groups_for(plan, geom.tile_u, stage);
@@ -1282,8 +1309,9 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
   const bool want_spans = plan->h_spans && num_grids == 1 &&
                           2 * geom.tiles_v <= plan->h_spans_cap;
   if (want_spans) {
+    // Spans in strips of tile_u / tile_phases columns (launch_touched_spans).
     plan->spans_tiles_v = geom.tiles_v;
-    plan->spans_tile_u = geom.tile_u;
+    plan->spans_tile_u = 1 << geom.strip_shift;
     plan->spans_tile_v = geom.tile_v;
     plan->spans_async = b.total > 0;
     plan->spans_written = true;
@@ -1298,8 +1326,7 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
     GG_CUDA(cudaMemsetAsync(plan->spans.p, 0xFF, half, s));
     GG_CUDA(cudaMemsetAsync(plan->spans.as<char>() + half, 0, half, s));
     GG_CUDA(launch_touched_spans(plan->tile_start.as<uint32_t>(), b.num_tiles,
-                                 geom.tiles_total, geom.tiles_u,
-                                 plan->spans.as<uint32_t>(),
+                                 geom, grid_size, plan->spans.as<uint32_t>(),
                                  plan->spans.as<uint32_t>() + geom.tiles_v,
                                  s));
     GG_CUDA(cudaMemcpyAsync(plan->h_spans, plan->spans.p, 2 * half,
@@ -1321,27 +1348,30 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
   plan->kept.rec_vis = b.vals;
   plan->kept.num_ctas = num_ctas;
   // Per pass: the upload it waits for, and the event of the last upper pass.
+  // Passes are (group, phase) with the phases of a group consecutive: a
+  // group's waits come before its first phase, its event after its last.
+  const int P = geom.tile_phases;
+  const int base_groups = geom.num_groups / P;
   std::vector<cudaEvent_t> wait_before(geom.num_groups, nullptr);
   std::vector<cudaEvent_t> record_after(geom.num_groups, nullptr);
   wait_before[0] = plan->grid_wait;
   if (geom.split_mask & 1) {
     if (plan->split_wait) wait_before[0] = plan->split_wait;
-    wait_before[1] = plan->grid_wait;
+    wait_before[P] = plan->grid_wait;
   }
-  const int upper_done = (geom.split_mask & 2) ? geom.num_groups - 2
+  const int upper_done = (geom.split_mask & 2) ? base_groups - 2
                          : geom.split_mask == 1 ? 0
                                                 : -1;
-  if (upper_done >= 0) record_after[upper_done] = plan->split_event;
+  if (upper_done >= 0) record_after[upper_done * P + P - 1] = plan->split_event;
   const uint32_t* tile_groups = nullptr;
   if (plan->host_grid) {
     if (num_grids != 1 || geom.split_mask != 0 || geom.num_groups >= 0xFFFF)
       return set_error(GG_ERR_UNSUPPORTED,
                        "direct grid access needs one grid, no split passes "
                        "and fewer than 65535 plane groups");
-    GG_TRY(plan->tile_groups.ensure((size_t)geom.tiles_total * 4));
-    GG_CUDA(launch_tile_groups(plan->tile_start.as<uint32_t>(),
-                               geom.num_groups, geom, grid_size,
-                               plan->tile_groups.as<uint32_t>(),
+    GG_TRY(plan->tile_groups.ensure((size_t)num_strips(geom) * 4));
+    GG_CUDA(launch_tile_groups(plan->tile_start.as<uint32_t>(), geom,
+                               grid_size, plan->tile_groups.as<uint32_t>(),
                                scalar64(plan, kDirectCells), s));
     tile_groups = plan->tile_groups.as<uint32_t>();
     plan->direct_launched = true;
@@ -1471,6 +1501,7 @@ int batched_pipeline(gg_plan* plan, const gg_kernels* K, int num_grids,
   po.blk_skip = nullptr;
   po.blk_macs = nullptr;
   const ChunkParts cp = chunk_parts(plan, num_chunks);
+  plan->call_phases = gridding_phases(plan, grid_size, num_grids);
 
   plan->mark(0, s);
   GG_CUDA(launch_place_batched<Real>(pp, view, po, plan->nterm.as<double>(),
@@ -1480,7 +1511,7 @@ int batched_pipeline(gg_plan* plan, const gg_kernels* K, int num_grids,
       plan->chunk_begin.as<unsigned long long>(), num_grids,
       plan->grid_chunk0.as<int>(), cp.norm, cp.skip, cp.macs,
       plan->forced_shape, d_norm, d_num_skipped, scalar64(plan, kMacs),
-      sc + kShape, s));
+      sc + kShape, s, plan->call_phases));
   GG_CUDA(launch_count_records(po.cell, po.meta, n, view, sc + kShape,
                                po.rec_count, s));
   GG_CUDA(exclusive_scan_u32(po.rec_count, T->rec_offset.as<uint32_t>(), n,
@@ -1573,6 +1604,7 @@ int batched_split(gg_plan* plan, const gg_kernels* K, int num_grids,
     c->plane_group_mb = plan->plane_group_mb;
     c->queue_order = plan->queue_order;
     c->lane_groups = plan->lane_groups;
+    c->tile_phases = plan->tile_phases;
     const int a = g0[k], b = g0[k + 1];
     const unsigned long long v0 = h_offsets[a];
     offs.assign(h_offsets + a, h_offsets + b + 1);
@@ -1709,6 +1741,7 @@ int degrid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   const size_t n = num_points;
   const StackView view = K->view();
   PlaceOut po;
+  plan->call_phases = 1;   // the degridding kernel's tiles have one phase
   GG_TRY(place_and_count<Real>(plan, K, pp, kDegridShape, nullptr, nullptr, s,
                                &po));
   Bins b;
@@ -2658,6 +2691,10 @@ GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* t) {
   if (t->lane_groups < 0 || t->lane_groups > 2)
     return set_error(GG_ERR_INVALID_ARG, "lane_groups = %d: 0, 1 or 2",
                      t->lane_groups);
+  if (t->tile_phases != 0 && t->tile_phases != 1 && t->tile_phases != 2 &&
+      t->tile_phases != 4)
+    return set_error(GG_ERR_INVALID_ARG, "tile_phases = %d: 0, 1, 2 or 4",
+                     t->tile_phases);
   const int old_shape = plan->forced_shape;
   GG_TRY(gg_plan_set_tile_shape(plan, t->tile_u));
   const int r = gg_plan_set_slice_staging(plan, t->slice_staging);
@@ -2671,6 +2708,7 @@ GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* t) {
   plan->plane_group_mb = t->plane_group_mb;
   plan->queue_order = t->tile_order;
   plan->lane_groups = t->lane_groups;
+  plan->tile_phases = t->tile_phases;
   return GG_OK;
 }
 
@@ -2685,12 +2723,13 @@ GG_API int gg_plan_get_tuning(const gg_plan* plan, gg_tuning* t) {
   t->plane_group_mb = plan->plane_group_mb;
   t->tile_order = plan->queue_order;
   t->lane_groups = plan->lane_groups;
+  t->tile_phases = plan->tile_phases;
   return GG_OK;
 }
 
 GG_API int gg_host_set_tuning(const gg_tuning* t) {
   t_last_error.clear();
-  const gg_tuning defaults{0, -1, 4, 2, 0, 0, 0, 0};
+  const gg_tuning defaults{0, -1, 4, 2, 0, 0, 0, 0, 0};
   int dev;
   GG_TRY(current_device(&dev));
   DeviceState* st;

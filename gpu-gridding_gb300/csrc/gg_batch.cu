@@ -135,7 +135,7 @@ k_batch_finalize(int num_grids, const int* __restrict__ grid_chunk0,
                  const double* __restrict__ chunk_norm,
                  const unsigned long long* __restrict__ chunk_skip,
                  const unsigned long long* __restrict__ chunk_macs,
-                 int forced_shape, double* d_norm,
+                 int forced_shape, int phases, double* d_norm,
                  unsigned long long* d_num_skipped,
                  unsigned long long* d_macs, uint32_t* d_shape) {
   unsigned long long points = 0, skips = 0, macs = 0;
@@ -157,7 +157,7 @@ k_batch_finalize(int num_grids, const int* __restrict__ grid_chunk0,
   macs = block_sum(macs);
   if (threadIdx.x == 0) {
     *d_macs = macs;
-    *d_shape = choose_shape(macs, points - skips, forced_shape);
+    *d_shape = choose_shape(macs, points - skips, forced_shape, phases);
   }
 }
 
@@ -182,13 +182,14 @@ cudaError_t launch_batch_totals(const uint32_t* meta, const double* nterm,
                                 int forced_shape, double* d_norm,
                                 unsigned long long* d_num_skipped,
                                 unsigned long long* d_macs, uint32_t* d_shape,
-                                cudaStream_t s) {
+                                cudaStream_t s, int phases) {
   if (num_chunks > 0)
     k_chunk_totals<<<num_chunks, kThreads, 0, s>>>(
         meta, nterm, view, chunk_begin, chunk_norm, chunk_skip, chunk_macs);
   k_batch_finalize<<<1, kThreads, 0, s>>>(
       num_grids, grid_chunk0, chunk_begin, chunk_norm, chunk_skip,
-      chunk_macs, forced_shape, d_norm, d_num_skipped, d_macs, d_shape);
+      chunk_macs, forced_shape, phases, d_norm, d_num_skipped, d_macs,
+      d_shape);
   return cudaGetLastError();
 }
 

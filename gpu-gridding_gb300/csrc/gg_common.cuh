@@ -183,7 +183,42 @@ struct TileGeom {
   // 0) -- the whole warp takes each record that meets its rows; 2 -- each
   // half-warp (16 columns) takes the records that meet its own columns.
   int lane_groups;
+  // Tile phases (1, 2 or 4): the tile columns of phase p start p * tile_u /
+  // tile_phases cells to the left of phase 0's, and each visibility is
+  // gridded on the phase whose tiles cut its footprint into the fewest
+  // columns (footprint_phase).  Tiles of different phases overlap, so each
+  // phase is a pass of its own: virtual group = group * tile_phases +
+  // phase.  With more than one phase tiles_u counts one more column (phase
+  // p's first column starts left of the grid, its last may end past it).
+  int tile_phases;
+  // Strips of tile_u / tile_phases columns (a power of two, 1 << strip_shift)
+  // by tile rows: the units in which a single-grid call records which
+  // passes touch which cells (strips_u strips per tile row).
+  int strip_shift;
+  int strips_u;
 };
+
+// Columns of the tile grid of virtual group `group` left of phase 0's
+// (tile_phases >= 1; a phase is one strip, 1 << strip_shift columns).
+__host__ __device__ inline int phase_shift(const TileGeom& g, int group) {
+  return (group % g.tile_phases) << g.strip_shift;
+}
+
+// Phase of a footprint spanning cells [c0, c1] (c0 >= 0): the one whose
+// tile columns cut it into the fewest pieces, the lowest on ties.
+__host__ __device__ inline int footprint_phase(int c0, int c1, int tile_u,
+                                               int phases) {
+  int best = 0, fewest = c1 / tile_u - c0 / tile_u;
+  for (int p = 1; p < phases; ++p) {
+    const int sh = p * (tile_u / phases);
+    const int n = (c1 + sh) / tile_u - (c0 + sh) / tile_u;
+    if (n < fewest) {
+      fewest = n;
+      best = p;
+    }
+  }
+  return best;
+}
 
 // Work item of the gridding kernel: a range of sorted records of one tile.
 struct WorkItem {

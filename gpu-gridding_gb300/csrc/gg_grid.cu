@@ -92,16 +92,21 @@ struct GridArgs {
   const uint32_t* tile_groups;
 };
 
-// Source and destination of a tile's read-modify-write in plane group
-// `group`: the scratch grid g, or the caller's grid h in direct mode.
+// Source and destination of a grid cell's read-modify-write in virtual
+// group `group`: the scratch grid g, or the caller's grid h in direct mode.
+// Direct mode keeps, per strip of tile_u / tile_phases columns of a tile
+// row, the first and last virtual group whose tiles hold records there
+// (k_tile_groups): the first reads the cells from h, the last writes them
+// to h, the others go through g.
 template <typename R2>
-__device__ __forceinline__ void tile_ends(const uint32_t* tile_groups, int rt,
-                                          int group, R2* g, R2* h, R2*& src,
-                                          R2*& dst) {
+__device__ __forceinline__ void cell_ends(const uint32_t* tile_groups,
+                                          const TileGeom& geom, int tv,
+                                          int col, int group, R2* g, R2* h,
+                                          R2*& src, R2*& dst) {
   src = g;
   dst = g;
   if (tile_groups) {
-    const uint32_t fl = tile_groups[rt];
+    const uint32_t fl = tile_groups[tv * geom.strips_u + (col >> geom.strip_shift)];
     if ((int)(fl & 0xFFFFu) == group) src = h;
     if ((int)(fl >> 16) == group) dst = h;
   }
@@ -190,7 +195,7 @@ __device__ bool produce(const GridArgs<Real>& a, Smem<Real, kStage>& sm) {
     if (!done) {
       item = a.items[it];
       const int tl = item.tile % tiles_per_grid;
-      u0 = (tl % a.geom.tiles_u) * WS::kTileU;
+      u0 = (tl % a.geom.tiles_u) * WS::kTileU - phase_shift(a.geom, a.group);
       v0 = (tl / a.geom.tiles_u) * WS::kTileV;
     }
     int b0 = item.rec_begin;
@@ -619,7 +624,8 @@ k_grid_tiles(GridArgs<Real> a) {
       const int rt = item.tile % a.geom.tiles_total;   // real tile
       const int gi = rt / tiles_per_grid;
       const int tl = rt - gi * tiles_per_grid;
-      const int u0 = (tl % a.geom.tiles_u) * WS::kTileU;
+      const int u0 =
+          (tl % a.geom.tiles_u) * WS::kTileU - phase_shift(a.geom, a.group);
       const int v0 = (tl / a.geom.tiles_u) * WS::kTileV;
       R2 out[kRows];
 #pragma unroll
@@ -634,14 +640,17 @@ k_grid_tiles(GridArgs<Real> a) {
       }
       const int col = u0 + lx;
       if (item.slot < 0) {
+        // Phase tiles reach past the grid's first and last columns.
+        const bool col_in = (unsigned)col < (unsigned)G_size;
         R2 *src, *dst;
-        tile_ends<R2>(a.tile_groups, rt, a.group,
+        cell_ends<R2>(a.tile_groups, a.geom, tl / a.geom.tiles_u,
+                      col_in ? col : 0, a.group,
                       (R2*)(a.grid + (long long)gi * a.grid_stride),
                       (R2*)a.host, src, dst);
 #pragma unroll
         for (int r = 0; r < kRows; ++r) {
           const int row = v0 + rowl + r;
-          if (row < G_size && col < G_size) {
+          if (row < G_size && col_in) {
             const size_t off = (size_t)row * G_size + col;
             R2 old = __ldcs(src + off);
             old.x += out[r].x;
@@ -684,18 +693,18 @@ __global__ void k_reduce_partials(const int4* __restrict__ split_tiles,
     const int rt = d.x % g.tiles_total;
     const int gi = rt / tiles_per_grid;
     const int tl = rt - gi * tiles_per_grid;
-    const int u0 = (tl % g.tiles_u) * WS::kTileU;
+    const int u0 = (tl % g.tiles_u) * WS::kTileU - phase_shift(g, group);
     const int v0 = (tl / g.tiles_u) * WS::kTileV;
-    R2 *src, *dst;
-    tile_ends<R2>(tile_groups, rt, group,
-                  (R2*)(grid + (long long)gi * grid_stride), (R2*)host, src,
-                  dst);
+    R2* const gg = (R2*)(grid + (long long)gi * grid_stride);
     for (int e = threadIdx.x; e < kCells; e += blockDim.x) {
       const int r = e / kConsumers, t = e % kConsumers;
       const int w = t >> 5, ln = t & 31;
       const int row = v0 + w * WS::kBand + (ln / TW) * kRows + r;
       const int col = u0 + ln % TW;
-      if (row >= G || col >= G) continue;
+      if (row >= G || (unsigned)col >= (unsigned)G) continue;
+      R2 *src, *dst;
+      cell_ends<R2>(tile_groups, g, tl / g.tiles_u, col, group, gg,
+                    (R2*)host, src, dst);
       const size_t off = (size_t)row * G + col;
       const R2 old = src[off];
       double sx = old.x, sy = old.y;
@@ -723,43 +732,57 @@ __global__ void k_tile_bounds(const uint32_t* __restrict__ keys, uint32_t n,
   }
 }
 
+// Per tile row of a single grid, the strips (tile_u / tile_phases columns)
+// that virtual tiles with records cover: [lo, hi).
 __global__ void k_touched_spans(const uint32_t* __restrict__ tile_start,
                                 int num_tiles, int tiles_total, int tiles_u,
+                                int phases, int strips_u,
                                 uint32_t* __restrict__ lo,
                                 uint32_t* __restrict__ hi) {
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < num_tiles;
        t += gridDim.x * blockDim.x) {
     if (tile_start[t + 1] == tile_start[t]) continue;
     const int r = t % tiles_total;
-    atomicMin(&lo[r / tiles_u], (uint32_t)(r % tiles_u));
-    atomicMax(&hi[r / tiles_u], (uint32_t)(r % tiles_u) + 1u);
+    const int p = (t / tiles_total) % phases;
+    const int a = max((r % tiles_u) * phases - p, 0);
+    const int b = min((r % tiles_u) * phases - p + phases, strips_u);
+    if (a >= b) continue;
+    atomicMin(&lo[r / tiles_u], (uint32_t)a);
+    atomicMax(&hi[r / tiles_u], (uint32_t)b);
   }
 }
 
-// out[t] = first | last << 16: the first and last plane group with records
-// in real tile t (0xFFFF | 0xFFFF << 16 when none), for a single grid.
-// *cells += the grid cells of the tiles that have records (clipped to the
+// out[tv * strips_u + sc] = first | last << 16: the first and last virtual
+// group whose tiles hold records in strip sc (tile_u / tile_phases columns)
+// of tile row tv (0xFFFF | 0xFFFF << 16 when none), for a single grid.  In
+// phase p the strip lies in tile column (sc + p) / tile_phases.
+// *cells += the grid cells of the strips that have records (clipped to the
 // grid), the cells a direct-mode call reads and writes at host.
 __global__ void k_tile_groups(const uint32_t* __restrict__ tile_start,
-                              int num_groups, int tiles_total, int tiles_u,
-                              int tile_u, int tile_v, int G,
-                              uint32_t* __restrict__ out,
+                              TileGeom geom, int G, uint32_t* __restrict__ out,
                               unsigned long long* cells) {
+  const int P = geom.tile_phases > 1 ? geom.tile_phases : 1;
+  const int sw = 1 << geom.strip_shift;
+  const int strips_u = geom.strips_u;
+  const int n = strips_u * geom.tiles_v;
   unsigned long long mine = 0;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < tiles_total;
-       t += gridDim.x * blockDim.x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    const int tv = i / strips_u, sc = i % strips_u;
     uint32_t first = 0xFFFFu, last = 0xFFFFu;
-    for (int g = 0; g < num_groups; ++g) {
-      const size_t v = (size_t)g * tiles_total + t;
+    for (int g = 0; g < geom.num_groups; ++g) {
+      const int tc = (sc + g % P) / P;
+      const size_t v =
+          (size_t)g * geom.tiles_total + (size_t)tv * geom.tiles_u + tc;
       if (tile_start[v + 1] > tile_start[v]) {
         if (first == 0xFFFFu) first = (uint32_t)g;
         last = (uint32_t)g;
       }
     }
-    out[t] = first | (last << 16);
+    out[i] = first | (last << 16);
     if (first != 0xFFFFu) {
-      const int u0 = (t % tiles_u) * tile_u, v0 = (t / tiles_u) * tile_v;
-      mine += (unsigned long long)min(tile_u, G - u0) * min(tile_v, G - v0);
+      const int u0 = sc * sw, v0 = tv * geom.tile_v;
+      mine += (unsigned long long)min(sw, G - u0) * min(geom.tile_v, G - v0);
     }
   }
   for (int o = 16; o > 0; o >>= 1) mine += __shfl_down_sync(0xffffffffu, mine, o);
@@ -913,23 +936,26 @@ cudaError_t launch_wait_probe(unsigned limit, uint32_t* error,
   return cudaGetLastError();
 }
 
-cudaError_t launch_tile_groups(const uint32_t* tile_start, int num_groups,
+cudaError_t launch_tile_groups(const uint32_t* tile_start,
                                const TileGeom& geom, int grid_size,
                                uint32_t* out, unsigned long long* cells,
                                cudaStream_t s) {
-  const int blocks = std::min(1024, (geom.tiles_total + 255) / 256);
-  k_tile_groups<<<blocks < 1 ? 1 : blocks, 256, 0, s>>>(
-      tile_start, num_groups, geom.tiles_total, geom.tiles_u, geom.tile_u,
-      geom.tile_v, grid_size, out, cells);
+  const int n = num_strips(geom);
+  const int blocks = std::min(1024, (n + 255) / 256);
+  k_tile_groups<<<blocks < 1 ? 1 : blocks, 256, 0, s>>>(tile_start, geom,
+                                                        grid_size, out, cells);
   return cudaGetLastError();
 }
 
 cudaError_t launch_touched_spans(const uint32_t* tile_start, int num_tiles,
-                                 int tiles_total, int tiles_u, uint32_t* lo,
-                                 uint32_t* hi, cudaStream_t s) {
+                                 const TileGeom& geom, int grid_size,
+                                 uint32_t* lo, uint32_t* hi, cudaStream_t s) {
+  (void)grid_size;
+  const int P = geom.tile_phases > 1 ? geom.tile_phases : 1;
   const int blocks = std::max(1, std::min((num_tiles + 255) / 256, 4096));
-  k_touched_spans<<<blocks, 256, 0, s>>>(tile_start, num_tiles, tiles_total,
-                                         tiles_u, lo, hi);
+  k_touched_spans<<<blocks, 256, 0, s>>>(tile_start, num_tiles,
+                                         geom.tiles_total, geom.tiles_u, P,
+                                         geom.strips_u, lo, hi);
   return cudaGetLastError();
 }
 

@@ -76,20 +76,30 @@ __host__ __device__ inline int tile_v_of_shape(int shape) {
   return 2048 / (32 >> shape);
 }
 
-// Tile shape and slice staging for a call, from its mean footprint side
-// sqrt(macs / gridded points): narrow tiles only for tiny footprints (a
-// 32-wide warp would leave most lanes outside them); kernel slices staged in
-// shared memory (bit 8) when footprints are small enough for their slices to
-// fit the slots, otherwise the kernel keeps its shared memory small so the
-// L1 cache serves the tap loads.  forced_shape >= 0 overrides the shape.
+// Tile shape, slice staging and tile phases for a call, from its mean
+// footprint side sqrt(macs / gridded points): narrow tiles only for tiny
+// footprints (a 32-wide warp would leave most lanes outside them); kernel
+// slices staged in shared memory (bit 8) when footprints are small enough
+// for their slices to fit the slots, otherwise the kernel keeps its shared
+// memory small so the L1 cache serves the tap loads; tile phases (bits 12
+// and 13: log2 of 1, 2 or 4) two when footprints are narrower than the
+// tile, where a second tile grid saves the most tile crossings, else one.
+// forced_shape >= 0 overrides the shape, phases > 0 the phases.
 __host__ __device__ inline uint32_t choose_shape(unsigned long long macs,
                                                  unsigned long long gridded,
-                                                 int forced_shape) {
+                                                 int forced_shape,
+                                                 int phases = 1) {
   const double side = gridded ? sqrt((double)macs / (double)gridded) : 0.0;
   int shape = forced_shape;
   if (shape < 0) shape = side >= 16.0 ? 0 : (side >= 8.0 ? 1 : 2);
   const uint32_t stage = side < 40.0 ? 1u : 0u;
-  return (uint32_t)shape | (stage << 8);
+  if (phases <= 0) phases = side < (double)tile_u_of_shape(shape) ? 2 : 1;
+  const uint32_t pbits = phases >= 4 ? 2u : (phases >= 2 ? 1u : 0u);
+  return (uint32_t)shape | (stage << 8) | (pbits << 12);
+}
+// Tile phases of a shape word made by choose_shape.
+__host__ __device__ inline int phases_of_shape(uint32_t word) {
+  return 1 << ((word >> 12) & 3u);
 }
 
 struct PlaceOut {
@@ -129,7 +139,8 @@ cudaError_t launch_place_finalize(const double* blk_norm,
                                   int forced_shape, double* d_norm,
                                   unsigned long long* d_num_skipped,
                                   unsigned long long* d_macs,
-                                  uint32_t* d_shape, cudaStream_t s);
+                                  uint32_t* d_shape, cudaStream_t s,
+                                  int phases = 1);
 // count[i] = tiles of shape *d_shape touched by visibility i (0 if skipped).
 cudaError_t launch_count_records(const uint32_t* cell, const uint32_t* meta,
                                  unsigned long long n, StackView view,
@@ -179,7 +190,7 @@ cudaError_t launch_batch_totals(const uint32_t* meta, const double* nterm,
                                 int forced_shape, double* d_norm,
                                 unsigned long long* d_num_skipped,
                                 unsigned long long* d_macs, uint32_t* d_shape,
-                                cudaStream_t s);
+                                cudaStream_t s, int phases = 1);
 
 // ---- work decomposition and gridding (gg_grid.cu) -------------------------
 cudaError_t launch_tile_bounds(const uint32_t* keys, uint32_t n, int shift,
@@ -189,14 +200,24 @@ cudaError_t launch_tile_bounds(const uint32_t* keys, uint32_t n, int shift,
 // that nothing arrives at, then set *error (see gg_plan_probe_bounded_wait).
 cudaError_t launch_wait_probe(unsigned limit, uint32_t* error,
                               cudaStream_t s);
-// Touched spans of a single-grid call: for every virtual tile t holding
-// records (tile_start[t + 1] > tile_start[t]), with real tile r = t mod
-// tiles_total at row r / tiles_u and column r mod tiles_u, lo[row] takes the
-// minimum column and hi[row] the maximum column + 1.  lo must start at
-// 0xFFFFFFFF and hi at 0.
+// Touched spans of a single-grid call, in strips of tile_u / tile_phases
+// columns: for every virtual tile t holding records (tile_start[t + 1] >
+// tile_start[t]) of tile row r, lo[r] takes the first strip it covers and
+// hi[r] the last + 1.  lo must start at 0xFFFFFFFF and hi at 0.
 cudaError_t launch_touched_spans(const uint32_t* tile_start, int num_tiles,
-                                 int tiles_total, int tiles_u, uint32_t* lo,
-                                 uint32_t* hi, cudaStream_t s);
+                                 const TileGeom& geom, int grid_size,
+                                 uint32_t* lo, uint32_t* hi, cudaStream_t s);
+// Strips of tile_u / tile_phases columns by tile rows of a single grid: the
+// units of the direct-mode group table and of the touched spans.
+inline int num_strips(const TileGeom& g) { return g.strips_u * g.tiles_v; }
+// Sets the strip fields of g (tile_u, tile_phases set) for a grid side.
+inline void set_strips(TileGeom& g, int grid_size) {
+  const int P = g.tile_phases > 1 ? g.tile_phases : 1;
+  int sh = 0;
+  while ((1 << (sh + 1)) <= g.tile_u / P) ++sh;
+  g.strip_shift = sh;
+  g.strips_u = (grid_size + (1 << sh) - 1) >> sh;
+}
 // Work-item queue of a call.  Tiles are virtual tiles (group * tiles_total
 // + tile, see TileGeom); the queue is group-major, and within a group the
 // chunks of split tiles come first.  group_items[g] .. group_items[g+1] is
@@ -241,14 +262,15 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                               const cudaEvent_t* record_after = nullptr,
                               Real* host_grid = nullptr,
                               const uint32_t* tile_groups = nullptr);
-// Direct mode of a single-grid call: per real tile, the first and last
-// plane group with records (first | last << 16, 0xFFFF when none), and
-// *cells += the grid cells of the tiles with records.  With tile_groups
-// given, launch_grid_tiles reads each such tile's cells from host_grid in
-// its first group's pass, writes them back there in its last group's, and
-// keeps the sums in between in grid: every cell takes the same additions in
-// the same order as when grid holds a copy of host_grid.
-cudaError_t launch_tile_groups(const uint32_t* tile_start, int num_groups,
+// Direct mode of a single-grid call: per strip (num_strips), the first and
+// last virtual group (plane group and tile phase) with records there
+// (first | last << 16, 0xFFFF when none), and *cells += the grid cells of
+// the strips with records.  With tile_groups given, launch_grid_tiles reads
+// each such strip's cells from host_grid in its first group's pass, writes
+// them back there in its last group's, and keeps the sums in between in
+// grid: every cell takes the same additions in the same order as when grid
+// holds a copy of host_grid.
+cudaError_t launch_tile_groups(const uint32_t* tile_start,
                                const TileGeom& geom, int grid_size,
                                uint32_t* out, unsigned long long* cells,
                                cudaStream_t s);

@@ -260,6 +260,8 @@ extern "C" GG_API int gg_grid_wproj_f_device_noalloc(
   geom.num_groups = 1;
   geom.tiles_total = geom.tiles_u * geom.tiles_v;
   geom.plane_group = nullptr;
+  geom.tile_phases = 1;
+  set_strips(geom, grid_size);
   const int num_tiles = geom.tiles_u * geom.tiles_v;
   const int tile_bits = ceil_log2_u((unsigned long long)num_tiles);
   int plane_bits = ceil_log2_u((unsigned long long)num_planes);

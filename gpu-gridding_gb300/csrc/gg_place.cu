@@ -117,7 +117,8 @@ __global__ void k_place_finalize(const double* __restrict__ blk_norm,
                                  const unsigned long long* __restrict__ blk_skip,
                                  const unsigned long long* __restrict__ blk_macs,
                                  int num_blocks, unsigned long long n_points,
-                                 int forced_shape, double* d_norm,
+                                 int forced_shape, int phases,
+                                 double* d_norm,
                                  unsigned long long* d_num_skipped,
                                  unsigned long long* d_macs,
                                  uint32_t* d_shape) {
@@ -147,12 +148,14 @@ __global__ void k_place_finalize(const double* __restrict__ blk_norm,
       if (d_norm) *d_norm += n;
       if (d_num_skipped) *d_num_skipped = s;
       if (d_macs) *d_macs = m;
-      if (d_shape) *d_shape = choose_shape(m, n_points - s, forced_shape);
+      if (d_shape)
+        *d_shape = choose_shape(m, n_points - s, forced_shape, phases);
     }
   }
 }
 
-// Records per visibility: tiles of the chosen shape its footprint touches.
+// Records per visibility: tiles of the chosen shape its footprint touches
+// (on its tile phase, see footprint_phase).
 __global__ void k_count(const uint32_t* __restrict__ cell,
                         const uint32_t* __restrict__ meta,
                         unsigned long long n, StackView v,
@@ -164,12 +167,16 @@ __global__ void k_count(const uint32_t* __restrict__ cell,
   const uint32_t m = meta[i];
   uint32_t c = 0;
   if (!meta_skipped(m)) {
-    const int shape = (int)(*d_shape & 0xFFu);
+    const uint32_t word = *d_shape;
+    const int shape = (int)(word & 0xFFu), phases = phases_of_shape(word);
     const int tw = tile_u_of_shape(shape), th = tile_v_of_shape(shape);
     const uint32_t ce = cell[i];
     const int gu = cell_u(ce), gv = cell_v(ce);
     const int s = v.support[meta_plane(m)];
-    c = (uint32_t)(((gu + s) / tw - (gu - s) / tw + 1) *
+    const int sh = phases > 1 ? footprint_phase(gu - s, gu + s, tw, phases) *
+                                    (tw / phases)
+                              : 0;
+    c = (uint32_t)(((gu + s + sh) / tw - (gu - s + sh) / tw + 1) *
                    ((gv + s) / th - (gv - s) / th + 1));
   }
   count[i] = c;
@@ -207,7 +214,12 @@ __global__ void k_emit(const uint32_t* __restrict__ cell,
   const int gu = cell_u(c), gv = cell_v(c);
   const int plane = meta_plane(m);
   const int s = v.support[plane];
-  const int tu0 = (gu - s) / g.tile_u, tu1 = (gu + s) / g.tile_u;
+  const int phase = g.tile_phases > 1 ? footprint_phase(gu - s, gu + s,
+                                                        g.tile_u,
+                                                        g.tile_phases)
+                                      : 0;
+  const int sh = phase * (g.tile_u / (g.tile_phases > 1 ? g.tile_phases : 1));
+  const int tu0 = (gu - s + sh) / g.tile_u, tu1 = (gu + s + sh) / g.tile_u;
   const int tv0 = (gv - s) / g.tile_v, tv1 = (gv + s) / g.tile_v;
   const int au = abs(meta_ou(m)), av = abs(meta_ov(m));
   uint32_t low = 0;
@@ -225,13 +237,17 @@ __global__ void k_emit(const uint32_t* __restrict__ cell,
         uint32_t group = g.plane_group ? (uint32_t)g.plane_group[plane] : 0u;
         if (g.split_tv > 0) {
           const uint32_t lower = tv >= g.split_tv ? 1u : 0u;
-          const uint32_t last = (uint32_t)(g.num_groups - 1 -
+          const int base_groups =
+              g.num_groups / (g.tile_phases > 1 ? g.tile_phases : 1);
+          const uint32_t last = (uint32_t)(base_groups - 1 -
                                            __popc((unsigned)g.split_mask));
           uint32_t v = group;
           if (g.split_mask & 1) v = group == 0 ? lower : group + 1;
           if ((g.split_mask & 2) && group == last) v += lower;
           group = v;
         }
+        if (g.tile_phases > 1)
+          group = group * (uint32_t)g.tile_phases + (uint32_t)phase;
         tile += group * (uint32_t)g.tiles_total;
       }
       keys[pos] = low_bits >= 32 ? low : ((tile << low_bits) | low);
@@ -293,10 +309,11 @@ cudaError_t launch_place_finalize(const double* blk_norm,
                                   int forced_shape, double* d_norm,
                                   unsigned long long* d_num_skipped,
                                   unsigned long long* d_macs,
-                                  uint32_t* d_shape, cudaStream_t s) {
+                                  uint32_t* d_shape, cudaStream_t s,
+                                  int phases) {
   k_place_finalize<<<1, 1024, 0, s>>>(blk_norm, blk_skip, blk_macs,
-                                      num_blocks, n, forced_shape, d_norm,
-                                      d_num_skipped, d_macs, d_shape);
+                                      num_blocks, n, forced_shape, phases,
+                                      d_norm, d_num_skipped, d_macs, d_shape);
   return cudaGetLastError();
 }
 
@@ -319,7 +336,7 @@ cudaError_t launch_norm_terms(const uint32_t* meta, const Real* weight,
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_place_finalize<<<1, 1024, 0, s>>>(blk_norm, nullptr, nullptr, nb, n, 0,
-                                      d_norm, nullptr, nullptr, nullptr);
+                                      1, d_norm, nullptr, nullptr, nullptr);
   return cudaGetLastError();
 }
 

@@ -204,6 +204,13 @@ GG_API int gg_plan_set_slice_staging(gg_plan* plan, int mode);
  *                  half-warp takes the records that meet its own 16
  *                  columns, so two narrow footprints are gridded side by
  *                  side; 0 (default) = 1
+ *   tile_phases    1, 2 or 4 tile grids offset by tile_u / tile_phases
+ *                  columns from one another; each visibility is gridded on
+ *                  the one whose tiles cut its footprint into the fewest
+ *                  columns (fewer lanes outside footprints, fewer records),
+ *                  one pass per tile grid; 0 (default): two when the
+ *                  call's mean footprint is narrower than the tile, else
+ *                  one
  * gg_plan_set_tile_shape and gg_plan_set_slice_staging set the first two
  * fields alone. */
 typedef struct
@@ -216,6 +223,7 @@ typedef struct
     int plane_group_mb;
     int tile_order;
     int lane_groups;
+    int tile_phases;
 } gg_tuning;
 
 GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* tuning);

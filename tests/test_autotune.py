@@ -84,7 +84,7 @@ def test_search_finds_separable_optimum(at):
     best, ms, trials = at.search(cost)
     assert best == {"tile_u": 16, "slice_staging": 1, "items_per_cta": 8,
                     "sort_detail": 1, "ctas_per_sm": 0, "plane_group_mb": 0,
-                    "tile_order": 0, "lane_groups": 0}
+                    "tile_order": 0, "lane_groups": 0, "tile_phases": 0}
     assert math.isclose(ms, 10.0)
     keys = [json.dumps(t, sort_keys=True) for t in calls]
     assert len(keys) == len(set(keys)) == len(trials)
@@ -103,7 +103,8 @@ def test_tuning_struct_round_trip(pkg):
     assert t.as_dict() == {"tile_u": 8, "slice_staging": -1,
                            "items_per_cta": 4, "sort_detail": 0,
                            "ctas_per_sm": 0, "plane_group_mb": 0,
-                           "tile_order": 0, "lane_groups": 0}
+                           "tile_order": 0, "lane_groups": 0,
+                           "tile_phases": 0}
 
 
 def test_host_search_keeps_the_fastest(at):

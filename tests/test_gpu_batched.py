@@ -56,12 +56,16 @@ def _run_batched(pkg, torch, wl, plan, stack):
     return grids.cpu().numpy(), norms.cpu().numpy(), skips.cpu().numpy()
 
 
-@pytest.mark.parametrize("group_mb", [1 << 20, 1])
-def test_batched_equals_single_calls(pkg, oracle_mod, torch, batch, group_mb):
+TUNINGS = [{"plane_group_mb": 1 << 20}, {"plane_group_mb": 1},
+           {"plane_group_mb": 1, "tile_phases": 2}, {"tile_phases": 4}]
+
+
+@pytest.mark.parametrize("tuning", TUNINGS)
+def test_batched_equals_single_calls(pkg, oracle_mod, torch, batch, tuning):
     wl = batch
     stack = pkg.KernelStack.from_workload(wl, "f")
     plan = pkg.Plan()
-    plan.set_tuning({"plane_group_mb": group_mb})
+    plan.set_tuning(tuning)
     grids, norms, skips = _run_batched(pkg, torch, wl, plan, stack)
     assert wl.num_grids == 6
     for c in range(wl.num_grids):
@@ -121,8 +125,8 @@ def _new_values(wl, seed):
     return vis, weight
 
 
-@pytest.mark.parametrize("group_mb", [1 << 20, 1])
-def test_replay_matches_batched_calls(pkg, torch, batch, group_mb):
+@pytest.mark.parametrize("tuning", TUNINGS)
+def test_replay_matches_batched_calls(pkg, torch, batch, tuning):
     """A replay with the original amplitudes reproduces the batched call bit
     for bit; with new amplitudes and weights it matches a fresh batched call
     on them bit for bit (the geometry depends on (u, v, w) only)."""
@@ -131,10 +135,11 @@ def test_replay_matches_batched_calls(pkg, torch, batch, group_mb):
     C, G = wl.num_grids, wl.grid_size
     stack = pkg.KernelStack.from_workload(wl, "f")
     plan = pkg.Plan()
-    plan.set_tuning({"plane_group_mb": group_mb})
+    plan.set_tuning(tuning)
     ref = _run_batched(pkg, torch, wl, plan, stack)
     # 1 MiB per pass: several plane groups; 1 TiB: a single pass.
-    assert (plan.stats()["num_plane_groups"] > 1) == (group_mb == 1)
+    assert (plan.stats()["num_plane_groups"] > 1) == (
+        tuning.get("plane_group_mb") == 1)
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     _same(_replay(pkg, torch, plan, stack, dev(wl.vis), dev(wl.weight), C, G),
           ref)
@@ -143,7 +148,7 @@ def test_replay_matches_batched_calls(pkg, torch, batch, group_mb):
     wl2 = copy.copy(wl)
     wl2.vis, wl2.weight = vis2, w2
     plan2 = pkg.Plan()
-    plan2.set_tuning({"plane_group_mb": group_mb})
+    plan2.set_tuning(tuning)
     _same(got, _run_batched(pkg, torch, wl2, plan2, stack))
 
 

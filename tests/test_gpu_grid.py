@@ -410,16 +410,18 @@ def _start_grid(G, seed, pinned=False, dtype=np.float32, torch=None):
     return t.numpy()
 
 
+@pytest.mark.parametrize("phases", [0, 4])
 @pytest.mark.parametrize("mode", ["copy", "in_place"])
 @pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("where", ["disk", "patch_centre", "patch_corner"])
 def test_dropin_copies_back_touched_spans(pkg, oracle_mod, synthetic, torch,
-                                          where, pinned, mode):
+                                          where, pinned, mode, phases):
     """The host-pointer call copies back only the tile rows' spans that
     hold records (or, in place, reads and writes only the tiles that hold
-    records).  With a random starting grid the result must be start + the
-    contributions everywhere, and bit-for-bit the start wherever nothing
-    was added (cells outside every footprint)."""
+    records), also with four tile phases (spans and host accesses in
+    strips of a quarter tile).  With a random starting grid the result
+    must be start + the contributions everywhere, and bit-for-bit the start
+    wherever nothing was added (cells outside every footprint)."""
     G = 1800
     if where == "disk":
         wl = synthetic.random_uniform_workload(
@@ -434,11 +436,15 @@ def test_dropin_copies_back_touched_spans(pkg, oracle_mod, synthetic, torch,
                 wl, uu=(wl.uu + np.float32(0.4 * extent)).astype(np.float32),
                 vv=(wl.vv - np.float32(0.4 * extent)).astype(np.float32))
     start = _start_grid(G, 3)
-    with _access(pkg, pkg.GRID_ACCESS_COPY if mode == "copy"
-                 else pkg.GRID_ACCESS_PAGEABLE):
-        g0, ns0, nm0 = pkg.grid_f(wl)
-        g1, ns1, nm1 = pkg.grid_f(wl, _start_grid(G, 3, pinned, torch=torch),
-                                  2.0)
+    pkg.set_host_tuning({"tile_phases": phases})
+    try:
+        with _access(pkg, pkg.GRID_ACCESS_COPY if mode == "copy"
+                     else pkg.GRID_ACCESS_PAGEABLE):
+            g0, ns0, nm0 = pkg.grid_f(wl)
+            g1, ns1, nm1 = pkg.grid_f(
+                wl, _start_grid(G, 3, pinned, torch=torch), 2.0)
+    finally:
+        pkg.set_host_tuning(None)
     assert ns1 == ns0 < wl.num_points
     assert abs(nm1 - (nm0 + 2.0)) <= 1e-12 * abs(nm1)
     assert max_rel(g1, start + g0) <= 1e-6
@@ -451,26 +457,30 @@ def test_dropin_copies_back_touched_spans(pkg, oracle_mod, synthetic, torch,
 
 
 @pytest.mark.parametrize("G", [4096, 4099])
-@pytest.mark.parametrize("groups_mb", [0, 1])
+@pytest.mark.parametrize("tuning", [{"plane_group_mb": 0},
+                                    {"plane_group_mb": 1},
+                                    {"plane_group_mb": 1, "tile_phases": 4},
+                                    {"tile_phases": 2}])
 @pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("prec", ["f", "d"])
 def test_dropin_split_passes(pkg, oracle_mod, synthetic, torch, prec, pinned,
-                             groups_mb, G):
+                             tuning, G):
     """On grids of 128 MiB and more the host-pointer call uploads the grid
     in two halves by rows and grids the first and last plane groups (or
     the only one) in two passes by tile rows, the upper rows first, and
     copies the upper rows back while the lower ones are gridded.  A random
     starting grid must still come back as start + contributions, bit for
     bit where nothing was added, with the reference's placement; with one
-    plane group and with several (1 MiB groups), on an even grid and on an
-    odd one (ragged last tiles; the split row a multiple of 256)."""
+    plane group and with several (1 MiB groups), with tile phases, on an
+    even grid and on an odd one (ragged last tiles; the split row a
+    multiple of 256)."""
     wl = synthetic.random_uniform_workload(
         "split", 60_000, G, 64, 2, 16, seed=23, cell_size_rad=1.2e-5,
         sigma_frac=0.15, clip_frac=0.45)
     dt = np.float32 if prec == "f" else np.float64
     grid_fn = pkg.grid_f if prec == "f" else pkg.grid_d
     start = _start_grid(G, 8, dtype=dt)
-    pkg.set_host_tuning({"plane_group_mb": groups_mb})
+    pkg.set_host_tuning(tuning)
     try:
         with _access(pkg, pkg.GRID_ACCESS_COPY):
             g0, ns0, nm0 = grid_fn(wl)
@@ -495,7 +505,10 @@ def test_dropin_split_passes(pkg, oracle_mod, synthetic, torch, prec, pinned,
 
 @pytest.mark.parametrize("G", [1800, 4099])
 @pytest.mark.parametrize("tuning", [{}, {"plane_group_mb": 1},
-                                    {"plane_group_mb": 1, "items_per_cta": 16}])
+                                    {"plane_group_mb": 1, "items_per_cta": 16},
+                                    {"tile_phases": 2},
+                                    {"plane_group_mb": 1, "items_per_cta": 16,
+                                     "tile_phases": 4}])
 @pytest.mark.parametrize("prec", ["f", "d"])
 def test_dropin_grid_access_modes(pkg, synthetic, torch, prec, tuning, G):
     """The caller's grid read and written in place by the gridding kernels
@@ -505,7 +518,9 @@ def test_dropin_grid_access_modes(pkg, synthetic, torch, prec, tuning, G):
     its last writes it back), with split heavy tiles (their partial sums
     reduced into the host grid) and with ragged edge tiles.  The copied
     grid agrees bit for bit below 128 MiB; above, its split passes size
-    their work items per pass, which changes only the rounding."""
+    their work items per pass, which changes only the rounding.  With tile
+    phases the host grid is read and written per strip of a phase's
+    tiles."""
     wl = synthetic.random_uniform_workload(
         "access", 40_000, G, 48, 2, 14, seed=31, cell_size_rad=2.4e-5,
         sigma_frac=0.12, clip_frac=0.45)

@@ -90,13 +90,15 @@ def test_skalow_placement_bit_exact(pkg, oracle_mod, skalow, torch, prec):
         assert np.array_equal(out[keep, col], p[key][keep]), key
 
 
-@pytest.mark.parametrize("tile_u", [0, 32, 16, 8])
-def test_skalow_grid_vs_oracles(pkg, skalow, torch, tile_u):
-    """Device-pointer call, automatic and forced tile shapes."""
+@pytest.mark.parametrize("tile_u,phases", [(0, 0), (32, 0), (16, 0), (8, 0),
+                                           (32, 2), (32, 4)])
+def test_skalow_grid_vs_oracles(pkg, skalow, torch, tile_u, phases):
+    """Device-pointer call, automatic and forced tile shapes, one, two and
+    four tile phases."""
     wl = skalow["wl"]
     stack = pkg.KernelStack.from_workload(wl, "f")
     plan = pkg.Plan()
-    plan.set_tile_shape(tile_u)
+    plan.set_tuning({"tile_u": tile_u, "tile_phases": phases})
     G = wl.grid_size
     grid = torch.zeros((G, G, 2), dtype=torch.float32, device="cuda")
     norm = torch.zeros(1, dtype=torch.float64, device="cuda")
@@ -115,7 +117,7 @@ def test_skalow_grid_vs_oracles(pkg, skalow, torch, tile_u):
     err_rms = rms_rel(g, skalow["g64"])
     tol_f = max(1e-5, skalow["err_f"] + 1e-6)
     err_vs_f = max_rel(g, skalow["gf"])
-    print(f"tile_u {tile_u}: vs FP64 max {err:.3e} rms {err_rms:.3e}; "
+    print(f"tile_u {tile_u} phases {phases}: vs FP64 max {err:.3e} rms {err_rms:.3e}; "
           f"vs _f {err_vs_f:.3e} (bound {tol_f:.3e}, _f vs FP64 "
           f"{skalow['err_f']:.3e})")
     assert err <= 1e-5

@@ -63,6 +63,14 @@ TUNINGS = [
     {"tile_u": 32, "slice_staging": 0, "items_per_cta": 4, "lane_groups": 1},
     {"tile_u": 32, "slice_staging": 0, "items_per_cta": 2, "lane_groups": 2,
      "plane_group_mb": 1},
+    {"tile_u": 32, "slice_staging": 0, "items_per_cta": 4, "tile_phases": 2},
+    {"tile_u": 32, "slice_staging": 1, "items_per_cta": 8, "tile_phases": 4,
+     "plane_group_mb": 1},
+    {"tile_u": 16, "slice_staging": 0, "items_per_cta": 2, "tile_phases": 4},
+    {"tile_u": 8, "slice_staging": 1, "items_per_cta": 4, "tile_phases": 2,
+     "plane_group_mb": 1},
+    {"tile_u": 32, "slice_staging": 0, "items_per_cta": 2, "lane_groups": 2,
+     "tile_phases": 2},
 ]
 
 
@@ -93,7 +101,8 @@ def test_tuning_rejects_bad_values(pkg, torch):
     before = plan.tuning()
     for bad in ({"tile_u": 12}, {"slice_staging": 2}, {"items_per_cta": 0},
                 {"items_per_cta": 65}, {"sort_detail": 3},
-                {"ctas_per_sm": -1}, {"tile_order": 2}, {"lane_groups": 3}):
+                {"ctas_per_sm": -1}, {"tile_order": 2}, {"lane_groups": 3},
+                {"tile_phases": 3}, {"tile_phases": 8}):
         with pytest.raises(pkg.GridError):
             plan.set_tuning(bad)
         assert plan.tuning() == before
@@ -138,7 +147,7 @@ def test_host_tuning_applies_to_dropin(pkg, torch, wl, fp64):
     default = pkg.host_tuning()
     tuned = {"tile_u": 16, "slice_staging": 0, "items_per_cta": 8,
              "sort_detail": 1, "ctas_per_sm": 0, "plane_group_mb": 1,
-             "tile_order": 1, "lane_groups": 1}
+             "tile_order": 1, "lane_groups": 1, "tile_phases": 2}
     try:
         pkg.set_host_tuning(tuned)
         assert pkg.host_tuning() == tuned
