@@ -1741,7 +1741,7 @@ int degrid_pipeline(gg_plan* plan, const gg_kernels* K, size_t num_points,
   const size_t n = num_points;
   const StackView view = K->view();
   PlaceOut po;
-  plan->call_phases = 1;   // the degridding kernel's tiles have one phase
+  plan->call_phases = gridding_phases(plan, grid_size, 1);
   GG_TRY(place_and_count<Real>(plan, K, pp, kDegridShape, nullptr, nullptr, s,
                                &po));
   Bins b;

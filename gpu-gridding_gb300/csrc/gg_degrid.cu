@@ -110,14 +110,16 @@ __device__ bool degrid_produce(const DegridArgs<Real>& a,
     it = __shfl_sync(0xffffffffu, it, 0);
     done = it >= end_item;
     WorkItem item{0, 0, 0, -1};
-    int tu = 0, tv = 0;
+    int tu = 0, tv = 0, sh = 0;
     if (!done) {
       item = a.items[it];
       const int tl = (item.tile % a.geom.tiles_total) % tiles_per_grid;
       tu = tl % a.geom.tiles_u;
       tv = tl / a.geom.tiles_u;
+      sh = phase_shift(a.geom, item.tile / a.geom.tiles_total);
     }
-    const int u0 = tu * DegridShape::kTileU, v0 = tv * DegridShape::kTileV;
+    const int u0 = tu * DegridShape::kTileU - sh;
+    const int v0 = tv * DegridShape::kTileV;
     int b0 = item.rec_begin;
     do {
       const int slot = (int)(k % kRing);
@@ -168,9 +170,10 @@ __device__ bool degrid_produce(const DegridArgs<Real>& a,
             }
             sm.band[slot][t] = band;
             // Rank of this tile among the visibility's tiles, in the order
-            // k_emit writes them (tile rows outer, tile columns inner).
-            const int tu0 = (gu - s) / DegridShape::kTileU;
-            const int tu1 = (gu + s) / DegridShape::kTileU;
+            // k_emit writes them (tile rows outer, tile columns inner, on
+            // the visibility's tile phase).
+            const int tu0 = (gu - s + sh) / DegridShape::kTileU;
+            const int tu1 = (gu + s + sh) / DegridShape::kTileU;
             const int tv0 = (gv - s) / DegridShape::kTileV;
             const uint32_t rank =
                 (uint32_t)((tv - tv0) * (tu1 - tu0 + 1) + (tu - tu0));
@@ -282,13 +285,17 @@ k_degrid_tiles(DegridArgs<Real> a) {
     if (head.z & 1) {  // first buffer of a work item: load its tile
       const WorkItem item = a.items[head.x];
       const int tl = (item.tile % a.geom.tiles_total) % tiles_per_grid;
-      const int col = (tl % a.geom.tiles_u) * DegridShape::kTileU + lane;
+      // Tiles of later phases start left of phase 0's (and may reach past
+      // either edge of the grid).
+      const int col = (tl % a.geom.tiles_u) * DegridShape::kTileU + lane -
+                      phase_shift(a.geom, item.tile / a.geom.tiles_total);
       const int row0 = (tl / a.geom.tiles_u) * DegridShape::kTileV + rowl;
+      const bool col_in = (unsigned)col < (unsigned)G;
 #pragma unroll
       for (int r = 0; r < kRows; ++r) {
         R2 g;
         g.x = g.y = 0;
-        if (row0 + r < G && col < G) g = grid[(size_t)(row0 + r) * G + col];
+        if (row0 + r < G && col_in) g = grid[(size_t)(row0 + r) * G + col];
         gx[r].x = gx[r].y = g.x;
         gy[r].x = gy[r].y = g.y;
       }

@@ -63,10 +63,14 @@ def _cdot(a, b):
     return complex(re.item(), im.item())
 
 
-@pytest.mark.parametrize("prec,tol", [("f", 1e-6), ("d", 1e-12)])
-def test_dot_product_identity(pkg, synthetic, torch, prec, tol):
+@pytest.mark.parametrize("prec,tol,phases", [("f", 1e-6, 0), ("d", 1e-12, 0),
+                                             ("f", 1e-6, 2), ("d", 1e-12, 4)])
+def test_dot_product_identity(pkg, synthetic, torch, prec, tol, phases):
+    """<G x, y> = <x, G^H y>, also with the gridding and the degridding on
+    two and four tile phases."""
     wl = synthetic.config0().subset(60_000)
     s = _setup(pkg, torch, wl, prec)
+    s["plan"].set_tuning({"tile_phases": phases})
     g = torch.Generator(device="cuda").manual_seed(1)
     x = torch.randn((wl.num_points, 2), generator=g, device="cuda",
                     dtype=s["dt"])
@@ -104,9 +108,11 @@ def test_dot_product_identity_cfg1_shape(pkg, synthetic, torch):
     assert rel <= 1e-6
 
 
-def test_degrid_matches_fp64_oracle(pkg, oracle_mod, torch):
+@pytest.mark.parametrize("phases", [0, 1, 2, 4])
+def test_degrid_matches_fp64_oracle(pkg, oracle_mod, torch, phases):
     wl, _ = load_golden("small_f")
     s = _setup(pkg, torch, wl, "f")
+    s["plan"].set_tuning({"tile_phases": phases})
     rng = np.random.default_rng(3)
     y = rng.standard_normal((wl.grid_size, wl.grid_size, 2))
     out = _adjoint(pkg, torch, s, torch.from_numpy(
@@ -194,7 +200,8 @@ def test_degrid_bit_identical_across_tunings(pkg, synthetic, torch):
     """Each record's partial result is formed the same way whichever CTA
     takes it, and each visibility adds its records in emission order, so
     plane groups, work-item splitting, record order and CTA count leave
-    the output bit for bit unchanged."""
+    the output bit for bit unchanged (tile phases change which tiles a
+    visibility's sum is cut into, so they are held at the default)."""
     wl = synthetic.config0().subset(40_000)
     s = _setup(pkg, torch, wl, "f")
     g = torch.Generator(device="cuda").manual_seed(7)
