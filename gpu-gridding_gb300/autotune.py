@@ -15,7 +15,8 @@ no placement, norm or skip count (gg_tuning in the C header):
   whole (1) or as two half-warp streams (2).
 * ``tile_phases``   -- 1, 2 or 4 tile grids offset by a fraction of a tile
   width; each visibility is gridded on the one that cuts its footprint
-  into the fewest tile columns, one pass per grid.
+  into the fewest tile columns (the later grids' tiles as partial tiles
+  added after the pass).
 
 :func:`search` runs a coordinate search over them with a caller-supplied
 timing function; :func:`autotune` times real gridding calls of a workload

@@ -669,6 +669,7 @@ struct gg_plan {
     bool stage = false;
     uint32_t num_records = 0;
     TileGeom geom{};
+    int group_span = 1;   // virtual groups per gridding launch
     const uint32_t* rec_vis = nullptr;
   } kept;
   ~gg_plan() {
@@ -1241,7 +1242,8 @@ int tile_queue_order(gg_plan* plan, const TileGeom& g, int grid_size,
 // (gridding; the degridder's items write no tile).
 template <typename Real>
 int build_work_items(gg_plan* plan, const Bins& b, int num_ctas, int passes,
-                     bool partial_tiles, cudaStream_t s, ItemBuffers* ib) {
+                     bool partial_tiles, cudaStream_t s, ItemBuffers* ib,
+                     int launch_span = 1) {
   using R2 = typename Vec2<Real>::type;
   uint32_t* sc = plan->scalars.as<uint32_t>();
   const int num_tiles = b.num_tiles;
@@ -1259,7 +1261,11 @@ int build_work_items(gg_plan* plan, const Bins& b, int num_ctas, int passes,
   GG_TRY(plan->item_b.ensure((size_t)num_tiles * 4 + 4));
   GG_TRY(plan->items.ensure(item_cap * sizeof(WorkItem)));
   GG_TRY(plan->split_tiles.ensure((size_t)num_tiles * sizeof(int4) + 16));
-  if (partial_tiles)
+  // Gridding launches that take all the tile phases of a plane group
+  // (launch_span = tile_phases): every tile of a later phase writes partial
+  // tiles, as many as the scans count (read back below).
+  const int pphases = partial_tiles && launch_span > 1 ? launch_span : 1;
+  if (partial_tiles && pphases == 1)
     GG_TRY(plan->partials.ensure(slot_cap * b.geom.tile_u * b.geom.tile_v *
                                  sizeof(R2)));
   GG_TRY(plan->group_items.ensure((size_t)(b.num_groups + 1) * 4));
@@ -1274,9 +1280,18 @@ int build_work_items(gg_plan* plan, const Bins& b, int num_ctas, int passes,
   ib->num_split = sc + kNumSplit;
   ib->counter = sc + kCounter;
   ib->scan_tmp = plan->scan_tmp.p;
+  ib->partial_phases = pphases;
   GG_TRY(tile_queue_order(plan, b.geom, b.grid_size, s, &ib->tile_order));
   GG_CUDA(launch_build_items(plan->tile_start.as<uint32_t>(), num_tiles,
                              b.total, chunk, *ib, s));
+  if (pphases > 1) {
+    uint32_t slots = 0;
+    GG_CUDA(cudaMemcpyAsync(&slots, ib->num_slots, sizeof(slots),
+                            cudaMemcpyDeviceToHost, s));
+    GG_CUDA(cudaStreamSynchronize(s));
+    GG_TRY(plan->partials.ensure(((size_t)slots + 1) * b.geom.tile_u *
+                                 b.geom.tile_v * sizeof(R2)));
+  }
   // item counts, 2 scans, item emit
   plan->stats.num_launches += 1 + 6 + 1;
   return GG_OK;
@@ -1343,13 +1358,22 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
   const int num_ctas = sms * per_sm;
   plan->stats.slice_staging = b.stage ? 1 : 0;
   ItemBuffers ib;
+  // The tile phases of a plane group share one launch, their later phases'
+  // tiles added as partial tiles after it -- except when the kernels read
+  // and write the caller's grid at host, where those additions would cross
+  // the host link after the launch instead of beside its work: there each
+  // phase has a launch of its own.  Items are sized per virtual group
+  // either way (a phase's tiles are smaller, and larger items leave longer
+  // tails).
+  const int span = plan->host_grid ? 1 : geom.tile_phases;
   GG_TRY(build_work_items<Real>(plan, b, num_ctas, geom.num_groups, true, s,
-                                &ib));
+                                &ib, span));
+  plan->kept.group_span = span;
   plan->kept.rec_vis = b.vals;
   plan->kept.num_ctas = num_ctas;
-  // Per pass: the upload it waits for, and the event of the last upper pass.
-  // Passes are (group, phase) with the phases of a group consecutive: a
-  // group's waits come before its first phase, its event after its last.
+  // The upload plane group g's first launch waits for (entry g * P), and
+  // the event after its last launch (entry g * P + P - 1) that marks the
+  // upper rows final.
   const int P = geom.tile_phases;
   const int base_groups = geom.num_groups / P;
   std::vector<cudaEvent_t> wait_before(geom.num_groups, nullptr);
@@ -1383,12 +1407,13 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
       po.cell, po.meta, po.vw, view, geom, grid_size, d_grid, grid_stride,
       plan->partials.as<Real>(), ib.split_tiles, ib.num_split, b.num_tiles,
       num_ctas, b.stage, s, wait_before.data(), record_after.data(),
-      (Real*)plan->host_grid, tile_groups));
+      (Real*)plan->host_grid, tile_groups, span));
   plan->split_launched = upper_done >= 0;
   plan->mark(4, s);
   plan->mark(5, s);
-  // per plane group the gridding pass and its partial reduction
-  plan->stats.num_launches += 2 * b.num_groups;
+  // the gridding launches, and per virtual group (plane group and tile
+  // phase) its partial reduction
+  plan->stats.num_launches += b.num_groups / span + b.num_groups;
   plan->events_valid = plan->profile;
   return GG_OK;
 }
@@ -1696,7 +1721,7 @@ int replay_pipeline(gg_plan* plan, const gg_kernels* K, const Real* vis,
       plan->meta.as<uint32_t>(), plan->vw.p, view, kp.geom, kp.grid_size,
       d_grids, grid_stride, plan->partials.as<Real>(),
       plan->split_tiles.as<int4>(), sc + kNumSplit, kp.num_tiles, kp.num_ctas,
-      kp.stage, s));
+      kp.stage, s, nullptr, nullptr, nullptr, nullptr, kp.group_span));
   return GG_OK;
 }
 

@@ -199,9 +199,10 @@ struct TileGeom {
 };
 
 // Columns of the tile grid of virtual group `group` left of phase 0's
-// (tile_phases >= 1; a phase is one strip, 1 << strip_shift columns).
+// (tile_phases a power of two >= 1; a phase is one strip, 1 << strip_shift
+// columns).
 __host__ __device__ inline int phase_shift(const TileGeom& g, int group) {
-  return (group % g.tile_phases) << g.strip_shift;
+  return (group & (g.tile_phases - 1)) << g.strip_shift;
 }
 
 // Phase of a footprint spanning cells [c0, c1] (c0 >= 0): the one whose

@@ -69,8 +69,9 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 template <typename Real>
 struct GridArgs {
   const WorkItem* items;
-  const uint32_t* group_items;  // queue range of this launch's plane group
-  int group;
+  const uint32_t* group_items;  // queue start of each virtual group
+  int group;                     // the launch's first virtual group
+  int group_span;                // virtual groups in the launch
   uint32_t* counter;
   uint32_t* error;          // set to 1 when a bounded wait runs out
   const uint32_t* rec_vis;
@@ -175,8 +176,10 @@ __device__ bool produce(const GridArgs<Real>& a, Smem<Real, kStage>& sm) {
   const int lane = threadIdx.x & 31;
   const int omax = a.view.omax;
   const int tiles_per_grid = a.geom.tiles_u * a.geom.tiles_v;
+  // The launch's items: those of its virtual groups (a plane group's tile
+  // phases, or one of them).
   const int first_item = (int)a.group_items[a.group];
-  const int end_item = (int)a.group_items[a.group + 1];
+  const int end_item = (int)a.group_items[a.group + a.group_span];
   const R2* __restrict__ taps = (const R2*)a.view.taps;
   SlotState st;
   for (int x = 0; x < kSlots; ++x) {
@@ -194,8 +197,9 @@ __device__ bool produce(const GridArgs<Real>& a, Smem<Real, kStage>& sm) {
     int u0 = 0, v0 = 0;
     if (!done) {
       item = a.items[it];
-      const int tl = item.tile % tiles_per_grid;
-      u0 = (tl % a.geom.tiles_u) * WS::kTileU - phase_shift(a.geom, a.group);
+      const int vg = item.tile / a.geom.tiles_total;   // virtual group
+      const int tl = (item.tile - vg * a.geom.tiles_total) % tiles_per_grid;
+      u0 = (tl % a.geom.tiles_u) * WS::kTileU - phase_shift(a.geom, vg);
       v0 = (tl / a.geom.tiles_u) * WS::kTileV;
     }
     int b0 = item.rec_begin;
@@ -624,8 +628,8 @@ k_grid_tiles(GridArgs<Real> a) {
       const int rt = item.tile % a.geom.tiles_total;   // real tile
       const int gi = rt / tiles_per_grid;
       const int tl = rt - gi * tiles_per_grid;
-      const int u0 =
-          (tl % a.geom.tiles_u) * WS::kTileU - phase_shift(a.geom, a.group);
+      const int vg = item.tile / a.geom.tiles_total;   // virtual group
+      const int u0 = (tl % a.geom.tiles_u) * WS::kTileU - phase_shift(a.geom, vg);
       const int v0 = (tl / a.geom.tiles_u) * WS::kTileV;
       R2 out[kRows];
 #pragma unroll
@@ -644,7 +648,7 @@ k_grid_tiles(GridArgs<Real> a) {
         const bool col_in = (unsigned)col < (unsigned)G_size;
         R2 *src, *dst;
         cell_ends<R2>(a.tile_groups, a.geom, tl / a.geom.tiles_u,
-                      col_in ? col : 0, a.group,
+                      col_in ? col : 0, vg,
                       (R2*)(a.grid + (long long)gi * a.grid_stride),
                       (R2*)a.host, src, dst);
 #pragma unroll
@@ -789,8 +793,6 @@ __global__ void k_tile_groups(const uint32_t* __restrict__ tile_start,
   if ((threadIdx.x & 31) == 0 && mine) atomicAdd(cells, mine);
 }
 
-// A[t] = chunks of tile t if it is split (more than one chunk), else 0;
-// B[t] = 1 if tile t has exactly one chunk.
 // Failure-path probe: every thread waits, bounded by `limit` probes, on an
 // mbarrier that nothing arrives at -- the wait the gridding kernels use --
 // so the wait runs out, the kernel sets the error flag and returns.
@@ -811,25 +813,31 @@ __device__ __forceinline__ int tile_at_rank(int i, int T,
 }
 
 // Counts per queue rank i (tile t = tile_at_rank(i)):
-// A[i] = chunks of t if it is split (more than one chunk), else 0;
-// B[i] = 1 if t has exactly one chunk.
+// A[i] = chunks of t if it writes partial tiles (more than one chunk, or
+// any chunk of a later tile phase), else 0;
+// B[i] = 1 if t owns its tile in one chunk.
 __global__ void k_item_counts(const uint32_t* __restrict__ tile_start,
                               int num_tiles, int num_groups,
                               const int* __restrict__ order, uint32_t chunk,
+                              int partial_phases,
                               uint32_t* __restrict__ A,
                               uint32_t* __restrict__ B) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= num_tiles) return;
-  const int t = tile_at_rank(i, num_tiles / num_groups, order);
+  const int T = num_tiles / num_groups;
+  const int t = tile_at_rank(i, T, order);
   const uint32_t c = tile_start[t + 1] - tile_start[t];
   const uint32_t chunks = (c + chunk - 1) / chunk;
-  A[i] = chunks > 1 ? chunks : 0;
-  B[i] = chunks == 1 ? 1 : 0;
+  // Later tile phases always write partial tiles (see ItemBuffers).
+  const bool split = chunks > 1 || (chunks == 1 && (i / T) % partial_phases);
+  A[i] = split ? chunks : 0;
+  B[i] = split ? 0 : chunks;
 }
 
-// The queue is group-major (see ItemBuffers); within plane group g the
-// chunks of split tiles come first (they are the largest items), then the
-// single-chunk tiles, each part in rank order.  With exclusive scans sA
+// The queue is group-major (see ItemBuffers); within virtual group g the
+// chunks of split tiles (every tile of a later tile phase counts as split)
+// come first (they are the largest items), then the single-chunk tiles,
+// each part in rank order.  With exclusive scans sA
 // (split chunks) and sB (single-chunk tiles) over the ranks, group g
 // starts at sA[gT] + sB[gT] (T = tiles per group), split chunk j of rank i
 // sits at sA[i] + sB[gT] + j and single rank i at sA[(g+1)T] + sB[i].
@@ -837,6 +845,7 @@ __global__ void k_item_counts(const uint32_t* __restrict__ tile_start,
 __global__ void k_item_emit(const uint32_t* __restrict__ tile_start,
                             int num_tiles, int num_groups,
                             const int* __restrict__ order, uint32_t chunk,
+                            int partial_phases,
                             const uint32_t* __restrict__ sA,
                             const uint32_t* __restrict__ sB,
                             const uint32_t* __restrict__ totA,
@@ -859,7 +868,7 @@ __global__ void k_item_emit(const uint32_t* __restrict__ tile_start,
   const uint32_t c = s1 - s0;
   if (c == 0) return;
   const uint32_t chunks = (c + chunk - 1) / chunk;
-  if (chunks == 1) {
+  if (chunks == 1 && g % partial_phases == 0) {
     WorkItem w;
     w.tile = t; w.rec_begin = (int)s0; w.rec_end = (int)s1; w.slot = -1;
     items[scanA((g + 1) * T) + sB[i]] = w;
@@ -966,8 +975,9 @@ cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
   uint32_t* A = b.chunks;
   uint32_t* B = b.split_chunks;
   const int blocks = (num_tiles + 256) / 256;   // one more thread: bounds
+  const int pp = b.partial_phases > 1 ? b.partial_phases : 1;
   k_item_counts<<<blocks, 256, 0, s>>>(tile_start, num_tiles, b.num_groups,
-                                       b.tile_order, chunk, A, B);
+                                       b.tile_order, chunk, pp, A, B);
   cudaError_t e;
   e = exclusive_scan_u32(A, A, num_tiles, b.num_slots, b.scan_tmp, s);
   if (e != cudaSuccess) return e;
@@ -977,7 +987,8 @@ cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
   e = cudaMemsetAsync(b.num_split, 0, sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
   k_item_emit<<<blocks, 256, 0, s>>>(tile_start, num_tiles, b.num_groups,
-                                     b.tile_order, chunk, A, B, b.num_slots,
+                                     b.tile_order, chunk, pp, A, B,
+                                     b.num_slots,
                                      b.counter,
                                      b.items, b.split_tiles, b.num_split,
                                      b.num_items, b.group_items);
@@ -1039,7 +1050,8 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                               int num_ctas, bool stage, cudaStream_t s,
                               const cudaEvent_t* wait_before,
                               const cudaEvent_t* record_after,
-                              Real* host_grid, const uint32_t* tile_groups) {
+                              Real* host_grid, const uint32_t* tile_groups,
+                              int group_span) {
   GridArgs<Real> a;
   a.items = items;
   a.group_items = group_items;
@@ -1066,7 +1078,9 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                                                 &smem, geom.lane_groups);
   if (e != cudaSuccess) return e;
   void* args[] = {&a};
-  for (int g = 0; g < geom.num_groups; ++g) {
+  const int span = group_span > 1 ? group_span : 1;
+  a.group_span = span;
+  for (int g = 0; g < geom.num_groups; g += span) {
     a.group = g;
     if (wait_before && wait_before[g]) {
       e = cudaStreamWaitEvent(s, wait_before[g], 0);
@@ -1076,12 +1090,14 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
     if (e != cudaSuccess) return e;
     e = cudaLaunchKernel(fn, dim3(num_ctas), dim3(kThreads), args, smem, s);
     if (e != cudaSuccess) return e;
-    e = launch_reduce_group<Real>(split_tiles, num_split, max_split,
-                                  partials, geom, g, grid_size, grid,
-                                  grid_stride, a.host, tile_groups, s);
-    if (e != cudaSuccess) return e;
-    if (record_after && record_after[g]) {
-      e = cudaEventRecord(record_after[g], s);
+    for (int p = 0; p < span; ++p) {
+      e = launch_reduce_group<Real>(split_tiles, num_split, max_split,
+                                    partials, geom, g + p, grid_size, grid,
+                                    grid_stride, a.host, tile_groups, s);
+      if (e != cudaSuccess) return e;
+    }
+    if (record_after && record_after[g + span - 1]) {
+      e = cudaEventRecord(record_after[g + span - 1], s);
       if (e != cudaSuccess) return e;
     }
   }
@@ -1095,12 +1111,12 @@ template cudaError_t launch_grid_tiles<float>(
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
     float*, long long, float*, const int4*, const uint32_t*, int, int, bool,
     cudaStream_t, const cudaEvent_t*, const cudaEvent_t*, float*,
-    const uint32_t*);
+    const uint32_t*, int);
 template cudaError_t launch_grid_tiles<double>(
     const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
     double*, long long, double*, const int4*, const uint32_t*, int, int, bool,
     cudaStream_t, const cudaEvent_t*, const cudaEvent_t*, double*,
-    const uint32_t*);
+    const uint32_t*, int);
 
 }  // namespace gg

@@ -82,8 +82,8 @@ __host__ __device__ inline int tile_v_of_shape(int shape) {
 // slices staged in shared memory (bit 8) when footprints are small enough
 // for their slices to fit the slots, otherwise the kernel keeps its shared
 // memory small so the L1 cache serves the tap loads; tile phases (bits 12
-// and 13: log2 of 1, 2 or 4) two when footprints are narrower than the
-// tile, where a second tile grid saves the most tile crossings, else one.
+// and 13: log2 of 1, 2 or 4) four when footprints are narrower than the
+// tile, where offset tile grids save the most tile crossings, else one.
 // forced_shape >= 0 overrides the shape, phases > 0 the phases.
 __host__ __device__ inline uint32_t choose_shape(unsigned long long macs,
                                                  unsigned long long gridded,
@@ -93,7 +93,7 @@ __host__ __device__ inline uint32_t choose_shape(unsigned long long macs,
   int shape = forced_shape;
   if (shape < 0) shape = side >= 16.0 ? 0 : (side >= 8.0 ? 1 : 2);
   const uint32_t stage = side < 40.0 ? 1u : 0u;
-  if (phases <= 0) phases = side < (double)tile_u_of_shape(shape) ? 2 : 1;
+  if (phases <= 0) phases = side < (double)tile_u_of_shape(shape) ? 4 : 1;
   const uint32_t pbits = phases >= 4 ? 2u : (phases >= 2 ? 1u : 0u);
   return (uint32_t)shape | (stage << 8) | (pbits << 12);
 }
@@ -237,16 +237,27 @@ struct ItemBuffers {
   // Queue order of the tiles within a group: rank r of group g is virtual
   // tile g * T + tile_order[r] (T = tiles per group); null = tile order.
   const int* tile_order = nullptr;
+  // > 1: the tiles of virtual groups g with g % partial_phases != 0 (tile
+  // phases after the first) write partial tiles even when they have one
+  // chunk, so that all the phases of a plane group share one launch.
+  int partial_phases = 1;
 };
 cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
                                uint32_t num_records, uint32_t chunk,
                                ItemBuffers b, cudaStream_t s);
-// One persistent launch per plane group, in group order, each followed by
-// the reduction of that group's split tiles (grid += their partials in
-// chunk order, FP64): the grid takes the groups' contributions in order.
-// wait_before[g] / record_after[g] (arrays of num_groups events, entries
-// may be null): s waits for the first before group g's pass and records
-// the second after it (and its reduction).
+// Persistent launches in virtual-group order, each over the work items of
+// group_span consecutive virtual groups: with group_span = tile_phases one
+// launch per plane group takes all its tile phases (the items were built
+// with ItemBuffers::partial_phases = tile_phases: the first phase's
+// single-chunk tiles are added to the grid by the launch, every other item
+// writes a partial tile); with group_span = 1 one launch per virtual group.
+// Each launch is followed by the reduction of its virtual groups' partial
+// tiles in group order (grid += their partials in chunk order, FP64): the
+// grid takes the groups' and phases' contributions in order.
+// wait_before[v] / record_after[v] (arrays of num_groups events, entries
+// may be null): s waits for the first before the launch that starts with
+// virtual group v and records the second after the launch (and its
+// reductions) that ends with v.
 template <typename Real>
 cudaError_t launch_grid_tiles(const WorkItem* items,
                               const uint32_t* group_items,
@@ -261,7 +272,8 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                               const cudaEvent_t* wait_before = nullptr,
                               const cudaEvent_t* record_after = nullptr,
                               Real* host_grid = nullptr,
-                              const uint32_t* tile_groups = nullptr);
+                              const uint32_t* tile_groups = nullptr,
+                              int group_span = 1);
 // Direct mode of a single-grid call: per strip (num_strips), the first and
 // last virtual group (plane group and tile phase) with records there
 // (first | last << 16, 0xFFFF when none), and *cells += the grid cells of

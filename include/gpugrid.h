@@ -208,9 +208,10 @@ GG_API int gg_plan_set_slice_staging(gg_plan* plan, int mode);
  *                  columns from one another; each visibility is gridded on
  *                  the one whose tiles cut its footprint into the fewest
  *                  columns (fewer lanes outside footprints, fewer records),
- *                  one pass per tile grid; 0 (default): two when the
- *                  call's mean footprint is narrower than the tile, else
- *                  one
+ *                  all in one pass per plane group (the tiles of later
+ *                  grids add partial tiles after it); 0 (default): four
+ *                  when the call's mean footprint is narrower than the
+ *                  tile, else one
  * gg_plan_set_tile_shape and gg_plan_set_slice_staging set the first two
  * fields alone. */
 typedef struct
