@@ -529,7 +529,8 @@ def host_grid_access() -> int:
 
 
 HOST_PHASES = ("staging", "placement", "binning", "work_items", "grid_tiles",
-               "finish")
+               "finish", "host_first_work", "host_synchronised",
+               "host_return")
 
 
 def set_host_profiling(enable: bool) -> None:

@@ -14,6 +14,7 @@
 // The host synchronises once, after step 2, to size the sort buffers.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -158,6 +159,9 @@ struct DeviceState {
   bool profile = false;
   bool profile_valid = false;
   cudaEvent_t call_start = nullptr, call_end = nullptr, copies_done = nullptr;
+  // Host clock of the last host-pointer call (ms from its entry): first
+  // device work queued, final synchronisation returned, return.
+  double host_ms[3] = {0.0, 0.0, 0.0};
 };
 
 std::mutex g_devices_mu;
@@ -560,7 +564,7 @@ struct gg_plan {
   DevBuf cell, meta, vw, rec_count, rec_offset;
   DevBuf blk_norm, blk_skip, blk_macs;
   DevBuf keys0, vals0, keys1, vals1, sort_tmp, scan_tmp;
-  DevBuf tile_start, item_a, item_b, items, split_tiles, partials;
+  DevBuf tile_start, item_a, item_b, items, split_tiles, partials, tile_slot;
   DevBuf scalars;  // device scalars, see Scalar below
   uint32_t* h_scalars = nullptr;  // pinned mirror
   gg_stats stats{};
@@ -1261,6 +1265,7 @@ int build_work_items(gg_plan* plan, const Bins& b, int num_ctas, int passes,
   GG_TRY(plan->item_b.ensure((size_t)num_tiles * 4 + 4));
   GG_TRY(plan->items.ensure(item_cap * sizeof(WorkItem)));
   GG_TRY(plan->split_tiles.ensure((size_t)num_tiles * sizeof(int4) + 16));
+  GG_TRY(plan->tile_slot.ensure((size_t)num_tiles * sizeof(int2) + 16));
   // Gridding launches that take all the tile phases of a plane group
   // (launch_span = tile_phases): every tile of a later phase writes partial
   // tiles, as many as the scans count (read back below).
@@ -1281,6 +1286,7 @@ int build_work_items(gg_plan* plan, const Bins& b, int num_ctas, int passes,
   ib->counter = sc + kCounter;
   ib->scan_tmp = plan->scan_tmp.p;
   ib->partial_phases = pphases;
+  ib->tile_slot = plan->tile_slot.as<int2>();
   GG_TRY(tile_queue_order(plan, b.geom, b.grid_size, s, &ib->tile_order));
   GG_CUDA(launch_build_items(plan->tile_start.as<uint32_t>(), num_tiles,
                              b.total, chunk, *ib, s));
@@ -1407,13 +1413,13 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
       po.cell, po.meta, po.vw, view, geom, grid_size, d_grid, grid_stride,
       plan->partials.as<Real>(), ib.split_tiles, ib.num_split, b.num_tiles,
       num_ctas, b.stage, s, wait_before.data(), record_after.data(),
-      (Real*)plan->host_grid, tile_groups, span));
+      (Real*)plan->host_grid, tile_groups, span, plan->tile_slot.as<int2>()));
   plan->split_launched = upper_done >= 0;
   plan->mark(4, s);
   plan->mark(5, s);
-  // the gridding launches, and per virtual group (plane group and tile
-  // phase) its partial reduction
-  plan->stats.num_launches += b.num_groups / span + b.num_groups;
+  // each gridding launch and its partial reduction (one per virtual group,
+  // or one over all the phases of a launch)
+  plan->stats.num_launches += 2 * (b.num_groups / span);
   plan->events_valid = plan->profile;
   return GG_OK;
 }
@@ -1721,7 +1727,8 @@ int replay_pipeline(gg_plan* plan, const gg_kernels* K, const Real* vis,
       plan->meta.as<uint32_t>(), plan->vw.p, view, kp.geom, kp.grid_size,
       d_grids, grid_stride, plan->partials.as<Real>(),
       plan->split_tiles.as<int4>(), sc + kNumSplit, kp.num_tiles, kp.num_ctas,
-      kp.stage, s, nullptr, nullptr, nullptr, nullptr, kp.group_span));
+      kp.stage, s, nullptr, nullptr, nullptr, nullptr, kp.group_span,
+      plan->tile_slot.as<int2>()));
   return GG_OK;
 }
 
@@ -1951,6 +1958,12 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
            const Real* uu, const Real* vv, const Real* ww, const Real* vis,
            const Real* weight, Real cell_size_rad, Real w_scale,
            int grid_size, size_t* num_skipped, double* norm, Real* grid) {
+  const auto t_entry = std::chrono::steady_clock::now();
+  auto since_entry = [&]() {
+    return std::chrono::duration<double, std::milli>(
+               std::chrono::steady_clock::now() - t_entry)
+        .count();
+  };
   if (!num_skipped || !norm || !grid)
     return set_error(GG_ERR_INVALID_ARG, "num_skipped, norm or grid is NULL");
   if (grid_size < 1 || grid_size > kMaxGridSize)
@@ -1996,6 +2009,7 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   // copy mode the grid goes up on the side stream behind the visibilities,
   // and only the gridding passes wait for it.
   st->profile_valid = false;
+  st->host_ms[0] = since_entry();
   if (st->profile) GG_CUDA(cudaEventRecord(st->call_start, s));
   cudaStream_t cs = st->copy_stream;
   // In place: the gridding kernels read and write the caller's grid over
@@ -2182,6 +2196,7 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
   GG_CUDA(cudaStreamSynchronize(s));
   GG_CUDA(cudaStreamSynchronize(cs));
   GG_CUDA(cudaStreamSynchronize(st->stack_stream));
+  st->host_ms[1] = since_entry();
   GG_TRY(check_device_error(plan, s));
   st->profile_valid = st->profile && plan->events_valid;
   *norm = norm_out;
@@ -2204,6 +2219,7 @@ int dropin(size_t num_w_planes, const int* support, int oversample,
                                : 0) +
                           (direct && plan->direct_launched ? 8 : 0)
                     : 0);
+  st->host_ms[2] = since_entry();
   return GG_OK;
 }
 
@@ -2812,6 +2828,7 @@ GG_API int gg_host_phase_ms(float* ms, int n) {
                           p->ev[3], p->ev[4], st->call_end};
   for (int i = 0; i < n && i < 6; ++i)
     GG_CUDA(cudaEventElapsedTime(&ms[i], marks[i], marks[i + 1]));
+  for (int i = 6; i < n && i < 9; ++i) ms[i] = (float)st->host_ms[i - 6];
   return GG_OK;
 }
 

@@ -725,6 +725,77 @@ __global__ void k_reduce_partials(const int4* __restrict__ split_tiles,
   }
 }
 
+// The partial tiles of one plane group's tile phases (virtual groups
+// group0 .. group0 + P - 1, one launch of the gridding kernel), added to
+// the grids in one pass: block b takes the cells of phase-0 tile position
+// b and adds to each cell, phase by phase, the partial tiles of the tile of
+// that phase that covers it (their chunks summed in FP64, rounded once per
+// phase) -- the additions, in the same order, that one reduction launch per
+// phase makes (k_reduce_partials).  tile_slot[virtual tile] = (first
+// partial slot, chunks), chunks 0 when the tile has no partial tiles.
+template <typename Real, int TW>
+__global__ void k_reduce_phases(const int2* __restrict__ tile_slot,
+                                const typename Vec2<Real>::type* __restrict__ partials,
+                                TileGeom g, int group0, int G, Real* grid,
+                                long long grid_stride) {
+  using R2 = typename Vec2<Real>::type;
+  using WS = WarpShape<TW>;
+  constexpr int kTV = WS::kTileV;
+  const int P = g.tile_phases;
+  const int sw = 1 << g.strip_shift;
+  const int real_u = g.tiles_u - 1;   // phase-0 tile columns
+  const int tiles_per_grid = g.tiles_u * g.tiles_v;
+  const int n = g.num_grids * real_u * g.tiles_v;
+  for (int b = blockIdx.x; b < n; b += gridDim.x) {
+    const int gi = b / (real_u * g.tiles_v);
+    const int rem = b - gi * real_u * g.tiles_v;
+    const int tv = rem / real_u, tu = rem - (rem / real_u) * real_u;
+    // Tiles of phase p over these columns: tile columns tu and tu + 1.
+    bool any = false;
+    for (int p = 0; p < P && !any; ++p)
+      for (int d = 0; d < (p ? 2 : 1); ++d) {
+        const size_t vt = (size_t)(group0 + p) * g.tiles_total +
+                          (size_t)gi * tiles_per_grid +
+                          (size_t)tv * g.tiles_u + tu + d;
+        any |= tile_slot[vt].y > 0;
+      }
+    if (!any) continue;
+    R2* gg = (R2*)(grid + (long long)gi * grid_stride);
+    for (int e = threadIdx.x; e < TW * kTV; e += blockDim.x) {
+      const int C = e % TW, R = e / TW;
+      const int col = tu * TW + C, row = tv * kTV + R;
+      if (row >= G || col >= G) continue;
+      // The cell's entry in a partial tile whose column is Cp (the
+      // kernel's thread-major layout: row R is warp R / kBand, lane row
+      // (R % kBand) / kRows, register row R % kRows).
+      const int w = R / WS::kBand, ly = (R % WS::kBand) / kRows;
+      const int rr = R % kRows;
+      R2 acc = gg[(size_t)row * G + col];
+      bool changed = false;
+      for (int p = 0; p < P; ++p) {
+        const int c = col + p * sw;       // column in phase p's tile grid
+        const int tc = c / TW, Cp = c - tc * TW;
+        const size_t vt = (size_t)(group0 + p) * g.tiles_total +
+                          (size_t)gi * tiles_per_grid +
+                          (size_t)tv * g.tiles_u + tc;
+        const int2 sl = tile_slot[vt];
+        if (sl.y == 0) continue;
+        const int ent = rr * kConsumers + w * 32 + ly * TW + Cp;
+        double sx = acc.x, sy = acc.y;
+        for (int k = 0; k < sl.y; ++k) {
+          const R2 q = partials[(size_t)(sl.x + k) * kCells + ent];
+          sx += q.x;
+          sy += q.y;
+        }
+        acc.x = (Real)sx;
+        acc.y = (Real)sy;
+        changed = true;
+      }
+      if (changed) gg[(size_t)row * G + col] = acc;
+    }
+  }
+}
+
 __global__ void k_tile_bounds(const uint32_t* __restrict__ keys, uint32_t n,
                               int shift, int num_tiles,
                               uint32_t* __restrict__ tile_start) {
@@ -854,7 +925,8 @@ __global__ void k_item_emit(const uint32_t* __restrict__ tile_start,
                             int4* __restrict__ split_tiles,
                             uint32_t* __restrict__ num_split,
                             uint32_t* __restrict__ num_items,
-                            uint32_t* __restrict__ group_items) {
+                            uint32_t* __restrict__ group_items,
+                            int2* __restrict__ tile_slot) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int T = num_tiles / num_groups;
   auto scanA = [&](int r) { return r < num_tiles ? sA[r] : *totA; };
@@ -866,9 +938,13 @@ __global__ void k_item_emit(const uint32_t* __restrict__ tile_start,
   const int t = tile_at_rank(i, T, order);
   const uint32_t s0 = tile_start[t], s1 = tile_start[t + 1];
   const uint32_t c = s1 - s0;
-  if (c == 0) return;
   const uint32_t chunks = (c + chunk - 1) / chunk;
-  if (chunks == 1 && g % partial_phases == 0) {
+  const bool owns = chunks == 1 && g % partial_phases == 0;
+  if (tile_slot)
+    tile_slot[t] = c == 0 || owns ? make_int2(0, 0)
+                                  : make_int2((int)sA[i], (int)chunks);
+  if (c == 0) return;
+  if (owns) {
     WorkItem w;
     w.tile = t; w.rec_begin = (int)s0; w.rec_end = (int)s1; w.slot = -1;
     items[scanA((g + 1) * T) + sB[i]] = w;
@@ -991,7 +1067,8 @@ cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
                                      b.num_slots,
                                      b.counter,
                                      b.items, b.split_tiles, b.num_split,
-                                     b.num_items, b.group_items);
+                                     b.num_items, b.group_items,
+                                     b.tile_slot);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   // The persistent kernel's work counter starts at zero.
@@ -1010,6 +1087,31 @@ int grid_tiles_ctas_per_sm(int tile_u, bool stage, int lane_groups) {
                                                     smem) != cudaSuccess)
     n = 1;
   return n < 1 ? 1 : n;
+}
+
+template <typename Real>
+cudaError_t launch_reduce_phases(const int2* tile_slot, const Real* partials,
+                                 TileGeom geom, int group0, int grid_size,
+                                 Real* grid, long long grid_stride,
+                                 cudaStream_t s) {
+  const long long n =
+      (long long)geom.num_grids * (geom.tiles_u - 1) * geom.tiles_v;
+  if (n <= 0) return cudaSuccess;
+  const int blocks = (int)std::min<long long>(n, 65535);
+  using P2 = const typename Vec2<Real>::type*;
+  switch (geom.tile_u) {
+    case 32: k_reduce_phases<Real, 32><<<blocks, 256, 0, s>>>(
+        tile_slot, (P2)partials, geom, group0, grid_size, grid, grid_stride);
+      break;
+    case 16: k_reduce_phases<Real, 16><<<blocks, 256, 0, s>>>(
+        tile_slot, (P2)partials, geom, group0, grid_size, grid, grid_stride);
+      break;
+    case 8: k_reduce_phases<Real, 8><<<blocks, 256, 0, s>>>(
+        tile_slot, (P2)partials, geom, group0, grid_size, grid, grid_stride);
+      break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 template <typename Real>
@@ -1051,7 +1153,7 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                               const cudaEvent_t* wait_before,
                               const cudaEvent_t* record_after,
                               Real* host_grid, const uint32_t* tile_groups,
-                              int group_span) {
+                              int group_span, const int2* tile_slot) {
   GridArgs<Real> a;
   a.items = items;
   a.group_items = group_items;
@@ -1090,11 +1192,17 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
     if (e != cudaSuccess) return e;
     e = cudaLaunchKernel(fn, dim3(num_ctas), dim3(kThreads), args, smem, s);
     if (e != cudaSuccess) return e;
-    for (int p = 0; p < span; ++p) {
-      e = launch_reduce_group<Real>(split_tiles, num_split, max_split,
-                                    partials, geom, g + p, grid_size, grid,
-                                    grid_stride, a.host, tile_groups, s);
+    if (span > 1 && tile_slot) {
+      e = launch_reduce_phases<Real>(tile_slot, partials, geom, g, grid_size,
+                                     grid, grid_stride, s);
       if (e != cudaSuccess) return e;
+    } else {
+      for (int p = 0; p < span; ++p) {
+        e = launch_reduce_group<Real>(split_tiles, num_split, max_split,
+                                      partials, geom, g + p, grid_size, grid,
+                                      grid_stride, a.host, tile_groups, s);
+        if (e != cudaSuccess) return e;
+      }
     }
     if (record_after && record_after[g + span - 1]) {
       e = cudaEventRecord(record_after[g + span - 1], s);
@@ -1111,12 +1219,12 @@ template cudaError_t launch_grid_tiles<float>(
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
     float*, long long, float*, const int4*, const uint32_t*, int, int, bool,
     cudaStream_t, const cudaEvent_t*, const cudaEvent_t*, float*,
-    const uint32_t*, int);
+    const uint32_t*, int, const int2*);
 template cudaError_t launch_grid_tiles<double>(
     const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
     double*, long long, double*, const int4*, const uint32_t*, int, int, bool,
     cudaStream_t, const cudaEvent_t*, const cudaEvent_t*, double*,
-    const uint32_t*, int);
+    const uint32_t*, int, const int2*);
 
 }  // namespace gg

@@ -241,6 +241,9 @@ struct ItemBuffers {
   // phases after the first) write partial tiles even when they have one
   // chunk, so that all the phases of a plane group share one launch.
   int partial_phases = 1;
+  // [num_tiles] (first partial slot, chunks) of each virtual tile, chunks 0
+  // when it writes none (filled when not null).
+  int2* tile_slot = nullptr;
 };
 cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
                                uint32_t num_records, uint32_t chunk,
@@ -252,8 +255,10 @@ cudaError_t launch_build_items(const uint32_t* tile_start, int num_tiles,
 // single-chunk tiles are added to the grid by the launch, every other item
 // writes a partial tile); with group_span = 1 one launch per virtual group.
 // Each launch is followed by the reduction of its virtual groups' partial
-// tiles in group order (grid += their partials in chunk order, FP64): the
-// grid takes the groups' and phases' contributions in order.
+// tiles in group order (grid += their partials in chunk order, FP64; all
+// the phases of a launch in one pass over the grid when tile_slot, the
+// item builder's map, is given): the grid takes the groups' and phases'
+// contributions in order.
 // wait_before[v] / record_after[v] (arrays of num_groups events, entries
 // may be null): s waits for the first before the launch that starts with
 // virtual group v and records the second after the launch (and its
@@ -273,7 +278,8 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                               const cudaEvent_t* record_after = nullptr,
                               Real* host_grid = nullptr,
                               const uint32_t* tile_groups = nullptr,
-                              int group_span = 1);
+                              int group_span = 1,
+                              const int2* tile_slot = nullptr);
 // Direct mode of a single-grid call: per strip (num_strips), the first and
 // last virtual group (plane group and tile phase) with records there
 // (first | last << 16, 0xFFFF when none), and *cells += the grid cells of

@@ -278,7 +278,7 @@ GG_API int gg_host_set_grid_access(int mode);
 GG_API int gg_host_get_grid_access(int* mode);
 
 /* Phase timing of the host-pointer gridding calls on the current device.
- * With profiling enabled, gg_host_phase_ms fills ms[0..n-1] (n <= 6) for
+ * With profiling enabled, gg_host_phase_ms fills ms[0..n-1] (n <= 9) for
  * the last such call that gridded at least one visibility:
  *   0 staging: the call's start to placement (kernel stack re-layout, the
  *     inputs' upload)
@@ -286,6 +286,11 @@ GG_API int gg_host_get_grid_access(int* mode);
  *     decomposition, tile-gridding passes)
  *   5 the rest: the end of the passes to the end of the call (grid copy
  *     back, scalars).
+ * and, measured on the host clock:
+ *   6 the call's entry to its first queued device work (checks, host-array
+ *     classification, buffers)
+ *   7 the call's entry to the return of its final synchronisation
+ *   8 the whole call, entry to return.
  * Off by default (no events recorded). */
 GG_API int gg_host_set_profiling(int enable);
 GG_API int gg_host_phase_ms(float* ms, int n);

@@ -645,9 +645,10 @@ def test_dropin_fresh_pageable_grid_is_copied(pkg, synthetic):
 
 
 def test_host_phase_times(pkg, synthetic):
-    """With profiling on, a host call's phase times are there and add up
-    to about its duration; off, none are recorded; a call without
-    visibilities leaves nothing to report."""
+    """With profiling on, a host call's phase times are there, its device
+    phases add up to about its duration and its host-clock marks are in
+    order; off, none are recorded; a call without visibilities leaves
+    nothing to report."""
     import time
     wl = synthetic.random_uniform_workload("phases", 50_000, 1024, 16, 2, 8,
                                            seed=47, cell_size_rad=6e-5)
@@ -661,7 +662,11 @@ def test_host_phase_times(pkg, synthetic):
         assert set(ph) == set(pkg.HOST_PHASES)
         assert all(v >= 0.0 for v in ph.values())
         assert ph["grid_tiles"] > 0.0
-        assert 0.0 < sum(ph.values()) <= wall * 1.05 + 0.1
+        device = sum(v for k, v in ph.items() if not k.startswith("host_"))
+        assert 0.0 < device <= wall * 1.05 + 0.1
+        assert (ph["host_first_work"] <= ph["host_synchronised"]
+                <= ph["host_return"] <= wall)
+        assert device <= ph["host_synchronised"] * 1.05 + 0.1
         empty = dataclasses.replace(wl, uu=wl.uu[:0], vv=wl.vv[:0],
                                     ww=wl.ww[:0], vis=wl.vis[:0],
                                     weight=wl.weight[:0])
