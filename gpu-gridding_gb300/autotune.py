@@ -139,13 +139,18 @@ class TuningCache:
 
 def search(measure: Callable[[dict], float],
            space: Iterable = SEARCH_SPACE,
-           start: Optional[dict] = None) -> tuple:
+           start: Optional[dict] = None, sweeps: int = 3) -> tuple:
     """Coordinate search: for each group of settings in turn, try its
-    values with the others at their best so far and keep the fastest.
-    ``measure(tuning) -> ms`` (inf for a failed configuration).  Returns
-    (best tuning, its ms, {repr(tuning): ms} of every trial)."""
+    values with the others at their best so far and keep the fastest;
+    sweep the groups again while a sweep changes the best (at most
+    ``sweeps`` times: the settings interact, e.g. the tile width that is
+    fastest with several plane groups need not be with one).  Each tuning
+    is measured once.  ``measure(tuning) -> ms`` (inf for a failed
+    configuration).  Returns (best tuning, its ms, {repr(tuning): ms} of
+    every trial)."""
     best = dict(start or DEFAULT_TUNING)
     trials: Dict[str, float] = {}
+    space = list(space)
 
     def timed(t):
         k = json.dumps(t, sort_keys=True)
@@ -154,13 +159,17 @@ def search(measure: Callable[[dict], float],
         return trials[k]
 
     best_ms = timed(best)
-    for names, values in space:
-        for vals in values:
-            t = dict(best)
-            t.update(zip(names, vals))
-            ms = timed(t)
-            if ms < best_ms:
-                best, best_ms = t, ms
+    for _ in range(max(1, sweeps)):
+        before = dict(best)
+        for names, values in space:
+            for vals in values:
+                t = dict(best)
+                t.update(zip(names, vals))
+                ms = timed(t)
+                if ms < best_ms:
+                    best, best_ms = t, ms
+        if best == before:
+            break
     return best, best_ms, trials
 
 

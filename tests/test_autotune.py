@@ -90,6 +90,25 @@ def test_search_finds_separable_optimum(at):
     assert len(keys) == len(set(keys)) == len(trials)
 
 
+def test_search_sweeps_again_when_settings_interact(at):
+    """The tile width that is fastest with the default plane groups loses
+    with one plane group: the first sweep settles on it, the second sweep
+    (from the one-group setting) finds the joint optimum."""
+    def cost(t):
+        one_group = t["plane_group_mb"] == 1 << 20
+        best_u = 32 if one_group else 16
+        c = 10.0 if one_group else 12.0
+        return c + (0 if t["tile_u"] == best_u else 1.0)
+
+    space = ((("tile_u", "slice_staging"), [(0, -1), (32, 0), (16, 0)]),
+             (("plane_group_mb",), [(0,), (1 << 20,)]))
+    one, _, _ = at.search(cost, space, sweeps=1)
+    assert (one["tile_u"], one["plane_group_mb"]) == (16, 1 << 20)
+    best, ms, _ = at.search(cost, space)
+    assert (best["tile_u"], best["plane_group_mb"]) == (32, 1 << 20)
+    assert ms == 10.0
+
+
 def test_search_skips_failed_configurations(at):
     def cost(t):
         return math.inf if t["tile_u"] == 8 else 5.0 - 0.1 * (t["tile_u"] == 32)
