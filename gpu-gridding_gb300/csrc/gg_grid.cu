@@ -731,67 +731,85 @@ __global__ void k_reduce_partials(const int4* __restrict__ split_tiles,
 // b and adds to each cell, phase by phase, the partial tiles of the tile of
 // that phase that covers it (their chunks summed in FP64, rounded once per
 // phase) -- the additions, in the same order, that one reduction launch per
-// phase makes (k_reduce_partials).  tile_slot[virtual tile] = (first
-// partial slot, chunks), chunks 0 when the tile has no partial tiles.
+// phase makes (k_reduce_partials).  A single chunk is added in the grid's
+// precision: the FP64 sum of two FP32 values rounded to FP32 is their
+// correctly rounded FP32 sum.  tile_slot[virtual tile] = (first partial
+// slot, chunks), chunks 0 when the tile has no partial tiles.  Each thread
+// keeps one column (blockDim.x a multiple of TW) and looks its phases'
+// tiles up once.
 template <typename Real, int TW>
-__global__ void k_reduce_phases(const int2* __restrict__ tile_slot,
-                                const typename Vec2<Real>::type* __restrict__ partials,
-                                TileGeom g, int group0, int G, Real* grid,
-                                long long grid_stride) {
+__global__ void __launch_bounds__(256)
+k_reduce_phases(const int2* __restrict__ tile_slot,
+                const typename Vec2<Real>::type* __restrict__ partials,
+                TileGeom g, int group0, int G, Real* grid,
+                long long grid_stride) {
   using R2 = typename Vec2<Real>::type;
   using WS = WarpShape<TW>;
   constexpr int kTV = WS::kTileV;
+  constexpr int kMaxPhases = 4;
+  constexpr int kRowStep = 256 / TW;    // rows between a thread's cells
   const int P = g.tile_phases;
   const int sw = 1 << g.strip_shift;
   const int real_u = g.tiles_u - 1;   // phase-0 tile columns
   const int tiles_per_grid = g.tiles_u * g.tiles_v;
   const int n = g.num_grids * real_u * g.tiles_v;
+  const int C = threadIdx.x % TW, R0 = threadIdx.x / TW;
   for (int b = blockIdx.x; b < n; b += gridDim.x) {
     const int gi = b / (real_u * g.tiles_v);
     const int rem = b - gi * real_u * g.tiles_v;
     const int tv = rem / real_u, tu = rem - (rem / real_u) * real_u;
-    // Tiles of phase p over these columns: tile columns tu and tu + 1.
-    bool any = false;
-    for (int p = 0; p < P && !any; ++p)
-      for (int d = 0; d < (p ? 2 : 1); ++d) {
-        const size_t vt = (size_t)(group0 + p) * g.tiles_total +
+    const int col = tu * TW + C;
+    // This column's tile in each phase: its slots and its column there.
+    int2 sl[kMaxPhases];
+    int cp[kMaxPhases];
+    bool mine = false;
+#pragma unroll
+    for (int p = 0; p < kMaxPhases; ++p) {
+      sl[p] = make_int2(0, 0);
+      cp[p] = 0;
+      if (p < P) {
+        const int c = col + p * sw;
+        const int tc = c / TW;
+        cp[p] = c - tc * TW;
+        sl[p] = tile_slot[(size_t)(group0 + p) * g.tiles_total +
                           (size_t)gi * tiles_per_grid +
-                          (size_t)tv * g.tiles_u + tu + d;
-        any |= tile_slot[vt].y > 0;
+                          (size_t)tv * g.tiles_u + tc];
+        mine |= sl[p].y > 0;
       }
-    if (!any) continue;
+    }
+    if (!__syncthreads_or(mine)) continue;
+    if (!mine || col >= G) continue;
     R2* gg = (R2*)(grid + (long long)gi * grid_stride);
-    for (int e = threadIdx.x; e < TW * kTV; e += blockDim.x) {
-      const int C = e % TW, R = e / TW;
-      const int col = tu * TW + C, row = tv * kTV + R;
-      if (row >= G || col >= G) continue;
+#pragma unroll 4
+    for (int R = R0; R < kTV; R += kRowStep) {
+      const int row = tv * kTV + R;
+      if (row >= G) break;
       // The cell's entry in a partial tile whose column is Cp (the
       // kernel's thread-major layout: row R is warp R / kBand, lane row
       // (R % kBand) / kRows, register row R % kRows).
       const int w = R / WS::kBand, ly = (R % WS::kBand) / kRows;
-      const int rr = R % kRows;
+      const int ent0 = (R % kRows) * kConsumers + w * 32 + ly * TW;
       R2 acc = gg[(size_t)row * G + col];
-      bool changed = false;
-      for (int p = 0; p < P; ++p) {
-        const int c = col + p * sw;       // column in phase p's tile grid
-        const int tc = c / TW, Cp = c - tc * TW;
-        const size_t vt = (size_t)(group0 + p) * g.tiles_total +
-                          (size_t)gi * tiles_per_grid +
-                          (size_t)tv * g.tiles_u + tc;
-        const int2 sl = tile_slot[vt];
-        if (sl.y == 0) continue;
-        const int ent = rr * kConsumers + w * 32 + ly * TW + Cp;
-        double sx = acc.x, sy = acc.y;
-        for (int k = 0; k < sl.y; ++k) {
-          const R2 q = partials[(size_t)(sl.x + k) * kCells + ent];
-          sx += q.x;
-          sy += q.y;
+#pragma unroll
+      for (int p = 0; p < kMaxPhases; ++p) {
+        if (sl[p].y == 0) continue;
+        const R2* q = partials + (size_t)sl[p].x * kCells + ent0 + cp[p];
+        if (sl[p].y == 1) {
+          const R2 v = *q;
+          acc.x += v.x;
+          acc.y += v.y;
+        } else {
+          double sx = acc.x, sy = acc.y;
+          for (int k = 0; k < sl[p].y; ++k) {
+            const R2 v = q[(size_t)k * kCells];
+            sx += v.x;
+            sy += v.y;
+          }
+          acc.x = (Real)sx;
+          acc.y = (Real)sy;
         }
-        acc.x = (Real)sx;
-        acc.y = (Real)sy;
-        changed = true;
       }
-      if (changed) gg[(size_t)row * G + col] = acc;
+      gg[(size_t)row * G + col] = acc;
     }
   }
 }
