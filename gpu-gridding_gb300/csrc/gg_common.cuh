@@ -205,14 +205,17 @@ __host__ __device__ inline int phase_shift(const TileGeom& g, int group) {
   return (group & (g.tile_phases - 1)) << g.strip_shift;
 }
 
-// Phase of a footprint spanning cells [c0, c1] (c0 >= 0): the one whose
-// tile columns cut it into the fewest pieces, the lowest on ties.
-__host__ __device__ inline int footprint_phase(int c0, int c1, int tile_u,
-                                               int phases) {
-  int best = 0, fewest = c1 / tile_u - c0 / tile_u;
+// Phase of a footprint spanning cells [c0, c1] (c0 >= 0) on tiles of
+// 1 << tile_shift columns: the one whose tile columns cut it into the
+// fewest pieces, the lowest on ties.  Phase p's columns start p strips
+// (1 << strip_shift columns) left of phase 0's.
+__host__ __device__ inline int footprint_phase(int c0, int c1,
+                                               int tile_shift,
+                                               int strip_shift, int phases) {
+  int best = 0, fewest = (c1 >> tile_shift) - (c0 >> tile_shift);
   for (int p = 1; p < phases; ++p) {
-    const int sh = p * (tile_u / phases);
-    const int n = (c1 + sh) / tile_u - (c0 + sh) / tile_u;
+    const int sh = p << strip_shift;
+    const int n = ((c1 + sh) >> tile_shift) - ((c0 + sh) >> tile_shift);
     if (n < fewest) {
       fewest = n;
       best = p;

@@ -169,15 +169,19 @@ __global__ void k_count(const uint32_t* __restrict__ cell,
   if (!meta_skipped(m)) {
     const uint32_t word = *d_shape;
     const int shape = (int)(word & 0xFFu), phases = phases_of_shape(word);
-    const int tw = tile_u_of_shape(shape), th = tile_v_of_shape(shape);
+    // Tiles are 32 >> shape by 64 << shape cells, phase strips
+    // (32 >> shape) / phases columns: divisions become shifts.
+    const int tws = 5 - shape, ths = 6 + shape;
+    const int sws = tws - (phases >= 4 ? 2 : phases >= 2 ? 1 : 0);
     const uint32_t ce = cell[i];
     const int gu = cell_u(ce), gv = cell_v(ce);
     const int s = v.support[meta_plane(m)];
-    const int sh = phases > 1 ? footprint_phase(gu - s, gu + s, tw, phases) *
-                                    (tw / phases)
-                              : 0;
-    c = (uint32_t)(((gu + s + sh) / tw - (gu - s + sh) / tw + 1) *
-                   ((gv + s) / th - (gv - s) / th + 1));
+    const int sh = phases > 1
+                       ? footprint_phase(gu - s, gu + s, tws, sws, phases)
+                             << sws
+                       : 0;
+    c = (uint32_t)((((gu + s + sh) >> tws) - ((gu - s + sh) >> tws) + 1) *
+                   (((gv + s) >> ths) - ((gv - s) >> ths) + 1));
   }
   count[i] = c;
 }
@@ -214,13 +218,15 @@ __global__ void k_emit(const uint32_t* __restrict__ cell,
   const int gu = cell_u(c), gv = cell_v(c);
   const int plane = meta_plane(m);
   const int s = v.support[plane];
-  const int phase = g.tile_phases > 1 ? footprint_phase(gu - s, gu + s,
-                                                        g.tile_u,
-                                                        g.tile_phases)
-                                      : 0;
-  const int sh = phase * (g.tile_u / (g.tile_phases > 1 ? g.tile_phases : 1));
-  const int tu0 = (gu - s + sh) / g.tile_u, tu1 = (gu + s + sh) / g.tile_u;
-  const int tv0 = (gv - s) / g.tile_v, tv1 = (gv + s) / g.tile_v;
+  // Tile sides and strips are powers of two: shifts, not divisions.
+  const int tws = __ffs(g.tile_u) - 1, ths = __ffs(g.tile_v) - 1;
+  const int phase = g.tile_phases > 1
+                        ? footprint_phase(gu - s, gu + s, tws, g.strip_shift,
+                                          g.tile_phases)
+                        : 0;
+  const int sh = phase << g.strip_shift;
+  const int tu0 = (gu - s + sh) >> tws, tu1 = (gu + s + sh) >> tws;
+  const int tv0 = (gv - s) >> ths, tv1 = (gv + s) >> ths;
   const int au = abs(meta_ou(m)), av = abs(meta_ov(m));
   uint32_t low = 0;
   if (g.phase_bits > 0) low = (uint32_t)(au * (v.omax + 1) + av);

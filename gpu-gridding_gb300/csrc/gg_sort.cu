@@ -162,77 +162,99 @@ k_radix_hist(const uint32_t* __restrict__ keys, size_t n, int shift,
 // in shared memory (in block order within a digit), then written out in
 // that order, so keys with the same digit go to consecutive addresses and a
 // warp's stores form a few contiguous runs instead of 32 scattered words.
-// hist holds the block's digit counts (digit-major, as k_radix_hist wrote
-// them) and offsets their exclusive scan (global start of each (digit,
-// block) run).
-__global__ void __launch_bounds__(kRadixThreads)
+// Warp w ranks its own 512 consecutive keys (lane l's j-th key is key
+// w * 512 + j * 32 + l of the block) against warp-private digit counters,
+// so the ranking needs no block barrier; one per-digit prefix over the
+// warps then places every key.  hist holds the block's digit counts
+// (digit-major, as k_radix_hist wrote them) and offsets their exclusive
+// scan (global start of each (digit, block) run).
+__global__ void __launch_bounds__(kRadixThreads, 3)
 k_radix_scatter(const uint32_t* __restrict__ keys,
                 const uint32_t* __restrict__ vals, size_t n, int shift,
                 int num_blocks, const uint32_t* __restrict__ hist,
                 const uint32_t* __restrict__ offsets,
                 uint32_t* __restrict__ keys_out,
                 uint32_t* __restrict__ vals_out) {
+  constexpr int kPerWarp = kRadixTile / kRadixWarps;   // 512
   __shared__ uint32_t s_keys[kRadixTile];
   __shared__ uint32_t s_vals[kRadixTile];
   __shared__ uint32_t digit_base[kRadixDigits];   // global run start
   __shared__ uint32_t local_start[kRadixDigits];  // block-local run start
-  __shared__ uint32_t placed[kRadixDigits];       // keys placed so far
+  // Per warp and digit: the warp's count, then the keys of the digit in
+  // the warps before it.
   __shared__ uint32_t warp_count[kRadixWarps][kRadixDigits];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const size_t cell = (size_t)threadIdx.x * num_blocks + blockIdx.x;
   digit_base[threadIdx.x] = offsets[cell];
+#pragma unroll
+  for (int w = 0; w < kRadixWarps; ++w) warp_count[w][threadIdx.x] = 0;
   uint32_t total;
+  // (block_exclusive_scan ends with a barrier: the counters are zeroed.)
   local_start[threadIdx.x] = block_exclusive_scan(hist[cell], &total);
-  placed[threadIdx.x] = 0;
   const uint32_t lt_mask = (1u << lane) - 1u;
   const size_t base = (size_t)blockIdx.x * kRadixTile;
   const int valid_n = (int)min((size_t)kRadixTile, n - base);
-  // The block's keys and values, all loads in flight together.
+  const int wbase = warp * kPerWarp;
+  // The warp's keys and values, all loads in flight together.
   uint32_t kr[kRadixRounds], vr[kRadixRounds];
 #pragma unroll
-  for (int r = 0; r < kRadixRounds; ++r) {
-    const int t = r * kRadixThreads + threadIdx.x;
-    kr[r] = t < valid_n ? keys[base + t] : 0u;
-    vr[r] = t < valid_n ? vals[base + t] : 0u;
+  for (int j = 0; j < kRadixRounds; ++j) {
+    const int t = wbase + j * 32 + lane;
+    kr[j] = t < valid_n ? keys[base + t] : 0u;
+    vr[j] = t < valid_n ? vals[base + t] : 0u;
   }
-  // Phase 1: stable placement in shared memory, 256 keys per round.
+  // Ranks within the warp, in key order: the digit's keys in the warp's
+  // earlier rounds plus the lower lanes of this round with the same digit.
+  uint32_t* cnt = warp_count[warp];
 #pragma unroll
-  for (int r = 0; r < kRadixRounds; ++r) {
-    if (r * kRadixThreads >= valid_n) break;   // block-uniform
-#pragma unroll
-    for (int w = 0; w < kRadixWarps; ++w) warp_count[w][threadIdx.x] = 0;
-    __syncthreads();
-    const int t = r * kRadixThreads + threadIdx.x;
-    const bool valid = t < valid_n;
-    const uint32_t key = kr[r];
-    const uint32_t val = vr[r];
+  for (int j = 0; j < kRadixRounds; ++j) {
+    const bool valid = wbase + j * 32 + lane < valid_n;
     // Invalid lanes take digit 256 so they never match a valid one.
-    const uint32_t digit = valid ? ((key >> shift) & 0xFF) : 256u;
+    const uint32_t digit = valid ? ((kr[j] >> shift) & 0xFF) : 256u;
     const uint32_t peers = __match_any_sync(0xffffffffu, digit);
-    const uint32_t rank = __popc(peers & lt_mask);
+    // The counter is read at digit & 0xFF: the load may be issued for
+    // invalid lanes too, and digit 256 would lie past the warp's row (past
+    // the whole array for the last warp).
+    const uint32_t c_before = cnt[digit & 0xFFu];
+    const uint32_t before = valid ? c_before : 0u;
+    // The rank waits in s_keys at the key's own index (free until the
+    // placement below, which reads it back first).
+    s_keys[wbase + j * 32 + lane] = before + __popc(peers & lt_mask);
+    __syncwarp();
     if (valid && lane == __ffs(peers) - 1)
-      warp_count[warp][digit] = __popc(peers);
-    __syncthreads();
-    // Per-digit prefix across warps (thread t owns digit t).
-    {
-      uint32_t running = placed[threadIdx.x];
-#pragma unroll
-      for (int w = 0; w < kRadixWarps; ++w) {
-        const uint32_t c = warp_count[w][threadIdx.x];
-        warp_count[w][threadIdx.x] = running;
-        running += c;
-      }
-      placed[threadIdx.x] = running;
-    }
-    __syncthreads();
-    if (valid) {
-      const uint32_t pos = local_start[digit] + warp_count[warp][digit] + rank;
-      s_keys[pos] = key;
-      s_vals[pos] = val;
-    }
-    __syncthreads();
+      cnt[digit & 0xFFu] = before + __popc(peers);
+    __syncwarp();
   }
-  // Phase 2: write the block out in digit order.
+  __syncthreads();
+  // Per digit (thread t owns digit t): the keys in the warps before each.
+  {
+    uint32_t running = 0;
+#pragma unroll
+    for (int w = 0; w < kRadixWarps; ++w) {
+      const uint32_t c = warp_count[w][threadIdx.x];
+      warp_count[w][threadIdx.x] = running;
+      running += c;
+    }
+  }
+  __syncthreads();   // every digit's prefix written before any is read
+  uint32_t pos[kRadixRounds];
+#pragma unroll
+  for (int j = 0; j < kRadixRounds; ++j) {
+    const uint32_t d = (kr[j] >> shift) & 0xFF;
+    pos[j] = local_start[d] + warp_count[warp][d] + s_keys[wbase + j * 32 + lane];
+  }
+  __syncthreads();   // every rank read before any key lands in s_keys
+#pragma unroll
+  for (int j = 0; j < kRadixRounds; ++j) {
+    // pos < valid_n for every valid key (the ranks of a digit fill its
+    // block-local run); the bound also keeps a stray rank in the array.
+    if (wbase + j * 32 + lane < valid_n && pos[j] < (uint32_t)kRadixTile) {
+      s_keys[pos[j]] = kr[j];
+      s_vals[pos[j]] = vr[j];
+    }
+  }
+  __syncthreads();
+  // Write the block out in digit order.
   for (int i = threadIdx.x; i < valid_n; i += kRadixThreads) {
     const uint32_t key = s_keys[i];
     const uint32_t d = (key >> shift) & 0xFF;
