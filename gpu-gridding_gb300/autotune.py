@@ -13,7 +13,7 @@ no placement, norm or skip count (gg_tuning in the C header):
 * ``tile_order``    -- tiles taken by distance from the centre or row by row,
 * ``lane_groups``   -- on 32-wide tiles, each consumer warp takes records
   whole (1) or as two half-warp streams (2).
-* ``tile_phases``   -- 1, 2 or 4 tile grids offset by a fraction of a tile
+* ``tile_phases``   -- 1, 2, 4 or 8 tile grids offset by a fraction of a tile
   width; each visibility is gridded on the one that cuts its footprint
   into the fewest tile columns (the later grids' tiles as partial tiles
   added after the pass).
@@ -58,7 +58,7 @@ SEARCH_SPACE = (
                            (1 << 20,)]),
     (("tile_order",), [(0,), (1,)]),
     (("lane_groups",), [(0,), (2,)]),
-    (("tile_phases",), [(0,), (2,), (4,)]),
+    (("tile_phases",), [(0,), (2,), (4,), (8,)]),
 )
 
 

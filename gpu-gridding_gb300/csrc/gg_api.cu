@@ -873,10 +873,10 @@ int max_tiles(int grid_size, int num_grids) {
 
 // Tile phases requested for a gridding call (TileGeom::tile_phases): the
 // plan's setting (0: chosen with the tile shape, see choose_shape), or 1
-// where four phases' extra sort-key bits and the split passes' would not
+// where eight phases' extra sort-key bits and the split passes' would not
 // fit 32-bit keys.
 int gridding_phases(const gg_plan* plan, int grid_size, int num_grids) {
-  if (ceil_log2((unsigned long long)max_tiles(grid_size, num_grids)) + 2 + 2 >
+  if (ceil_log2((unsigned long long)max_tiles(grid_size, num_grids)) + 3 + 2 >
       32)
     return 1;
   return plan->tile_phases;
@@ -2733,8 +2733,8 @@ GG_API int gg_plan_set_tuning(gg_plan* plan, const gg_tuning* t) {
     return set_error(GG_ERR_INVALID_ARG, "lane_groups = %d: 0, 1 or 2",
                      t->lane_groups);
   if (t->tile_phases != 0 && t->tile_phases != 1 && t->tile_phases != 2 &&
-      t->tile_phases != 4)
-    return set_error(GG_ERR_INVALID_ARG, "tile_phases = %d: 0, 1, 2 or 4",
+      t->tile_phases != 4 && t->tile_phases != 8)
+    return set_error(GG_ERR_INVALID_ARG, "tile_phases = %d: 0, 1, 2, 4 or 8",
                      t->tile_phases);
   const int old_shape = plan->forced_shape;
   GG_TRY(gg_plan_set_tile_shape(plan, t->tile_u));

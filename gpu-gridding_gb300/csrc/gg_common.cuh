@@ -183,7 +183,7 @@ struct TileGeom {
   // 0) -- the whole warp takes each record that meets its rows; 2 -- each
   // half-warp (16 columns) takes the records that meet its own columns.
   int lane_groups;
-  // Tile phases (1, 2 or 4): the tile columns of phase p start p * tile_u /
+  // Tile phases (1, 2, 4 or 8): the tile columns of phase p start p * tile_u /
   // tile_phases cells to the left of phase 0's, and each visibility is
   // gridded on the phase whose tiles cut its footprint into the fewest
   // columns (footprint_phase).  Tiles of different phases overlap, so each

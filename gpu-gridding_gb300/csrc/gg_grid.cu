@@ -736,8 +736,9 @@ __global__ void k_reduce_partials(const int4* __restrict__ split_tiles,
 // correctly rounded FP32 sum.  tile_slot[virtual tile] = (first partial
 // slot, chunks), chunks 0 when the tile has no partial tiles.  Each thread
 // keeps one column (blockDim.x a multiple of TW) and looks its phases'
-// tiles up once.
-template <typename Real, int TW>
+// tiles up once.  kMaxPhases >= tile_phases (4 or 8: the lookups of eight
+// phases take registers that four do not need).
+template <typename Real, int TW, int kMaxPhases>
 __global__ void __launch_bounds__(256)
 k_reduce_phases(const int2* __restrict__ tile_slot,
                 const typename Vec2<Real>::type* __restrict__ partials,
@@ -746,7 +747,6 @@ k_reduce_phases(const int2* __restrict__ tile_slot,
   using R2 = typename Vec2<Real>::type;
   using WS = WarpShape<TW>;
   constexpr int kTV = WS::kTileV;
-  constexpr int kMaxPhases = 4;
   constexpr int kRowStep = 256 / TW;    // rows between a thread's cells
   const int P = g.tile_phases;
   const int sw = 1 << g.strip_shift;
@@ -1115,20 +1115,26 @@ cudaError_t launch_reduce_phases(const int2* tile_slot, const Real* partials,
   const long long n =
       (long long)geom.num_grids * (geom.tiles_u - 1) * geom.tiles_v;
   if (n <= 0) return cudaSuccess;
+  if (geom.tile_phases > 8) return cudaErrorInvalidValue;
   const int blocks = (int)std::min<long long>(n, 65535);
   using P2 = const typename Vec2<Real>::type*;
+  const bool eight = geom.tile_phases > 4;
+#define GG_REDUCE_PHASES(TW_, MP_)                                          \
+  k_reduce_phases<Real, TW_, MP_><<<blocks, 256, 0, s>>>(                   \
+      tile_slot, (P2)partials, geom, group0, grid_size, grid, grid_stride)
   switch (geom.tile_u) {
-    case 32: k_reduce_phases<Real, 32><<<blocks, 256, 0, s>>>(
-        tile_slot, (P2)partials, geom, group0, grid_size, grid, grid_stride);
+    case 32:
+      if (eight) GG_REDUCE_PHASES(32, 8); else GG_REDUCE_PHASES(32, 4);
       break;
-    case 16: k_reduce_phases<Real, 16><<<blocks, 256, 0, s>>>(
-        tile_slot, (P2)partials, geom, group0, grid_size, grid, grid_stride);
+    case 16:
+      if (eight) GG_REDUCE_PHASES(16, 8); else GG_REDUCE_PHASES(16, 4);
       break;
-    case 8: k_reduce_phases<Real, 8><<<blocks, 256, 0, s>>>(
-        tile_slot, (P2)partials, geom, group0, grid_size, grid, grid_stride);
+    case 8:
+      if (eight) GG_REDUCE_PHASES(8, 8); else GG_REDUCE_PHASES(8, 4);
       break;
     default: return cudaErrorInvalidValue;
   }
+#undef GG_REDUCE_PHASES
   return cudaGetLastError();
 }
 

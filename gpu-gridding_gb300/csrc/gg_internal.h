@@ -82,7 +82,7 @@ __host__ __device__ inline int tile_v_of_shape(int shape) {
 // slices staged in shared memory (bit 8) when footprints are small enough
 // for their slices to fit the slots, otherwise the kernel keeps its shared
 // memory small so the L1 cache serves the tap loads; tile phases (bits 12
-// and 13: log2 of 1, 2 or 4) four when footprints are narrower than the
+// and 13: log2 of 1, 2, 4 or 8) four when footprints are narrower than the
 // tile, where offset tile grids save the most tile crossings, else one.
 // forced_shape >= 0 overrides the shape, phases > 0 the phases.
 __host__ __device__ inline uint32_t choose_shape(unsigned long long macs,
@@ -94,7 +94,8 @@ __host__ __device__ inline uint32_t choose_shape(unsigned long long macs,
   if (shape < 0) shape = side >= 16.0 ? 0 : (side >= 8.0 ? 1 : 2);
   const uint32_t stage = side < 40.0 ? 1u : 0u;
   if (phases <= 0) phases = side < (double)tile_u_of_shape(shape) ? 4 : 1;
-  const uint32_t pbits = phases >= 4 ? 2u : (phases >= 2 ? 1u : 0u);
+  const uint32_t pbits =
+      phases >= 8 ? 3u : (phases >= 4 ? 2u : (phases >= 2 ? 1u : 0u));
   return (uint32_t)shape | (stage << 8) | (pbits << 12);
 }
 // Tile phases of a shape word made by choose_shape.

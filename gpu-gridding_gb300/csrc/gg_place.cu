@@ -172,7 +172,7 @@ __global__ void k_count(const uint32_t* __restrict__ cell,
     // Tiles are 32 >> shape by 64 << shape cells, phase strips
     // (32 >> shape) / phases columns: divisions become shifts.
     const int tws = 5 - shape, ths = 6 + shape;
-    const int sws = tws - (phases >= 4 ? 2 : phases >= 2 ? 1 : 0);
+    const int sws = tws - (phases >= 8 ? 3 : phases >= 4 ? 2 : phases >= 2);
     const uint32_t ce = cell[i];
     const int gu = cell_u(ce), gv = cell_v(ce);
     const int s = v.support[meta_plane(m)];

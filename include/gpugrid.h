@@ -204,7 +204,7 @@ GG_API int gg_plan_set_slice_staging(gg_plan* plan, int mode);
  *                  half-warp takes the records that meet its own 16
  *                  columns, so two narrow footprints are gridded side by
  *                  side; 0 (default) = 1
- *   tile_phases    1, 2 or 4 tile grids offset by tile_u / tile_phases
+ *   tile_phases    1, 2, 4 or 8 tile grids offset by tile_u / tile_phases
  *                  columns from one another; each visibility is gridded on
  *                  the one whose tiles cut its footprint into the fewest
  *                  columns (fewer lanes outside footprints, fewer records),

@@ -91,10 +91,10 @@ def test_skalow_placement_bit_exact(pkg, oracle_mod, skalow, torch, prec):
 
 
 @pytest.mark.parametrize("tile_u,phases", [(0, 0), (32, 0), (16, 0), (8, 0),
-                                           (32, 2), (32, 4)])
+                                           (32, 2), (32, 4), (32, 8)])
 def test_skalow_grid_vs_oracles(pkg, skalow, torch, tile_u, phases):
-    """Device-pointer call, automatic and forced tile shapes, one, two and
-    four tile phases."""
+    """Device-pointer call, automatic and forced tile shapes, one, two, four
+    and eight tile phases."""
     wl = skalow["wl"]
     stack = pkg.KernelStack.from_workload(wl, "f")
     plan = pkg.Plan()

@@ -71,6 +71,9 @@ TUNINGS = [
      "plane_group_mb": 1},
     {"tile_u": 32, "slice_staging": 0, "items_per_cta": 2, "lane_groups": 2,
      "tile_phases": 2},
+    {"tile_u": 32, "slice_staging": 0, "items_per_cta": 4, "tile_phases": 8},
+    {"tile_u": 8, "slice_staging": 0, "items_per_cta": 4, "tile_phases": 8,
+     "plane_group_mb": 1},
 ]
 
 
@@ -102,7 +105,7 @@ def test_tuning_rejects_bad_values(pkg, torch):
     for bad in ({"tile_u": 12}, {"slice_staging": 2}, {"items_per_cta": 0},
                 {"items_per_cta": 65}, {"sort_detail": 3},
                 {"ctas_per_sm": -1}, {"tile_order": 2}, {"lane_groups": 3},
-                {"tile_phases": 3}, {"tile_phases": 8}):
+                {"tile_phases": 3}, {"tile_phases": 16}):
         with pytest.raises(pkg.GridError):
             plan.set_tuning(bad)
         assert plan.tuning() == before
