@@ -213,7 +213,7 @@ def parse_args():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="cfg2",
                     choices=sorted(WORKLOAD_TEXT))
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the grid-error check against the FP64 "
@@ -712,9 +712,13 @@ def run_ours(args):
             host_tuning = at.autotune_host(pkg, e2e_step, plan.tuning())
         e2e_step()
         barrier()
+        call_ms, inside_ms = [], []
         te = time.perf_counter()
         for _ in range(args.e2e_steps):
+            t_call = time.perf_counter()
             e2e_step()
+            call_ms.append((time.perf_counter() - t_call) * 1e3)
+            inside_ms.append(pkg.host_last_call_ms()["return"])
         te = (time.perf_counter() - te) / args.e2e_steps
         te = max_over_ranks(te, dist, dev)
         # Bytes the drop-in copied in its last call (every step copies the
@@ -731,6 +735,8 @@ def run_ours(args):
                "grid_access": ["copy", "pinned", "pageable"][
                    pkg.host_grid_access()],
                "host_tuning": host_tuning or pkg.host_tuning(),
+               "call_ms": [round(t, 3) for t in call_ms],
+               "call_ms_in_library": [round(t, 3) for t in inside_ms],
                "phase_ms": host_phases}
         # The same call on pageable (malloc) buffers, as a numpy caller
         # passes them (the grid's pages already touched).
@@ -747,15 +753,19 @@ def run_ours(args):
 
         e2e_pageable()
         barrier()
+        call_ms_p = []
         tp = time.perf_counter()
         for _ in range(args.e2e_steps):
+            t_call = time.perf_counter()
             e2e_pageable()
+            call_ms_p.append((time.perf_counter() - t_call) * 1e3)
         tp = (time.perf_counter() - tp) / args.e2e_steps
         tp = max_over_ranks(tp, dist, dev)
         h2d_p, d2h_p = pkg.host_last_transfer()
         e2e["pageable"] = {"value": replica_throughput(world, num_vis, tp),
                            "unit": UNIT, "h2d_bytes_per_step": h2d_p,
-                           "d2h_bytes_per_step": d2h_p}
+                           "d2h_bytes_per_step": d2h_p,
+                           "call_ms": [round(t, 3) for t in call_ms_p]}
         del hp, gp
 
     # The operations either side of the gridder on the same workload: the

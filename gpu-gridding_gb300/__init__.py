@@ -39,6 +39,7 @@ EXPORTED_SYMBOLS = (
     "gg_plan_destroy", "gg_plan_last_stats", "gg_plan_set_tile_shape",
     "gg_plan_set_slice_staging", "gg_plan_set_tuning", "gg_plan_get_tuning",
     "gg_host_set_tuning", "gg_host_get_tuning", "gg_host_last_transfer",
+    "gg_host_last_call_ms",
     "gg_host_set_grid_access", "gg_host_get_grid_access",
     "gg_host_set_profiling", "gg_host_phase_ms",
     "gg_plan_probe_bounded_wait", "gg_plan_set_batch_limit",
@@ -200,6 +201,9 @@ def _declare(L):
     L.gg_host_get_tuning.restype = ctypes.c_int
     L.gg_host_last_transfer.argtypes = [ctypes.POINTER(ctypes.c_ulonglong)] * 2
     L.gg_host_last_transfer.restype = ctypes.c_int
+    L.gg_host_last_call_ms.argtypes = [ctypes.POINTER(ctypes.c_double),
+                                       ctypes.c_int]
+    L.gg_host_last_call_ms.restype = ctypes.c_int
     L.gg_host_set_grid_access.argtypes = [ctypes.c_int]
     L.gg_host_set_grid_access.restype = ctypes.c_int
     L.gg_host_get_grid_access.argtypes = [ctypes.POINTER(ctypes.c_int)]
@@ -509,6 +513,16 @@ def host_last_transfer() -> tuple:
     a, b = ctypes.c_ulonglong(0), ctypes.c_ulonglong(0)
     _check(lib().gg_host_last_transfer(ctypes.byref(a), ctypes.byref(b)))
     return int(a.value), int(b.value)
+
+
+def host_last_call_ms() -> dict:
+    """Host-clock marks (ms from entry) of the last host-pointer gridding
+    call on the current device: first queued work, final synchronisation,
+    return."""
+    ms = (ctypes.c_double * 3)()
+    _check(lib().gg_host_last_call_ms(ms, 3))
+    return dict(zip(("first_work", "synchronised", "return"),
+                    (float(x) for x in ms)))
 
 
 # How the host-pointer gridding calls reach the caller's grid and cube (see

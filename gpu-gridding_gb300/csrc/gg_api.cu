@@ -2859,6 +2859,18 @@ GG_API int gg_host_last_transfer(unsigned long long* h2d_bytes,
   return GG_OK;
 }
 
+GG_API int gg_host_last_call_ms(double* ms, int n) {
+  t_last_error.clear();
+  if (!ms || n < 0) return set_error(GG_ERR_INVALID_ARG, "NULL argument");
+  int dev;
+  GG_TRY(current_device(&dev));
+  DeviceState* st;
+  GG_TRY(device_state(dev, &st));
+  std::lock_guard<std::mutex> lk(st->mu);
+  for (int i = 0; i < n && i < 3; ++i) ms[i] = st->host_ms[i];
+  return GG_OK;
+}
+
 GG_API int gg_host_get_tuning(gg_tuning* t) {
   t_last_error.clear();
   if (!t) return set_error(GG_ERR_INVALID_ARG, "tuning is NULL");

@@ -304,6 +304,12 @@ GG_API int gg_host_phase_ms(float* ms, int n);
 GG_API int gg_host_last_transfer(unsigned long long* h2d_bytes,
                                  unsigned long long* d2h_bytes);
 
+/* Host-clock marks (ms from the call's entry) of the last host-pointer
+ * gridding call on the current device, profiled or not: ms[0] its first
+ * queued device work, ms[1] the return of its final synchronisation, ms[2]
+ * its return (n <= 3 are filled; zeros before the first call). */
+GG_API int gg_host_last_call_ms(double* ms, int n);
+
 /* Phase timing.  With profiling enabled, every gridding call made with the
  * plan records CUDA events on its stream around five phases:
  *   0 placement (placement, skip/norm reduction, record offsets)

@@ -667,6 +667,8 @@ def test_host_phase_times(pkg, synthetic):
         assert (ph["host_first_work"] <= ph["host_synchronised"]
                 <= ph["host_return"] <= wall)
         assert device <= ph["host_synchronised"] * 1.05 + 0.1
+        marks = pkg.host_last_call_ms()
+        assert marks["return"] == pytest.approx(ph["host_return"], abs=1e-3)
         empty = dataclasses.replace(wl, uu=wl.uu[:0], vv=wl.vv[:0],
                                     ww=wl.ww[:0], vis=wl.vis[:0],
                                     weight=wl.weight[:0])
@@ -675,9 +677,15 @@ def test_host_phase_times(pkg, synthetic):
             pkg.host_phase_ms()
     finally:
         pkg.set_host_profiling(False)
+    t0 = time.perf_counter()
     pkg.grid_f(wl)
+    wall = (time.perf_counter() - t0) * 1e3
     with pytest.raises(pkg.GridError):
         pkg.host_phase_ms()
+    # The host-clock marks are kept without profiling too.
+    marks = pkg.host_last_call_ms()
+    assert 0.0 <= marks["first_work"] <= marks["synchronised"] \
+        <= marks["return"] <= wall
 
 
 def test_grid_access_mode_setting(pkg):
