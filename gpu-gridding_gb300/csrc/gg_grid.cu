@@ -10,9 +10,9 @@
 // kernel taps of its own cells and accumulates -- no atomics, no
 // shared-memory read-modify-write.  A tile with one item is then added to
 // the grid in place with one coalesced read-modify-write; a tile split over
-// several items writes one partial tile per item and k_reduce_partials adds
-// them to the grid in item order, so the result does not depend on
-// scheduling.
+// several items writes one partial tile per item and k_reduce_partials (or
+// k_reduce_phases) adds them to the grid in item order, so the result does
+// not depend on scheduling.
 //
 // The CTA is warp-specialised.  One producer warp takes work items, gathers
 // and prepares their records and streams them through a ring of kRing
@@ -26,6 +26,16 @@
 // Three warp shapes share the 2048-cell tile: TW = 32 (32 x 64 tiles, for
 // large footprints), 16 (16 x 128) and 8 (8 x 256, for small footprints,
 // where a 32-wide warp would leave most lanes outside the footprint).
+//
+// Tile phases (TileGeom::tile_phases): up to eight tile grids, each offset
+// by a strip of TW / phases columns from the last; every visibility's
+// records are on the grid that cuts its footprint into the fewest tile
+// columns, so fewer warp steps fall on footprints cut by a tile boundary.
+// One launch takes all the phases of a plane group: phase 0's single-item
+// tiles add to the grid as above, every other item writes a partial tile,
+// and k_reduce_phases adds those per cell in phase order after the launch
+// (one launch per phase where the grid is the caller's host memory in
+// place, each phase's tiles then added directly).
 //
 // The reference's equivalent is oskar_process_tiles_dynamic
 // (oskar_grid_wproj_gpu.cu:840-1309), a one-warp-per-32x16-tile kernel that
