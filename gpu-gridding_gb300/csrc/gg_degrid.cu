@@ -18,7 +18,9 @@
 // (rec_offset[visibility] + its tile's rank among the visibility's tiles).
 // k_degrid_finish then adds each visibility's partial results in emission
 // order.  Nothing is accumulated with atomics, so the result does
-// not depend on scheduling.
+// not depend on scheduling.  With tile phases (see gg_grid.cu) a
+// visibility's records are on its phase's tiles; the degridder only reads
+// the grid, so the tiles of all phases share its one launch.
 //
 // The reference has no degridder; this one is pinned by the dot-product
 // identity <G x, y> = <x, G^H y> against the forward kernel and by the FP64

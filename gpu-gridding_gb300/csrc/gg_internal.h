@@ -130,9 +130,9 @@ cudaError_t launch_norm_terms(const uint32_t* meta, const Real* weight,
                               double* blk_norm, double* d_norm,
                               cudaStream_t s);
 // Sums the per-block partials: *d_norm += norm, *d_num_skipped = skips,
-// *d_macs = macs (all device pointers), and picks the tile shape for the
-// call into *d_shape: forced_shape if >= 0, else from the mean footprint
-// area (macs / gridded points).
+// *d_macs = macs (all device pointers), and picks the tile shape and tile
+// phases for the call into *d_shape (choose_shape): forced_shape if >= 0,
+// phases if > 0, else from the mean footprint area (macs / gridded points).
 cudaError_t launch_place_finalize(const double* blk_norm,
                                   const unsigned long long* blk_skip,
                                   const unsigned long long* blk_macs,
@@ -142,7 +142,8 @@ cudaError_t launch_place_finalize(const double* blk_norm,
                                   unsigned long long* d_macs,
                                   uint32_t* d_shape, cudaStream_t s,
                                   int phases = 1);
-// count[i] = tiles of shape *d_shape touched by visibility i (0 if skipped).
+// count[i] = tiles of shape *d_shape touched by visibility i on its tile
+// phase (footprint_phase; 0 if skipped).
 cudaError_t launch_count_records(const uint32_t* cell, const uint32_t* meta,
                                  unsigned long long n, StackView view,
                                  const uint32_t* d_shape, uint32_t* count,
