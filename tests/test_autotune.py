@@ -127,8 +127,9 @@ def test_tuning_struct_round_trip(pkg):
 
 
 def test_host_search_keeps_the_fastest(at):
-    """autotune_host re-times the host calls over the tile order and the
-    plane groups from the plan's settings and applies the fastest."""
+    """autotune_host re-times the host calls over the tile order, the
+    plane groups and the tile phases from the plan's settings and applies
+    the fastest."""
     applied = []
 
     class FakePkg:
@@ -142,4 +143,5 @@ def test_host_search_keeps_the_fastest(at):
     assert applied[-1] == {k: got[k] for k in base}
     tried = {(t["tile_order"], t["plane_group_mb"]) for t in applied}
     assert (0, 64) in tried and (1, 64) in tried
+    assert {t["tile_phases"] for t in applied} >= {0, 1, 2}
     assert got["ms"] >= 0
