@@ -180,8 +180,8 @@ def _device_name(torch) -> str:
 #: Settings the host-pointer calls are re-timed over, starting from the
 #: plan's tuning: where the grid is the caller's host memory used in place,
 #: the tile order and the plane groups change how its pages are touched,
-#: and each tile phase has a launch of its own (so fewer phases than the
-#: device plan's can pay).
+#: and the tile phases' reduction reads and writes it after the gridding
+#: launch (so fewer phases than the device plan's can pay).
 HOST_SEARCH = (("tile_order", (0, 1)), ("plane_group_mb", (None, 1 << 20)),
                ("tile_phases", (None, 1, 2)))
 

@@ -1365,13 +1365,11 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
   plan->stats.slice_staging = b.stage ? 1 : 0;
   ItemBuffers ib;
   // The tile phases of a plane group share one launch, their later phases'
-  // tiles added as partial tiles after it -- except when the kernels read
-  // and write the caller's grid at host, where those additions would cross
-  // the host link after the launch instead of beside its work: there each
-  // phase has a launch of its own.  Items are sized per virtual group
-  // either way (a phase's tiles are smaller, and larger items leave longer
-  // tails).
-  const int span = plan->host_grid ? 1 : geom.tile_phases;
+  // tiles added as partial tiles after it (where the kernels use the
+  // caller's grid at host, those additions read and write it per strip).
+  // Items are sized per virtual group (a phase's tiles are smaller, and
+  // larger items leave longer tails).
+  const int span = geom.tile_phases;
   GG_TRY(build_work_items<Real>(plan, b, num_ctas, geom.num_groups, true, s,
                                 &ib, span));
   plan->kept.group_span = span;
@@ -1413,7 +1411,8 @@ int bin_and_grid(gg_plan* plan, const gg_kernels* K, size_t n,
       po.cell, po.meta, po.vw, view, geom, grid_size, d_grid, grid_stride,
       plan->partials.as<Real>(), ib.split_tiles, ib.num_split, b.num_tiles,
       num_ctas, b.stage, s, wait_before.data(), record_after.data(),
-      (Real*)plan->host_grid, tile_groups, span, plan->tile_slot.as<int2>()));
+      (Real*)plan->host_grid, tile_groups, span, plan->tile_slot.as<int2>(),
+      plan->tile_start.as<uint32_t>()));
   plan->split_launched = upper_done >= 0;
   plan->mark(4, s);
   plan->mark(5, s);
@@ -1728,7 +1727,7 @@ int replay_pipeline(gg_plan* plan, const gg_kernels* K, const Real* vis,
       d_grids, grid_stride, plan->partials.as<Real>(),
       plan->split_tiles.as<int4>(), sc + kNumSplit, kp.num_tiles, kp.num_ctas,
       kp.stage, s, nullptr, nullptr, nullptr, nullptr, kp.group_span,
-      plan->tile_slot.as<int2>()));
+      plan->tile_slot.as<int2>(), plan->tile_start.as<uint32_t>()));
   return GG_OK;
 }
 

@@ -34,8 +34,8 @@
 // One launch takes all the phases of a plane group: phase 0's single-item
 // tiles add to the grid as above, every other item writes a partial tile,
 // and k_reduce_phases adds those per cell in phase order after the launch
-// (one launch per phase where the grid is the caller's host memory in
-// place, each phase's tiles then added directly).
+// (where the grid is the caller's host memory in place, reading and writing
+// it per strip as the strip's first and last passes would).
 //
 // The reference's equivalent is oskar_process_tiles_dynamic
 // (oskar_grid_wproj_gpu.cu:840-1309), a one-warp-per-32x16-tile kernel that
@@ -753,7 +753,9 @@ __global__ void __launch_bounds__(256)
 k_reduce_phases(const int2* __restrict__ tile_slot,
                 const typename Vec2<Real>::type* __restrict__ partials,
                 TileGeom g, int group0, int G, Real* grid,
-                long long grid_stride) {
+                long long grid_stride, Real* host,
+                const uint32_t* __restrict__ tile_groups,
+                const uint32_t* __restrict__ tile_start) {
   using R2 = typename Vec2<Real>::type;
   using WS = WarpShape<TW>;
   constexpr int kTV = WS::kTileV;
@@ -790,6 +792,26 @@ k_reduce_phases(const int2* __restrict__ tile_slot,
     if (!__syncthreads_or(mine)) continue;
     if (!mine || col >= G) continue;
     R2* gg = (R2*)(grid + (long long)gi * grid_stride);
+    // Direct mode (the caller's grid at host in place, one grid): the
+    // column's strip was last added to at host unless phase 0's tile here
+    // added itself to the scratch grid in the launch (it had records, one
+    // item) or an earlier plane group touched the strip; the additions
+    // here are the strip's last when its last virtual group is in this
+    // launch.
+    R2* src = gg;
+    R2* dst = gg;
+    if (tile_groups) {
+      const uint32_t fl =
+          tile_groups[tv * g.strips_u + (col >> g.strip_shift)];
+      const int first = (int)(fl & 0xFFFFu), last = (int)(fl >> 16);
+      const size_t vt0 = (size_t)group0 * g.tiles_total +
+                         (size_t)gi * tiles_per_grid +
+                         (size_t)tv * g.tiles_u + tu;
+      const bool added0 =
+          sl[0].y == 0 && tile_start[vt0 + 1] > tile_start[vt0];
+      if (!added0 && first >= group0) src = (R2*)host;
+      if (last < group0 + P) dst = (R2*)host;
+    }
 #pragma unroll 4
     for (int R = R0; R < kTV; R += kRowStep) {
       const int row = tv * kTV + R;
@@ -799,7 +821,7 @@ k_reduce_phases(const int2* __restrict__ tile_slot,
       // (R % kBand) / kRows, register row R % kRows).
       const int w = R / WS::kBand, ly = (R % WS::kBand) / kRows;
       const int ent0 = (R % kRows) * kConsumers + w * 32 + ly * TW;
-      R2 acc = gg[(size_t)row * G + col];
+      R2 acc = src[(size_t)row * G + col];
 #pragma unroll
       for (int p = 0; p < kMaxPhases; ++p) {
         if (sl[p].y == 0) continue;
@@ -819,7 +841,7 @@ k_reduce_phases(const int2* __restrict__ tile_slot,
           acc.y = (Real)sy;
         }
       }
-      gg[(size_t)row * G + col] = acc;
+      dst[(size_t)row * G + col] = acc;
     }
   }
 }
@@ -1121,7 +1143,8 @@ template <typename Real>
 cudaError_t launch_reduce_phases(const int2* tile_slot, const Real* partials,
                                  TileGeom geom, int group0, int grid_size,
                                  Real* grid, long long grid_stride,
-                                 cudaStream_t s) {
+                                 Real* host, const uint32_t* tile_groups,
+                                 const uint32_t* tile_start, cudaStream_t s) {
   const long long n =
       (long long)geom.num_grids * (geom.tiles_u - 1) * geom.tiles_v;
   if (n <= 0) return cudaSuccess;
@@ -1131,7 +1154,8 @@ cudaError_t launch_reduce_phases(const int2* tile_slot, const Real* partials,
   const bool eight = geom.tile_phases > 4;
 #define GG_REDUCE_PHASES(TW_, MP_)                                          \
   k_reduce_phases<Real, TW_, MP_><<<blocks, 256, 0, s>>>(                   \
-      tile_slot, (P2)partials, geom, group0, grid_size, grid, grid_stride)
+      tile_slot, (P2)partials, geom, group0, grid_size, grid, grid_stride, \
+      host, tile_groups, tile_start)
   switch (geom.tile_u) {
     case 32:
       if (eight) GG_REDUCE_PHASES(32, 8); else GG_REDUCE_PHASES(32, 4);
@@ -1187,7 +1211,8 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                               const cudaEvent_t* wait_before,
                               const cudaEvent_t* record_after,
                               Real* host_grid, const uint32_t* tile_groups,
-                              int group_span, const int2* tile_slot) {
+                              int group_span, const int2* tile_slot,
+                              const uint32_t* tile_start) {
   GridArgs<Real> a;
   a.items = items;
   a.group_items = group_items;
@@ -1228,7 +1253,8 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
     if (e != cudaSuccess) return e;
     if (span > 1 && tile_slot) {
       e = launch_reduce_phases<Real>(tile_slot, partials, geom, g, grid_size,
-                                     grid, grid_stride, s);
+                                     grid, grid_stride, a.host, tile_groups,
+                                     tile_start, s);
       if (e != cudaSuccess) return e;
     } else {
       for (int p = 0; p < span; ++p) {
@@ -1253,12 +1279,12 @@ template cudaError_t launch_grid_tiles<float>(
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
     float*, long long, float*, const int4*, const uint32_t*, int, int, bool,
     cudaStream_t, const cudaEvent_t*, const cudaEvent_t*, float*,
-    const uint32_t*, int, const int2*);
+    const uint32_t*, int, const int2*, const uint32_t*);
 template cudaError_t launch_grid_tiles<double>(
     const WorkItem*, const uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
     const uint32_t*, const uint32_t*, const void*, StackView, TileGeom, int,
     double*, long long, double*, const int4*, const uint32_t*, int, int, bool,
     cudaStream_t, const cudaEvent_t*, const cudaEvent_t*, double*,
-    const uint32_t*, int, const int2*);
+    const uint32_t*, int, const int2*, const uint32_t*);
 
 }  // namespace gg

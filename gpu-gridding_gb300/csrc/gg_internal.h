@@ -281,7 +281,8 @@ cudaError_t launch_grid_tiles(const WorkItem* items,
                               Real* host_grid = nullptr,
                               const uint32_t* tile_groups = nullptr,
                               int group_span = 1,
-                              const int2* tile_slot = nullptr);
+                              const int2* tile_slot = nullptr,
+                              const uint32_t* tile_start = nullptr);
 // Direct mode of a single-grid call: per strip (num_strips), the first and
 // last virtual group (plane group and tile phase) with records there
 // (first | last << 16, 0xFFFF when none), and *cells += the grid cells of
