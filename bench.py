@@ -493,6 +493,13 @@ def cpu_sample(wl, target):
     return wl.strided(k), k
 
 
+def ordinal(k):
+    """1st, 2nd, 3rd, 4th, ..., 11th, 12th, 13th, 21st, 32nd, ..."""
+    if 10 <= k % 100 <= 20:
+        return f"{k}th"
+    return f"{k}" + {1: "st", 2: "nd", 3: "rd"}.get(k % 10, "th")
+
+
 def single_thread_rate(wl):
     """Mvis/s of the serial restatement of oskar_grid_wproj_f on one host
     thread, on a strided sample of about CPU_SAMPLE_VIS_1T visibilities."""
@@ -504,7 +511,7 @@ def single_thread_rate(wl):
     t = time.perf_counter() - t0
     return {"value": sample.num_points / t / 1e6, "unit": UNIT, "cores": 1,
             "kind": "port",
-            "sample": f"every {k}th visibility ({sample.num_points} vis), "
+            "sample": f"every {ordinal(k)} visibility ({sample.num_points} vis), "
                       "serial restatement of oskar_grid_wproj_f, one run"}
 
 
@@ -521,7 +528,7 @@ def run_reference(args):
     t = statistics.mean(times)
     value = sample.num_points / t / 1e6
     what = ("whole workload" if k == 1 else
-            f"every {k}th visibility of the workload")
+            f"every {ordinal(k)} visibility of the workload")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
