@@ -511,7 +511,9 @@ def single_thread_rate(wl):
     t = time.perf_counter() - t0
     return {"value": sample.num_points / t / 1e6, "unit": UNIT, "cores": 1,
             "kind": "port",
-            "sample": f"every {ordinal(k)} visibility ({sample.num_points} vis), "
+            "sample": ("every visibility" if k == 1 else
+                       f"every {ordinal(k)} visibility")
+                      + f" ({sample.num_points} vis), "
                       "serial restatement of oskar_grid_wproj_f, one run"}
 
 
