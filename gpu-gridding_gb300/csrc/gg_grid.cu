@@ -812,6 +812,47 @@ k_reduce_phases(const int2* __restrict__ tile_slot,
       if (!added0 && first >= group0) src = (R2*)host;
       if (last < group0 + P) dst = (R2*)host;
     }
+    if constexpr (sizeof(Real) == 4 && kMaxPhases <= 4) {
+      bool several = false;
+#pragma unroll
+      for (int p = 0; p < kMaxPhases; ++p) several |= sl[p].y > 1;
+      if (!several) {
+        // Every phase adds at most one chunk to this column: all of the
+        // thread's loads (its rows of the grid and of up to kMaxPhases
+        // partial tiles) go out before the first addition, so the block
+        // waits out one memory latency rather than one per row.  The
+        // additions are the loop's below, in the same order.
+        constexpr int kRowsPer = kTV / kRowStep;
+        R2 acc[kRowsPer], pv[kMaxPhases][kRowsPer];
+#pragma unroll
+        for (int i = 0; i < kRowsPer; ++i) {
+          const int R = R0 + i * kRowStep;
+          const int row = tv * kTV + R;
+          const bool in = row < G;
+          const int w = R / WS::kBand, ly = (R % WS::kBand) / kRows;
+          const int ent0 = (R % kRows) * kConsumers + w * 32 + ly * TW;
+          acc[i] = in ? src[(size_t)row * G + col] : R2{};
+#pragma unroll
+          for (int p = 0; p < kMaxPhases; ++p)
+            pv[p][i] = in && sl[p].y > 0
+                           ? partials[(size_t)sl[p].x * kCells + ent0 + cp[p]]
+                           : R2{};
+        }
+#pragma unroll
+        for (int i = 0; i < kRowsPer; ++i) {
+          const int row = tv * kTV + R0 + i * kRowStep;
+          if (row >= G) break;
+#pragma unroll
+          for (int p = 0; p < kMaxPhases; ++p) {
+            if (sl[p].y == 0) continue;
+            acc[i].x += pv[p][i].x;
+            acc[i].y += pv[p][i].y;
+          }
+          dst[(size_t)row * G + col] = acc[i];
+        }
+        continue;
+      }
+    }
 #pragma unroll 4
     for (int R = R0; R < kTV; R += kRowStep) {
       const int row = tv * kTV + R;
