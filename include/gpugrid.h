@@ -172,10 +172,12 @@ GG_API int gg_plan_set_tile_shape(gg_plan* plan, int tile_u);
 GG_API int gg_plan_set_slice_staging(gg_plan* plan, int mode);
 
 /* Launch and decomposition parameters of a plan's gridding calls, as set
- * by an autotuner (or by hand).  Every setting changes speed only; tile_u
- * and sort_detail also change the order in which contributions to a cell
- * are added (results then differ by FP32 rounding, not in placement, norm
- * or num_skipped).
+ * by an autotuner (or by hand).  Every setting changes speed only:
+ * placement, norm and num_skipped are the same under all of them.  The
+ * settings that change how a cell's contributions are grouped or ordered
+ * (tile_u, items_per_cta, sort_detail, ctas_per_sm -- through the number of
+ * work items --, plane_group_mb, tile_phases) change the grid by FP32
+ * rounding; slice_staging leaves it bit-identical.
  *   tile_u         32, 16 or 8 (cells across a tile); 0 = chosen per call
  *   slice_staging  -1 chosen per call, 0 off, 1 on (bit-identical results)
  *   items_per_cta  work items per persistent CTA in each gridding pass
